@@ -1,0 +1,333 @@
+"""GB300-native Hartree-Fock hot path with the reference's API surface.
+
+Python mirror of the reference's host classes (Molecular, ParameterManager,
+HFBuilder, RHF) over the C ABI of libgansu_gb300.so.  Device buffers are torch
+CUDA tensors; every compute call goes through the CUDA library, and there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from ._capi import (HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
+                    check, lib)
+
+BASIS_DIR = Path(__file__).resolve().parent / "basis"
+ANGSTROM_TO_BOHR = 1.8897259886
+
+__all__ = [
+    "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
+    "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "basis_path",
+]
+
+
+def basis_path(name: str) -> str:
+    """Path of a bundled Gaussian basis file, e.g. basis_path('sto-3g')."""
+    p = Path(name)
+    if p.exists():
+        return str(p)
+    cand = BASIS_DIR / (name if name.endswith(".gbs") else name + ".gbs")
+    if not cand.exists():
+        raise FileNotFoundError(f"basis set {name!r} not found in {BASIS_DIR}")
+    return str(cand)
+
+
+class Molecular:
+    """Mirror of gansu::Molecular (include/molecular.hpp:53-294)."""
+
+    def __init__(self, atoms, gbs_filename: str, charge: int = 0, beta_to_alpha: int = 0):
+        """atoms: iterable of (atomic_number, x, y, z) in bohr."""
+        atoms = list(atoms)
+        arr = (Atom * len(atoms))(*[Atom(int(z), float(x), float(y), float(w)) for z, x, y, w in atoms])
+        h = C.c_void_p()
+        check(lib().hf_molecule_from_atoms(arr, len(atoms), str(gbs_filename).encode(), charge, beta_to_alpha,
+                                           C.byref(h)), "hf_molecule_from_atoms")
+        self._init_from_handle(h)
+
+    @classmethod
+    def from_files(cls, xyz_filename: str, gbs_filename: str, charge: int = 0, beta_to_alpha: int = 0):
+        h = C.c_void_p()
+        check(lib().hf_molecule_from_files(str(xyz_filename).encode(), str(gbs_filename).encode(), charge,
+                                           beta_to_alpha, C.byref(h)), "hf_molecule_from_files")
+        obj = cls.__new__(cls)
+        obj._init_from_handle(h)
+        return obj
+
+    def _init_from_handle(self, h):
+        L = lib()
+        vals = [C.c_int() for _ in range(6)]
+        check(L.hf_molecule_sizes(h, *[C.byref(v) for v in vals]), "hf_molecule_sizes")
+        (self.num_basis, self.num_primitives, self.num_atoms, self.num_electrons, self.num_alpha_spins,
+         self.num_beta_spins) = [v.value for v in vals]
+        self._prims = (PrimitiveShell * self.num_primitives)()
+        self._cgto = (C.c_double * self.num_basis)()
+        self._atoms = (Atom * self.num_atoms)()
+        check(L.hf_molecule_get(h, self._prims, self._cgto, self._atoms), "hf_molecule_get")
+        L.hf_molecule_destroy(h)
+
+    # getters named as in the reference
+    def get_num_basis(self) -> int:
+        return self.num_basis
+
+    def get_num_electrons(self) -> int:
+        return self.num_electrons
+
+    def get_primitive_shells(self):
+        return self._prims
+
+    def get_cgto_normalization_factors(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self._cgto).copy()
+
+    def get_atoms(self):
+        return [(a.atomic_number, a.x, a.y, a.z) for a in self._atoms]
+
+    def primitive_table(self) -> dict:
+        """Primitive shells as numpy columns (exponent, coefficient, xyz, shell_type, basis_index, atom_index)."""
+        p = self._prims
+        return {
+            "exponent": np.array([q.exponent for q in p]),
+            "coefficient": np.array([q.coefficient for q in p]),
+            "xyz": np.array([[q.x, q.y, q.z] for q in p]),
+            "shell_type": np.array([q.shell_type for q in p], dtype=np.int32),
+            "basis_index": np.array([q.basis_index for q in p], dtype=np.int64),
+            "atom_index": np.array([q.atom_index for q in p], dtype=np.int32),
+        }
+
+
+def _ptr(t) -> int:
+    return 0 if t is None else int(t.data_ptr())
+
+
+def _stream(stream) -> C.c_void_p:
+    if stream is None:
+        return C.c_void_p(0)
+    return C.c_void_p(int(getattr(stream, "cuda_stream", stream)))
+
+
+class Engine:
+    """Device-resident integral engine (the ERI plugin's precomputation)."""
+
+    def __init__(self, mol: Molecular, schwarz_screening_threshold: float = 1e-12):
+        import torch  # device memory and streams
+
+        self.torch = torch
+        self.mol = mol
+        self.N = mol.num_basis
+        h = C.c_void_p()
+        check(lib().hf_engine_create(mol._prims, mol.num_primitives, mol._cgto, mol.num_basis, mol._atoms,
+                                     mol.num_atoms, float(schwarz_screening_threshold), C.byref(h)),
+              "hf_engine_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hf_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _empty(self, *shape):
+        return self.torch.zeros(*shape, dtype=self.torch.float64, device="cuda")
+
+    def stats(self) -> dict:
+        ns, npair, nq = C.c_int(), C.c_longlong(), C.c_longlong()
+        check(lib().hf_engine_stats(self._h, C.byref(ns), C.byref(npair), C.byref(nq)), "hf_engine_stats")
+        return {"num_shells": ns.value, "num_shell_pairs": npair.value, "num_quartets": nq.value}
+
+    def core_hamiltonian(self, stream=None):
+        S, H = self._empty(self.N, self.N), self._empty(self.N, self.N)
+        check(lib().hf_compute_core_hamiltonian(self._h, _ptr(S), _ptr(H), _stream(stream)),
+              "hf_compute_core_hamiltonian")
+        return S, H
+
+    def primitive_pair_bounds(self) -> np.ndarray:
+        n = self.mol.num_primitives
+        out = np.zeros((n, n))
+        check(lib().hf_primitive_pair_bounds(self._h, out.ctypes.data_as(C.POINTER(C.c_double))),
+              "hf_primitive_pair_bounds")
+        return out
+
+    def eri_matrix(self, stream=None):
+        eri = self._empty(self.N, self.N, self.N, self.N)
+        check(lib().hf_compute_eri_matrix(self._h, _ptr(eri), _stream(stream)), "hf_compute_eri_matrix")
+        return eri
+
+    def fock_stored(self, D, H, eri, stream=None):
+        F = self._empty(self.N, self.N)
+        check(lib().hf_compute_fock_stored_rhf(_ptr(D), _ptr(H), _ptr(eri), _ptr(F), self.N, _stream(stream)),
+              "hf_compute_fock_stored_rhf")
+        return F
+
+    def fock_direct(self, D, H, precision=HF_PRECISION_FP64, mixed_threshold=1e-7, out=None, stream=None):
+        F = out if out is not None else self._empty(self.N, self.N)
+        check(lib().hf_compute_fock_direct_rhf(self._h, _ptr(D), _ptr(H), _ptr(F), precision, mixed_threshold,
+                                               _stream(stream)), "hf_compute_fock_direct_rhf")
+        return F
+
+    def jk(self, D, precision=HF_PRECISION_FP64, mixed_threshold=1e-7, stream=None):
+        J, K = self._empty(self.N, self.N), self._empty(self.N, self.N)
+        check(lib().hf_compute_jk_direct(self._h, _ptr(D), _ptr(J), _ptr(K), precision, mixed_threshold,
+                                         _stream(stream)), "hf_compute_jk_direct")
+        return J, K
+
+    def diis_error(self, S, X, F, D, include_transform=False, stream=None):
+        E = self._empty(self.N, self.N)
+        check(lib().hf_compute_diis_error(self._h, _ptr(S), _ptr(X), _ptr(F), _ptr(D), _ptr(E),
+                                          int(include_transform), _stream(stream)), "hf_compute_diis_error")
+        return E
+
+    def fock_diis(self, errors, focks, stream=None):
+        m = errors.shape[0]
+        F = self._empty(self.N, self.N)
+        check(lib().hf_compute_fock_diis(self._h, _ptr(errors), _ptr(focks), _ptr(F), m, _stream(stream)),
+              "hf_compute_fock_diis")
+        return F
+
+    def rhf_scf(self, num_electrons: int, options: dict | None = None, want_matrices: bool = False):
+        opt = ScfOptions()
+        lib().hf_scf_options_default(C.byref(opt))
+        for k, v in (options or {}).items():
+            setattr(opt, k, v)
+        res = ScfResult()
+        outs = [self._empty(self.N, self.N), self._empty(self.N, self.N), self._empty(self.N),
+                self._empty(self.N, self.N)] if want_matrices else [None] * 4
+        st = lib().hf_rhf_scf(self._h, int(num_electrons), C.byref(opt), C.byref(res), *[_ptr(t) for t in outs])
+        out = {f: getattr(res, f) for f, _ in ScfResult._fields_}
+        out["status"] = st
+        if st not in (0, 4):
+            check(st, "hf_rhf_scf")
+        if want_matrices:
+            out["density"], out["fock"], out["orbital_energies"], out["coefficients"] = outs
+        return out
+
+
+# ------------------------------------------------------------ parameters
+_DEFAULTS = {
+    "parameter_file": "", "xyzfilename": "", "gbsfilename": "", "verbose": "0", "method": "rhf", "charge": "0",
+    "beta_to_alpha": "0", "eri_method": "stored", "auxiliary_gbsfilename": "", "maxiter": "100",
+    "convergence_energy_threshold": "1e-6", "schwarz_screening_threshold": "1e-12", "initial_guess": "core",
+    "convergence_method": "diis", "damping_factor": "0.9", "diis_size": "8", "diis_include_transform": "0",
+    "rohf_parameter_name": "roothaan", "geometry_optimization": "0", "geometry_optimization_method": "powell",
+    "export_sad_cache": "0",
+    # added by this engine, same parsing rules
+    "precision": "fp64", "mixed_threshold": "1e-7", "incremental_fock": "0",
+}
+_SHORT = {"-m": "method", "-v": "verbose", "-p": "parameter_file", "-x": "xyzfilename", "-g": "gbsfilename",
+          "-ag": "auxiliary_gbsfilename", "-c": "charge"}
+_KEEP_CASE = {"xyzfilename", "gbsfilename", "parameter_file"}
+
+
+class ParameterManager:
+    """Mirror of gansu::ParameterManager (src/parameter_manager.cpp:40-224):
+    string values with defaults, short options, ``key = value`` recipes,
+    values lower-cased except file names, unknown keys rejected."""
+
+    def __init__(self, set_default_values: bool = True):
+        self._p: dict[str, str] = dict(_DEFAULTS) if set_default_values else {}
+
+    def __setitem__(self, key, value):
+        if key not in _DEFAULTS:
+            raise KeyError(f"Unknown parameter: {key}")
+        v = str(value)
+        self._p[key] = v if key in _KEEP_CASE else v.lower()
+
+    def __getitem__(self, key):
+        return self._p[key]
+
+    def get(self, key, typ=str):
+        v = self._p[key]
+        if typ is bool:
+            return v not in ("0", "false", "")
+        return typ(v)
+
+    def parse_command_line_args(self, argv):
+        i = 0
+        while i < len(argv):
+            k = argv[i]
+            key = _SHORT.get(k, k[2:] if k.startswith("--") else None)
+            if key is None or i + 1 >= len(argv):
+                raise KeyError(f"Invalid option: {k}")
+            self[key] = argv[i + 1]
+            i += 2
+        if self._p.get("parameter_file"):
+            self.load_from_file(self._p["parameter_file"], override=False)
+
+    def load_from_file(self, path, override=True):
+        for line in Path(path).read_text().splitlines():
+            line = line.split("#", 1)[0].strip()
+            if not line or "=" not in line:
+                continue
+            k, v = (s.strip() for s in line.split("=", 1))
+            if k not in _DEFAULTS:
+                raise KeyError(f"Unknown parameter: {k}")
+            if override or self._p.get(k, _DEFAULTS[k]) == _DEFAULTS[k]:
+                self[k] = v
+
+
+class RHF:
+    """Mirror of gansu::RHF (include/rhf.hpp, src/rhf.cu) for the direct and
+    stored ERI methods: ``solve()`` runs the SCF on the GPU."""
+
+    def __init__(self, molecular: Molecular, parameters: ParameterManager):
+        if molecular.num_alpha_spins != molecular.num_beta_spins:
+            raise ValueError("In restricted Hartree Fock method, the number of alpha and beta electrons should be equal.")
+        self.mol = molecular
+        self.params = parameters
+        method = parameters["eri_method"]
+        if method not in ("stored", "direct"):
+            raise ValueError(f"Invalid ERI method name: {method}")
+        if parameters["convergence_method"] != "diis":
+            raise ValueError("only the DIIS convergence method is provided by this engine")
+        if parameters["initial_guess"] != "core":
+            raise ValueError("only the core-Hamiltonian initial guess is provided by this engine")
+        self.engine = Engine(molecular, parameters.get("schwarz_screening_threshold", float))
+        self.result = None
+
+    def solve(self) -> float:
+        p = self.params
+        opts = {
+            "max_iter": p.get("maxiter", int),
+            "convergence_threshold": p.get("convergence_energy_threshold", float),
+            "diis_size": p.get("diis_size", int),
+            "diis_include_transform": int(p.get("diis_include_transform", bool)),
+            "precision": HF_PRECISION_MIXED if p["precision"] == "mixed" else HF_PRECISION_FP64,
+            "mixed_threshold": p.get("mixed_threshold", float),
+            "incremental": int(p.get("incremental_fock", bool)),
+            "verbose": p.get("verbose", int),
+        }
+        self.result = self.engine.rhf_scf(self.mol.num_electrons, opts, want_matrices=True)
+        return self.result["total_energy"]
+
+    def get_total_energy(self) -> float:
+        return self.result["total_energy"]
+
+    def get_energy(self) -> float:
+        return self.result["electronic_energy"]
+
+    def get_nuclear_repulsion_energy(self) -> float:
+        return self.result["nuclear_repulsion"]
+
+    def report(self) -> str:
+        r = self.result
+        return (f"Total energy: {r['total_energy']:.12f}\nIterations: {r['iterations']}\n"
+                f"Converged: {bool(r['converged'])}\n")
+
+
+class HFBuilder:
+    """Mirror of gansu::HFBuilder::buildHF (include/builder.hpp:43-106)."""
+
+    @staticmethod
+    def buildHF(parameters: ParameterManager) -> RHF:
+        method = parameters["method"]
+        if method != "rhf":
+            raise ValueError(f"method {method!r}: this engine provides RHF")
+        mol = Molecular.from_files(parameters["xyzfilename"], parameters["gbsfilename"],
+                                   parameters.get("charge", int), parameters.get("beta_to_alpha", int))
+        return RHF(mol, parameters)

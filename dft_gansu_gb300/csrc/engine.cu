@@ -1,0 +1,427 @@
+// Engine construction (the ERI plugin's precomputation).
+//
+//  1. contracted shells are rebuilt from the primitive list: primitives that
+//     share basis_index and shell_type form one shell (the reference keeps
+//     them as independent primitive shells, include/types.hpp:116-125);
+//  2. shell pairs per class (la >= lb) with their primitive pairs: Gaussian
+//     product data, the prefactor K and the reference's primitive Schwarz
+//     bound Q = sqrt(max_comp (ab|ab)) (src/schwarz.txt:239-470), evaluated on
+//     the host with the same MD templates the kernels use;
+//  3. pairs of each class sorted by Qs = sum of primitive bounds (descending),
+//     so that for a bra the kets passing Qs_bra*Qs_ket >= thr form a prefix.
+//     Qs >= max primitive bound, so this contracted pre-test never drops a
+//     primitive quartet the reference keeps; the exact primitive test runs
+//     inside the kernel;
+//  4. the Boys table (F_n(k/32), n < 32) generated from the series definition.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <numeric>
+
+#include "engine.hpp"
+#include "md_math.cuh"
+
+namespace gb {
+
+// sqrt(2 pi^{5/2}) folded into every primitive-pair prefactor K
+static const double kKFold = std::sqrt(2.0 * std::pow(kPi, 2.5));
+
+void host_boys_table(std::vector<double>& table)
+{
+    table.assign(static_cast<size_t>(kBoysOrders) * kBoysPoints, 0.0);
+    const int nmax = kBoysOrders - 1;
+    for (int k = 0; k < kBoysPoints; ++k) {
+        const long double x = k * static_cast<long double>(kBoysStep);
+        if (k == 0) {
+            for (int n = 0; n <= nmax; ++n) table[static_cast<size_t>(n) * kBoysPoints] = 1.0 / (2 * n + 1);
+            continue;
+        }
+        const long double ex = expl(-x);
+        long double term = 1.0L / (2 * nmax + 1), sum = term;
+        for (int j = 1; j < 4000; ++j) {
+            term *= 2.0L * x / (2 * nmax + 2 * j + 1);
+            sum += term;
+            if (term < 1e-24L * sum) break;
+        }
+        long double f = ex * sum;
+        table[static_cast<size_t>(nmax) * kBoysPoints + k] = static_cast<double>(f);
+        for (int n = nmax; n > 0; --n) {
+            f = (2.0L * x * f + ex) / (2 * n - 1);
+            table[static_cast<size_t>(n - 1) * kBoysPoints + k] = static_cast<double>(f);
+        }
+    }
+}
+
+namespace {
+
+// Diagonal (ij|ij)' of one primitive pair for all component pairs, times the
+// reference's component factors; returns sqrt(max).
+template <int LA, int LB>
+double prim_pair_bound_t(const PrimPair64& pp, double abx, double aby, double abz, const double* boys)
+{
+    constexpr int NA = ncart(LA), NB = ncart(LB), L = 2 * (LA + LB), LAB = LA + LB;
+    HermiteE<double, LA, LB> Ex, Ey, Ez;
+    const double oo2p = 0.5 / pp.p;
+    Ex.build(pp.PAx, pp.PAx + abx, oo2p);
+    Ey.build(pp.PAy, pp.PAy + aby, oo2p);
+    Ez.build(pp.PAz, pp.PAz + abz, oo2p);
+    double Fs[L + 1];
+    boys_fp64<L>(0.0, boys, Fs);
+    double scale = pp.K * pp.K / (pp.p * pp.p * std::sqrt(2.0 * pp.p));
+    const double m2rho = -pp.p;  // rho = p*p/(2p) = p/2, -2 rho = -p
+    for (int n = 0; n <= L; ++n) { Fs[n] *= scale; scale *= m2rho; }
+    HermiteR<double, L> R;
+    R.build(Fs, 0.0, 0.0, 0.0);
+    double mx = 0.0;
+    for (int ia = 0; ia < NA; ++ia)
+        for (int ib = 0; ib < NB; ++ib) {
+            const int ax = cart_exp(LA, ia, 0), ay = cart_exp(LA, ia, 1), az = cart_exp(LA, ia, 2);
+            const int bx = cart_exp(LB, ib, 0), by = cart_exp(LB, ib, 1), bz = cart_exp(LB, ib, 2);
+            double s = 0.0;
+            for (int t = 0; t <= ax + bx; ++t)
+                for (int u = 0; u <= ay + by; ++u)
+                    for (int v = 0; v <= az + bz; ++v) {
+                        const double e1 = Ex.e[ax][bx][t] * Ey.e[ay][by][u] * Ez.e[az][bz][v];
+                        for (int tau = 0; tau <= ax + bx; ++tau)
+                            for (int nu = 0; nu <= ay + by; ++nu)
+                                for (int phi = 0; phi <= az + bz; ++phi) {
+                                    const double e2 = Ex.e[ax][bx][tau] * Ey.e[ay][by][nu] * Ez.e[az][bz][phi];
+                                    const double sg = ((tau + nu + phi) & 1) ? -1.0 : 1.0;
+                                    s += e1 * sg * e2 * R.r[t + tau][u + nu][v + phi];
+                                }
+                    }
+            (void)LAB;
+            const double cf = component_factor(LA, ia) * component_factor(LB, ib);
+            mx = std::max(mx, std::fabs(s) * cf * cf);
+        }
+    return std::sqrt(mx);
+}
+
+double prim_pair_bound(int la, int lb, const PrimPair64& pp, double abx, double aby, double abz, const double* boys)
+{
+    switch (la * 3 + lb) {
+    case 0: return prim_pair_bound_t<0, 0>(pp, abx, aby, abz, boys);
+    case 3: return prim_pair_bound_t<1, 0>(pp, abx, aby, abz, boys);
+    case 4: return prim_pair_bound_t<1, 1>(pp, abx, aby, abz, boys);
+    case 6: return prim_pair_bound_t<2, 0>(pp, abx, aby, abz, boys);
+    case 7: return prim_pair_bound_t<2, 1>(pp, abx, aby, abz, boys);
+    case 8: return prim_pair_bound_t<2, 2>(pp, abx, aby, abz, boys);
+    default: return 0.0;
+    }
+}
+
+// Primitive coefficient times the component-independent part of the
+// reference's primitive norm: 2^L (2/pi)^{3/4} a^{(2L+3)/4}.
+double scaled_coef(double c, double a, int L)
+{
+    return c * std::pow(2.0, L) * std::pow(2.0 / kPi, 0.75) * std::pow(a, (2.0 * L + 3.0) / 4.0);
+}
+
+PrimPair64 make_prim_pair(double a, double ca, const double* A, double b, double cb, const double* B)
+{
+    PrimPair64 r;
+    const double p = a + b;
+    const double ab2 = (A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) + (A[2] - B[2]) * (A[2] - B[2]);
+    r.p = p;
+    r.K = ca * cb * std::exp(-a * b / p * ab2) * kKFold;
+    r.Q = 0.0;
+    r.Px = (a * A[0] + b * B[0]) / p;
+    r.Py = (a * A[1] + b * B[1]) / p;
+    r.Pz = (a * A[2] + b * B[2]) / p;
+    // P - A = b/p (B - A), formed from the difference to avoid cancellation
+    r.PAx = b / p * (B[0] - A[0]);
+    r.PAy = b / p * (B[1] - A[1]);
+    r.PAz = b / p * (B[2] - A[2]);
+    r.pad = b;
+    return r;
+}
+
+template <class T>
+T* dev_upload(const std::vector<T>& v, int& status)
+{
+    T* d = nullptr;
+    const size_t n = std::max<size_t>(v.size(), 1);
+    cudaError_t e = cudaMalloc(&d, n * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        status = (e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;
+        return nullptr;
+    }
+    if (!v.empty()) {
+        e = cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            set_error(std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+            status = HF_ERR_CUDA;
+        }
+    }
+    return d;
+}
+
+template <class T>
+int dev_alloc(T*& p, size_t n)
+{
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return (e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;
+    }
+    return HF_OK;
+}
+
+}  // namespace
+
+Engine::~Engine()
+{
+    void* ptrs[] = {d_pairs,  d_pp64,   d_pp32,       d_boys64,     d_boys32,     d_scale,   d_atoms,
+                    d_entry_bra, d_entry_cnt, d_entry_zero, d_pair_qs, d_off_static, d_cp_meta, plan.off64, plan.off32,
+                    plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
+                    scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
+                    scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (cublas) cublasDestroy(cublas);
+    if (cusolver) cusolverDnDestroy(cusolver);
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const double* cgto_norm, int num_basis,
+                     const hf_atom* atoms, int num_atoms, double schwarz_threshold, hf_engine** out)
+{
+    clear_error();
+    if (!prims || !cgto_norm || !atoms || !out || num_primitives <= 0 || num_basis <= 0 || num_atoms <= 0)
+        return set_error("hf_engine_create: null pointer or empty input"), HF_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    for (int i = 0; i < num_primitives; ++i) {
+        const auto& p = prims[i];
+        if (p.shell_type < 0 || p.shell_type > kMaxL)
+            return set_error("hf_engine_create: shell type " + std::to_string(p.shell_type) +
+                             " not supported (s, p, d shells)"),
+                   HF_ERR_INVALID_ARGUMENT;
+        if (p.basis_index + ncart(p.shell_type) > static_cast<size_t>(num_basis) || !(p.exponent > 0.0))
+            return set_error("hf_engine_create: primitive " + std::to_string(i) + " out of range"),
+                   HF_ERR_INVALID_ARGUMENT;
+        if (i > 0 && prims[i - 1].shell_type > p.shell_type)
+            return set_error("hf_engine_create: primitives must be sorted by shell type"), HF_ERR_INVALID_ARGUMENT;
+    }
+    auto e = std::make_unique<Engine>();
+    e->num_basis = num_basis;
+    e->num_atoms = num_atoms;
+    e->num_prims = num_primitives;
+    e->schwarz_threshold = schwarz_threshold;
+    e->prims.assign(prims, prims + num_primitives);
+    e->cgto.assign(cgto_norm, cgto_norm + num_basis);
+    e->atoms.assign(atoms, atoms + num_atoms);
+    e->cgto_max = *std::max_element(e->cgto.begin(), e->cgto.end());
+
+    // ---- contracted shells: group by (shell_type, basis_index)
+    std::map<std::pair<int, size_t>, std::vector<int>> groups;
+    for (int i = 0; i < num_primitives; ++i) groups[{prims[i].shell_type, prims[i].basis_index}].push_back(i);
+    std::vector<double> sh_alpha, sh_coef;  // scaled coefficient per shell primitive
+    for (auto& kv : groups) {
+        Shell s;
+        s.l = kv.first.first;
+        s.bf = static_cast<int>(kv.first.second);
+        s.nprim = static_cast<int>(kv.second.size());
+        s.prim_off = static_cast<int>(sh_alpha.size());
+        const auto& p0 = prims[kv.second[0]];
+        s.x = p0.x; s.y = p0.y; s.z = p0.z;
+        s.atom = p0.atom_index;
+        for (int idx : kv.second) {
+            sh_alpha.push_back(prims[idx].exponent);
+            sh_coef.push_back(scaled_coef(prims[idx].coefficient, prims[idx].exponent, s.l));
+        }
+        e->shells.push_back(s);
+    }
+    e->num_shells = static_cast<int>(e->shells.size());
+    e->scale.assign(num_basis, 0.0);
+    for (const Shell& s : e->shells)
+        for (int i = 0; i < ncart(s.l); ++i) e->scale[s.bf + i] = e->cgto[s.bf + i] * component_factor(s.l, i);
+
+    std::vector<double> boys;
+    host_boys_table(boys);
+
+    // ---- shell pairs per class
+    for (int la = 0; la <= kMaxL; ++la)
+        for (int lb = 0; lb <= la; ++lb) {
+            PairClass pc{la, lb, static_cast<int>(e->pairs.size()), 0};
+            struct Tmp {
+                ShellPairDev sp;
+                std::vector<PrimPair64> pp;
+            };
+            std::vector<Tmp> tmp;
+            for (int A = 0; A < e->num_shells; ++A) {
+                if (e->shells[A].l != la) continue;
+                for (int B = 0; B < e->num_shells; ++B) {
+                    if (e->shells[B].l != lb) continue;
+                    if (la == lb && B > A) continue;
+                    const Shell& sa = e->shells[A];
+                    const Shell& sb = e->shells[B];
+                    const double Ac[3] = {sa.x, sa.y, sa.z}, Bc[3] = {sb.x, sb.y, sb.z};
+                    Tmp t;
+                    t.sp = ShellPairDev{};
+                    t.sp.A = A; t.sp.B = B; t.sp.bfA = sa.bf; t.sp.bfB = sb.bf;
+                    t.sp.la = la; t.sp.lb = lb;
+                    t.sp.ABx = Ac[0] - Bc[0]; t.sp.ABy = Ac[1] - Bc[1]; t.sp.ABz = Ac[2] - Bc[2];
+                    double qs = 0.0, qm = 0.0;
+                    for (int i = 0; i < sa.nprim; ++i)
+                        for (int j = 0; j < sb.nprim; ++j) {
+                            PrimPair64 pp = make_prim_pair(sh_alpha[sa.prim_off + i], sh_coef[sa.prim_off + i], Ac,
+                                                           sh_alpha[sb.prim_off + j], sh_coef[sb.prim_off + j], Bc);
+                            pp.Q = prim_pair_bound(la, lb, pp, t.sp.ABx, t.sp.ABy, t.sp.ABz, boys.data());
+                            qs += pp.Q;
+                            qm = std::max(qm, pp.Q);
+                            t.pp.push_back(pp);
+                        }
+                    t.sp.Qs = qs;
+                    t.sp.Qmax = qm;
+                    tmp.push_back(std::move(t));
+                }
+            }
+            std::stable_sort(tmp.begin(), tmp.end(), [](const Tmp& a, const Tmp& b) { return a.sp.Qs > b.sp.Qs; });
+            for (auto& t : tmp) {
+                t.sp.pp_off = static_cast<int>(e->pp64.size());
+                t.sp.pp_n = static_cast<int>(t.pp.size());
+                e->pp64.insert(e->pp64.end(), t.pp.begin(), t.pp.end());
+                e->pairs.push_back(t.sp);
+            }
+            pc.count = static_cast<int>(tmp.size());
+            e->pair_classes.push_back(pc);
+        }
+
+    // ---- class pairs and bra entries (contracted pre-screen on Qs)
+    const double thr = schwarz_threshold;
+    for (int X = 0; X < static_cast<int>(e->pair_classes.size()); ++X)
+        for (int Y = 0; Y <= X; ++Y) {
+            const PairClass& px = e->pair_classes[X];
+            const PairClass& py = e->pair_classes[Y];
+            ClassPair cp{X, Y, static_cast<int>(e->entry_bra.size()), 0, 0};
+            e->off_static.push_back(0);
+            long long acc = 0;
+            for (int i = 0; i < px.count; ++i) {
+                const double qi = e->pairs[px.begin + i].Qs;
+                // kets sorted by Qs descending: count those with qi*qj >= thr
+                int lo = 0, hi = py.count;
+                while (lo < hi) {
+                    const int mid = (lo + hi) / 2;
+                    if (qi * e->pairs[py.begin + mid].Qs >= thr) lo = mid + 1; else hi = mid;
+                }
+                int cnt = lo;
+                if (X == Y) cnt = std::min(cnt, i + 1);
+                if (cnt <= 0) continue;
+                e->entry_bra.push_back(px.begin + i);
+                e->entry_cnt.push_back(cnt);
+                acc += cnt;
+                e->off_static.push_back(acc);
+            }
+            cp.nentry = static_cast<int>(e->entry_bra.size()) - cp.entry_begin;
+            cp.n_survivors = acc;
+            e->total_survivors += acc;
+            e->class_pairs.push_back(cp);
+        }
+
+    // ---- device upload
+    int st = HF_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaFree(nullptr) != cudaSuccess)
+        return set_error("hf_engine_create: no usable CUDA device"), HF_ERR_CUDA;
+    cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    std::vector<PrimPair32> pp32(e->pp64.size());
+    for (size_t i = 0; i < pp32.size(); ++i) {
+        const PrimPair64& a = e->pp64[i];
+        pp32[i] = PrimPair32{static_cast<float>(a.p),   static_cast<float>(a.K),   static_cast<float>(a.Q),
+                             static_cast<float>(a.Px),  static_cast<float>(a.Py),  static_cast<float>(a.Pz),
+                             static_cast<float>(a.PAx), static_cast<float>(a.PAy), static_cast<float>(a.PAz),
+                             static_cast<float>(a.pad)};
+    }
+    std::vector<float> boys32(boys.begin(), boys.end());
+    std::vector<double> atom4(4 * num_atoms);
+    for (int i = 0; i < num_atoms; ++i) {
+        atom4[4 * i] = atoms[i].x; atom4[4 * i + 1] = atoms[i].y; atom4[4 * i + 2] = atoms[i].z;
+        atom4[4 * i + 3] = atoms[i].atomic_number;
+    }
+    std::vector<double> qs(e->pairs.size());
+    for (size_t i = 0; i < qs.size(); ++i) qs[i] = e->pairs[i].Qs;
+    std::vector<int> zeros(e->entry_bra.size(), 0);
+    e->d_pairs = dev_upload(e->pairs, st);
+    e->d_pp64 = dev_upload(e->pp64, st);
+    e->d_pp32 = dev_upload(pp32, st);
+    e->d_boys64 = dev_upload(boys, st);
+    e->d_boys32 = dev_upload(boys32, st);
+    e->d_scale = dev_upload(e->scale, st);
+    e->d_atoms = dev_upload(atom4, st);
+    e->d_entry_bra = dev_upload(e->entry_bra, st);
+    e->d_entry_cnt = dev_upload(e->entry_cnt, st);
+    e->d_entry_zero = dev_upload(zeros, st);
+    e->d_pair_qs = dev_upload(qs, st);
+    e->d_off_static = dev_upload(e->off_static, st);
+    {
+        const int ncp = static_cast<int>(e->class_pairs.size());
+        std::vector<int> meta(4 * ncp);
+        for (int k = 0; k < ncp; ++k) {
+            meta[k] = e->class_pairs[k].entry_begin;
+            meta[ncp + k] = e->class_pairs[k].nentry;
+            meta[2 * ncp + k] = e->pair_classes[e->class_pairs[k].Y].begin;
+            meta[3 * ncp + k] = e->class_pairs[k].entry_begin + k;
+        }
+        e->d_cp_meta = dev_upload(meta, st);
+    }
+    if (st != HF_OK) return st;
+    const size_t nn = static_cast<size_t>(num_basis) * num_basis;
+    const size_t noff = e->off_static.size();
+    if ((st = dev_alloc(e->plan.off64, noff)) || (st = dev_alloc(e->plan.off32, noff)) ||
+        (st = dev_alloc(e->plan.lo32, e->entry_bra.size())) || (st = dev_alloc(e->d_Dp64, nn)) ||
+        (st = dev_alloc(e->d_Dp32, nn)) || (st = dev_alloc(e->d_Jp, nn)) || (st = dev_alloc(e->d_Kp, nn)) ||
+        (st = dev_alloc(e->d_scalar, 16)) || (st = dev_alloc(e->d_counters, 4)))
+        return st;
+    if (cudaMemset(e->d_counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess)
+        return set_error("cudaMemset failed"), HF_ERR_CUDA;
+    if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) return set_error("cublasCreate failed"), HF_ERR_CUDA;
+    if (cusolverDnCreate(&e->cusolver) != CUSOLVER_STATUS_SUCCESS)
+        return set_error("cusolverDnCreate failed"), HF_ERR_CUDA;
+    *out = reinterpret_cast<hf_engine*>(e.release());
+    return HF_OK;
+}
+
+void hf_engine_destroy(hf_engine* eng) { delete reinterpret_cast<Engine*>(eng); }
+
+int hf_engine_stats(const hf_engine* eng, int* num_shells, long long* num_shell_pairs, long long* num_quartets)
+{
+    if (!eng) return set_error("null engine"), HF_ERR_INVALID_ARGUMENT;
+    const Engine* e = reinterpret_cast<const Engine*>(eng);
+    if (num_shells) *num_shells = e->num_shells;
+    if (num_shell_pairs) *num_shell_pairs = static_cast<long long>(e->pairs.size());
+    if (num_quartets) *num_quartets = e->total_survivors;
+    return HF_OK;
+}
+
+int hf_primitive_pair_bounds(hf_engine* eng, double* h_out)
+{
+    clear_error();
+    if (!eng || !h_out) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine* e = reinterpret_cast<Engine*>(eng);
+    std::vector<double> boys;
+    host_boys_table(boys);
+    const int n = e->num_prims;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const auto& a = e->prims[i];
+            const auto& b = e->prims[j];
+            // bound is symmetric in (a, b): evaluate with the higher l first
+            const auto& P = (a.shell_type >= b.shell_type) ? a : b;
+            const auto& Q = (a.shell_type >= b.shell_type) ? b : a;
+            const double Ac[3] = {P.x, P.y, P.z}, Bc[3] = {Q.x, Q.y, Q.z};
+            PrimPair64 pp = make_prim_pair(P.exponent, scaled_coef(P.coefficient, P.exponent, P.shell_type), Ac,
+                                           Q.exponent, scaled_coef(Q.coefficient, Q.exponent, Q.shell_type), Bc);
+            h_out[static_cast<size_t>(i) * n + j] = prim_pair_bound(P.shell_type, Q.shell_type, pp, Ac[0] - Bc[0],
+                                                                    Ac[1] - Bc[1], Ac[2] - Bc[2], boys.data());
+        }
+    return HF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Engine: everything the hot path needs, resident on the device.
+#pragma once
+#include <cuda_runtime.h>
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <array>
+#include <vector>
+
+#include "engine_types.hpp"
+#include "internal.hpp"
+#include "md_math.cuh"
+
+namespace gb {
+
+constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
+
+struct Shell {
+    int l, nprim, prim_off, bf, atom;
+    double x, y, z;
+};
+
+// (la, lb) pair classes with la >= lb, ordered (0,0),(1,0),(1,1),(2,0),(2,1),(2,2)
+struct PairClass {
+    int la, lb;
+    int begin, count;  // global pair index range
+};
+
+// bra class X >= ket class Y
+struct ClassPair {
+    int X, Y;
+    int entry_begin, nentry;  // bra entries (global entry index range)
+    long long n_survivors;    // contracted quartets passing the contracted bound test
+};
+
+// Device buffers of one mixed-precision plan (per Fock build).
+struct MixedPlan {
+    long long* off64 = nullptr;  // per class pair: nentry+1 (packed by entry_begin + class pair index)
+    long long* off32 = nullptr;
+    int* lo32 = nullptr;
+};
+
+struct Engine {
+    int num_basis = 0, num_shells = 0, num_atoms = 0, num_prims = 0;
+    double schwarz_threshold = 1e-12;
+    double cgto_max = 1.0;
+
+    std::vector<hf_primitive_shell> prims;  // as given (sorted by type)
+    std::vector<double> cgto;
+    std::vector<hf_atom> atoms;
+    std::vector<Shell> shells;
+    std::vector<double> scale;              // s_i = cgto_i * component factor
+    std::vector<ShellPairDev> pairs;        // host copy
+    std::vector<PrimPair64> pp64;
+    std::vector<PairClass> pair_classes;
+    std::vector<ClassPair> class_pairs;
+    std::vector<int> entry_bra, entry_cnt;  // per bra entry
+    std::vector<long long> off_static;      // per class pair, nentry+1 (packed: entry_begin + cp)
+    long long total_survivors = 0;
+    std::vector<double> prim_bound;         // per primitive of the input list pair (dense), filled lazily
+
+    // device
+    ShellPairDev* d_pairs = nullptr;
+    PrimPair64* d_pp64 = nullptr;
+    PrimPair32* d_pp32 = nullptr;
+    double* d_boys64 = nullptr;
+    float* d_boys32 = nullptr;
+    double* d_scale = nullptr;
+    double* d_atoms = nullptr;  // natom x 4: x, y, z, Z
+    int* d_entry_bra = nullptr;
+    int* d_entry_cnt = nullptr;
+    int* d_entry_zero = nullptr;
+    double* d_pair_qs = nullptr;  // Qs per global pair (for the mixed plan)
+    long long* d_off_static = nullptr;
+    int* d_cp_meta = nullptr;     // per class pair: entry_begin | nentry | ket_base | off_base
+    MixedPlan plan;
+    double* d_Dp64 = nullptr;
+    float* d_Dp32 = nullptr;
+    double* d_Jp = nullptr;
+    double* d_Kp = nullptr;
+    double* d_scalar = nullptr;  // small scratch scalars (8 doubles)
+    unsigned long long* d_counters = nullptr;  // [0] prim quartets FP64, [1] FP32
+
+    cublasHandle_t cublas = nullptr;
+    cusolverDnHandle_t cusolver = nullptr;
+    int num_sms = 152;
+
+    // SCF workspaces (allocated on first SCF call, reused)
+    struct Scf {
+        int n = 0, m = 0;
+        double *S = nullptr, *H = nullptr, *X = nullptr, *F = nullptr, *D = nullptr, *Dprev = nullptr,
+               *G = nullptr, *dD = nullptr, *C = nullptr, *W = nullptr, *eps = nullptr, *T1 = nullptr,
+               *T2 = nullptr, *E = nullptr, *Es = nullptr, *Fs = nullptr, *work = nullptr, *diis = nullptr,
+               *J = nullptr, *K = nullptr;
+        int* info = nullptr;
+        int lwork = 0;
+    } scf;
+
+    ~Engine();
+};
+
+// entry point tables implemented by the per-class objects
+using FockLauncher = void (*)(bool fp32, const FockClassLaunch&, int grid, cudaStream_t);
+using EriLauncher = void (*)(const FockClassLaunch&, const double* scale, double* eri, int grid, cudaStream_t);
+FockLauncher fock_launcher(int la, int lb, int lc, int ld);
+EriLauncher eri_launcher(int la, int lb, int lc, int ld);
+
+// fock.cu
+int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
+             cudaStream_t s, bool accumulate_counters = true);
+int finish_fock(Engine& e, const double* d_H, const double* d_J, const double* d_K, double* d_F, cudaStream_t s);
+int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s);
+
+// one_electron.cu
+int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s);
+
+// host MD helpers (engine.cu)
+void host_boys_table(std::vector<double>& table);
+
+}  // namespace gb

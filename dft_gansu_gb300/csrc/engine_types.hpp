@@ -1,0 +1,63 @@
+// Device-side data layout of the engine (HBM-resident for the engine's life).
+//
+//   contracted shell pairs   ShellPairDev[npairs]    grouped by pair class, each
+//                            class sorted by the contracted bound Qs descending
+//   primitive pairs          PrimPair64[] + PrimPair32[] (same order), per shell
+//                            pair a contiguous run [pp_off, pp_off + pp_n)
+//   quartet work entries     per class pair: entry_bra[], entry_lo[], off[]
+//                            (exclusive prefix over the per-bra ket counts)
+//   Boys table               double[32][1281] and float copy, x = k/32
+//   J', K' accumulators      double N x N each; D' = s D s in double and float
+#pragma once
+#include <cstdint>
+
+namespace gb {
+
+// One contracted shell pair (A,B), l_A >= l_B (A >= B when l_A == l_B).
+struct ShellPairDev {
+    int A, B;          // contracted shell indices
+    int bfA, bfB;      // first basis function of each shell
+    int pp_off, pp_n;  // primitive-pair run
+    int la, lb;
+    double ABx, ABy, ABz;  // A - B
+    double Qmax;           // max primitive-pair Schwarz bound (reference definition)
+    double Qs;             // sum of primitive-pair bounds (bounds the contracted integral)
+    double pad;
+};
+static_assert(sizeof(ShellPairDev) == 80, "ShellPairDev layout");
+
+// One primitive pair of a shell pair.  K carries the contraction coefficients,
+// the component-independent part of the primitive norms, exp(-ab/p |AB|^2)
+// and sqrt(2 pi^{5/2}) so that a primitive quartet prefactor is
+// K_ab K_cd / (p q sqrt(p+q)).
+struct PrimPair64 {
+    double p, K, Q;
+    double Px, Py, Pz;
+    double PAx, PAy, PAz;
+    double pad;
+};
+struct PrimPair32 {
+    float p, K, Q;
+    float Px, Py, Pz;
+    float PAx, PAy, PAz;
+    float pad;
+};
+
+struct FockClassLaunch {
+    const ShellPairDev* pairs;     // all shell pairs (global indices)
+    const void* prim_pairs;        // PrimPair64* or PrimPair32*
+    const void* boys_table;        // double* or float*
+    const void* density;           // D' (double* or float*), N x N
+    double* J;                     // J' accumulator
+    double* K;                     // K' accumulator
+    const long long* off;          // nentry+1 prefix offsets
+    const int* entry_bra;          // global bra pair index per entry
+    const int* entry_lo;           // first ket (class-relative) per entry
+    int nentry;
+    int ket_base;                  // global index of the ket class's first pair
+    int num_basis;
+    double schwarz_threshold;
+    unsigned long long* prim_quartet_counter;
+};
+
+}  // namespace gb

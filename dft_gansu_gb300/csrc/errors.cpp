@@ -1,0 +1,18 @@
+// Thread-local error message behind hf_last_error(); C++ exceptions never
+// cross the C ABI (the reference throws, include/utils.hpp:91).
+#include <string>
+
+#include "internal.hpp"
+
+namespace gb {
+namespace {
+thread_local std::string g_last_error;
+}
+void set_error(const std::string& msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+}  // namespace gb
+
+extern "C" {
+const char* hf_last_error(void) { return gb::g_last_error.c_str(); }
+const char* hf_version(void) { return "gansu_gb300 0.1.0 (sm_103a)"; }
+}

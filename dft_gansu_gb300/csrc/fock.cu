@@ -1,0 +1,387 @@
+// Fock-build orchestration: density scaling, the mixed-precision plan, the
+// per-class launches and the symmetrising finish.
+//
+//   D' = s D s                      (s_i = cgto_i * component factor)
+//   J', K' accumulated by the class kernels (fock_kernel.cuh)
+//   J = s (2 (J' + J'^T)) s,  K = s (K' + K'^T) s,  F = H + J - K/2
+//                                   (src/gpu_kernels.cu:230-287 semantics)
+//
+// Mixed precision: a quartet goes to the FP32 queue when
+// Qs_bra * Qs_ket * c_max^4 * max|D| < mixed_threshold, i.e. when the bound on
+// its Fock contribution is below the threshold (c_max = largest CGTO factor,
+// Qs = sum of primitive-pair Schwarz bounds).  Kets of a bra are sorted by Qs,
+// so each bra's FP64 kets are a prefix of its surviving kets; the plan kernel
+// finds that prefix by bisection and prefix-sums both queues on the device,
+// so no host round trip is needed between the density and the launches.
+#include <algorithm>
+
+#include "engine.hpp"
+#include "fock_kernel.cuh"
+
+namespace gb {
+
+// ------------------------------------------------------------------ tables
+#define GB_DECL(a, b, c, d)                                                                                   \
+    void launch_fock_##a##_##b##_##c##_##d(bool, const FockClassLaunch&, int, cudaStream_t);                 \
+    void launch_eri_##a##_##b##_##c##_##d(const FockClassLaunch&, const double*, double*, int, cudaStream_t);
+#define GB_CLASSES(X)                                                                                         \
+    X(0, 0, 0, 0) X(1, 0, 0, 0) X(1, 0, 1, 0) X(1, 1, 0, 0) X(1, 1, 1, 0) X(1, 1, 1, 1) X(2, 0, 0, 0)         \
+    X(2, 0, 1, 0) X(2, 0, 1, 1) X(2, 0, 2, 0) X(2, 1, 0, 0) X(2, 1, 1, 0) X(2, 1, 1, 1) X(2, 1, 2, 0)         \
+    X(2, 1, 2, 1) X(2, 2, 0, 0) X(2, 2, 1, 0) X(2, 2, 1, 1) X(2, 2, 2, 0) X(2, 2, 2, 1) X(2, 2, 2, 2)
+GB_CLASSES(GB_DECL)
+#undef GB_DECL
+
+FockLauncher fock_launcher(int la, int lb, int lc, int ld)
+{
+#define GB_CASE(a, b, c, d)                                                 \
+    if (la == a && lb == b && lc == c && ld == d) return &launch_fock_##a##_##b##_##c##_##d;
+    GB_CLASSES(GB_CASE)
+#undef GB_CASE
+    return nullptr;
+}
+
+EriLauncher eri_launcher(int la, int lb, int lc, int ld)
+{
+#define GB_CASE(a, b, c, d)                                                 \
+    if (la == a && lb == b && lc == c && ld == d) return &launch_eri_##a##_##b##_##c##_##d;
+    GB_CLASSES(GB_CASE)
+#undef GB_CASE
+    return nullptr;
+}
+
+namespace {
+
+constexpr int kPlanThreads = 256;
+
+__global__ void scale_density_kernel(const double* __restrict__ D, const double* __restrict__ s, int n,
+                                     double* __restrict__ Dp64, float* __restrict__ Dp32)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int i = static_cast<int>(k / n), j = static_cast<int>(k % n);
+        const double v = s[i] * D[k] * s[j];
+        Dp64[k] = v;
+        if (Dp32) Dp32[k] = static_cast<float>(v);
+    }
+}
+
+__global__ void absmax_kernel(const double* __restrict__ A, long long n, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    double m = 0.0;
+    for (long long k = threadIdx.x; k < n; k += blockDim.x) m = fmax(m, fabs(A[k]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) *out = m;
+    }
+}
+
+// Exclusive-scan helper over one block (values of this pass), returns the
+// pass total; the running base is kept by the caller.
+__device__ long long block_scan_exclusive(long long v, long long* smem, long long& total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    long long x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) smem[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        long long w = (lane < (blockDim.x >> 5)) ? smem[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        smem[lane] = w;  // inclusive warp totals
+    }
+    __syncthreads();
+    const long long warp_base = (wid > 0) ? smem[wid - 1] : 0;
+    total = smem[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_base + x - v;
+}
+
+struct PlanArgs {
+    const int* entry_bra;
+    const int* entry_cnt;
+    const double* pair_qs;
+    const int* cp_entry_begin;  // per class pair
+    const int* cp_nentry;
+    const int* cp_ket_base;
+    const int* cp_off_base;     // start of the class pair's offsets
+    const double* dmax;
+    double factor;              // c_max^4
+    double mixed_threshold;
+    long long* off64;
+    long long* off32;
+    int* lo32;
+};
+
+// One block per class pair.
+__global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
+{
+    __shared__ long long smem[32];
+    const int cp = blockIdx.x;
+    const int eb = a.cp_entry_begin[cp], ne = a.cp_nentry[cp], kb = a.cp_ket_base[cp], ob = a.cp_off_base[cp];
+    const double dm = *a.dmax * a.factor;
+    long long base64 = 0, base32 = 0;
+    if (threadIdx.x == 0) { a.off64[ob] = 0; a.off32[ob] = 0; }
+    for (int start = 0; start < ne; start += blockDim.x) {
+        const int i = start + threadIdx.x;
+        long long c64 = 0, c32 = 0;
+        if (i < ne) {
+            const int e = eb + i;
+            const int cnt = a.entry_cnt[e];
+            const double qb = a.pair_qs[a.entry_bra[e]] * dm;
+            int lo = 0, hi = cnt;  // first ket with qb*Qs_ket < thr
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (qb * a.pair_qs[kb + mid] >= a.mixed_threshold) lo = mid + 1; else hi = mid;
+            }
+            c64 = lo;
+            c32 = cnt - lo;
+            a.lo32[e] = lo;
+        }
+        long long t64, t32;
+        const long long x64 = block_scan_exclusive(c64, smem, t64);
+        const long long x32 = block_scan_exclusive(c32, smem, t32);
+        if (i < ne) {
+            a.off64[ob + i + 1] = base64 + x64 + c64;
+            a.off32[ob + i + 1] = base32 + x32 + c32;
+        }
+        base64 += t64;
+        base32 += t32;
+    }
+}
+
+__global__ void finish_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
+                              const double* __restrict__ s, const double* __restrict__ H, int n,
+                              double* __restrict__ J, double* __restrict__ K, double* __restrict__ F)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int i = static_cast<int>(k / n), j = static_cast<int>(k % n);
+        const long long kt = static_cast<long long>(j) * n + i;
+        const double ss = s[i] * s[j];
+        const double jv = 2.0 * (Jp[k] + Jp[kt]) * ss;
+        const double kv = (Kp[k] + Kp[kt]) * ss;
+        if (J) J[k] = jv;
+        if (K) K[k] = kv;
+        if (F) F[k] = H[k] + jv - 0.5 * kv;
+    }
+}
+
+int grid_for(long long work, int num_sms)
+{
+    const long long blocks = (work + kFockThreads - 1) / kFockThreads;
+    return static_cast<int>(std::max<long long>(1, std::min<long long>(blocks, static_cast<long long>(num_sms) * 16)));
+}
+
+FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off, const int* lo)
+{
+    const ClassPair& cp = e.class_pairs[cpi];
+    FockClassLaunch L;
+    L.pairs = e.d_pairs;
+    L.prim_pairs = fp32 ? static_cast<const void*>(e.d_pp32) : static_cast<const void*>(e.d_pp64);
+    L.boys_table = fp32 ? static_cast<const void*>(e.d_boys32) : static_cast<const void*>(e.d_boys64);
+    L.density = fp32 ? static_cast<const void*>(e.d_Dp32) : static_cast<const void*>(e.d_Dp64);
+    L.J = e.d_Jp;
+    L.K = e.d_Kp;
+    L.off = off + cp.entry_begin + cpi;
+    L.entry_bra = e.d_entry_bra + cp.entry_begin;
+    L.entry_lo = lo + cp.entry_begin;
+    L.nentry = cp.nentry;
+    L.ket_base = e.pair_classes[cp.Y].begin;
+    L.num_basis = e.num_basis;
+    L.schwarz_threshold = e.schwarz_threshold;
+    L.prim_quartet_counter = e.d_counters + (fp32 ? 1 : 0);
+    return L;
+}
+
+}  // namespace
+
+int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s)
+{
+    const long long nn = static_cast<long long>(e.num_basis) * e.num_basis;
+    const int grid = static_cast<int>(std::min<long long>((nn + 255) / 256, 4096));
+    scale_density_kernel<<<grid, 256, 0, s>>>(d_D, e.d_scale, e.num_basis, e.d_Dp64, want_fp32 ? e.d_Dp32 : nullptr);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
+             cudaStream_t s, bool /*accumulate_counters*/)
+{
+    const size_t nn = static_cast<size_t>(e.num_basis) * e.num_basis;
+    const bool mixed = (precision == HF_PRECISION_MIXED);
+    int st = scale_density(e, d_D, mixed, s);
+    if (st) return st;
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_Jp, 0, nn * sizeof(double), s));
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_Kp, 0, nn * sizeof(double), s));
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    if (!mixed) {
+        for (int c = 0; c < ncp; ++c) {
+            const ClassPair& cp = e.class_pairs[c];
+            if (cp.n_survivors == 0) continue;
+            const PairClass& X = e.pair_classes[cp.X];
+            const PairClass& Y = e.pair_classes[cp.Y];
+            FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
+            if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
+            f(false, make_launch(e, c, false, e.d_off_static, e.d_entry_zero), grid_for(cp.n_survivors, e.num_sms), s);
+            GB_LAUNCH_CHECK();
+        }
+    } else {
+        absmax_kernel<<<1, 1024, 0, s>>>(d_D, static_cast<long long>(nn), e.d_scalar);
+        GB_LAUNCH_CHECK();
+        PlanArgs a;
+        a.entry_bra = e.d_entry_bra;
+        a.entry_cnt = e.d_entry_cnt;
+        a.pair_qs = e.d_pair_qs;
+        a.cp_entry_begin = e.d_cp_meta;
+        a.cp_nentry = e.d_cp_meta + ncp;
+        a.cp_ket_base = e.d_cp_meta + 2 * ncp;
+        a.cp_off_base = e.d_cp_meta + 3 * ncp;
+        a.dmax = e.d_scalar;
+        const double c2 = e.cgto_max * e.cgto_max;
+        a.factor = c2 * c2;
+        a.mixed_threshold = mixed_thr;
+        a.off64 = e.plan.off64;
+        a.off32 = e.plan.off32;
+        a.lo32 = e.plan.lo32;
+        mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
+        GB_LAUNCH_CHECK();
+        for (int c = 0; c < ncp; ++c) {
+            const ClassPair& cp = e.class_pairs[c];
+            if (cp.n_survivors == 0) continue;
+            const PairClass& X = e.pair_classes[cp.X];
+            const PairClass& Y = e.pair_classes[cp.Y];
+            FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
+            if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
+            const int grid = grid_for(cp.n_survivors, e.num_sms);
+            f(false, make_launch(e, c, false, e.plan.off64, e.d_entry_zero), grid, s);
+            GB_LAUNCH_CHECK();
+            f(true, make_launch(e, c, true, e.plan.off32, e.plan.lo32), grid, s);
+            GB_LAUNCH_CHECK();
+        }
+    }
+    if (d_J || d_K) {
+        const int grid = static_cast<int>(std::min<long long>((static_cast<long long>(nn) + 255) / 256, 4096));
+        finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, nullptr, e.num_basis, d_J, d_K, nullptr);
+        GB_LAUNCH_CHECK();
+    }
+    return HF_OK;
+}
+
+int finish_fock(Engine& e, const double* d_H, const double* d_J, const double* d_K, double* d_F, cudaStream_t s)
+{
+    (void)d_J; (void)d_K;
+    const long long nn = static_cast<long long>(e.num_basis) * e.num_basis;
+    const int grid = static_cast<int>(std::min<long long>((nn + 255) / 256, 4096));
+    finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, d_H, e.num_basis, nullptr, nullptr, d_F);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+}  // namespace gb
+
+// ------------------------------------------------------------ stored path
+namespace gb {
+namespace {
+
+// F_ij = H_ij + sum_kl D_kl [(ij|kl) - 1/2 (ik|jl)]  (src/gpu_kernels.cu:230-287);
+// one warp per (i, j), lanes stride over l.
+__global__ void stored_fock_kernel(const double* __restrict__ D, const double* __restrict__ H,
+                                   const double* __restrict__ eri, double* __restrict__ F, int n)
+{
+    const long long warp = (blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long nn = static_cast<long long>(n) * n;
+    if (warp >= nn) return;
+    const long long i = warp / n, j = warp % n;
+    double acc = 0.0;
+    for (long long k = 0; k < n; ++k)
+        for (long long l = lane; l < n; l += 32) {
+            const double d = D[k * n + l];
+            acc += d * (eri[((i * n + j) * n + k) * n + l] - 0.5 * eri[((i * n + k) * n + j) * n + l]);
+        }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) F[warp] = H[warp] + acc;
+}
+
+}  // namespace
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int hf_compute_jk_direct(hf_engine* eng, const double* d_density, double* d_J, double* d_K, int precision,
+                         double mixed_threshold, void* stream)
+{
+    clear_error();
+    if (!eng || !d_density || !d_J || !d_K) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    if (precision != HF_PRECISION_FP64 && precision != HF_PRECISION_MIXED)
+        return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
+    return build_jk(*reinterpret_cast<Engine*>(eng), d_density, d_J, d_K, precision, mixed_threshold,
+                    static_cast<cudaStream_t>(stream));
+}
+
+int hf_compute_fock_direct_rhf(hf_engine* eng, const double* d_density, const double* d_core_hamiltonian,
+                               double* d_fock, int precision, double mixed_threshold, void* stream)
+{
+    clear_error();
+    if (!eng || !d_density || !d_core_hamiltonian || !d_fock) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    if (precision != HF_PRECISION_FP64 && precision != HF_PRECISION_MIXED)
+        return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int st = build_jk(e, d_density, nullptr, nullptr, precision, mixed_threshold, s);
+    if (st) return st;
+    return finish_fock(e, d_core_hamiltonian, nullptr, nullptr, d_fock, s);
+}
+
+int hf_compute_eri_matrix(hf_engine* eng, double* d_eri, void* stream)
+{
+    clear_error();
+    if (!eng || !d_eri) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t n = e.num_basis;
+    GB_CUDA_TRY(cudaMemsetAsync(d_eri, 0, n * n * n * n * sizeof(double), s));
+    for (int c = 0; c < static_cast<int>(e.class_pairs.size()); ++c) {
+        const ClassPair& cp = e.class_pairs[c];
+        if (cp.n_survivors == 0) continue;
+        const PairClass& X = e.pair_classes[cp.X];
+        const PairClass& Y = e.pair_classes[cp.Y];
+        EriLauncher f = eri_launcher(X.la, X.lb, Y.la, Y.lb);
+        if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
+        f(make_launch(e, c, false, e.d_off_static, e.d_entry_zero), e.d_scale, d_eri, grid_for(cp.n_survivors, e.num_sms),
+          s);
+        GB_LAUNCH_CHECK();
+    }
+    return HF_OK;
+}
+
+int hf_compute_fock_stored_rhf(const double* d_density, const double* d_core_hamiltonian, const double* d_eri,
+                               double* d_fock, int num_basis, void* stream)
+{
+    clear_error();
+    if (!d_density || !d_core_hamiltonian || !d_eri || !d_fock || num_basis <= 0)
+        return set_error("null argument or bad size"), HF_ERR_INVALID_ARGUMENT;
+    const long long warps = static_cast<long long>(num_basis) * num_basis;
+    const long long blocks = (warps * 32 + 255) / 256;
+    stored_fock_kernel<<<static_cast<unsigned>(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        d_density, d_core_hamiltonian, d_eri, d_fock, num_basis);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,46 @@
+// Internal host-side types of libgansu_gb300 (never exposed through the C ABI).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "gansu_gb300.h"
+
+namespace gb {
+
+// ------------------------------------------------------------ errors
+void set_error(const std::string& msg);
+void clear_error();
+
+struct Molecule {
+    std::vector<hf_atom> atoms;
+    std::vector<hf_primitive_shell> prims;  // sorted by shell type
+    std::vector<double> cgto;               // per basis function
+    int num_basis = 0;
+    int num_electrons = 0, num_alpha = 0, num_beta = 0;
+};
+
+int element_to_z(const std::string& sym);
+const char* z_to_element(int z);
+double cgto_factor(int L, const std::vector<double>& a, const std::vector<double>& c);
+
+}  // namespace gb
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#define GB_CUDA_TRY(expr)                                                                                 \
+    do {                                                                                                  \
+        cudaError_t _e = (expr);                                                                          \
+        if (_e != cudaSuccess) {                                                                          \
+            gb::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));                            \
+            return (_e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;                \
+        }                                                                                                 \
+    } while (0)
+#define GB_LAUNCH_CHECK()                                                                                 \
+    do {                                                                                                  \
+        cudaError_t _e = cudaGetLastError();                                                              \
+        if (_e != cudaSuccess) {                                                                          \
+            gb::set_error(std::string("kernel launch: ") + cudaGetErrorString(_e));                       \
+            return HF_ERR_CUDA;                                                                           \
+        }                                                                                                 \
+    } while (0)
+#endif

@@ -1,0 +1,466 @@
+// Restricted Hartree-Fock SCF on the device, following the reference loop
+// (HF::single_point_energy, src/hf.cu:245-314):
+//   X = U s^{-1/2}, eigenvalues below 1e-6 zeroed      src/hf.cu:171-243, src/gpu_kernels.cu:28-43
+//   core guess: C from H, D, F = F(D)                   include/rhf.hpp:378-396
+//   loop: C from F (F' = X^T F X, syevd, C = X C')     src/gpu_manager.cu:529-599
+//         D = 2 C_occ C_occ^T                           src/gpu_kernels.cu:54-69
+//         F = F(D); E = 1/2 (<D,H> + <D,F>)             src/gpu_manager.cu:827-836
+//         stop when |E - E_prev| < threshold            src/hf.cu:297-300
+//         DIIS: e = FDS - SDF, cyclic store of (e, F), extrapolate once two
+//         pairs are stored                              include/rhf.hpp:298-327
+// The DIIS B matrix, its bordered FP64 solve (partial-pivot Gaussian
+// elimination, the algorithm of the reference's getrf/getrs) and the
+// extrapolation all run on the device: no host round trip per DIIS step.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <limits>
+
+#include "engine.hpp"
+
+namespace gb {
+
+namespace {
+
+constexpr int kMaxDiis = 16;
+
+int gemm_rm(cublasHandle_t h, bool ta, bool tb, int n, const double* A, const double* B, double* C,
+            double alpha = 1.0, double beta = 0.0)
+{
+    // row-major C = op(A) op(B)  <=>  column-major C^T = op(B)^T op(A)^T
+    const cublasStatus_t st = cublasDgemm(h, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N, n, n, n,
+                                          &alpha, B, n, A, n, &beta, C, n);
+    if (st != CUBLAS_STATUS_SUCCESS) return set_error("cublasDgemm failed"), HF_ERR_CUDA;
+    return HF_OK;
+}
+
+__global__ void transform_kernel(const double* __restrict__ W, const double* __restrict__ s, int n,
+                                 double* __restrict__ X)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int i = static_cast<int>(k / n), c = static_cast<int>(k % n);
+        const double v = s[c];
+        const double d = (v < 1e-6) ? 0.0 : 1.0 / sqrt(v);
+        X[k] = W[static_cast<long long>(c) * n + i] * d;  // U[i][c] * s_c^{-1/2}
+    }
+}
+
+__global__ void density_kernel(const double* __restrict__ C, int n, int nocc, double* __restrict__ D)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long i = k / n, j = k % n;
+        double s = 0.0;
+        for (int o = 0; o < nocc; ++o) s += C[i * n + o] * C[j * n + o];
+        D[k] = 2.0 * s;
+    }
+}
+
+__global__ void energy_kernel(const double* __restrict__ D, const double* __restrict__ H,
+                              const double* __restrict__ F, long long nn, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) s += D[k] * (H[k] + F[k]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) *out = 0.5 * s;
+    }
+}
+
+__global__ void sub_kernel(const double* __restrict__ A, const double* __restrict__ B, long long nn,
+                           double* __restrict__ C)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        C[k] = A[k] - B[k];
+}
+
+// G (+)= s (2 (J' + J'^T) - 1/2 (K' + K'^T)) s ; F = H + G
+__global__ void fock_from_jk_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
+                                    const double* __restrict__ s, const double* __restrict__ H, int n, int accumulate,
+                                    double* __restrict__ G, double* __restrict__ F)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int i = static_cast<int>(k / n), j = static_cast<int>(k % n);
+        const long long kt = static_cast<long long>(j) * n + i;
+        const double g = (2.0 * (Jp[k] + Jp[kt]) - 0.5 * (Kp[k] + Kp[kt])) * s[i] * s[j];
+        const double gn = accumulate ? G[k] + g : g;
+        G[k] = gn;
+        F[k] = H[k] + gn;
+    }
+}
+
+// B_ij = <e_i, e_j> for i <= j < m; one block per (i, j).
+__global__ void diis_dots_kernel(const double* __restrict__ Es, int m, long long nn, double* __restrict__ B)
+{
+    __shared__ double red[32];
+    int p = blockIdx.x, i = 0;
+    while (p >= m - i) { p -= m - i; ++i; }
+    const int j = i + p;
+    const double* a = Es + i * nn;
+    const double* b = Es + j * nn;
+    double s = 0.0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) s += a[k] * b[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) { B[i * kMaxDiis + j] = s; B[j * kMaxDiis + i] = s; }
+    }
+}
+
+// Bordered system [B -1; -1 0] c = [0 .. 0 -1], Gaussian elimination with
+// partial pivoting in FP64 (one thread; m+1 <= 17).  Coefficients to coef[].
+__global__ void diis_solve_kernel(const double* __restrict__ B, int m, double* __restrict__ coef, int* status)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int n = m + 1;
+    double A[kMaxDiis + 1][kMaxDiis + 2];
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+            if (i < m && j < m) A[i][j] = B[i * kMaxDiis + j];
+            else if (i == m && j == m) A[i][j] = 0.0;
+            else A[i][j] = -1.0;
+        }
+        A[i][n] = (i == m) ? -1.0 : 0.0;
+    }
+    int bad = 0;
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
+        if (A[piv][c] == 0.0) { bad = 1; continue; }
+        if (piv != c)
+            for (int k = 0; k <= n; ++k) { const double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
+        for (int r = c + 1; r < n; ++r) {
+            const double f = A[r][c] / A[c][c];
+            for (int k = c; k <= n; ++k) A[r][k] -= f * A[c][k];
+        }
+    }
+    double x[kMaxDiis + 1];
+    for (int r = n - 1; r >= 0; --r) {
+        double s = A[r][n];
+        for (int k = r + 1; k < n; ++k) s -= A[r][k] * x[k];
+        x[r] = (A[r][r] != 0.0) ? s / A[r][r] : 0.0;
+    }
+    for (int i = 0; i < m; ++i) coef[i] = x[i];
+    *status = bad;
+}
+
+__global__ void diis_combine_kernel(const double* __restrict__ Fs, const double* __restrict__ coef, int m, long long nn,
+                                    double* __restrict__ F)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        double s = 0.0;
+        for (int i = 0; i < m; ++i) s += coef[i] * Fs[i * nn + k];
+        F[k] = s;
+    }
+}
+
+int grid_nn(long long nn) { return static_cast<int>(std::min<long long>((nn + 255) / 256, 8192)); }
+
+template <class T>
+int alloc(T*& p, size_t n)
+{
+    if (p) return HF_OK;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return (e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;
+    }
+    return HF_OK;
+}
+
+int ensure_scf(Engine& e, int m)
+{
+    auto& w = e.scf;
+    const int n = e.num_basis;
+    const size_t nn = static_cast<size_t>(n) * n;
+    if (w.n == n && w.m >= m) return HF_OK;
+    if (w.m < m && w.Es) { cudaFree(w.Es); cudaFree(w.Fs); w.Es = w.Fs = nullptr; }
+    int st;
+    if ((st = alloc(w.S, nn)) || (st = alloc(w.H, nn)) || (st = alloc(w.X, nn)) || (st = alloc(w.F, nn)) ||
+        (st = alloc(w.D, nn)) || (st = alloc(w.Dprev, nn)) || (st = alloc(w.G, nn)) || (st = alloc(w.dD, nn)) ||
+        (st = alloc(w.C, nn)) || (st = alloc(w.W, nn)) || (st = alloc(w.eps, n)) || (st = alloc(w.T1, nn)) ||
+        (st = alloc(w.T2, nn)) || (st = alloc(w.E, nn)) || (st = alloc(w.Es, nn * m)) || (st = alloc(w.Fs, nn * m)) ||
+        (st = alloc(w.diis, kMaxDiis * kMaxDiis + kMaxDiis + 8)) || (st = alloc(w.info, 4)))
+        return st;
+    if (!w.work) {
+        if (cusolverDnDsyevd_bufferSize(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, w.W, n, w.eps,
+                                        &w.lwork) != CUSOLVER_STATUS_SUCCESS)
+            return set_error("cusolverDnDsyevd_bufferSize failed"), HF_ERR_SOLVER;
+        if ((st = alloc(w.work, static_cast<size_t>(w.lwork)))) return st;
+    }
+    w.n = n;
+    w.m = m;
+    return HF_OK;
+}
+
+// eigen-decomposition of the symmetric A (row-major) into W (column-major
+// eigenvectors) and ascending eigenvalues
+int syevd(Engine& e, const double* A, cudaStream_t s)
+{
+    auto& w = e.scf;
+    const size_t nn = static_cast<size_t>(w.n) * w.n;
+    GB_CUDA_TRY(cudaMemcpyAsync(w.W, A, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (cusolverDnDsyevd(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, w.n, w.W, w.n, w.eps, w.work,
+                         w.lwork, w.info) != CUSOLVER_STATUS_SUCCESS)
+        return set_error("cusolverDnDsyevd failed"), HF_ERR_SOLVER;
+    return HF_OK;
+}
+
+int coefficients(Engine& e, const double* F, cudaStream_t s)
+{
+    auto& w = e.scf;
+    int st;
+    if ((st = gemm_rm(e.cublas, true, false, w.n, w.X, F, w.T1))) return st;   // X^T F
+    if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, w.X, w.T2))) return st;  // X^T F X
+    if ((st = syevd(e, w.T2, s))) return st;
+    return gemm_rm(e.cublas, false, true, w.n, w.X, w.W, w.C);  // C = X C'
+}
+
+int diis_error(Engine& e, const double* S, const double* X, const double* F, const double* D, double* E,
+               bool include_transform, cudaStream_t s)
+{
+    auto& w = e.scf;
+    const long long nn = static_cast<long long>(w.n) * w.n;
+    int st;
+    if ((st = gemm_rm(e.cublas, false, false, w.n, F, D, w.T1))) return st;
+    if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, S, w.T2))) return st;  // FDS
+    if ((st = gemm_rm(e.cublas, false, false, w.n, S, D, w.T1))) return st;
+    if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, F, E))) return st;     // SDF
+    sub_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T2, E, nn, E);
+    GB_LAUNCH_CHECK();
+    if (include_transform) {
+        if ((st = gemm_rm(e.cublas, false, false, w.n, X, E, w.T1))) return st;
+        if ((st = gemm_rm(e.cublas, false, true, w.n, w.T1, X, E))) return st;
+    }
+    return HF_OK;
+}
+
+int diis_extrapolate(Engine& e, const double* Es, const double* Fs, int m, double* Fout, cudaStream_t s)
+{
+    auto& w = e.scf;
+    const long long nn = static_cast<long long>(w.n) * w.n;
+    double* B = w.diis;
+    double* coef = w.diis + kMaxDiis * kMaxDiis;
+    diis_dots_kernel<<<m * (m + 1) / 2, 512, 0, s>>>(Es, m, nn, B);
+    GB_LAUNCH_CHECK();
+    diis_solve_kernel<<<1, 32, 0, s>>>(B, m, coef, w.info + 1);
+    GB_LAUNCH_CHECK();
+    diis_combine_kernel<<<grid_nn(nn), 256, 0, s>>>(Fs, coef, m, nn, Fout);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+double nuclear_repulsion(const Engine& e)
+{
+    double v = 0.0;
+    for (size_t i = 0; i + 1 < e.atoms.size(); ++i)
+        for (size_t j = i + 1; j < e.atoms.size(); ++j) {
+            const double dx = e.atoms[i].x - e.atoms[j].x, dy = e.atoms[i].y - e.atoms[j].y,
+                         dz = e.atoms[i].z - e.atoms[j].z;
+            v += e.atoms[i].atomic_number * e.atoms[j].atomic_number / std::sqrt(dx * dx + dy * dy + dz * dz);
+        }
+    return v;
+}
+
+}  // namespace
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+void hf_scf_options_default(hf_scf_options* o)
+{
+    if (!o) return;
+    o->max_iter = 100;
+    o->convergence_threshold = 1e-6;
+    o->diis_size = 8;
+    o->diis_include_transform = 0;
+    o->precision = HF_PRECISION_FP64;
+    o->mixed_threshold = 1e-7;
+    o->incremental = 0;
+    o->rebuild_every = 0;
+    o->verbose = 0;
+}
+
+int hf_compute_diis_error(hf_engine* eng, const double* d_overlap, const double* d_transform, const double* d_fock,
+                          const double* d_density, double* d_error, int include_transform, void* stream)
+{
+    clear_error();
+    if (!eng || !d_overlap || !d_fock || !d_density || !d_error || (include_transform && !d_transform))
+        return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    int st = ensure_scf(e, std::max(e.scf.m, 2));
+    if (st) return st;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cublasSetStream(e.cublas, s);
+    return diis_error(e, d_overlap, d_transform, d_fock, d_density, d_error, include_transform != 0, s);
+}
+
+int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d_focks, double* d_new_fock,
+                         int num_prev, void* stream)
+{
+    clear_error();
+    if (!eng || !d_errors || !d_focks || !d_new_fock) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    if (num_prev < 2 || num_prev > kMaxDiis)
+        return set_error("DIIS requires between 2 and 16 previous Fock matrices"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    int st = ensure_scf(e, std::max(e.scf.m, 2));
+    if (st) return st;
+    return diis_extrapolate(e, d_errors, d_focks, num_prev, d_new_fock, static_cast<cudaStream_t>(stream));
+}
+
+int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, hf_scf_result* res,
+               double* d_density_out, double* d_fock_out, double* d_orbital_energies_out, double* d_coefficients_out)
+{
+    clear_error();
+    if (!eng || !res) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    hf_scf_options opt;
+    if (opt_in) opt = *opt_in; else hf_scf_options_default(&opt);
+    if (num_electrons <= 0 || (num_electrons & 1))
+        return set_error("RHF needs an even, positive number of electrons"), HF_ERR_INVALID_ARGUMENT;
+    const int nocc = num_electrons / 2;
+    const int n = e.num_basis;
+    if (nocc > n) return set_error("more occupied orbitals than basis functions"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.diis_size < 1 || opt.diis_size > kMaxDiis)
+        return set_error("diis_size must be in [1, 16]"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.precision != HF_PRECISION_FP64 && opt.precision != HF_PRECISION_MIXED)
+        return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
+    const int m = opt.diis_size;
+    int st = ensure_scf(e, m);
+    if (st) return st;
+    auto& w = e.scf;
+    const long long nn = static_cast<long long>(n) * n;
+    cudaStream_t s = nullptr;
+    cublasSetStream(e.cublas, s);
+    cusolverDnSetStream(e.cusolver, s);
+    *res = hf_scf_result{};
+    res->nuclear_repulsion = nuclear_repulsion(e);
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_counters, 0, 4 * sizeof(unsigned long long), s));
+    GB_CUDA_TRY(cudaMemsetAsync(w.info, 0, 4 * sizeof(int), s));
+
+    cudaEvent_t f0, f1;
+    cudaEventCreate(&f0);
+    cudaEventCreate(&f1);
+    double fock_ms = 0.0;
+    int fock_builds = 0;
+    double* h_energy = nullptr;
+    cudaMallocHost(&h_energy, sizeof(double));
+
+    // one Fock build: F = H + G(D), full or incremental
+    auto fock_build = [&](bool first) -> int {
+        cudaEventRecord(f0, s);
+        const bool incremental = opt.incremental && !first &&
+                                 !(opt.rebuild_every > 0 && fock_builds % opt.rebuild_every == 0);
+        int r;
+        if (incremental) {
+            sub_kernel<<<grid_nn(nn), 256, 0, s>>>(w.D, w.Dprev, nn, w.dD);
+            GB_LAUNCH_CHECK();
+            if ((r = build_jk(e, w.dD, nullptr, nullptr, opt.precision, opt.mixed_threshold, s))) return r;
+        } else {
+            if ((r = build_jk(e, w.D, nullptr, nullptr, opt.precision, opt.mixed_threshold, s))) return r;
+        }
+        fock_from_jk_kernel<<<grid_nn(nn), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, w.H, n, incremental ? 1 : 0, w.G, w.F);
+        GB_LAUNCH_CHECK();
+        GB_CUDA_TRY(cudaMemcpyAsync(w.Dprev, w.D, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        cudaEventRecord(f1, s);
+        ++fock_builds;
+        return HF_OK;
+    };
+    auto elapsed = [&]() {
+        float ms = 0.f;
+        cudaEventSynchronize(f1);
+        cudaEventElapsedTime(&ms, f0, f1);
+        return static_cast<double>(ms);
+    };
+
+    const auto t_setup = std::chrono::steady_clock::now();
+    // core Hamiltonian, X, core guess
+    if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
+    if ((st = syevd(e, w.S, s))) return st;
+    transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
+    GB_LAUNCH_CHECK();
+    if ((st = coefficients(e, w.H, s))) return st;
+    density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
+    GB_LAUNCH_CHECK();
+    if ((st = fock_build(true))) return st;
+    fock_ms += elapsed();
+    res->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_setup).count();
+
+    const auto t_loop = std::chrono::steady_clock::now();
+    double prev = std::numeric_limits<double>::max(), energy = 0.0;
+    int iter = 0, diis_iter = 0;
+    bool converged = false;
+    while (iter < opt.max_iter) {
+        if ((st = coefficients(e, w.F, s))) return st;
+        density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
+        GB_LAUNCH_CHECK();
+        if ((st = fock_build(false))) return st;
+        energy_kernel<<<1, 1024, 0, s>>>(w.D, w.H, w.F, nn, e.d_scalar + 4);
+        GB_LAUNCH_CHECK();
+        GB_CUDA_TRY(cudaMemcpyAsync(h_energy, e.d_scalar + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
+        fock_ms += elapsed();
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+        energy = *h_energy;
+        const double diff = std::fabs(energy - prev);
+        if (opt.verbose)
+            std::printf("---- Iteration: %d ----  Energy: %.17g Total energy: %.17g Difference: %.17g\n", iter, energy,
+                        energy + res->nuclear_repulsion, diff);
+        if (!std::isfinite(energy)) return set_error("SCF energy is not finite"), HF_ERR_NOT_CONVERGED;
+        if (diff < opt.convergence_threshold) { converged = true; break; }
+        ++iter;
+        prev = energy;
+        // DIIS update (Convergence_RHF_DIIS::get_new_fock_matrix)
+        const int slot = diis_iter % m;
+        if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, opt.diis_include_transform != 0, s))) return st;
+        GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + slot * nn, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        const int nprev = std::min(diis_iter + 1, m);
+        if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, w.F, s))) return st;
+        ++diis_iter;
+    }
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    res->scf_ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_loop).count();
+    int info[4] = {0, 0, 0, 0};
+    GB_CUDA_TRY(cudaMemcpy(info, w.info, sizeof(info), cudaMemcpyDeviceToHost));
+    unsigned long long cnt[4] = {0, 0, 0, 0};
+    GB_CUDA_TRY(cudaMemcpy(cnt, e.d_counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+    cudaFreeHost(h_energy);
+    cudaEventDestroy(f0);
+    cudaEventDestroy(f1);
+    res->electronic_energy = energy;
+    res->total_energy = energy + res->nuclear_repulsion;
+    res->iterations = iter;
+    res->converged = converged ? 1 : 0;
+    res->fock_ms_total = fock_ms;
+    res->fp64_quartets = static_cast<long long>(cnt[0]);
+    res->fp32_quartets = static_cast<long long>(cnt[1]);
+    if (info[0] != 0) return set_error("syevd reported info " + std::to_string(info[0])), HF_ERR_SOLVER;
+    if (d_density_out) GB_CUDA_TRY(cudaMemcpy(d_density_out, w.D, nn * sizeof(double), cudaMemcpyDeviceToDevice));
+    if (d_fock_out) GB_CUDA_TRY(cudaMemcpy(d_fock_out, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice));
+    if (d_orbital_energies_out) {
+        // orbital energies of the last diagonalised Fock matrix
+        GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
+    }
+    if (d_coefficients_out) GB_CUDA_TRY(cudaMemcpy(d_coefficients_out, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice));
+    return converged ? HF_OK : (set_error("SCF did not converge"), HF_ERR_NOT_CONVERGED);
+}
+
+}  // extern "C"

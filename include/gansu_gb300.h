@@ -1,0 +1,183 @@
+/*
+ * gansu_gb300.h - C ABI of the GB300-native Hartree-Fock hot path.
+ *
+ * Every entry point is plain C: host or device pointers, sizes, a CUDA stream
+ * handle passed as void*, and an int status (HF_OK = 0).  No exception and no
+ * C++ or torch type crosses this boundary.  Matrices are row-major N x N FP64
+ * in device memory, symmetric, owned by the caller, exactly as the reference's
+ * gansu::gpu free functions expect them (include/gpu_manager.hpp:34-109).
+ *
+ * The library is one shared object (libgansu_gb300.so) built for sm_103a.
+ * There is no CPU fallback: on a machine without a usable GPU every compute
+ * entry point returns HF_ERR_CUDA.
+ */
+#ifndef GANSU_GB300_H
+#define GANSU_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+    HF_OK = 0,
+    HF_ERR_INVALID_ARGUMENT = 1, /* bad size, null pointer, unsupported shell type */
+    HF_ERR_CUDA = 2,             /* a CUDA runtime call failed (message: hf_last_error) */
+    HF_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed */
+    HF_ERR_NOT_CONVERGED = 4,    /* SCF hit maxiter */
+    HF_ERR_SOLVER = 5,           /* cuSOLVER reported failure (info != 0) */
+    HF_ERR_IO = 6,               /* basis / xyz file could not be read or parsed */
+    HF_ERR_NOT_SPD = 7           /* metric not positive definite (RI) */
+};
+
+/* Last error message of the calling thread (never NULL). */
+const char* hf_last_error(void);
+/* Library version string. */
+const char* hf_version(void);
+
+/* ----------------------------------------------------------- input model */
+/* Binary layout of gansu::PrimitiveShell (include/types.hpp:116-125). */
+typedef struct {
+    double exponent;
+    double coefficient;
+    double x, y, z;
+    int shell_type;
+    size_t basis_index;
+    int atom_index;
+} hf_primitive_shell;
+
+/* Binary layout of gansu::Atom (include/types.hpp:131-135); coordinates in bohr. */
+typedef struct {
+    int atomic_number;
+    double x, y, z;
+} hf_atom;
+
+typedef struct hf_molecule hf_molecule;
+
+/* Replaces gansu::Molecular(xyz, gbs, charge, beta_to_alpha)
+ * (include/molecular.hpp:56-109): parses the XYZ file (angstrom -> bohr,
+ * src/parseXYZ.cpp:43-119) and the Gaussian basis file
+ * (src/basis_set.cpp:32-124), expands primitive shells per atom and stably
+ * sorts them by shell type (include/molecular.hpp:117-186). */
+int hf_molecule_from_files(const char* xyz_path, const char* gbs_path, int charge, int beta_to_alpha,
+                           hf_molecule** out);
+/* Same from atoms already in bohr (the Molecular(atoms, gbs, ...) constructor). */
+int hf_molecule_from_atoms(const hf_atom* atoms, int num_atoms, const char* gbs_path, int charge,
+                           int beta_to_alpha, hf_molecule** out);
+void hf_molecule_destroy(hf_molecule* mol);
+/* Sizes: basis functions, primitive shells, atoms, electrons, alpha, beta. */
+int hf_molecule_sizes(const hf_molecule* mol, int* num_basis, int* num_primitives, int* num_atoms,
+                      int* num_electrons, int* num_alpha, int* num_beta);
+/* Copies out the primitive shells (sorted by shell type), the CGTO
+ * normalisation factors (num_basis doubles, reference convention including its
+ * integer-division exponent for odd L) and the atoms. */
+int hf_molecule_get(const hf_molecule* mol, hf_primitive_shell* prims, double* cgto_norm, hf_atom* atoms);
+
+/* ---------------------------------------------------------------- engine */
+/* An engine holds everything the Fock build needs on the device: contracted
+ * shells rebuilt from the primitive list, shell pairs with their primitive
+ * pair data and Schwarz bounds, the quartet work lists sorted by bound, the
+ * Boys table and all SCF workspaces.  Creating it is the precomputation of the
+ * reference's ERI plugin (ERI::precomputation, include/eri.hpp:36-63;
+ * ERI_Direct::precomputation, src/eri.cu:323-347).  No allocation happens in
+ * the per-iteration calls below. */
+typedef struct hf_engine hf_engine;
+
+/* Precision tier of the direct Fock build. */
+enum {
+    HF_PRECISION_FP64 = 0,  /* every surviving quartet in FP64 */
+    HF_PRECISION_MIXED = 1  /* Q_ab*Q_cd*max|D| < mixed_threshold -> FP32 */
+};
+
+/* host arrays; prims must be sorted by shell type as hf_molecule_get returns them */
+int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const double* cgto_norm, int num_basis,
+                     const hf_atom* atoms, int num_atoms, double schwarz_threshold, hf_engine** out);
+void hf_engine_destroy(hf_engine* eng);
+/* Number of contracted shells and surviving contracted shell quartets. */
+int hf_engine_stats(const hf_engine* eng, int* num_shells, long long* num_shell_pairs, long long* num_quartets);
+
+/* Replaces gansu::gpu::computeCoreHamiltonianMatrix (src/gpu_manager.cu:333-404):
+ * S and H = T + V (point nuclei, charge = atomic number), device N x N. */
+int hf_compute_core_hamiltonian(hf_engine* eng, double* d_overlap, double* d_core_hamiltonian, void* stream);
+
+/* Replaces gansu::gpu::computeSchwarzUpperBounds (src/gpu_manager.cu:2154-2179):
+ * primitive-pair bounds sqrt(max_comp (ab|ab)) as a dense host matrix
+ * out[i*num_primitives + j] over the engine's primitive order. */
+int hf_primitive_pair_bounds(hf_engine* eng, double* h_out);
+
+/* Replaces gansu::gpu::computeERIMatrix (src/gpu_manager.cu:434-517): the full
+ * N^4 tensor ((i*N+j)*N+k)*N+l in device memory, primitive-Schwarz screened.
+ * For small molecules and parity tests only (N^4 doubles). */
+int hf_compute_eri_matrix(hf_engine* eng, double* d_eri, void* stream);
+
+/* Replaces gansu::gpu::computeFockMatrix_RHF (src/gpu_manager.cu:678-691):
+ * F = H + sum_kl D_kl[(ij|kl) - 1/2 (ik|jl)] from a stored tensor. */
+int hf_compute_fock_stored_rhf(const double* d_density, const double* d_core_hamiltonian, const double* d_eri,
+                               double* d_fock, int num_basis, void* stream);
+
+/* Replaces gansu::gpu::computeFockMatrix_Direct_RHF (src/gpu_manager.cu:2212-2227,
+ * a stub that throws in the reference): Schwarz-screened McMurchie-Davidson
+ * ERIs fused with the J/K contraction, no ERI tensor stored.
+ * F = H + J - K/2. precision: HF_PRECISION_FP64 or HF_PRECISION_MIXED. */
+int hf_compute_fock_direct_rhf(hf_engine* eng, const double* d_density, const double* d_core_hamiltonian,
+                               double* d_fock, int precision, double mixed_threshold, void* stream);
+
+/* Coulomb and exchange matrices J_ij = sum D_kl (ij|kl), K_ij = sum D_kl (ik|jl)
+ * (the pieces of computeJMatrix/computeKMatrix, src/gpu_manager.cu:2327-2540). */
+int hf_compute_jk_direct(hf_engine* eng, const double* d_density, double* d_J, double* d_K, int precision,
+                         double mixed_threshold, void* stream);
+
+/* Replaces gansu::gpu::computeDIISErrorMatrix (src/gpu_manager.cu:1020-1067):
+ * E = FDS - SDF, and X E X^T when include_transform != 0. */
+int hf_compute_diis_error(hf_engine* eng, const double* d_overlap, const double* d_transform, const double* d_fock,
+                          const double* d_density, double* d_error, int include_transform, void* stream);
+
+/* Replaces gansu::gpu::computeFockMatrixDIIS (src/gpu_manager.cu:1078-1194):
+ * B_ij = <e_i, e_j>, bordered system solved in FP64, F = sum_i c_i F_i.
+ * num_prev in [2, 16]; d_errors/d_focks hold num_prev N x N matrices. */
+int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d_focks, double* d_new_fock,
+                         int num_prev, void* stream);
+
+/* ------------------------------------------------------------------- SCF */
+typedef struct {
+    int max_iter;                   /* reference default 100 */
+    double convergence_threshold;   /* |dE| threshold, reference default 1e-6 */
+    int diis_size;                  /* reference default 8 */
+    int diis_include_transform;     /* reference default 0 */
+    int precision;                  /* HF_PRECISION_FP64 / HF_PRECISION_MIXED */
+    double mixed_threshold;         /* FP32 cut for Q_ab*Q_cd*max|dD| */
+    int incremental;                /* 1: build G(dD) and accumulate (mixed tier) */
+    int rebuild_every;              /* full rebuild period for the incremental build, 0 = never */
+    int verbose;                    /* print per-iteration lines like the reference */
+} hf_scf_options;
+
+typedef struct {
+    double electronic_energy;       /* 1/2 sum D (H + F) */
+    double nuclear_repulsion;
+    double total_energy;
+    int iterations;                 /* reference convention: iter_ at exit (src/hf.cu:297-300) */
+    int converged;
+    double fock_ms_total;           /* summed device time of the Fock builds */
+    double scf_ms_total;            /* wall time of the SCF loop (iterations only) */
+    double setup_ms;                /* core Hamiltonian + X + guess */
+    long long fp64_quartets;        /* summed over all Fock builds */
+    long long fp32_quartets;
+} hf_scf_result;
+
+void hf_scf_options_default(hf_scf_options* opt);
+
+/* Restricted HF SCF on the device (RHF::solve -> HF::single_point_energy,
+ * src/hf.cu:245-314): X = U s^{-1/2} (s < 1e-6 -> 0), core-Hamiltonian guess,
+ * DIIS as Convergence_RHF_DIIS (include/rhf.hpp:298-327), convergence on |dE|.
+ * Optional outputs (device, may be NULL): final density, Fock, orbital energies,
+ * coefficients. */
+int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt, hf_scf_result* result,
+               double* d_density_out, double* d_fock_out, double* d_orbital_energies_out,
+               double* d_coefficients_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GANSU_GB300_H */

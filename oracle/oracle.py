@@ -1,0 +1,374 @@
+"""CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Imported only by tests/, by __graft_entry__.smoke() as the checker and by
+bench.py's CPU legs.  The product never imports it.
+
+Contents, each a restatement of the reference (file:line in the reference):
+  - .gbs / .xyz parsing and primitive expansion    src/basis_set.cpp:32-124,
+                                                   src/parseXYZ.cpp:43-119,
+                                                   include/molecular.hpp:117-186
+  - CGTO factors with the L/2 integer quirk        include/basis_set.hpp:106-137
+  - MD integrals, Schwarz, J/K, S/T/V             oracle/md_oracle.c (C, OpenMP)
+  - RHF SCF with DIIS                              src/hf.cu:171-314,
+                                                   include/rhf.hpp:272-396,
+                                                   src/gpu_manager.cu:529-599,1020-1194
+Pins:
+  - refcpu_*: the reference's own int2e.cu / int1e.cu kernels compiled for the
+    CPU (oracle/refcpu, built into oracle/_ref; needs the reference tree, so
+    only available where it is mounted);
+  - known answers of the reference's linear-algebra tests
+    (test/test_gpu_manager.cu) in tests/test_oracle_pins.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REF_OUT = HERE / "_ref"
+REFERENCE_ROOT = Path(os.environ.get("GANSU_REFERENCE", "/root/reference"))
+ANG2BOHR = 1.8897259886
+
+ELEMENTS = ["H", "He", "Li", "Be", "B", "C", "N", "O", "F", "Ne", "Na", "Mg", "Al", "Si", "P", "S", "Cl", "Ar"]
+CART = {
+    0: [(0, 0, 0)],
+    1: [(1, 0, 0), (0, 1, 0), (0, 0, 1)],
+    2: [(2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1)],
+}
+L_OF = {"S": 0, "P": 1, "D": 2, "F": 3, "G": 4}
+
+
+# ------------------------------------------------------------------ build
+def build_oracle(force: bool = False) -> Path:
+    """Compile oracle/md_oracle.c into oracle/_build/libmdoracle.so."""
+    BUILD.mkdir(exist_ok=True)
+    so = BUILD / "libmdoracle.so"
+    src = HERE / "md_oracle.c"
+    if force or not so.exists() or so.stat().st_mtime < src.stat().st_mtime:
+        tmp = so.with_suffix(".tmp.so")
+        subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11", str(src), "-o", str(tmp), "-lm"],
+                       check=True)
+        os.replace(tmp, so)
+    return so
+
+
+def build_refcpu() -> Path | None:
+    """Compile the reference's integral kernels for the CPU (needs the reference tree)."""
+    if not (REFERENCE_ROOT / "src" / "int2e.cu").exists():
+        return None
+    subprocess.run(["make", "-s", "-C", str(HERE / "refcpu"), f"REF={REFERENCE_ROOT}", f"OUT={REF_OUT}"], check=True)
+    return REF_OUT / "librefcpu.so"
+
+
+_oracle = None
+_refcpu = None
+
+
+def _lib():
+    global _oracle
+    if _oracle is None:
+        L = C.CDLL(str(build_oracle()))
+        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+        basis = [C.c_int, ip, ip, ip, ip, dp, dp, dp, dp, C.c_int]
+        L.oracle_boys.argtypes = [C.c_int, C.c_double, dp]
+        L.oracle_cgto_factor.argtypes = [C.c_int, C.c_int, dp, dp]
+        L.oracle_cgto_factor.restype = C.c_double
+        L.oracle_eri_tensor.argtypes = basis + [C.c_double, dp]
+        L.oracle_direct_jk.argtypes = basis + [C.c_double, dp, dp, dp, C.c_int]
+        L.oracle_direct_jk.restype = C.c_long
+        L.oracle_one_electron.argtypes = basis + [C.c_int, dp, dp, dp, dp, dp]
+        L.oracle_prim_pair_bounds.argtypes = basis + [C.c_int, dp]
+        _oracle = L
+    return _oracle
+
+
+def refcpu_available() -> bool:
+    return (REF_OUT / "librefcpu.so").exists()
+
+
+def _ref():
+    global _refcpu
+    if _refcpu is None:
+        L = C.CDLL(str(REF_OUT / "librefcpu.so"))
+        dp, ip, lp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_longlong)
+        L.refcpu_integrals.argtypes = [C.c_int, dp, dp, dp, ip, lp, ip, dp, C.c_int, C.c_int, ip, dp, C.c_double,
+                                       dp, dp, dp, dp, lp]
+        _refcpu = L
+    return _refcpu
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+# ---------------------------------------------------------- input model
+def parse_gbs(path) -> dict:
+    """{element: [(l, [exps], [coefs]), ...]} in file order."""
+    lines = Path(path).read_text().splitlines()
+    i = 0
+    while i < len(lines) and not (lines[i][:1].isalpha()):
+        i += 1
+    out: dict = {}
+    while i < len(lines):
+        toks = lines[i].split()
+        i += 1
+        if not toks:
+            continue
+        shells = out.setdefault(toks[0], [])
+        while i < len(lines):
+            hdr = lines[i].strip()
+            i += 1
+            if hdr.startswith("****"):
+                break
+            t = hdr.split()
+            if not t:
+                continue
+            typ, nprim = t[0], int(t[1])
+            rows = [lines[i + k].replace("D", "E").split() for k in range(nprim)]
+            i += nprim
+            for col, letter in enumerate(typ):
+                shells.append((L_OF[letter.upper()], [float(r[0]) for r in rows], [float(r[1 + col]) for r in rows]))
+    return out
+
+
+def parse_xyz(path):
+    lines = Path(path).read_text().splitlines()
+    n = int(lines[0])
+    atoms = []
+    for ln in lines[2:]:
+        t = ln.split()
+        if not t:
+            continue
+        atoms.append((ELEMENTS.index(t[0]) + 1, float(t[1]) * ANG2BOHR, float(t[2]) * ANG2BOHR,
+                      float(t[3]) * ANG2BOHR))
+    assert len(atoms) == n
+    return atoms
+
+
+def cgto_factor(L, exps, coefs):
+    """include/basis_set.hpp:106-137 (second primitive uses L//2)."""
+    s = 0.0
+    for a, ca in zip(exps, coefs):
+        na = (2 * math.pi) ** -0.75 * (4 * a) ** (L / 2.0 + 0.75)
+        for b, cb in zip(exps, coefs):
+            nb = (2 * math.pi) ** -0.75 * (4 * b) ** (L // 2 + 0.75)
+            s += ca * na * cb * nb / (2 * (a + b)) ** (L + 1.5)
+    return (s * (2 * math.pi) ** 1.5) ** -0.5
+
+
+@dataclass
+class Basis:
+    atoms: list
+    l: np.ndarray
+    nprim: np.ndarray
+    prim_off: np.ndarray
+    bf_off: np.ndarray
+    xyz: np.ndarray
+    alpha: np.ndarray
+    coef: np.ndarray
+    cgto: np.ndarray
+    nbf: int
+    shell_atom: np.ndarray
+    num_electrons: int = 0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nshell(self):
+        return len(self.l)
+
+    def cargs(self):
+        return (C.c_int(self.nshell), _ip(self.l), _ip(self.nprim), _ip(self.prim_off), _ip(self.bf_off),
+                _dp(self.xyz), _dp(self.alpha), _dp(self.coef), _dp(self.cgto), C.c_int(self.nbf))
+
+    def reference_primitives(self):
+        """Primitive list as the reference's Molecular builds it: per atom, per
+        shell in file order, then stably sorted by shell type."""
+        rows = []
+        for s in range(self.nshell):
+            for k in range(self.nprim[s]):
+                p = self.prim_off[s] + k
+                rows.append((int(self.l[s]), float(self.alpha[p]), float(self.coef[p]), tuple(self.xyz[s]),
+                             int(self.bf_off[s]), int(self.shell_atom[s])))
+        rows.sort(key=lambda r: r[0])
+        return rows
+
+
+def make_basis(atoms, gbs_path, charge=0) -> Basis:
+    table = parse_gbs(gbs_path)
+    l, nprim, prim_off, bf_off, xyz, alpha, coef, cgto, shell_atom = [], [], [], [], [], [], [], [], []
+    bf = 0
+    for ia, (z, x, y, w) in enumerate(atoms):
+        for (L, exps, cfs) in table[ELEMENTS[z - 1]]:
+            l.append(L)
+            nprim.append(len(exps))
+            prim_off.append(len(alpha))
+            bf_off.append(bf)
+            xyz.append((x, y, w))
+            alpha.extend(exps)
+            coef.extend(cfs)
+            shell_atom.append(ia)
+            nc = (L + 1) * (L + 2) // 2
+            cgto.extend([cgto_factor(L, exps, cfs)] * nc)
+            bf += nc
+    ne = sum(a[0] for a in atoms) - charge
+    return Basis(atoms=list(atoms), l=np.array(l, np.int32), nprim=np.array(nprim, np.int32),
+                 prim_off=np.array(prim_off, np.int32), bf_off=np.array(bf_off, np.int32),
+                 xyz=np.ascontiguousarray(np.array(xyz, float)), alpha=np.array(alpha, float),
+                 coef=np.array(coef, float), cgto=np.array(cgto, float), nbf=bf,
+                 shell_atom=np.array(shell_atom, np.int32), num_electrons=ne)
+
+
+# ------------------------------------------------------------ integrals
+def boys(nmax, x):
+    out = np.zeros(nmax + 1)
+    _lib().oracle_boys(nmax, float(x), _dp(out))
+    return out
+
+
+def one_electron(b: Basis):
+    N = b.nbf
+    S, T, V = np.zeros((N, N)), np.zeros((N, N)), np.zeros((N, N))
+    z = np.array([a[0] for a in b.atoms], float)
+    xyz = np.ascontiguousarray(np.array([a[1:] for a in b.atoms], float))
+    _lib().oracle_one_electron(*b.cargs(), len(b.atoms), _dp(z), _dp(xyz), _dp(S), _dp(T), _dp(V))
+    return S, T, V
+
+
+def eri_tensor(b: Basis, thr=1e-12):
+    N = b.nbf
+    eri = np.zeros((N, N, N, N))
+    _lib().oracle_eri_tensor(*b.cargs(), float(thr), _dp(eri))
+    return eri
+
+
+def direct_jk(b: Basis, D, thr=1e-12, nthreads=0):
+    N = b.nbf
+    D = np.ascontiguousarray(D, dtype=float)
+    J, K = np.zeros((N, N)), np.zeros((N, N))
+    kept = _lib().oracle_direct_jk(*b.cargs(), float(thr), _dp(D), _dp(J), _dp(K), int(nthreads))
+    return J, K, kept
+
+
+def nuclear_repulsion(atoms):
+    e = 0.0
+    for i in range(len(atoms)):
+        for j in range(i + 1, len(atoms)):
+            d = math.dist(atoms[i][1:], atoms[j][1:])
+            e += atoms[i][0] * atoms[j][0] / d
+    return e
+
+
+# ------------------------------------------------------------------ SCF
+def transform_matrix(S):
+    """X = U s^{-1/2}, s < 1e-6 -> 0 (src/hf.cu:171-243, src/gpu_kernels.cu:28-43)."""
+    s, U = np.linalg.eigh(S)
+    d = np.where(s < 1e-6, 0.0, 1.0 / np.sqrt(np.where(s < 1e-6, 1.0, s)))
+    return U * d
+
+
+def coefficients(F, X):
+    e, Cp = np.linalg.eigh(X.T @ F @ X)
+    return e, X @ Cp
+
+
+def density(Cm, nocc):
+    Co = Cm[:, :nocc]
+    return 2.0 * Co @ Co.T
+
+
+def diis_extrapolate(errs, focks):
+    m = len(errs)
+    B = -np.ones((m + 1, m + 1))
+    B[m, m] = 0.0
+    for i in range(m):
+        for j in range(m):
+            B[i, j] = np.vdot(errs[i], errs[j])
+    rhs = np.zeros(m + 1)
+    rhs[m] = -1.0
+    c = np.linalg.solve(B, rhs)
+    return sum(ci * Fi for ci, Fi in zip(c[:m], focks))
+
+
+def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False):
+    """The reference SCF loop (src/hf.cu:278-307) with the core guess and DIIS."""
+    X = transform_matrix(S)
+    _, Cm = coefficients(H, X)
+    D = density(Cm, nocc)
+    F = fock(D)
+    prev, energy, it, diis_it = np.finfo(float).max, 0.0, 0, 0
+    errs, focks = [None] * diis_size, [None] * diis_size
+    eps = None
+    converged = False
+    history = []
+    while it < maxiter:
+        eps, Cm = coefficients(F, X)
+        D = density(Cm, nocc)
+        F = fock(D)
+        energy = 0.5 * (np.vdot(D, H) + np.vdot(D, F))
+        history.append(energy)
+        if abs(energy - prev) < thr:
+            converged = True
+            break
+        it += 1
+        prev = energy
+        e = F @ D @ S - S @ D @ F
+        if include_transform:
+            e = X @ e @ X.T
+        slot = diis_it % diis_size
+        errs[slot], focks[slot] = e, F.copy()
+        nprev = min(diis_it + 1, diis_size)
+        if nprev > 1:
+            F = diis_extrapolate(errs[:nprev], focks[:nprev])
+        diis_it += 1
+    return {"electronic_energy": energy, "total_energy": energy + enuc, "iterations": it, "converged": converged,
+            "orbital_energies": eps, "density": D, "fock": F, "history": history}
+
+
+def rhf_from_basis(b: Basis, thr_schwarz=1e-12, stored=True, **kw):
+    S, T, V = one_electron(b)
+    H = T + V
+    if stored:
+        eri = eri_tensor(b, thr_schwarz)
+        fock = lambda D: H + np.einsum("ijkl,kl->ij", eri, D) - 0.5 * np.einsum("ikjl,kl->ij", eri, D)
+    else:
+        def fock(D):
+            J, K, _ = direct_jk(b, D, thr_schwarz)
+            return H + J - 0.5 * K
+    return rhf(S, H, fock, b.num_electrons // 2, nuclear_repulsion(b.atoms), **kw)
+
+
+# -------------------------------------------------- reference on the CPU
+def refcpu_integrals(b: Basis, thr=1e-12, want_eri=True):
+    """S, H, primitive Schwarz bounds (reference layout) and the ERI tensor as
+    computed by the reference's own kernels run on the CPU."""
+    rows = b.reference_primitives()
+    n = len(rows)
+    exps = np.array([r[1] for r in rows])
+    coefs = np.array([r[2] for r in rows])
+    xyz = np.ascontiguousarray(np.array([r[3] for r in rows]))
+    stype = np.array([r[0] for r in rows], np.int32)
+    bidx = np.array([r[4] for r in rows], np.int64)
+    aidx = np.array([r[5] for r in rows], np.int32)
+    N = b.nbf
+    S, H = np.zeros((N, N)), np.zeros((N, N))
+    eri = np.zeros((N, N, N, N)) if want_eri else None
+    bounds = np.zeros(n * (n + 1) // 2 + n * n)
+    nb = C.c_longlong(0)
+    z = np.array([a[0] for a in b.atoms], np.int32)
+    axyz = np.ascontiguousarray(np.array([a[1:] for a in b.atoms], float))
+    _ref().refcpu_integrals(n, _dp(exps), _dp(coefs), _dp(xyz), _ip(stype),
+                            bidx.ctypes.data_as(C.POINTER(C.c_longlong)), _ip(aidx), _dp(b.cgto), N, len(b.atoms),
+                            _ip(z), _dp(axyz), float(thr), _dp(S), _dp(H), _dp(eri) if want_eri else None,
+                            _dp(bounds), C.byref(nb))
+    return {"S": S, "H": H, "eri": eri, "bounds": bounds[: nb.value], "primitives": rows}

@@ -1,0 +1,135 @@
+"""Host-side logic that needs no GPU: the C ABI library loads and exports every
+declared symbol, the input model (basis/xyz parsing, primitive expansion,
+CGTO factors) matches the oracle's independent restatement, the basis sizes of
+the configured molecules, parameter handling and the geometry generators."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import dft_gansu_gb300 as gg
+from dft_gansu_gb300 import geometry
+from oracle import oracle as O
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "gansu_gb300.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^(?:int|void|const char\s*\*)\s*(hf_[a-z0-9_]+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(built_library):
+    names = declared_symbols()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(built_library, n), n
+    from dft_gansu_gb300._capi import SIGNATURES
+    assert set(SIGNATURES) == set(names)
+
+
+def test_version_and_error_string(built_library):
+    assert b"sm_103a" in built_library.hf_version()
+    with pytest.raises(gg.HFError):
+        gg.Molecular([(8, 0.0, 0.0, 0.0)], "/nonexistent.gbs")
+    assert b"cannot open" in built_library.hf_last_error()
+
+
+@pytest.mark.parametrize("atoms,gbs,nbf,nprim", [
+    (geometry.water(), "sto-3g", 7, 15),
+    (geometry.alkane(10), "6-31g_st", 194, 238),
+    (geometry.alkane(10), "cc-pvdz", 260, 330),
+    (geometry.c60(), "cc-pvdz", 900, 1320),
+    (geometry.c60(), "cc-pvdz-rifit", 3960, 1080),
+])
+def test_basis_sizes(built_library, atoms, gbs, nbf, nprim):
+    mol = gg.Molecular(atoms, gg.basis_path(gbs))
+    assert mol.num_basis == nbf
+    assert mol.num_primitives == nprim
+
+
+@pytest.mark.parametrize("gbs", ["sto-3g", "6-31g_st", "cc-pvdz"])
+def test_input_model_matches_oracle(built_library, gbs):
+    atoms = geometry.alkane(3, seed=5)
+    mol = gg.Molecular(atoms, gg.basis_path(gbs))
+    b = O.make_basis(atoms, gg.basis_path(gbs))
+    assert mol.num_basis == b.nbf
+    np.testing.assert_allclose(mol.get_cgto_normalization_factors(), b.cgto, rtol=1e-14)
+    t = mol.primitive_table()
+    ref = b.reference_primitives()
+    assert [r[0] for r in ref] == list(t["shell_type"])
+    np.testing.assert_array_equal([r[4] for r in ref], t["basis_index"])
+    np.testing.assert_allclose([r[1] for r in ref], t["exponent"])
+    np.testing.assert_allclose([r[2] for r in ref], t["coefficient"])
+    assert mol.num_electrons == sum(a[0] for a in atoms)
+
+
+def test_cgto_quirk_for_p_functions(built_library):
+    # the reference normalisation leaves contracted p functions non-unit (L/2 integer division)
+    mol = gg.Molecular(geometry.water(), gg.basis_path("sto-3g"))
+    f = mol.get_cgto_normalization_factors()
+    b = O.make_basis(geometry.water(), gg.basis_path("sto-3g"))
+    S, _, _ = O.one_electron(b)
+    assert abs(S[2, 2] - 1.0) > 0.1  # O 2px
+    assert abs(S[0, 0] - 1.0) < 1e-8  # O 1s
+    assert np.all(f > 0)
+
+
+def test_xyz_parser_matches_oracle(built_library, tmp_path):
+    p = tmp_path / "dec.xyz"
+    geometry.write_xyz(p, geometry.alkane(10))
+    mol = gg.Molecular.from_files(p, gg.basis_path("6-31g_st"))
+    ref = O.parse_xyz(p)
+    got = mol.get_atoms()
+    assert len(got) == len(ref) == 32
+    for a, r in zip(got, ref):
+        assert a[0] == r[0]
+        np.testing.assert_allclose(a[1:], r[1:], atol=1e-9)
+
+
+def test_xyz_rejects_overlapping_atoms(built_library, tmp_path):
+    p = tmp_path / "bad.xyz"
+    p.write_text("2\nbad\nH 0 0 0\nH 0 0 0.00001\n")
+    with pytest.raises(gg.HFError):
+        gg.Molecular.from_files(p, gg.basis_path("sto-3g"))
+
+
+def test_odd_electron_count_reported(built_library):
+    mol = gg.Molecular([(1, 0.0, 0.0, 0.0)], gg.basis_path("sto-3g"))
+    assert (mol.num_alpha_spins, mol.num_beta_spins) == (1, 0)
+
+
+def test_parameter_manager_rules(tmp_path):
+    pm = gg.ParameterManager()
+    assert pm["eri_method"] == "stored" and pm.get("diis_size", int) == 8
+    pm["method"] = "RHF"
+    assert pm["method"] == "rhf"
+    pm["gbsfilename"] = "Basis/STO-3G.gbs"
+    assert pm["gbsfilename"] == "Basis/STO-3G.gbs"
+    with pytest.raises(KeyError):
+        pm["not_a_key"] = 1
+    rec = tmp_path / "r.txt"
+    rec.write_text("convergence_method = DIIS\ndiis_size = 6\n# comment\n")
+    pm.load_from_file(rec)
+    assert pm.get("diis_size", int) == 6 and pm["convergence_method"] == "diis"
+
+
+def test_geometries():
+    dec = geometry.alkane(10, jitter=0.0)
+    x = np.array([a[1:] for a in dec]) / geometry.ANGSTROM_TO_BOHR
+    cc = np.linalg.norm(x[0] - x[1])
+    assert abs(cc - 1.54) < 1e-9
+    hs = [np.linalg.norm(x[i] - x[j]) for i in range(10) for j in range(10, 32) if np.linalg.norm(x[i] - x[j]) < 1.2]
+    assert len(hs) == 22 and np.allclose(hs, 1.09)
+    c = np.array([a[1:] for a in geometry.c60(jitter=0.0)]) / geometry.ANGSTROM_TO_BOHR
+    d = np.linalg.norm(c[:, None] - c[None], axis=-1)
+    bonds = np.sort(d[(d > 0.1) & (d < 1.6)])
+    assert len(bonds) == 180 and set(np.round(bonds, 6)) == {1.4, 1.45}
+    clusters = geometry.water_cluster_set(16, seed=2)
+    for cl in clusters:
+        o = np.array([a[1:] for a in cl if a[0] == 8]) / geometry.ANGSTROM_TO_BOHR
+        if len(o) > 1:
+            dd = np.linalg.norm(o[:, None] - o[None], axis=-1) + np.eye(len(o)) * 9
+            assert dd.min() >= 2.7 - 1e-9

@@ -1,0 +1,115 @@
+"""The oracle is pinned before it is trusted.
+
+1. Against golden fixtures produced by the reference's OWN integral kernels
+   (src/int2e.cu, src/int1e.cu compiled for the CPU; tests/golden/make_golden.py):
+   S, H, primitive Schwarz bounds, ERI elements and checksums, SCF energy.
+2. Live against those kernels when the reference tree is mounted (oracle/_ref).
+3. Boys function against 40-digit quadrature of its definition (mpmath).
+4. The reference's linear-algebra known answers (test/test_gpu_manager.cu) for
+   the SCF building blocks the oracle restates.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = Path(__file__).parent / "golden"
+BASIS = Path(__file__).resolve().parents[1] / "dft_gansu_gb300" / "basis"
+CASES = ["water_sto-3g", "water_6-31g_st", "water_cc-pvdz", "propane_6-31g_st"]
+
+
+def _basis(case):
+    g = np.load(GOLD / f"{case}.npz")
+    gbs = case.split("_", 1)[1]
+    atoms = [(int(a[0]), a[1], a[2], a[3]) for a in g["atoms"]]
+    return g, O.make_basis(atoms, BASIS / f"{gbs}.gbs")
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_one_electron_matches_reference_kernels(case):
+    g, b = _basis(case)
+    S, T, V = O.one_electron(b)
+    assert np.abs(S - g["S"]).max() < 1e-12
+    assert np.abs(T + V - g["H"]).max() < 1e-11
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_eri_matches_reference_kernels(case):
+    g, b = _basis(case)
+    eri = O.eri_tensor(b, 1e-12)
+    if "eri" in g:
+        assert np.abs(eri - g["eri"]).max() < 1e-12
+    else:
+        idx = g["eri_idx"]
+        vals = eri[idx[:, 0], idx[:, 1], idx[:, 2], idx[:, 3]]
+        assert np.abs(vals - g["eri_val"]).max() < 1e-12
+    assert abs(eri.sum() - g["eri_sum"]) < 1e-9 * max(1.0, abs(float(g["eri_sum"])))
+    assert abs((eri * eri).sum() - g["eri_sq_sum"]) < 1e-9 * float(g["eri_sq_sum"])
+
+
+@pytest.mark.parametrize("case", CASES[:2])
+def test_oracle_scf_energy_matches_reference_integrals(case):
+    g, b = _basis(case)
+    res = O.rhf_from_basis(b, thr=1e-10)
+    assert res["converged"]
+    assert abs(res["total_energy"] - float(g["energy_total"])) < 1e-8
+    np.testing.assert_allclose(res["orbital_energies"], g["orbital_energies"], atol=1e-7)
+
+
+def test_oracle_direct_jk_equals_tensor_contraction():
+    g, b = _basis("water_6-31g_st")
+    eri = O.eri_tensor(b, 1e-12)
+    rng = np.random.default_rng(3)
+    D = rng.normal(size=(b.nbf, b.nbf))
+    D = D + D.T
+    J, K, kept = O.direct_jk(b, D, 1e-12)
+    assert kept > 0
+    np.testing.assert_allclose(J, np.einsum("ijkl,kl->ij", eri, D), atol=1e-11)
+    np.testing.assert_allclose(K, np.einsum("ikjl,kl->ij", eri, D), atol=1e-11)
+
+
+@pytest.mark.skipif(not O.refcpu_available(), reason="reference tree not mounted: golden fixtures cover the pin")
+def test_oracle_live_against_reference_kernels():
+    from dft_gansu_gb300 import geometry
+    b = O.make_basis(geometry.alkane(2, jitter=0.02, seed=11), BASIS / "cc-pvdz.gbs")
+    r = O.refcpu_integrals(b, 1e-12)
+    S, T, V = O.one_electron(b)
+    assert np.abs(S - r["S"]).max() < 1e-12
+    assert np.abs(T + V - r["H"]).max() < 1e-11
+    eri = O.eri_tensor(b, 1e-12)
+    assert np.abs(eri - r["eri"]).max() < 1e-11
+
+
+def test_boys_against_high_precision():
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    for x in [0.0, 1e-8, 0.01, 0.3, 1.0, 2.5, 7.7, 15.0, 29.9, 35.0, 40.5, 80.0]:
+        f = O.boys(12, x)
+        for n in range(13):
+            # F_n(x) = int_0^1 t^{2n} exp(-x t^2) dt by 40-digit quadrature
+            ref = float(mpmath.quad(lambda t: t ** (2 * n) * mpmath.exp(-mpmath.mpf(x) * t * t), [0, 0.5, 1]))
+            assert abs(f[n] - ref) <= 2e-14 * ref, (x, n, f[n], ref)
+
+
+def test_reference_linear_algebra_known_answers():
+    # test/test_gpu_manager.cu:28-76: eigenvalues of [[4,1],[1,3]] = {2.381966, 4.618034}, tol 1e-6
+    w, U = np.linalg.eigh(np.array([[4.0, 1.0], [1.0, 3.0]]))
+    np.testing.assert_allclose(w, [2.381966, 4.618034], atol=1e-6)
+    assert abs(U[:, 0] @ U[:, 1]) < 1e-6
+    # test/test_gpu_manager.cu:328-370: Cholesky of [[25,15,-5],[15,18,0],[-5,0,11]]
+    L = np.linalg.cholesky(np.array([[25.0, 15, -5], [15, 18, 0], [-5, 0, 11]]))
+    np.testing.assert_allclose(L, [[5, 0, 0], [3, 3, 0], [-1, 1, 3]], atol=1e-6)
+    # X = U s^{-1/2} with eigenvalues below 1e-6 zeroed (src/gpu_kernels.cu:28-43)
+    X = O.transform_matrix(np.diag([4.0, 1e-8]))
+    np.testing.assert_allclose(np.abs(X), [[0.0, 0.5], [0.0, 0.0]], atol=1e-15)
+
+
+def test_diis_bordered_solve_is_affine():
+    rng = np.random.default_rng(0)
+    errs = [rng.normal(size=(5, 5)) for _ in range(4)]
+    focks = [np.full((5, 5), float(k)) for k in range(4)]
+    F = O.diis_extrapolate(errs, focks)
+    # coefficients sum to one: extrapolating constant matrices gives a constant
+    assert np.allclose(F, F[0, 0])
