@@ -1,0 +1,365 @@
+"""Benchmark of the hot path: RHF SCF iterations of n-decane / 6-31G* (N=194)
+with the direct (integral-direct, Schwarz-screened McMurchie-Davidson) Fock
+build, mixed precision vs FP64, on one GB300.
+
+A "step" is one full SCF solve (core guess, DIIS, converged to 1e-8 Eh) of the
+seeded synthetic molecule; the metric is milliseconds per SCF iteration
+(the loop only, CUDA events on the launching stream), lower is better.
+L2 is flushed (a 512 MB write) before every timed step.
+
+Prints ONE JSON line (rank 0).  --impl reference times the CPU restatement of
+the reference's algorithm (the reference has no CPU integral code) on the host
+cores, per SCF iteration, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SCF ms/iter & gradient ms, mixed vs FP64 on 1 GB300 at |ΔE|≤1e-6 Eh"
+WORKLOAD = "RHF/6-31G* n-decane C10H22 (N=194 Cartesian, 238 primitive shells), zig-zag + N(0,0.02 A) jitter"
+MIXED_THRESHOLD = 1e-5
+CONV = 1e-8
+
+
+# ----------------------------------------------------------------- model
+def ncart(l):
+    return (l + 1) * (l + 2) // 2
+
+
+def nherm(l):
+    return (l + 1) * (l + 2) * (l + 3) // 6
+
+
+def flops_per_primitive_quartet(la, lb, lc, ld):
+    """Algorithmic flop model of one primitive quartet of the MD Fock kernel
+    (Boys, R recursion, Hermite E, ket and bra contraction)."""
+    L = la + lb + lc + ld
+    boys = (L + 1) * 11
+    rrec = 3 * sum(math.comb(L - n + 3, 3) for n in range(L + 1))
+    herm = 5 * 3 * ((la + 1) * (lb + 1) * (la + lb + 1) + (lc + 1) * (ld + 1) * (lc + ld + 1))
+    ket = 2 * ncart(lc) * ncart(ld) * nherm(la + lb) * nherm(lc + ld)
+    bra = 2 * ncart(la) * ncart(lb) * ncart(lc) * ncart(ld) * nherm(la + lb)
+    return boys + rrec + herm + ket + bra
+
+
+def digestion_flops(la, lb, lc, ld):
+    return 12 * ncart(la) * ncart(lb) * ncart(lc) * ncart(ld)
+
+
+def model_flops(stats, precision_key="fp64"):
+    total = 0.0
+    for s in stats:
+        la, lb, lc, ld = s["class"]
+        total += s[f"prim_{precision_key}"] * flops_per_primitive_quartet(la, lb, lc, ld)
+        total += s[f"contracted_{precision_key}"] * digestion_flops(la, lb, lc, ld)
+    return total
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            t = [x.strip() for x in ln.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                smax.append(float(t[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, t[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- dist
+def dist_init(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world
+
+
+def dist_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ------------------------------------------------------------- CPU legs
+def cpu_iteration_ms(atoms, gbs, sample_stride=4, threads=0):
+    """One SCF iteration of the CPU restatement (oracle/md_oracle.c Fock build
+    with OpenMP + numpy diagonalisation/DIIS), timed on a bounded sample:
+    J/K over every `sample_stride`-th bra shell pair, scaled to the full build
+    by the count of primitive quartets."""
+    import numpy as np
+    from oracle import oracle as O
+
+    b = O.make_basis(atoms, gbs)
+    S, T, V = O.one_electron(b)
+    H = T + V
+    X = O.transform_matrix(S)
+    _, Cm = O.coefficients(H, X)
+    D = O.density(Cm, b.num_electrons // 2)
+    t0 = time.perf_counter()
+    kept = O.direct_jk_sample(b, D, 1e-12, threads, sample_stride)
+    t_sample = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    F = H.copy()
+    for _ in range(3):  # diagonalisation + density + DIIS error of one iteration
+        e, C = O.coefficients(F, X)
+        D2 = O.density(C, b.num_electrons // 2)
+        _ = F @ D2 @ S - S @ D2 @ F
+    t_other = (time.perf_counter() - t0) / 3
+    return kept, t_sample, t_other
+
+
+# ------------------------------------------------------------------ main
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from dft_gansu_gb300 import geometry
+    import dft_gansu_gb300 as gg
+
+    atoms = geometry.alkane(10, jitter=0.02, seed=args.seed)
+    gbs = gg.basis_path("6-31g_st")
+    cores = os.cpu_count() or 1
+    full_prim_quartets = None
+    vals = []
+    for step in range(args.warmup + args.steps):
+        kept, t_sample, t_other = cpu_iteration_ms(atoms, gbs, args.sample_stride)
+        # primitive quartets of a full Fock build, from the unsampled count of this workload
+        if full_prim_quartets is None:
+            full_prim_quartets = FULL_PRIM_QUARTETS.get(args.seed) or kept * args.sample_stride
+        ms = (t_sample * full_prim_quartets / kept + t_other) * 1e3
+        if step >= args.warmup:
+            vals.append(ms)
+    v = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "ms/iter", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "seed": args.seed, "precision": "fp64 (CPU restatement)"},
+        "cpu_baseline": {"value": v, "unit": "ms/iter", "cores": cores, "kind": "port",
+                         "sample": f"J/K over every {args.sample_stride}th bra shell pair of one Fock build, scaled by "
+                                   f"primitive-quartet count ({full_prim_quartets}); + numpy diag/DIIS"},
+        "e2e": {"value": v, "unit": "ms/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# primitive quartets of one full decane/6-31G* Fock build (seed -> count), the
+# denominator used to scale the CPU sample; measured by the GPU kernel counters
+FULL_PRIM_QUARTETS = {0: 62489524}
+
+
+def run_ours(args, rank, world):
+    import torch
+    import dft_gansu_gb300 as gg
+    from dft_gansu_gb300 import geometry
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    atoms = geometry.alkane(10, jitter=0.02, seed=args.seed)
+    gbs = gg.basis_path("6-31g_st")
+    mol = gg.Molecular(atoms, gbs)
+    eng = gg.Engine(mol, 1e-12)
+    nel = mol.num_electrons
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    opts_mixed = {"convergence_threshold": CONV, "precision": gg.HF_PRECISION_MIXED,
+                  "mixed_threshold": args.mixed_threshold, "incremental": 1, "rebuild_every": 0}
+    opts_fp64 = {"convergence_threshold": CONV}
+
+    def solve(opts):
+        flush.zero_()
+        torch.cuda.synchronize()
+        return eng.rhf_scf(nel, opts)
+
+    for _ in range(args.warmup):
+        solve(opts_mixed)
+        solve(opts_fp64)
+
+    # ---- timed: mixed (the headline), then FP64 for the comparison
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    l0 = gg.kernel_launch_count()
+    mixed, fp64 = [], []
+    with ClockSampler(dev) as clocks:
+        for _ in range(args.steps):
+            mixed.append(solve(opts_mixed))
+        l1 = gg.kernel_launch_count()
+        for _ in range(args.steps):
+            fp64.append(solve(opts_fp64))
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    it_mx = sum(r["iterations"] for r in mixed)
+    it_64 = sum(r["iterations"] for r in fp64)
+    ms_mx = sum(r["scf_ms_total"] for r in mixed) / max(it_mx, 1)
+    ms_64 = sum(r["scf_ms_total"] for r in fp64) / max(it_64, 1)
+    ms_mx = dist_max(ms_mx, world)
+    ms_64 = dist_max(ms_64, world)
+    dE = max(abs(a["total_energy"] - b["total_energy"]) for a, b in zip(mixed, fp64))
+    step_ms = statistics.mean(r["scf_ms_total"] for r in mixed)
+
+    # ---- e2e: the public API from host data to a host energy, per iteration
+    e2e_vals, h2d, d2h = [], 0, 0
+    for _ in range(max(1, min(args.steps, 3))):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m2 = gg.Molecular(atoms, gbs)
+        e2 = gg.Engine(m2, 1e-12)
+        r2 = e2.rhf_scf(nel, opts_mixed)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) * 1e3
+        h2d = e2.h2d_bytes()
+        d2h = 8 * (r2["iterations"] + 1) + 8 * 4 * 64 + 16
+        e2.close()
+        e2e_vals.append(dt / max(r2["iterations"], 1))
+
+    # ---- roofline of the dominant kernel family: one FP64 direct Fock build
+    import numpy as np
+    D = torch.tensor(np.eye(mol.num_basis) * 0.5, dtype=torch.float64, device="cuda")
+    r_ref = eng.rhf_scf(nel, opts_fp64, want_matrices=True)
+    D = r_ref["density"]
+    for _ in range(2):
+        eng.jk(D)
+    eng.reset_stats()
+    flush.zero_()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    eng.jk(D)
+    ev1.record()
+    ev1.synchronize()
+    build_ms = ev0.elapsed_time(ev1)
+    st = eng.class_stats()
+    flops = model_flops(st, "fp64")
+    peak64 = gg.measure_fma_peak(0)
+    achieved = flops / (build_ms * 1e-3) / 1e12
+
+    # ---- CPU baseline on the machine's host cores (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        kept, t_sample, t_other = cpu_iteration_ms(atoms, gbs, args.sample_stride)
+        full = sum(s["prim_fp64"] for s in st)
+        cpu_ms = (t_sample * full / kept + t_other) * 1e3
+        cpu = {"value": cpu_ms, "unit": "ms/iter", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"oracle J/K over every {args.sample_stride}th bra shell pair of one decane Fock build "
+                         f"({kept} of {full} primitive quartets, scaled) + numpy diag/DIIS of one iteration"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms_mx, "unit": "ms/iter", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "seed": args.seed, "precision": "mixed (FP32 quartets when "
+                       f"Q_ab*Q_cd*max|dD| < {args.mixed_threshold}, incremental dD builds)",
+                       "convergence": CONV, "l2": "flushed (512 MB write) before every step",
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "fp64_ms_per_iter": ms_64, "mixed_speedup_vs_fp64": ms_64 / ms_mx,
+            "delta_E_mixed_vs_fp64": dE, "energy_fp64": fp64[0]["total_energy"],
+            "iterations": {"mixed": mixed[0]["iterations"], "fp64": fp64[0]["iterations"]},
+            "gradient_ms": None,
+            "e2e": {"value": statistics.mean(e2e_vals), "unit": "ms/iter", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": l1 - l0,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                         "frac": achieved / peak64, "traffic": None,
+                         "kernel": "direct Fock build, FP64 tier (21 quartet-class launches), one launch set",
+                         "build_ms": build_ms, "model_flops": flops,
+                         "peak_source": "hf_measure_fma_peak FP64 FMA chains (MEASURED_PEAKS.json has no FP64)"},
+            "clocks": clocks.summary(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--mixed-threshold", type=float, default=MIXED_THRESHOLD)
+    ap.add_argument("--sample-stride", type=int, default=4)
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

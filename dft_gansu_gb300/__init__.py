@@ -97,6 +97,18 @@ class Molecular:
         }
 
 
+def kernel_launch_count() -> int:
+    """Kernels launched by libgansu_gb300 in this process."""
+    return int(lib().hf_kernel_launch_count())
+
+
+def measure_fma_peak(precision: int) -> float:
+    """Sustained FMA TFLOP/s of the current GPU (0: FP64, 1: FP32)."""
+    v = C.c_double()
+    check(lib().hf_measure_fma_peak(precision, C.byref(v)), "hf_measure_fma_peak")
+    return v.value
+
+
 def _ptr(t) -> int:
     return 0 if t is None else int(t.data_ptr())
 
@@ -140,6 +152,24 @@ class Engine:
         ns, npair, nq = C.c_int(), C.c_longlong(), C.c_longlong()
         check(lib().hf_engine_stats(self._h, C.byref(ns), C.byref(npair), C.byref(nq)), "hf_engine_stats")
         return {"num_shells": ns.value, "num_shell_pairs": npair.value, "num_quartets": nq.value}
+
+    def class_stats(self) -> list:
+        n = C.c_int()
+        check(lib().hf_engine_class_stats(self._h, 0, C.byref(n), None, None, None, None, None), "hf_engine_class_stats")
+        k = n.value
+        cl = (C.c_int * (4 * k))()
+        arrs = [(C.c_longlong * k)() for _ in range(4)]
+        check(lib().hf_engine_class_stats(self._h, k, C.byref(n), cl, *arrs), "hf_engine_class_stats")
+        return [{"class": tuple(cl[4 * i:4 * i + 4]), "prim_fp64": arrs[0][i], "prim_fp32": arrs[1][i],
+                 "contracted_fp64": arrs[2][i], "contracted_fp32": arrs[3][i]} for i in range(k)]
+
+    def reset_stats(self):
+        check(lib().hf_engine_reset_stats(self._h), "hf_engine_reset_stats")
+
+    def h2d_bytes(self) -> int:
+        v = C.c_longlong()
+        check(lib().hf_engine_transfer_bytes(self._h, C.byref(v)), "hf_engine_transfer_bytes")
+        return v.value
 
     def core_hamiltonian(self, stream=None):
         S, H = self._empty(self.N, self.N), self._empty(self.N, self.N)

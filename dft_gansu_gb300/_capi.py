@@ -91,6 +91,11 @@ SIGNATURES = {
                               C.POINTER(_P)]),
     "hf_engine_destroy": (None, [_P]),
     "hf_engine_stats": (_I, [_P, C.POINTER(_I), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "hf_engine_class_stats": (_I, [_P, _I, C.POINTER(_I), C.POINTER(_I)] + [C.POINTER(C.c_longlong)] * 4),
+    "hf_engine_reset_stats": (_I, [_P]),
+    "hf_engine_transfer_bytes": (_I, [_P, C.POINTER(C.c_longlong)]),
+    "hf_kernel_launch_count": (C.c_longlong, []),
+    "hf_measure_fma_peak": (_I, [_I, C.POINTER(_D)]),
     "hf_compute_core_hamiltonian": (_I, [_P, _P, _P, _P]),
     "hf_primitive_pair_bounds": (_I, [_P, C.POINTER(_D)]),
     "hf_compute_eri_matrix": (_I, [_P, _P, _P]),

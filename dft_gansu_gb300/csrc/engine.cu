@@ -377,13 +377,18 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
     if ((st = dev_alloc(e->plan.off64, noff)) || (st = dev_alloc(e->plan.off32, noff)) ||
         (st = dev_alloc(e->plan.lo32, e->entry_bra.size())) || (st = dev_alloc(e->d_Dp64, nn)) ||
         (st = dev_alloc(e->d_Dp32, nn)) || (st = dev_alloc(e->d_Jp, nn)) || (st = dev_alloc(e->d_Kp, nn)) ||
-        (st = dev_alloc(e->d_scalar, 16)) || (st = dev_alloc(e->d_counters, 4)))
+        (st = dev_alloc(e->d_scalar, 16)) || (st = dev_alloc(e->d_counters, kCounterSlots)))
         return st;
-    if (cudaMemset(e->d_counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess)
+    if (cudaMemset(e->d_counters, 0, kCounterSlots * sizeof(unsigned long long)) != cudaSuccess)
         return set_error("cudaMemset failed"), HF_ERR_CUDA;
     if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) return set_error("cublasCreate failed"), HF_ERR_CUDA;
     if (cusolverDnCreate(&e->cusolver) != CUSOLVER_STATUS_SUCCESS)
         return set_error("cusolverDnCreate failed"), HF_ERR_CUDA;
+    e->bytes_h2d = static_cast<long long>(
+        e->pairs.size() * sizeof(ShellPairDev) + e->pp64.size() * sizeof(PrimPair64) + pp32.size() * sizeof(PrimPair32) +
+        boys.size() * (sizeof(double) + sizeof(float)) + e->scale.size() * sizeof(double) + atom4.size() * sizeof(double) +
+        (2 * e->entry_bra.size() + zeros.size()) * sizeof(int) + qs.size() * sizeof(double) +
+        e->off_static.size() * sizeof(long long) + 4 * e->class_pairs.size() * sizeof(int));
     *out = reinterpret_cast<hf_engine*>(e.release());
     return HF_OK;
 }
@@ -397,6 +402,50 @@ int hf_engine_stats(const hf_engine* eng, int* num_shells, long long* num_shell_
     if (num_shells) *num_shells = e->num_shells;
     if (num_shell_pairs) *num_shell_pairs = static_cast<long long>(e->pairs.size());
     if (num_quartets) *num_quartets = e->total_survivors;
+    return HF_OK;
+}
+
+int hf_engine_class_stats(hf_engine* eng, int max_classes, int* num_classes, int* class_l, long long* prim_fp64,
+                          long long* prim_fp32, long long* contracted_fp64, long long* contracted_fp32)
+{
+    clear_error();
+    if (!eng || !num_classes) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine* e = reinterpret_cast<Engine*>(eng);
+    const int ncp = static_cast<int>(e->class_pairs.size());
+    *num_classes = ncp;
+    if (max_classes < ncp) return HF_OK;
+    std::vector<unsigned long long> c(kCounterSlots, 0);
+    if (cudaMemcpy(c.data(), e->d_counters, kCounterSlots * sizeof(unsigned long long), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+        return set_error("cudaMemcpy of counters failed"), HF_ERR_CUDA;
+    for (int k = 0; k < ncp; ++k) {
+        const PairClass& X = e->pair_classes[e->class_pairs[k].X];
+        const PairClass& Y = e->pair_classes[e->class_pairs[k].Y];
+        if (class_l) {
+            class_l[4 * k] = X.la; class_l[4 * k + 1] = X.lb; class_l[4 * k + 2] = Y.la; class_l[4 * k + 3] = Y.lb;
+        }
+        if (prim_fp64) prim_fp64[k] = static_cast<long long>(c[4 * k + 0]);
+        if (contracted_fp64) contracted_fp64[k] = static_cast<long long>(c[4 * k + 1]);
+        if (prim_fp32) prim_fp32[k] = static_cast<long long>(c[4 * k + 2]);
+        if (contracted_fp32) contracted_fp32[k] = static_cast<long long>(c[4 * k + 3]);
+    }
+    return HF_OK;
+}
+
+int hf_engine_reset_stats(hf_engine* eng)
+{
+    clear_error();
+    if (!eng) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine* e = reinterpret_cast<Engine*>(eng);
+    if (cudaMemset(e->d_counters, 0, kCounterSlots * sizeof(unsigned long long)) != cudaSuccess)
+        return set_error("cudaMemset failed"), HF_ERR_CUDA;
+    return HF_OK;
+}
+
+int hf_engine_transfer_bytes(const hf_engine* eng, long long* h2d_bytes)
+{
+    if (!eng || !h2d_bytes) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    *h2d_bytes = reinterpret_cast<const Engine*>(eng)->bytes_h2d;
     return HF_OK;
 }
 

@@ -14,6 +14,9 @@
 namespace gb {
 
 constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
+constexpr int kNumClassPairs = kNumPairClasses * (kNumPairClasses + 1) / 2;
+// per class pair and precision: {primitive quartets, contracted quartets}
+constexpr int kCounterSlots = kNumClassPairs * 2 * 2;
 
 struct Shell {
     int l, nprim, prim_off, bf, atom;
@@ -79,7 +82,8 @@ struct Engine {
     double* d_Jp = nullptr;
     double* d_Kp = nullptr;
     double* d_scalar = nullptr;  // small scratch scalars (8 doubles)
-    unsigned long long* d_counters = nullptr;  // [0] prim quartets FP64, [1] FP32
+    unsigned long long* d_counters = nullptr;  // [class pair][precision][prim, contracted]
+    long long bytes_h2d = 0;                   // bytes uploaded by engine creation
 
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;

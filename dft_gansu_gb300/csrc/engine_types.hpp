@@ -57,7 +57,7 @@ struct FockClassLaunch {
     int ket_base;                  // global index of the ket class's first pair
     int num_basis;
     double schwarz_threshold;
-    unsigned long long* prim_quartet_counter;
+    unsigned long long* counters;  // [0] primitive quartets, [1] contracted quartets
 };
 
 }  // namespace gb

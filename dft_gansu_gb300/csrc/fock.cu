@@ -202,7 +202,7 @@ FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off,
     L.ket_base = e.pair_classes[cp.Y].begin;
     L.num_basis = e.num_basis;
     L.schwarz_threshold = e.schwarz_threshold;
-    L.prim_quartet_counter = e.d_counters + (fp32 ? 1 : 0);
+    L.counters = e.d_counters + 2 * (2 * cpi + (fp32 ? 1 : 0));
     return L;
 }
 

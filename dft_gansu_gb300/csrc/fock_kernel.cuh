@@ -185,7 +185,7 @@ fock_direct_kernel(const FockClassLaunch launch)
     const T* __restrict__ boys_table = static_cast<const T*>(launch.boys_table);
     const T thr = static_cast<T>(launch.schwarz_threshold);
     const int N = launch.num_basis;
-    long long prim_quartets = 0;
+    long long prim_quartets = 0, contracted = 0;
 
     for (long long base = static_cast<long long>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < total;
          base += stride) {
@@ -215,6 +215,7 @@ fock_direct_kernel(const FockClassLaunch launch)
             if (kp.A == kp.B) fsym *= T(0.5);
             if (bra == ket) fsym *= T(0.5);
             prim_quartets += quartet_block<T, LA, LB, LC, LD>(bp, kp, pp, boys_table, thr, I);
+            ++contracted;
         }
 
         // ------------------------------------------------------- digestion
@@ -329,11 +330,18 @@ fock_direct_kernel(const FockClassLaunch launch)
             }
         }
     }
-    // primitive-quartet statistics (one atomic per warp)
+    // statistics (one atomic per warp): [0] primitive quartets, [1] contracted quartets
     unsigned long long pq = static_cast<unsigned long long>(prim_quartets);
+    unsigned long long cq = static_cast<unsigned long long>(contracted);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, o);
-    if (lane == 0 && pq) atomicAdd(launch.prim_quartet_counter, pq);
+    for (int o = 16; o > 0; o >>= 1) {
+        pq += __shfl_xor_sync(0xffffffffu, pq, o);
+        cq += __shfl_xor_sync(0xffffffffu, cq, o);
+    }
+    if (lane == 0 && (pq || cq)) {
+        atomicAdd(launch.counters, pq);
+        atomicAdd(launch.counters + 1, cq);
+    }
 }
 
 // Stored-ERI path (the reference's computeERIMatrix, src/gpu_manager.cu:434-517):

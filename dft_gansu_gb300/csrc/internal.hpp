@@ -10,6 +10,8 @@ namespace gb {
 // ------------------------------------------------------------ errors
 void set_error(const std::string& msg);
 void clear_error();
+// process-wide count of kernel launches issued by this library
+void count_launch();
 
 struct Molecule {
     std::vector<hf_atom> atoms;
@@ -37,6 +39,7 @@ double cgto_factor(int L, const std::vector<double>& a, const std::vector<double
     } while (0)
 #define GB_LAUNCH_CHECK()                                                                                 \
     do {                                                                                                  \
+        gb::count_launch();                                                                               \
         cudaError_t _e = cudaGetLastError();                                                              \
         if (_e != cudaSuccess) {                                                                          \
             gb::set_error(std::string("kernel launch: ") + cudaGetErrorString(_e));                       \

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <limits>
+#include <vector>
 
 #include "engine.hpp"
 
@@ -354,7 +355,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     cusolverDnSetStream(e.cusolver, s);
     *res = hf_scf_result{};
     res->nuclear_repulsion = nuclear_repulsion(e);
-    GB_CUDA_TRY(cudaMemsetAsync(e.d_counters, 0, 4 * sizeof(unsigned long long), s));
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_counters, 0, kCounterSlots * sizeof(unsigned long long), s));
     GB_CUDA_TRY(cudaMemsetAsync(w.info, 0, 4 * sizeof(int), s));
 
     cudaEvent_t f0, f1;
@@ -405,7 +406,10 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     fock_ms += elapsed();
     res->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_setup).count();
 
-    const auto t_loop = std::chrono::steady_clock::now();
+    cudaEvent_t l0, l1;
+    cudaEventCreate(&l0);
+    cudaEventCreate(&l1);
+    cudaEventRecord(l0, s);
     double prev = std::numeric_limits<double>::max(), energy = 0.0;
     int iter = 0, diis_iter = 0;
     bool converged = false;
@@ -436,12 +440,24 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, w.F, s))) return st;
         ++diis_iter;
     }
-    GB_CUDA_TRY(cudaStreamSynchronize(s));
-    res->scf_ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_loop).count();
+    cudaEventRecord(l1, s);
+    GB_CUDA_TRY(cudaEventSynchronize(l1));
+    {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, l0, l1);
+        res->scf_ms_total = ms;  // device timeline of the SCF loop (CUDA events on the launching stream)
+    }
+    cudaEventDestroy(l0);
+    cudaEventDestroy(l1);
     int info[4] = {0, 0, 0, 0};
     GB_CUDA_TRY(cudaMemcpy(info, w.info, sizeof(info), cudaMemcpyDeviceToHost));
-    unsigned long long cnt[4] = {0, 0, 0, 0};
-    GB_CUDA_TRY(cudaMemcpy(cnt, e.d_counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> cnt(kCounterSlots, 0);
+    GB_CUDA_TRY(cudaMemcpy(cnt.data(), e.d_counters, kCounterSlots * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    unsigned long long prim64 = 0, prim32 = 0;
+    for (int c = 0; c < kNumClassPairs; ++c) {
+        prim64 += cnt[4 * c + 0];
+        prim32 += cnt[4 * c + 2];
+    }
     cudaFreeHost(h_energy);
     cudaEventDestroy(f0);
     cudaEventDestroy(f1);
@@ -450,8 +466,8 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     res->iterations = iter;
     res->converged = converged ? 1 : 0;
     res->fock_ms_total = fock_ms;
-    res->fp64_quartets = static_cast<long long>(cnt[0]);
-    res->fp32_quartets = static_cast<long long>(cnt[1]);
+    res->fp64_quartets = static_cast<long long>(prim64);
+    res->fp32_quartets = static_cast<long long>(prim32);
     if (info[0] != 0) return set_error("syevd reported info " + std::to_string(info[0])), HF_ERR_SOLVER;
     if (d_density_out) GB_CUDA_TRY(cudaMemcpy(d_density_out, w.D, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     if (d_fock_out) GB_CUDA_TRY(cudaMemcpy(d_fock_out, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice));

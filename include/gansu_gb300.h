@@ -98,6 +98,23 @@ void hf_engine_destroy(hf_engine* eng);
 /* Number of contracted shells and surviving contracted shell quartets. */
 int hf_engine_stats(const hf_engine* eng, int* num_shells, long long* num_shell_pairs, long long* num_quartets);
 
+/* Per quartet class (bra la,lb | ket lc,ld) counts accumulated by the direct
+ * Fock builds since the last reset: primitive and contracted quartets evaluated
+ * in each precision.  *num_classes receives the class count; arrays are filled
+ * when max_classes >= *num_classes (class_l gets 4 ints per class).  No
+ * reference counterpart: the flop model of the roofline uses these counts. */
+int hf_engine_class_stats(hf_engine* eng, int max_classes, int* num_classes, int* class_l, long long* prim_fp64,
+                          long long* prim_fp32, long long* contracted_fp64, long long* contracted_fp32);
+int hf_engine_reset_stats(hf_engine* eng);
+/* Bytes copied host -> device by hf_engine_create. */
+int hf_engine_transfer_bytes(const hf_engine* eng, long long* h2d_bytes);
+/* Number of CUDA kernels this library has launched in the process. */
+long long hf_kernel_launch_count(void);
+/* Diagnostic: sustained FMA throughput of the current GPU in TFLOP/s for
+ * precision 0 (FP64) or 1 (FP32), the denominators of the integral-kernel
+ * roofline. */
+int hf_measure_fma_peak(int precision, double* tflops);
+
 /* Replaces gansu::gpu::computeCoreHamiltonianMatrix (src/gpu_manager.cu:333-404):
  * S and H = T + V (point nuclei, charge = atomic number), device N x N. */
 int hf_compute_core_hamiltonian(hf_engine* eng, double* d_overlap, double* d_core_hamiltonian, void* stream);
@@ -160,7 +177,7 @@ typedef struct {
     int iterations;                 /* reference convention: iter_ at exit (src/hf.cu:297-300) */
     int converged;
     double fock_ms_total;           /* summed device time of the Fock builds */
-    double scf_ms_total;            /* wall time of the SCF loop (iterations only) */
+    double scf_ms_total;            /* SCF loop (iterations only), CUDA events on the stream */
     double setup_ms;                /* core Hamiltonian + X + guess */
     long long fp64_quartets;        /* summed over all Fock builds */
     long long fp32_quartets;

@@ -398,9 +398,23 @@ int oracle_eri_tensor(int nshell, const int* l, const int* nprim, const int* pri
 /* Direct J and K: J_ij = sum_kl D_kl (ij|kl), K_ij = sum_kl D_kl (ik|jl), over
  * unique shell quartets with 8-fold symmetry, primitive screening at thr.
  * Returns the number of primitive quartets evaluated (unique quartets). */
+long oracle_direct_jk_sample(int nshell, const int* l, const int* nprim, const int* prim_off, const int* bf_off,
+                             const double* xyz, const double* alpha, const double* coef, const double* cgto, int nbf,
+                             double thr, const double* Dm, double* J, double* K, int nthreads, int bra_stride);
+
 long oracle_direct_jk(int nshell, const int* l, const int* nprim, const int* prim_off, const int* bf_off,
                       const double* xyz, const double* alpha, const double* coef, const double* cgto, int nbf,
                       double thr, const double* Dm, double* J, double* K, int nthreads)
+{
+    return oracle_direct_jk_sample(nshell, l, nprim, prim_off, bf_off, xyz, alpha, coef, cgto, nbf, thr, Dm, J, K,
+                                   nthreads, 1);
+}
+
+/* Same as oracle_direct_jk over the bra pairs ij with ij % bra_stride == 0
+ * only: a bounded sample of the work for CPU timing (J, K then incomplete). */
+long oracle_direct_jk_sample(int nshell, const int* l, const int* nprim, const int* prim_off, const int* bf_off,
+                             const double* xyz, const double* alpha, const double* coef, const double* cgto, int nbf,
+                             double thr, const double* Dm, double* J, double* K, int nthreads, int bra_stride)
 {
     or_basis bs;
     or_make_basis(&bs, nshell, l, nprim, prim_off, bf_off, xyz, alpha, coef, cgto, nbf);
@@ -432,6 +446,7 @@ long oracle_direct_jk(int nshell, const int* l, const int* nprim, const int* pri
         double* blk = (double*)malloc(sizeof(double) * 15 * 15 * 15 * 15);
 #pragma omp for schedule(dynamic, 4)
         for (int ij = 0; ij < npair; ++ij) {
+            if (bra_stride > 1 && ij % bra_stride) continue;
             for (int kl = 0; kl <= ij; ++kl) {
                 if (qmax[ij] * qmax[kl] < thr) continue;
                 int A = pa[ij], B = pb[ij], C = pa[kl], D = pb[kl];

@@ -83,6 +83,8 @@ def _lib():
         L.oracle_eri_tensor.argtypes = basis + [C.c_double, dp]
         L.oracle_direct_jk.argtypes = basis + [C.c_double, dp, dp, dp, C.c_int]
         L.oracle_direct_jk.restype = C.c_long
+        L.oracle_direct_jk_sample.argtypes = basis + [C.c_double, dp, dp, dp, C.c_int, C.c_int]
+        L.oracle_direct_jk_sample.restype = C.c_long
         L.oracle_one_electron.argtypes = basis + [C.c_int, dp, dp, dp, dp, dp]
         L.oracle_prim_pair_bounds.argtypes = basis + [C.c_int, dp]
         _oracle = L
@@ -258,6 +260,16 @@ def direct_jk(b: Basis, D, thr=1e-12, nthreads=0):
     J, K = np.zeros((N, N)), np.zeros((N, N))
     kept = _lib().oracle_direct_jk(*b.cargs(), float(thr), _dp(D), _dp(J), _dp(K), int(nthreads))
     return J, K, kept
+
+
+def direct_jk_sample(b: Basis, D, thr=1e-12, nthreads=0, bra_stride=1):
+    """J/K over every bra_stride-th bra shell pair (timing sample); returns the
+    primitive quartets evaluated."""
+    N = b.nbf
+    D = np.ascontiguousarray(D, dtype=float)
+    J, K = np.zeros((N, N)), np.zeros((N, N))
+    return _lib().oracle_direct_jk_sample(*b.cargs(), float(thr), _dp(D), _dp(J), _dp(K), int(nthreads),
+                                          int(bra_stride))
 
 
 def nuclear_repulsion(atoms):

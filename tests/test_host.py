@@ -18,7 +18,7 @@ HEADER = ROOT / "include" / "gansu_gb300.h"
 
 def declared_symbols():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^(?:int|void|const char\s*\*)\s*(hf_[a-z0-9_]+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:int|void|long long|const char\s*\*)\s*(hf_[a-z0-9_]+)\s*\(", text, re.M)))
 
 
 def test_library_exports_every_declared_symbol(built_library):
