@@ -55,6 +55,8 @@ class ScfOptions(C.Structure):
         ("mixed_threshold", C.c_double),
         ("incremental", C.c_int),
         ("rebuild_every", C.c_int),
+        ("full_build_precision", C.c_int),
+        ("eigensolver", C.c_int),
         ("verbose", C.c_int),
     ]
 
@@ -69,6 +71,8 @@ class ScfResult(C.Structure):
         ("fock_ms_total", C.c_double),
         ("scf_ms_total", C.c_double),
         ("setup_ms", C.c_double),
+        ("diag_ms_total", C.c_double),
+        ("diis_ms_total", C.c_double),
         ("fp64_quartets", C.c_longlong),
         ("fp32_quartets", C.c_longlong),
     ]

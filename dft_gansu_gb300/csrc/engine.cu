@@ -29,7 +29,9 @@ static const double kKFold = std::sqrt(2.0 * std::pow(kPi, 2.5));
 
 void host_boys_table(std::vector<double>& table)
 {
-    table.assign(static_cast<size_t>(kBoysOrders) * kBoysPoints, 0.0);
+    table.assign(static_cast<size_t>(kBoysRows) * kBoysPoints, 0.0);
+    for (int k = 0; k < kBoysPoints; ++k)
+        table[static_cast<size_t>(kBoysExpRow) * kBoysPoints + k] = static_cast<double>(expl(-k * (long double)kBoysStep));
     const int nmax = kBoysOrders - 1;
     for (int k = 0; k < kBoysPoints; ++k) {
         const long double x = k * static_cast<long double>(kBoysStep);
@@ -124,7 +126,9 @@ PrimPair64 make_prim_pair(double a, double ca, const double* A, double b, double
     const double p = a + b;
     const double ab2 = (A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) + (A[2] - B[2]) * (A[2] - B[2]);
     r.p = p;
+    r.invp = 1.0 / p;
     r.K = ca * cb * std::exp(-a * b / p * ab2) * kKFold;
+    r.KoP = r.K / p;
     r.Q = 0.0;
     r.Px = (a * A[0] + b * B[0]) / p;
     r.Py = (a * A[1] + b * B[1]) / p;
@@ -133,7 +137,7 @@ PrimPair64 make_prim_pair(double a, double ca, const double* A, double b, double
     r.PAx = b / p * (B[0] - A[0]);
     r.PAy = b / p * (B[1] - A[1]);
     r.PAz = b / p * (B[2] - A[2]);
-    r.pad = b;
+    r.b = b;
     return r;
 }
 
@@ -177,9 +181,10 @@ Engine::~Engine()
                     d_entry_bra, d_entry_cnt, d_entry_zero, d_pair_qs, d_off_static, d_cp_meta, plan.off64, plan.off32,
                     plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
                     scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
-                    scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info};
+                    scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (scf.syevj_params) cusolverDnDestroySyevjInfo(scf.syevj_params);
     if (cublas) cublasDestroy(cublas);
     if (cusolver) cusolverDnDestroy(cusolver);
 }
@@ -334,10 +339,10 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
     std::vector<PrimPair32> pp32(e->pp64.size());
     for (size_t i = 0; i < pp32.size(); ++i) {
         const PrimPair64& a = e->pp64[i];
-        pp32[i] = PrimPair32{static_cast<float>(a.p),   static_cast<float>(a.K),   static_cast<float>(a.Q),
-                             static_cast<float>(a.Px),  static_cast<float>(a.Py),  static_cast<float>(a.Pz),
-                             static_cast<float>(a.PAx), static_cast<float>(a.PAy), static_cast<float>(a.PAz),
-                             static_cast<float>(a.pad)};
+        pp32[i] = PrimPair32{static_cast<float>(a.p),   static_cast<float>(a.invp), static_cast<float>(a.K),
+                             static_cast<float>(a.KoP), static_cast<float>(a.Q),    static_cast<float>(a.Px),
+                             static_cast<float>(a.Py),  static_cast<float>(a.Pz),   static_cast<float>(a.PAx),
+                             static_cast<float>(a.PAy), static_cast<float>(a.PAz),  static_cast<float>(a.b)};
     }
     std::vector<float> boys32(boys.begin(), boys.end());
     std::vector<double> atom4(4 * num_atoms);

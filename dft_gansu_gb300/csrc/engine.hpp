@@ -97,7 +97,9 @@ struct Engine {
                *T2 = nullptr, *E = nullptr, *Es = nullptr, *Fs = nullptr, *work = nullptr, *diis = nullptr,
                *J = nullptr, *K = nullptr;
         int* info = nullptr;
-        int lwork = 0;
+        int lwork = 0, lwork_j = 0;
+        double* work_j = nullptr;
+        syevjInfo_t syevj_params = nullptr;
     } scf;
 
     ~Engine();

@@ -28,19 +28,20 @@ static_assert(sizeof(ShellPairDev) == 80, "ShellPairDev layout");
 
 // One primitive pair of a shell pair.  K carries the contraction coefficients,
 // the component-independent part of the primitive norms, exp(-ab/p |AB|^2)
-// and sqrt(2 pi^{5/2}) so that a primitive quartet prefactor is
-// K_ab K_cd / (p q sqrt(p+q)).
+// and sqrt(2 pi^{5/2}); KoP = K/p, so that a primitive quartet prefactor is
+// KoP_ab KoP_cd / sqrt(p+q).  b is the exponent of the second primitive
+// (kinetic-energy integrals).
 struct PrimPair64 {
-    double p, K, Q;
+    double p, invp, K, KoP, Q;
     double Px, Py, Pz;
     double PAx, PAy, PAz;
-    double pad;
+    double b;
 };
 struct PrimPair32 {
-    float p, K, Q;
+    float p, invp, K, KoP, Q;
     float Px, Py, Pz;
     float PAx, PAy, PAz;
-    float pad;
+    float b;
 };
 
 struct FockClassLaunch {

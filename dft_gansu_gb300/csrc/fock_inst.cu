@@ -14,18 +14,28 @@
 
 namespace gb {
 
+constexpr int kNCD = ncart(GB_LC) * ncart(GB_LD);
+
+// grid: blocks for one thread per quartet; the generic path needs kNCD times more
 void GB_CAT(launch_fock, GB_SUFFIX)(bool fp32, const FockClassLaunch& launch, int grid, cudaStream_t stream)
 {
-    if (fp32)
-        fock_direct_kernel<float, GB_LA, GB_LB, GB_LC, GB_LD><<<grid, kFockThreads, 0, stream>>>(launch);
-    else
-        fock_direct_kernel<double, GB_LA, GB_LB, GB_LC, GB_LD><<<grid, kFockThreads, 0, stream>>>(launch);
+    if (fp32) {
+        if constexpr (FockSplit<float, GB_LA, GB_LB, GB_LC, GB_LD>::value == 1)
+            fock_direct_kernel<float, GB_LA, GB_LB, GB_LC, GB_LD><<<grid, kFockThreads, 0, stream>>>(launch);
+        else
+            launch_fock_generic(true, launch, kNCD, grid * kNCD, stream);
+    } else {
+        if constexpr (FockSplit<double, GB_LA, GB_LB, GB_LC, GB_LD>::value == 1)
+            fock_direct_kernel<double, GB_LA, GB_LB, GB_LC, GB_LD><<<grid, kFockThreads, 0, stream>>>(launch);
+        else
+            launch_fock_generic(false, launch, kNCD, grid * kNCD, stream);
+    }
 }
 
 void GB_CAT(launch_eri, GB_SUFFIX)(const FockClassLaunch& launch, const double* scale, double* eri, int grid,
                                   cudaStream_t stream)
 {
-    eri_tensor_kernel<GB_LA, GB_LB, GB_LC, GB_LD><<<grid, kFockThreads, 0, stream>>>(launch, scale, eri);
+    launch_eri_generic(launch, kNCD, scale, eri, grid * kNCD, stream);
 }
 
 }  // namespace gb

@@ -2,10 +2,13 @@
 // ERIs fused with the J/K contraction.  No ERI tensor is stored.
 //
 // Work decomposition: for one quartet class (bra shell-pair class (LA,LB),
-// ket class (LC,LD)) each thread evaluates ONE contracted shell quartet
-// (AB|CD): it loops over the primitive quartets that pass the reference's
-// primitive Schwarz test (src/int2e.cu:1677-1680), accumulates all
-// ncart(LA)*ncart(LB)*ncart(LC)*ncart(LD) integrals in registers and then
+// ket class (LC,LD)) a thread evaluates one contracted shell quartet (AB|CD)
+// with every loop unrolled at compile time; classes whose block of ncart^4
+// integrals exceeds the register budget (FockSplit) run in the generic kernel
+// of fock_generic.cu instead, one ket component pair per thread.  The thread
+// loops over the primitive
+// quartets that pass the reference's primitive Schwarz test
+// (src/int2e.cu:1677-1680), accumulates its integrals in registers and
 // digests them into J' and K' with the 8-fold permutational symmetry:
 //     J'_ab += D'_cd v   J'_cd += D'_ab v
 //     K'_ac += D'_bd v   K'_bd += D'_ac v   K'_ad += D'_bc v   K'_bc += D'_ad v
@@ -17,9 +20,8 @@
 // reproduces the reference's CGTO convention (include/basis_set.hpp:106-137).
 //
 // Items of a class are laid out as a flat list: entry e (a bra pair) owns kets
-// [lo[e], lo[e] + off[e+1] - off[e]).  Threads stride over the flat list; a
-// warp whose lanes all share one bra reduces its J'_ab sums with shuffles
-// before a single atomic.
+// [lo[e], lo[e] + off[e+1] - off[e]).  A warp whose lanes all share one bra
+// reduces its J'_ab sums with shuffles before a single atomic.
 #pragma once
 #include "md_math.cuh"
 #include "engine_types.hpp"
@@ -37,6 +39,17 @@ struct FockTypes<double> {
 template <>
 struct FockTypes<float> {
     using PP = PrimPair32;
+};
+
+// Threads per contracted quartet: 1, or one per ket component pair when the
+// block of ncart^4 integrals (or the d x d Hermite tables of a (dd| bra)
+// exceed the register budget of the type; those classes run generic.
+template <class T, int LA, int LB, int LC, int LD>
+struct FockSplit {
+    static constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
+    static constexpr int kLimit = sizeof(T) == 8 ? 36 : 81;
+    static constexpr bool kLarge = (NAB * NCD > kLimit) || (LA == 2 && LB == 2);
+    static constexpr int value = kLarge ? NCD : 1;
 };
 
 __device__ __forceinline__ int find_entry(const long long* __restrict__ off, int n, long long w)
@@ -58,19 +71,21 @@ __device__ __forceinline__ T warp_sum(T v)
     return v;
 }
 
-// Accumulates the contracted quartet (AB|CD)' into I[ab][cd] over the
-// primitive quartets that pass the reference's primitive Schwarz test.
-// Returns the number of primitive quartets evaluated.
-template <class T, int LA, int LB, int LC, int LD>
+__device__ __forceinline__ double fast_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float fast_rsqrt(float x) { return rsqrtf(x); }
+
+// Accumulates the ket component pairs [CD0, CD1) of the contracted quartet
+// (AB|CD)' into I[ab][cd - CD0], over the primitive quartets that pass the
+// primitive Schwarz test.  Returns the number of primitive quartets.
+template <class T, int LA, int LB, int LC, int LD, int CD0, int CD1>
 __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const ShellPairDev& kp,
                                              const typename FockTypes<T>::PP* __restrict__ pp,
                                              const T* __restrict__ boys_table, T thr,
-                                             T (&I)[ncart(LA) * ncart(LB)][ncart(LC) * ncart(LD)])
+                                             T (&I)[ncart(LA) * ncart(LB)][CD1 - CD0])
 {
     using PP = typename FockTypes<T>::PP;
-    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    constexpr int NB = ncart(LB), ND = ncart(LD);
     constexpr int LAB = LA + LB, LCD = LC + LD, LT = LAB + LCD;
-    (void)NA;
     int count = 0;
     const T qket_max = static_cast<T>(kp.Qmax);
     const T abx = static_cast<T>(bp.ABx), aby = static_cast<T>(bp.ABy), abz = static_cast<T>(bp.ABz);
@@ -80,7 +95,7 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
         if (pb.Q * qket_max < thr) continue;
         const T p = pb.p;
         HermiteE<T, LA, LB> Ex, Ey, Ez;
-        const T oo2p = T(0.5) / p;
+        const T oo2p = T(0.5) * pb.invp;
         Ex.build(pb.PAx, pb.PAx + abx, oo2p);
         Ey.build(pb.PAy, pb.PAy + aby, oo2p);
         Ez.build(pb.PAz, pb.PAz + abz, oo2p);
@@ -90,78 +105,77 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
             ++count;
             const T q = pk.p;
             HermiteE<T, LC, LD> Fx, Fy, Fz;
-            const T oo2q = T(0.5) / q;
+            const T oo2q = T(0.5) * pk.invp;
             Fx.build(pk.PAx, pk.PAx + cdx, oo2q);
             Fy.build(pk.PAy, pk.PAy + cdy, oo2q);
             Fz.build(pk.PAz, pk.PAz + cdz, oo2q);
-            const T pq = p + q;
-            const T rho = p * q / pq;
+            // rho = pq/(p+q); prefactor K_ab K_cd / (p q sqrt(p+q)) with K/p stored
+            const T r = fast_rsqrt(p + q);
+            const T rho = p * q * (r * r);
             const T X = pb.Px - pk.Px, Y = pb.Py - pk.Py, Z = pb.Pz - pk.Pz;
             T Fs[LT + 1];
             BoysEval<T>::template run<LT>(rho * (X * X + Y * Y + Z * Z), boys_table, Fs);
-            T scale = pb.K * pk.K / (p * q * sqrt(pq));
+            T scale = pb.KoP * pk.KoP * r;
             const T m2rho = T(-2) * rho;
 #pragma unroll
             for (int n = 0; n <= LT; ++n) { Fs[n] *= scale; scale *= m2rho; }
             HermiteR<T, LT> R;
             R.build(Fs, X, Y, Z);
 #pragma unroll
-            for (int ic = 0; ic < NC; ++ic) {
+            for (int cd = CD0; cd < CD1; ++cd) {
+                const int ic = cd / ND, id = cd % ND;
+                const int cx = cart_exp(LC, ic, 0), cy = cart_exp(LC, ic, 1), cz = cart_exp(LC, ic, 2);
+                const int dx = cart_exp(LD, id, 0), dy = cart_exp(LD, id, 1), dz = cart_exp(LD, id, 2);
+                // ket contraction into the bra Hermite index
+                T Xh[LAB + 1][LAB + 1][LAB + 1];
 #pragma unroll
-                for (int id = 0; id < ND; ++id) {
-                    const int cx = cart_exp(LC, ic, 0), cy = cart_exp(LC, ic, 1), cz = cart_exp(LC, ic, 2);
-                    const int dx = cart_exp(LD, id, 0), dy = cart_exp(LD, id, 1), dz = cart_exp(LD, id, 2);
-                    // ket contraction into the bra Hermite index
-                    T Xh[LAB + 1][LAB + 1][LAB + 1];
+                for (int t = 0; t <= LAB; ++t)
 #pragma unroll
-                    for (int t = 0; t <= LAB; ++t)
+                    for (int u = 0; u + t <= LAB; ++u)
 #pragma unroll
-                        for (int u = 0; u + t <= LAB; ++u)
-#pragma unroll
-                            for (int v = 0; v + u + t <= LAB; ++v) {
-                                T s = T(0);
-#pragma unroll
-                                for (int tau = 0; tau <= LCD; ++tau) {
-                                    if (tau > cx + dx) continue;
-#pragma unroll
-                                    for (int nu = 0; nu <= LCD; ++nu) {
-                                        if (nu > cy + dy) continue;
-                                        const T exy = Fx.e[cx][dx][tau] * Fy.e[cy][dy][nu];
-#pragma unroll
-                                        for (int phi = 0; phi <= LCD; ++phi) {
-                                            if (phi > cz + dz) continue;
-                                            const T c = exy * Fz.e[cz][dz][phi];
-                                            const T r = R.r[t + tau][u + nu][v + phi];
-                                            if ((tau + nu + phi) & 1) s -= c * r; else s += c * r;
-                                        }
-                                    }
-                                }
-                                Xh[t][u][v] = s;
-                            }
-                    // bra contraction
-#pragma unroll
-                    for (int ia = 0; ia < ncart(LA); ++ia) {
-#pragma unroll
-                        for (int ib = 0; ib < NB; ++ib) {
-                            const int ax = cart_exp(LA, ia, 0), ay = cart_exp(LA, ia, 1), az = cart_exp(LA, ia, 2);
-                            const int bx = cart_exp(LB, ib, 0), by = cart_exp(LB, ib, 1), bz = cart_exp(LB, ib, 2);
+                        for (int v = 0; v + u + t <= LAB; ++v) {
                             T s = T(0);
 #pragma unroll
-                            for (int t = 0; t <= LAB; ++t) {
-                                if (t > ax + bx) continue;
+                            for (int tau = 0; tau <= LCD; ++tau) {
+                                if (tau > cx + dx) continue;
 #pragma unroll
-                                for (int u = 0; u <= LAB; ++u) {
-                                    if (u > ay + by) continue;
-                                    const T exy = Ex.e[ax][bx][t] * Ey.e[ay][by][u];
+                                for (int nu = 0; nu <= LCD; ++nu) {
+                                    if (nu > cy + dy) continue;
+                                    const T exy = Fx.e[cx][dx][tau] * Fy.e[cy][dy][nu];
 #pragma unroll
-                                    for (int v = 0; v <= LAB; ++v) {
-                                        if (v > az + bz) continue;
-                                        s += exy * Ez.e[az][bz][v] * Xh[t][u][v];
+                                    for (int phi = 0; phi <= LCD; ++phi) {
+                                        if (phi > cz + dz) continue;
+                                        const T c = exy * Fz.e[cz][dz][phi];
+                                        const T rv = R.r[t + tau][u + nu][v + phi];
+                                        if ((tau + nu + phi) & 1) s -= c * rv; else s += c * rv;
                                     }
                                 }
                             }
-                            I[ia * NB + ib][ic * ND + id] += s;
+                            Xh[t][u][v] = s;
                         }
+                // bra contraction
+#pragma unroll
+                for (int ia = 0; ia < ncart(LA); ++ia) {
+#pragma unroll
+                    for (int ib = 0; ib < NB; ++ib) {
+                        const int ax = cart_exp(LA, ia, 0), ay = cart_exp(LA, ia, 1), az = cart_exp(LA, ia, 2);
+                        const int bx = cart_exp(LB, ib, 0), by = cart_exp(LB, ib, 1), bz = cart_exp(LB, ib, 2);
+                        T s = T(0);
+#pragma unroll
+                        for (int t = 0; t <= LAB; ++t) {
+                            if (t > ax + bx) continue;
+#pragma unroll
+                            for (int u = 0; u <= LAB; ++u) {
+                                if (u > ay + by) continue;
+                                const T exy = Ex.e[ax][bx][t] * Ey.e[ay][by][u];
+#pragma unroll
+                                for (int v = 0; v <= LAB; ++v) {
+                                    if (v > az + bz) continue;
+                                    s += exy * Ez.e[az][bz][v] * Xh[t][u][v];
+                                }
+                            }
+                        }
+                        I[ia * NB + ib][cd - CD0] += s;
                     }
                 }
             }
@@ -170,165 +184,177 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
     return count;
 }
 
+struct QuartetRef {
+    int bra, ket;
+    bool active;
+};
+
+// Evaluates and digests ket components [CD0, CD1) of one quartet per lane.
+template <class T, int LA, int LB, int LC, int LD, int CD0, int CD1>
+__device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const QuartetRef q, int lane,
+                                                long long& prim_quartets)
+{
+    using PP = typename FockTypes<T>::PP;
+    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    constexpr int NCH = CD1 - CD0;
+    const T* __restrict__ Dp = static_cast<const T*>(L.density);
+    const int N = L.num_basis;
+
+    T I[NA * NB][NCH];
+#pragma unroll
+    for (int i = 0; i < NA * NB; ++i)
+#pragma unroll
+        for (int j = 0; j < NCH; ++j) I[i][j] = T(0);
+
+    int bfA = 0, bfB = 0, bfC = 0, bfD = 0;
+    T fsym = T(0);
+    if (q.active) {
+        const ShellPairDev bp = L.pairs[q.bra];
+        const ShellPairDev kp = L.pairs[q.ket];
+        bfA = bp.bfA; bfB = bp.bfB; bfC = kp.bfA; bfD = kp.bfB;
+        fsym = T(1);
+        if (bp.A == bp.B) fsym *= T(0.5);
+        if (kp.A == kp.B) fsym *= T(0.5);
+        if (q.bra == q.ket) fsym *= T(0.5);
+        prim_quartets += quartet_block<T, LA, LB, LC, LD, CD0, CD1>(
+            bp, kp, static_cast<const PP*>(L.prim_pairs), static_cast<const T*>(L.boys_table),
+            static_cast<T>(L.schwarz_threshold), I);
+    }
+
+    double* __restrict__ Jp = L.J;
+    double* __restrict__ Kp = L.K;
+    const int bra0 = __shfl_sync(0xffffffffu, q.bra, 0);
+    const bool uniform_bra = __all_sync(0xffffffffu, (!q.active) || q.bra == bra0) && bra0 >= 0;
+    // J'_ab += sum_cd D'_cd v  (a partial sum when the thread holds a component chunk)
+    {
+        T dcd[NCH];
+#pragma unroll
+        for (int cd = CD0; cd < CD1; ++cd)
+            dcd[cd - CD0] = q.active ? Dp[(bfC + cd / ND) * N + bfD + cd % ND] : T(0);
+        const int bfA0 = __shfl_sync(0xffffffffu, bfA, 0), bfB0 = __shfl_sync(0xffffffffu, bfB, 0);
+#pragma unroll
+        for (int ab = 0; ab < NA * NB; ++ab) {
+            T s = T(0);
+#pragma unroll
+            for (int j = 0; j < NCH; ++j) s += dcd[j] * I[ab][j];
+            s *= fsym;
+            if (uniform_bra) {
+                s = warp_sum(s);
+                if (lane == 0) atomicAdd(&Jp[(bfA0 + ab / NB) * N + bfB0 + ab % NB], static_cast<double>(s));
+            } else if (q.active) {
+                atomicAdd(&Jp[(bfA + ab / NB) * N + bfB + ab % NB], static_cast<double>(s));
+            }
+        }
+    }
+    if (!q.active) return;
+    T dab[NA * NB];
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+        for (int ib = 0; ib < NB; ++ib) dab[ia * NB + ib] = Dp[(bfA + ia) * N + bfB + ib];
+    // J'_cd += sum_ab D'_ab v
+#pragma unroll
+    for (int cd = CD0; cd < CD1; ++cd) {
+        T s = T(0);
+#pragma unroll
+        for (int ab = 0; ab < NA * NB; ++ab) s += dab[ab] * I[ab][cd - CD0];
+        atomicAdd(&Jp[(bfC + cd / ND) * N + bfD + cd % ND], static_cast<double>(s * fsym));
+    }
+    // K'_ac += sum_bd D'_bd v ; K'_ad += sum_bc D'_bc v
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia) {
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic) {
+            if (ic * ND + ND <= CD0 || ic * ND >= CD1) continue;  // c not held by this thread
+            T s = T(0);
+#pragma unroll
+            for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                for (int id = 0; id < ND; ++id) {
+                    const int cd = ic * ND + id;
+                    if (cd < CD0 || cd >= CD1) continue;
+                    s += Dp[(bfB + ib) * N + bfD + id] * I[ia * NB + ib][cd - CD0];
+                }
+            atomicAdd(&Kp[(bfA + ia) * N + bfC + ic], static_cast<double>(s * fsym));
+        }
+#pragma unroll
+        for (int id = 0; id < ND; ++id) {
+            bool held = false;
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic) held |= (ic * ND + id >= CD0 && ic * ND + id < CD1);
+            if (!held) continue;
+            T s = T(0);
+#pragma unroll
+            for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                for (int ic = 0; ic < NC; ++ic) {
+                    const int cd = ic * ND + id;
+                    if (cd < CD0 || cd >= CD1) continue;
+                    s += Dp[(bfB + ib) * N + bfC + ic] * I[ia * NB + ib][cd - CD0];
+                }
+            atomicAdd(&Kp[(bfA + ia) * N + bfD + id], static_cast<double>(s * fsym));
+        }
+    }
+    // K'_bd += sum_ac D'_ac v ; K'_bc += sum_ad D'_ad v
+#pragma unroll
+    for (int ib = 0; ib < NB; ++ib) {
+#pragma unroll
+        for (int id = 0; id < ND; ++id) {
+            bool held = false;
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic) held |= (ic * ND + id >= CD0 && ic * ND + id < CD1);
+            if (!held) continue;
+            T s = T(0);
+#pragma unroll
+            for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                for (int ic = 0; ic < NC; ++ic) {
+                    const int cd = ic * ND + id;
+                    if (cd < CD0 || cd >= CD1) continue;
+                    s += Dp[(bfA + ia) * N + bfC + ic] * I[ia * NB + ib][cd - CD0];
+                }
+            atomicAdd(&Kp[(bfB + ib) * N + bfD + id], static_cast<double>(s * fsym));
+        }
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic) {
+            if (ic * ND + ND <= CD0 || ic * ND >= CD1) continue;
+            T s = T(0);
+#pragma unroll
+            for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                for (int id = 0; id < ND; ++id) {
+                    const int cd = ic * ND + id;
+                    if (cd < CD0 || cd >= CD1) continue;
+                    s += Dp[(bfA + ia) * N + bfD + id] * I[ia * NB + ib][cd - CD0];
+                }
+            atomicAdd(&Kp[(bfB + ib) * N + bfC + ic], static_cast<double>(s * fsym));
+        }
+    }
+}
+
 template <class T, int LA, int LB, int LC, int LD>
 __global__ void __launch_bounds__(kFockThreads)
 fock_direct_kernel(const FockClassLaunch launch)
 {
-    using PP = typename FockTypes<T>::PP;
-    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
-
+    static_assert(FockSplit<T, LA, LB, LC, LD>::value == 1, "large classes use the generic kernel");
+    constexpr int NCD = ncart(LC) * ncart(LD);
     const long long total = launch.off[launch.nentry];
     const int lane = threadIdx.x & 31;
-    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-    const T* __restrict__ Dp = static_cast<const T*>(launch.density);
-    const PP* __restrict__ pp = static_cast<const PP*>(launch.prim_pairs);
-    const T* __restrict__ boys_table = static_cast<const T*>(launch.boys_table);
-    const T thr = static_cast<T>(launch.schwarz_threshold);
-    const int N = launch.num_basis;
+    const long long nwarps = (total + 31) >> 5;
+    const long long warp_stride = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
     long long prim_quartets = 0, contracted = 0;
 
-    for (long long base = static_cast<long long>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < total;
-         base += stride) {
-        const long long w = base + lane;
-        const bool active = w < total;
-        int bra = -1, ket = -1;
-        if (active) {
+    for (long long wid = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; wid < nwarps;
+         wid += warp_stride) {
+        const long long w = wid * 32 + lane;
+        QuartetRef q{-1, -1, w < total};
+        if (q.active) {
             const int e = find_entry(launch.off, launch.nentry, w);
-            bra = __ldg(launch.entry_bra + e);
-            ket = launch.ket_base + __ldg(launch.entry_lo + e) + static_cast<int>(w - __ldg(launch.off + e));
-        }
-
-        T I[NA * NB][NC * ND];
-#pragma unroll
-        for (int i = 0; i < NA * NB; ++i)
-#pragma unroll
-            for (int j = 0; j < NC * ND; ++j) I[i][j] = T(0);
-
-        int bfA = 0, bfB = 0, bfC = 0, bfD = 0;
-        T fsym = T(0);
-        if (active) {
-            const ShellPairDev bp = launch.pairs[bra];
-            const ShellPairDev kp = launch.pairs[ket];
-            bfA = bp.bfA; bfB = bp.bfB; bfC = kp.bfA; bfD = kp.bfB;
-            fsym = T(1);
-            if (bp.A == bp.B) fsym *= T(0.5);
-            if (kp.A == kp.B) fsym *= T(0.5);
-            if (bra == ket) fsym *= T(0.5);
-            prim_quartets += quartet_block<T, LA, LB, LC, LD>(bp, kp, pp, boys_table, thr, I);
+            q.bra = __ldg(launch.entry_bra + e);
+            q.ket = launch.ket_base + __ldg(launch.entry_lo + e) + static_cast<int>(w - __ldg(launch.off + e));
             ++contracted;
         }
-
-        // ------------------------------------------------------- digestion
-        double* __restrict__ Jp = launch.J;
-        double* __restrict__ Kp = launch.K;
-        const int bra0 = __shfl_sync(0xffffffffu, bra, 0);
-        const bool uniform_bra = __all_sync(0xffffffffu, (!active) || bra == bra0) && bra0 >= 0;
-        // J'_ab += sum_cd D'_cd v
-        {
-            T dcd[NC * ND];
-#pragma unroll
-            for (int ic = 0; ic < NC; ++ic)
-#pragma unroll
-                for (int id = 0; id < ND; ++id)
-                    dcd[ic * ND + id] = active ? Dp[(bfC + ic) * N + bfD + id] : T(0);
-            const int bfA0 = __shfl_sync(0xffffffffu, bfA, 0), bfB0 = __shfl_sync(0xffffffffu, bfB, 0);
-#pragma unroll
-            for (int ab = 0; ab < NA * NB; ++ab) {
-                T s = T(0);
-#pragma unroll
-                for (int cd = 0; cd < NC * ND; ++cd) s += dcd[cd] * I[ab][cd];
-                s *= fsym;
-                if (uniform_bra) {
-                    s = warp_sum(s);
-                    if (lane == 0) atomicAdd(&Jp[(bfA0 + ab / NB) * N + bfB0 + ab % NB], static_cast<double>(s));
-                } else if (active) {
-                    atomicAdd(&Jp[(bfA + ab / NB) * N + bfB + ab % NB], static_cast<double>(s));
-                }
-            }
-        }
-        if (active) {
-            // J'_cd += sum_ab D'_ab v
-            T dab[NA * NB];
-#pragma unroll
-            for (int ia = 0; ia < NA; ++ia)
-#pragma unroll
-                for (int ib = 0; ib < NB; ++ib) dab[ia * NB + ib] = Dp[(bfA + ia) * N + bfB + ib];
-#pragma unroll
-            for (int cd = 0; cd < NC * ND; ++cd) {
-                T s = T(0);
-#pragma unroll
-                for (int ab = 0; ab < NA * NB; ++ab) s += dab[ab] * I[ab][cd];
-                atomicAdd(&Jp[(bfC + cd / ND) * N + bfD + cd % ND], static_cast<double>(s * fsym));
-            }
-            // K'_ac += sum_bd D'_bd v ; K'_bd += sum_ac D'_ac v
-            {
-                T dbd[NB * ND], dac[NA * NC];
-#pragma unroll
-                for (int ib = 0; ib < NB; ++ib)
-#pragma unroll
-                    for (int id = 0; id < ND; ++id) dbd[ib * ND + id] = Dp[(bfB + ib) * N + bfD + id];
-#pragma unroll
-                for (int ia = 0; ia < NA; ++ia)
-#pragma unroll
-                    for (int ic = 0; ic < NC; ++ic) dac[ia * NC + ic] = Dp[(bfA + ia) * N + bfC + ic];
-#pragma unroll
-                for (int ia = 0; ia < NA; ++ia)
-#pragma unroll
-                    for (int ic = 0; ic < NC; ++ic) {
-                        T s = T(0);
-#pragma unroll
-                        for (int ib = 0; ib < NB; ++ib)
-#pragma unroll
-                            for (int id = 0; id < ND; ++id) s += dbd[ib * ND + id] * I[ia * NB + ib][ic * ND + id];
-                        atomicAdd(&Kp[(bfA + ia) * N + bfC + ic], static_cast<double>(s * fsym));
-                    }
-#pragma unroll
-                for (int ib = 0; ib < NB; ++ib)
-#pragma unroll
-                    for (int id = 0; id < ND; ++id) {
-                        T s = T(0);
-#pragma unroll
-                        for (int ia = 0; ia < NA; ++ia)
-#pragma unroll
-                            for (int ic = 0; ic < NC; ++ic) s += dac[ia * NC + ic] * I[ia * NB + ib][ic * ND + id];
-                        atomicAdd(&Kp[(bfB + ib) * N + bfD + id], static_cast<double>(s * fsym));
-                    }
-            }
-            // K'_ad += sum_bc D'_bc v ; K'_bc += sum_ad D'_ad v
-            {
-                T dbc[NB * NC], dad[NA * ND];
-#pragma unroll
-                for (int ib = 0; ib < NB; ++ib)
-#pragma unroll
-                    for (int ic = 0; ic < NC; ++ic) dbc[ib * NC + ic] = Dp[(bfB + ib) * N + bfC + ic];
-#pragma unroll
-                for (int ia = 0; ia < NA; ++ia)
-#pragma unroll
-                    for (int id = 0; id < ND; ++id) dad[ia * ND + id] = Dp[(bfA + ia) * N + bfD + id];
-#pragma unroll
-                for (int ia = 0; ia < NA; ++ia)
-#pragma unroll
-                    for (int id = 0; id < ND; ++id) {
-                        T s = T(0);
-#pragma unroll
-                        for (int ib = 0; ib < NB; ++ib)
-#pragma unroll
-                            for (int ic = 0; ic < NC; ++ic) s += dbc[ib * NC + ic] * I[ia * NB + ib][ic * ND + id];
-                        atomicAdd(&Kp[(bfA + ia) * N + bfD + id], static_cast<double>(s * fsym));
-                    }
-#pragma unroll
-                for (int ib = 0; ib < NB; ++ib)
-#pragma unroll
-                    for (int ic = 0; ic < NC; ++ic) {
-                        T s = T(0);
-#pragma unroll
-                        for (int ia = 0; ia < NA; ++ia)
-#pragma unroll
-                            for (int id = 0; id < ND; ++id) s += dad[ia * ND + id] * I[ia * NB + ib][ic * ND + id];
-                        atomicAdd(&Kp[(bfB + ib) * N + bfC + ic], static_cast<double>(s * fsym));
-                    }
-            }
-        }
+        process_quartet<T, LA, LB, LC, LD, 0, NCD>(launch, q, lane, prim_quartets);
     }
     // statistics (one atomic per warp): [0] primitive quartets, [1] contracted quartets
     unsigned long long pq = static_cast<unsigned long long>(prim_quartets);
@@ -344,49 +370,9 @@ fock_direct_kernel(const FockClassLaunch launch)
     }
 }
 
-// Stored-ERI path (the reference's computeERIMatrix, src/gpu_manager.cu:434-517):
-// the same contracted quartets, scaled by s_a s_b s_c s_d and written to all
-// eight permutations of a dense N^4 tensor ((i*N+j)*N+k)*N+l.  Every element
-// is written by exactly one quartet (coincident permutations carry equal
-// values), so plain stores suffice.
-template <int LA, int LB, int LC, int LD>
-__global__ void __launch_bounds__(kFockThreads)
-eri_tensor_kernel(const FockClassLaunch launch, const double* __restrict__ scale, double* __restrict__ eri)
-{
-    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
-    const long long total = launch.off[launch.nentry];
-    const long long N = launch.num_basis;
-    for (long long w = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; w < total;
-         w += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int e = find_entry(launch.off, launch.nentry, w);
-        const int bra = __ldg(launch.entry_bra + e);
-        const int ket = launch.ket_base + __ldg(launch.entry_lo + e) + static_cast<int>(w - __ldg(launch.off + e));
-        const ShellPairDev bp = launch.pairs[bra];
-        const ShellPairDev kp = launch.pairs[ket];
-        double I[NA * NB][NC * ND];
-#pragma unroll
-        for (int i = 0; i < NA * NB; ++i)
-#pragma unroll
-            for (int j = 0; j < NC * ND; ++j) I[i][j] = 0.0;
-        quartet_block<double, LA, LB, LC, LD>(bp, kp, static_cast<const PrimPair64*>(launch.prim_pairs),
-                                              static_cast<const double*>(launch.boys_table),
-                                              launch.schwarz_threshold, I);
-        for (int ia = 0; ia < NA; ++ia)
-            for (int ib = 0; ib < NB; ++ib)
-                for (int ic = 0; ic < NC; ++ic)
-                    for (int id = 0; id < ND; ++id) {
-                        const long long a = bp.bfA + ia, b = bp.bfB + ib, c = kp.bfA + ic, d = kp.bfB + id;
-                        const double v = I[ia * NB + ib][ic * ND + id] * scale[a] * scale[b] * scale[c] * scale[d];
-                        eri[((a * N + b) * N + c) * N + d] = v;
-                        eri[((b * N + a) * N + c) * N + d] = v;
-                        eri[((a * N + b) * N + d) * N + c] = v;
-                        eri[((b * N + a) * N + d) * N + c] = v;
-                        eri[((c * N + d) * N + a) * N + b] = v;
-                        eri[((d * N + c) * N + a) * N + b] = v;
-                        eri[((c * N + d) * N + b) * N + a] = v;
-                        eri[((d * N + c) * N + b) * N + a] = v;
-                    }
-    }
-}
+// Classes above the register budget and the stored-ERI tensor: fock_generic.cu
+void launch_fock_generic(bool fp32, const FockClassLaunch& launch, int ncd, int grid, cudaStream_t stream);
+void launch_eri_generic(const FockClassLaunch& launch, int ncd, const double* scale, double* eri, int grid,
+                        cudaStream_t stream);
 
 }  // namespace gb

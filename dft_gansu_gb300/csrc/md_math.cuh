@@ -23,11 +23,13 @@ namespace gb {
 constexpr int kMaxL = 2;            // AO shells up to d (every configured basis)
 constexpr int kMaxLTotal = 4 * kMaxL + 1;  // +1 order for derivative integrals
 constexpr int kBoysOrders = 32;     // tabulated orders 0..31
+constexpr int kBoysExpRow = kBoysOrders;  // extra table row: exp(-x_k)
+constexpr int kBoysRows = kBoysOrders + 1;
 constexpr int kBoysTaylor = 6;      // Taylor terms around a grid point (FP64)
 constexpr int kBoysTaylorF = 4;     // Taylor terms (FP32)
 constexpr double kBoysStep = 1.0 / 32.0;
-constexpr int kBoysPoints = 1281;   // grid x = 0 .. 40
-constexpr double kBoysXMax = 40.0;  // asymptotic branch beyond this (FP64)
+constexpr int kBoysPoints = 2049;   // grid x = 0 .. 64
+constexpr double kBoysXMax = 64.0;  // asymptotic branch beyond this (FP64)
 constexpr float kBoysXMaxF = 30.0f; // asymptotic branch beyond this (FP32)
 constexpr double kPi = 3.14159265358979323846;
 
@@ -74,12 +76,15 @@ __host__ __device__ inline double component_factor(int l, int i)
 }
 
 // ------------------------------------------------------------------ Boys
-// Tabulated F_n(x_k), x_k = k/32, n < kBoysOrders: table[n * kBoysPoints + k].
-// F_{nmax}(x) from a Taylor expansion about the nearest grid point
-// (dF_n/dx = -F_{n+1}), then the stable downward recursion
-// F_{n-1} = (2x F_n + e^{-x}) / (2n - 1).  Beyond the grid: F_0 = sqrt(pi/x)/2
-// (erf(sqrt x) = 1 to the precision of the type) and the upward recursion
-// F_{n+1} = ((2n+1) F_n - e^{-x}) / (2x), stable for large x.
+// Tabulated F_n(x_k), x_k = k/32, n < kBoysOrders: table[n * kBoysPoints + k],
+// plus exp(-x_k) in row kBoysExpRow.  F_{nmax}(x) from a Taylor expansion
+// about the nearest grid point (dF_n/dx = -F_{n+1}), then the stable downward
+// recursion F_{n-1} = (2x F_n + e^{-x}) / (2n - 1), with
+// e^{-x} = e^{-x_k} e^{x_k - x} and the second factor from its degree-6
+// Taylor polynomial (|x_k - x| <= 1/64: error below 1e-16).  Beyond the grid:
+// F_0 = sqrt(pi/x)/2 (erf(sqrt x) = 1 to the precision of the type) and the
+// upward recursion F_{n+1} = ((2n+1) F_n - e^{-x}) / (2x), stable for large
+// x; for x >= 64, e^{-x} is below 1e-27 and is dropped.
 template <int NMAX>
 __host__ __device__ __forceinline__ void boys_fp64(double x, const double* __restrict__ table, double (&F)[NMAX + 1])
 {
@@ -89,19 +94,30 @@ __host__ __device__ __forceinline__ void boys_fp64(double x, const double* __res
         const double* t = table + NMAX * kBoysPoints + k;
         double f = t[(kBoysTaylor - 1) * kBoysPoints];
 #pragma unroll
-        for (int j = kBoysTaylor - 1; j >= 1; --j) f = t[(j - 1) * kBoysPoints] + f * dx / j;
+        for (int j = kBoysTaylor - 1; j >= 1; --j) f = t[(j - 1) * kBoysPoints] + f * dx * (1.0 / j);
         F[NMAX] = f;
         if (NMAX > 0) {
-            const double ex = exp(-x);
+            double e = 1.0 / 720.0;
+            e = e * dx + 1.0 / 120.0;
+            e = e * dx + 1.0 / 24.0;
+            e = e * dx + 1.0 / 6.0;
+            e = e * dx + 0.5;
+            e = e * dx + 1.0;
+            e = e * dx + 1.0;
+            const double ex = table[kBoysExpRow * kBoysPoints + k] * e;
 #pragma unroll
             for (int n = NMAX; n >= 1; --n) F[n - 1] = (2.0 * x * F[n] + ex) * (1.0 / (2 * n - 1));
         }
     } else {
-        const double rx = 1.0 / x;
-        const double ex = (NMAX > 0) ? exp(-x) : 0.0;
-        F[0] = 0.5 * sqrt(kPi * rx);
+#ifdef __CUDA_ARCH__
+        const double r = rsqrt(x);
+#else
+        const double r = 1.0 / sqrt(x);
+#endif
+        const double rx = r * r;
+        F[0] = 0.88622692545275801365 * r;  // sqrt(pi)/2
 #pragma unroll
-        for (int n = 0; n < NMAX; ++n) F[n + 1] = ((n + 0.5) * F[n] - 0.5 * ex) * rx;
+        for (int n = 0; n < NMAX; ++n) F[n + 1] = (n + 0.5) * F[n] * rx;
     }
 }
 

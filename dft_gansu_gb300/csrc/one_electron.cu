@@ -36,7 +36,7 @@ one_electron_kernel(const ShellPairDev* __restrict__ pairs, int begin, int count
         for (int j = 0; j < NB; ++j) s_[i][j] = t_[i][j] = v_[i][j] = 0.0;
     for (int ip = 0; ip < sp.pp_n; ++ip) {
         const PrimPair64 q = pp[sp.pp_off + ip];
-        const double p = q.p, b = q.pad, oo2p = 0.5 / p;
+        const double p = q.p, b = q.b, oo2p = 0.5 * q.invp;
         const double k1 = q.K / kfold;
         HermiteE<double, LA, LB + 2> Ex, Ey, Ez;
         Ex.build(q.PAx, q.PAx + sp.ABx, oo2p);

@@ -205,31 +205,47 @@ int ensure_scf(Engine& e, int m)
             return set_error("cusolverDnDsyevd_bufferSize failed"), HF_ERR_SOLVER;
         if ((st = alloc(w.work, static_cast<size_t>(w.lwork)))) return st;
     }
+    if (!w.syevj_params) {
+        if (cusolverDnCreateSyevjInfo(&w.syevj_params) != CUSOLVER_STATUS_SUCCESS)
+            return set_error("cusolverDnCreateSyevjInfo failed"), HF_ERR_SOLVER;
+        cusolverDnXsyevjSetTolerance(w.syevj_params, 1e-15);
+        cusolverDnXsyevjSetMaxSweeps(w.syevj_params, 100);
+        if (cusolverDnDsyevj_bufferSize(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n, w.W, n, w.eps,
+                                        &w.lwork_j, w.syevj_params) != CUSOLVER_STATUS_SUCCESS)
+            return set_error("cusolverDnDsyevj_bufferSize failed"), HF_ERR_SOLVER;
+        if ((st = alloc(w.work_j, static_cast<size_t>(w.lwork_j)))) return st;
+    }
     w.n = n;
     w.m = m;
     return HF_OK;
 }
 
 // eigen-decomposition of the symmetric A (row-major) into W (column-major
-// eigenvectors) and ascending eigenvalues
-int syevd(Engine& e, const double* A, cudaStream_t s)
+// eigenvectors) and ascending eigenvalues; solver 0 = syevd, 1 = syevj
+int syevd(Engine& e, const double* A, cudaStream_t s, int solver = 0)
 {
     auto& w = e.scf;
     const size_t nn = static_cast<size_t>(w.n) * w.n;
     GB_CUDA_TRY(cudaMemcpyAsync(w.W, A, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (solver == 1) {
+        if (cusolverDnDsyevj(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, w.n, w.W, w.n, w.eps,
+                             w.work_j, w.lwork_j, w.info, w.syevj_params) != CUSOLVER_STATUS_SUCCESS)
+            return set_error("cusolverDnDsyevj failed"), HF_ERR_SOLVER;
+        return HF_OK;
+    }
     if (cusolverDnDsyevd(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, w.n, w.W, w.n, w.eps, w.work,
                          w.lwork, w.info) != CUSOLVER_STATUS_SUCCESS)
         return set_error("cusolverDnDsyevd failed"), HF_ERR_SOLVER;
     return HF_OK;
 }
 
-int coefficients(Engine& e, const double* F, cudaStream_t s)
+int coefficients(Engine& e, const double* F, cudaStream_t s, int solver = 0)
 {
     auto& w = e.scf;
     int st;
     if ((st = gemm_rm(e.cublas, true, false, w.n, w.X, F, w.T1))) return st;   // X^T F
     if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, w.X, w.T2))) return st;  // X^T F X
-    if ((st = syevd(e, w.T2, s))) return st;
+    if ((st = syevd(e, w.T2, s, solver))) return st;
     return gemm_rm(e.cublas, false, true, w.n, w.X, w.W, w.C);  // C = X C'
 }
 
@@ -298,6 +314,8 @@ void hf_scf_options_default(hf_scf_options* o)
     o->mixed_threshold = 1e-7;
     o->incremental = 0;
     o->rebuild_every = 0;
+    o->full_build_precision = HF_PRECISION_FP64;
+    o->eigensolver = 0;
     o->verbose = 0;
 }
 
@@ -358,10 +376,15 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     GB_CUDA_TRY(cudaMemsetAsync(e.d_counters, 0, kCounterSlots * sizeof(unsigned long long), s));
     GB_CUDA_TRY(cudaMemsetAsync(w.info, 0, 4 * sizeof(int), s));
 
-    cudaEvent_t f0, f1;
+    cudaEvent_t f0, f1, c0, c1, q0, q1;
     cudaEventCreate(&f0);
     cudaEventCreate(&f1);
-    double fock_ms = 0.0;
+    cudaEventCreate(&c0);
+    cudaEventCreate(&c1);
+    cudaEventCreate(&q0);
+    cudaEventCreate(&q1);
+    double fock_ms = 0.0, diag_ms = 0.0, diis_ms = 0.0;
+    bool diis_timed = false;
     int fock_builds = 0;
     double* h_energy = nullptr;
     cudaMallocHost(&h_energy, sizeof(double));
@@ -377,7 +400,8 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
             GB_LAUNCH_CHECK();
             if ((r = build_jk(e, w.dD, nullptr, nullptr, opt.precision, opt.mixed_threshold, s))) return r;
         } else {
-            if ((r = build_jk(e, w.D, nullptr, nullptr, opt.precision, opt.mixed_threshold, s))) return r;
+            const int prec = (opt.precision == HF_PRECISION_MIXED) ? opt.full_build_precision : opt.precision;
+            if ((r = build_jk(e, w.D, nullptr, nullptr, prec, opt.mixed_threshold, s))) return r;
         }
         fock_from_jk_kernel<<<grid_nn(nn), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, w.H, n, incremental ? 1 : 0, w.G, w.F);
         GB_LAUNCH_CHECK();
@@ -386,24 +410,24 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         ++fock_builds;
         return HF_OK;
     };
-    auto elapsed = [&]() {
+    auto elapsed = [&](cudaEvent_t a, cudaEvent_t b) {
         float ms = 0.f;
-        cudaEventSynchronize(f1);
-        cudaEventElapsedTime(&ms, f0, f1);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
         return static_cast<double>(ms);
     };
 
     const auto t_setup = std::chrono::steady_clock::now();
     // core Hamiltonian, X, core guess
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
-    if ((st = syevd(e, w.S, s))) return st;
+    if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
     transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
     GB_LAUNCH_CHECK();
-    if ((st = coefficients(e, w.H, s))) return st;
+    if ((st = coefficients(e, w.H, s, opt.eigensolver))) return st;
     density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
     GB_LAUNCH_CHECK();
     if ((st = fock_build(true))) return st;
-    fock_ms += elapsed();
+    fock_ms += elapsed(f0, f1);
     res->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_setup).count();
 
     cudaEvent_t l0, l1;
@@ -414,14 +438,18 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     int iter = 0, diis_iter = 0;
     bool converged = false;
     while (iter < opt.max_iter) {
-        if ((st = coefficients(e, w.F, s))) return st;
+        cudaEventRecord(c0, s);
+        if ((st = coefficients(e, w.F, s, opt.eigensolver))) return st;
         density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
         GB_LAUNCH_CHECK();
+        cudaEventRecord(c1, s);
         if ((st = fock_build(false))) return st;
         energy_kernel<<<1, 1024, 0, s>>>(w.D, w.H, w.F, nn, e.d_scalar + 4);
         GB_LAUNCH_CHECK();
         GB_CUDA_TRY(cudaMemcpyAsync(h_energy, e.d_scalar + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
-        fock_ms += elapsed();
+        fock_ms += elapsed(f0, f1);
+        diag_ms += elapsed(c0, c1);
+        if (diis_timed) diis_ms += elapsed(q0, q1);
         GB_CUDA_TRY(cudaStreamSynchronize(s));
         energy = *h_energy;
         const double diff = std::fabs(energy - prev);
@@ -433,11 +461,14 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         ++iter;
         prev = energy;
         // DIIS update (Convergence_RHF_DIIS::get_new_fock_matrix)
+        cudaEventRecord(q0, s);
+        diis_timed = true;
         const int slot = diis_iter % m;
         if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, opt.diis_include_transform != 0, s))) return st;
         GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + slot * nn, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
         const int nprev = std::min(diis_iter + 1, m);
         if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, w.F, s))) return st;
+        cudaEventRecord(q1, s);
         ++diis_iter;
     }
     cudaEventRecord(l1, s);
@@ -459,8 +490,9 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         prim32 += cnt[4 * c + 2];
     }
     cudaFreeHost(h_energy);
-    cudaEventDestroy(f0);
-    cudaEventDestroy(f1);
+    for (cudaEvent_t ev : {f0, f1, c0, c1, q0, q1}) cudaEventDestroy(ev);
+    res->diag_ms_total = diag_ms;
+    res->diis_ms_total = diis_ms;
     res->electronic_energy = energy;
     res->total_energy = energy + res->nuclear_repulsion;
     res->iterations = iter;

@@ -167,6 +167,8 @@ typedef struct {
     double mixed_threshold;         /* FP32 cut for Q_ab*Q_cd*max|dD| */
     int incremental;                /* 1: build G(dD) and accumulate (mixed tier) */
     int rebuild_every;              /* full rebuild period for the incremental build, 0 = never */
+    int full_build_precision;       /* precision of full (non-incremental) builds under the mixed tier */
+    int eigensolver;                /* 0: cuSOLVER syevd (divide and conquer), 1: syevj (Jacobi) */
     int verbose;                    /* print per-iteration lines like the reference */
 } hf_scf_options;
 
@@ -179,6 +181,8 @@ typedef struct {
     double fock_ms_total;           /* summed device time of the Fock builds */
     double scf_ms_total;            /* SCF loop (iterations only), CUDA events on the stream */
     double setup_ms;                /* core Hamiltonian + X + guess */
+    double diag_ms_total;           /* F' = X^T F X, eigensolver, C = X C', density (loop) */
+    double diis_ms_total;           /* DIIS error, B matrix, solve and extrapolation (loop) */
     long long fp64_quartets;        /* summed over all Fock builds */
     long long fp32_quartets;
 } hf_scf_result;
