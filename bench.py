@@ -29,7 +29,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "SCF ms/iter & gradient ms, mixed vs FP64 on 1 GB300 at |ΔE|≤1e-6 Eh"
 WORKLOAD = "RHF/6-31G* n-decane C10H22 (N=194 Cartesian, 238 primitive shells), zig-zag + N(0,0.02 A) jitter"
-MIXED_THRESHOLD = 1e-5
+MIXED_THRESHOLD = 0.1
 CONV = 1e-8
 
 
@@ -234,7 +234,8 @@ def run_ours(args, rank, world):
     nel = mol.num_electrons
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     opts_mixed = {"convergence_threshold": CONV, "precision": gg.HF_PRECISION_MIXED,
-                  "mixed_threshold": args.mixed_threshold, "incremental": 1, "rebuild_every": 0}
+                  "mixed_threshold": args.mixed_threshold, "incremental": 1, "rebuild_every": 0,
+                  "full_build_precision": gg.HF_PRECISION_FP64}
     opts_fp64 = {"convergence_threshold": CONV}
 
     def solve(opts):
@@ -320,13 +321,17 @@ def run_ours(args, rank, world):
             "metric": METRIC, "value": ms_mx, "unit": "ms/iter", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "seed": args.seed, "precision": "mixed (FP32 quartets when "
-                       f"Q_ab*Q_cd*max|dD| < {args.mixed_threshold}, incremental dD builds)",
+            "config": {"workload": WORKLOAD, "seed": args.seed, "precision": "mixed (FP64 first build, then "
+                       f"incremental dD builds with FP32 quartets where Q_ab*Q_cd*max|dD| < {args.mixed_threshold})",
                        "convergence": CONV, "l2": "flushed (512 MB write) before every step",
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "fp64_ms_per_iter": ms_64, "mixed_speedup_vs_fp64": ms_64 / ms_mx,
             "delta_E_mixed_vs_fp64": dE, "energy_fp64": fp64[0]["total_energy"],
             "iterations": {"mixed": mixed[0]["iterations"], "fp64": fp64[0]["iterations"]},
+            "breakdown_ms_per_iter": {
+                "fock": statistics.mean(r["fock_ms_total"] / (r["iterations"] + 1) for r in mixed),
+                "diag": statistics.mean(r["diag_ms_total"] / max(r["iterations"], 1) for r in mixed),
+                "diis": statistics.mean(r["diis_ms_total"] / max(r["iterations"], 1) for r in mixed)},
             "gradient_ms": None,
             "e2e": {"value": statistics.mean(e2e_vals), "unit": "ms/iter", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -171,8 +171,13 @@ def test_scf_mixed_within_tolerance(built_library, cuda, incremental):
     g, atoms, gbs = _case("propane_6-31g_st")
     mol, eng = _engine(atoms, gbs)
     r64 = eng.rhf_scf(mol.num_electrons, {"convergence_threshold": 1e-10}, want_matrices=True)
+    # incremental: FP64 first build, then dD builds under the mixed rule; otherwise
+    # every (full) build under the mixed rule
     rmx = eng.rhf_scf(mol.num_electrons, {"convergence_threshold": 1e-10, "precision": gg.HF_PRECISION_MIXED,
-                                          "mixed_threshold": 1e-7, "incremental": incremental},
+                                          "mixed_threshold": 1e-7 if not incremental else 1e-2,
+                                          "incremental": incremental,
+                                          "full_build_precision": gg.HF_PRECISION_MIXED if not incremental
+                                          else gg.HF_PRECISION_FP64},
                       want_matrices=True)
     assert rmx["converged"] == 1
     assert abs(rmx["total_energy"] - r64["total_energy"]) < 1e-6
