@@ -108,6 +108,7 @@ SIGNATURES = {
     "hf_compute_jk_direct": (_I, [_P, _P, _P, _P, _I, _D, _P]),
     "hf_compute_diis_error": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_diis": (_I, [_P, _P, _P, _P, _I, _P]),
+    "hf_compute_fock_diis_noalloc": (_I, [_P, _P, _P, _I, _I, _P]),
     "hf_scf_options_default": (None, [C.POINTER(ScfOptions)]),
     "hf_rhf_scf": (_I, [_P, _I, C.POINTER(ScfOptions), C.POINTER(ScfResult), _P, _P, _P, _P]),
 }

@@ -157,6 +157,20 @@ int hf_compute_diis_error(hf_engine* eng, const double* d_overlap, const double*
 int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d_focks, double* d_new_fock,
                          int num_prev, void* stream);
 
+/* DIIS extrapolation that allocates nothing (no reference counterpart: the
+ * reference's computeFockMatrixDIIS allocates on every call).  For callers
+ * that cannot allocate device memory while an SCF step runs -- a CUDA graph
+ * being recorded, an application whose device memory belongs to its own pool,
+ * a thread that must not synchronise the device.  Same result as
+ * hf_compute_fock_diis without an engine: F = sum_i c_i F_i from num_prev
+ * (2..16) stored error/Fock pairs, N = num_basis.  Its scratch is a static
+ * device array of 280 doubles held by every GPU that loads the library; the
+ * first call on a device looks its address up (make that call before any
+ * stream capture).  Calls that overlap on the GPU share the scratch and race:
+ * serialise them. */
+int hf_compute_fock_diis_noalloc(const double* d_errors, const double* d_focks, double* d_new_fock, int num_prev,
+                                 int num_basis, void* stream);
+
 /* ------------------------------------------------------------------- SCF */
 typedef struct {
     int max_iter;                   /* reference default 100 */
