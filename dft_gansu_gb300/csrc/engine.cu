@@ -178,8 +178,8 @@ int dev_alloc(T*& p, size_t n)
 Engine::~Engine()
 {
     void* ptrs[] = {d_pairs,  d_pp64,   d_pp32,       d_boys64,     d_boys32,     d_scale,   d_atoms,
-                    d_entry_bra, d_entry_cnt, d_entry_zero, d_pair_qs, d_off_static, d_cp_meta, plan.off64, plan.off32,
-                    plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
+                    d_entry_bra, d_entry_cnt, d_entry_lo0, d_pair_qs, d_off_static, d_cp_meta, plan.off64, plan.off32,
+                    plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_Jp32, d_Kp32, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
                     scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
                     scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j};
     for (void* p : ptrs)
@@ -288,10 +288,23 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
                     tmp.push_back(std::move(t));
                 }
             }
-            std::stable_sort(tmp.begin(), tmp.end(), [](const Tmp& a, const Tmp& b) { return a.sp.Qs > b.sp.Qs; });
-            for (auto& t : tmp) {
+            // groups of equal primitive-pair count (so the lanes of a warp run
+            // the same primitive loops), each group sorted by Qs descending
+            std::stable_sort(tmp.begin(), tmp.end(), [](const Tmp& a, const Tmp& b) {
+                if (a.pp.size() != b.pp.size()) return a.pp.size() > b.pp.size();
+                return a.sp.Qs > b.sp.Qs;
+            });
+            for (size_t k = 0; k < tmp.size(); ++k) {
+                Tmp& t = tmp[k];
+                if (k == 0 || tmp[k - 1].pp.size() != t.pp.size())
+                    pc.groups.push_back({static_cast<int>(k), 0});
+                pc.groups.back().second++;
                 t.sp.pp_off = static_cast<int>(e->pp64.size());
                 t.sp.pp_n = static_cast<int>(t.pp.size());
+                t.sp.fABx = static_cast<float>(t.sp.ABx);
+                t.sp.fABy = static_cast<float>(t.sp.ABy);
+                t.sp.fABz = static_cast<float>(t.sp.ABz);
+                t.sp.fQmax = static_cast<float>(t.sp.Qmax);
                 e->pp64.insert(e->pp64.end(), t.pp.begin(), t.pp.end());
                 e->pairs.push_back(t.sp);
             }
@@ -310,19 +323,22 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
             long long acc = 0;
             for (int i = 0; i < px.count; ++i) {
                 const double qi = e->pairs[px.begin + i].Qs;
-                // kets sorted by Qs descending: count those with qi*qj >= thr
-                int lo = 0, hi = py.count;
-                while (lo < hi) {
-                    const int mid = (lo + hi) / 2;
-                    if (qi * e->pairs[py.begin + mid].Qs >= thr) lo = mid + 1; else hi = mid;
+                for (const auto& g : py.groups) {
+                    // kets of a group sorted by Qs descending: count those with qi*qj >= thr
+                    int lo = 0, hi = g.second;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) / 2;
+                        if (qi * e->pairs[py.begin + g.first + mid].Qs >= thr) lo = mid + 1; else hi = mid;
+                    }
+                    int cnt = lo;
+                    if (X == Y) cnt = std::min(cnt, i - g.first + 1);  // each unordered pair once
+                    if (cnt <= 0) continue;
+                    e->entry_bra.push_back(px.begin + i);
+                    e->entry_lo0.push_back(g.first);
+                    e->entry_cnt.push_back(cnt);
+                    acc += cnt;
+                    e->off_static.push_back(acc);
                 }
-                int cnt = lo;
-                if (X == Y) cnt = std::min(cnt, i + 1);
-                if (cnt <= 0) continue;
-                e->entry_bra.push_back(px.begin + i);
-                e->entry_cnt.push_back(cnt);
-                acc += cnt;
-                e->off_static.push_back(acc);
             }
             cp.nentry = static_cast<int>(e->entry_bra.size()) - cp.entry_begin;
             cp.n_survivors = acc;
@@ -352,7 +368,7 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
     }
     std::vector<double> qs(e->pairs.size());
     for (size_t i = 0; i < qs.size(); ++i) qs[i] = e->pairs[i].Qs;
-    std::vector<int> zeros(e->entry_bra.size(), 0);
+    const std::vector<int>& lo0 = e->entry_lo0;
     e->d_pairs = dev_upload(e->pairs, st);
     e->d_pp64 = dev_upload(e->pp64, st);
     e->d_pp32 = dev_upload(pp32, st);
@@ -362,7 +378,7 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
     e->d_atoms = dev_upload(atom4, st);
     e->d_entry_bra = dev_upload(e->entry_bra, st);
     e->d_entry_cnt = dev_upload(e->entry_cnt, st);
-    e->d_entry_zero = dev_upload(zeros, st);
+    e->d_entry_lo0 = dev_upload(lo0, st);
     e->d_pair_qs = dev_upload(qs, st);
     e->d_off_static = dev_upload(e->off_static, st);
     {
@@ -382,6 +398,7 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
     if ((st = dev_alloc(e->plan.off64, noff)) || (st = dev_alloc(e->plan.off32, noff)) ||
         (st = dev_alloc(e->plan.lo32, e->entry_bra.size())) || (st = dev_alloc(e->d_Dp64, nn)) ||
         (st = dev_alloc(e->d_Dp32, nn)) || (st = dev_alloc(e->d_Jp, nn)) || (st = dev_alloc(e->d_Kp, nn)) ||
+        (st = dev_alloc(e->d_Jp32, nn)) || (st = dev_alloc(e->d_Kp32, nn)) ||
         (st = dev_alloc(e->d_scalar, 16)) || (st = dev_alloc(e->d_counters, kCounterSlots)))
         return st;
     if (cudaMemset(e->d_counters, 0, kCounterSlots * sizeof(unsigned long long)) != cudaSuccess)
@@ -392,7 +409,7 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
     e->bytes_h2d = static_cast<long long>(
         e->pairs.size() * sizeof(ShellPairDev) + e->pp64.size() * sizeof(PrimPair64) + pp32.size() * sizeof(PrimPair32) +
         boys.size() * (sizeof(double) + sizeof(float)) + e->scale.size() * sizeof(double) + atom4.size() * sizeof(double) +
-        (2 * e->entry_bra.size() + zeros.size()) * sizeof(int) + qs.size() * sizeof(double) +
+        (3 * e->entry_bra.size()) * sizeof(int) + qs.size() * sizeof(double) +
         e->off_static.size() * sizeof(long long) + 4 * e->class_pairs.size() * sizeof(int));
     *out = reinterpret_cast<hf_engine*>(e.release());
     return HF_OK;

@@ -5,6 +5,7 @@
 #include <cusolverDn.h>
 
 #include <array>
+#include <utility>
 #include <vector>
 
 #include "engine_types.hpp"
@@ -27,6 +28,7 @@ struct Shell {
 struct PairClass {
     int la, lb;
     int begin, count;  // global pair index range
+    std::vector<std::pair<int, int>> groups;  // (class-relative start, size) of equal primitive-pair count
 };
 
 // bra class X >= ket class Y
@@ -57,7 +59,8 @@ struct Engine {
     std::vector<PrimPair64> pp64;
     std::vector<PairClass> pair_classes;
     std::vector<ClassPair> class_pairs;
-    std::vector<int> entry_bra, entry_cnt;  // per bra entry
+    std::vector<int> entry_bra, entry_cnt;  // per (bra, ket group) entry
+    std::vector<int> entry_lo0;              // class-relative first ket of the entry's group
     std::vector<long long> off_static;      // per class pair, nentry+1 (packed: entry_begin + cp)
     long long total_survivors = 0;
     std::vector<double> prim_bound;         // per primitive of the input list pair (dense), filled lazily
@@ -72,7 +75,7 @@ struct Engine {
     double* d_atoms = nullptr;  // natom x 4: x, y, z, Z
     int* d_entry_bra = nullptr;
     int* d_entry_cnt = nullptr;
-    int* d_entry_zero = nullptr;
+    int* d_entry_lo0 = nullptr;
     double* d_pair_qs = nullptr;  // Qs per global pair (for the mixed plan)
     long long* d_off_static = nullptr;
     int* d_cp_meta = nullptr;     // per class pair: entry_begin | nentry | ket_base | off_base
@@ -81,6 +84,9 @@ struct Engine {
     float* d_Dp32 = nullptr;
     double* d_Jp = nullptr;
     double* d_Kp = nullptr;
+    float* d_Jp32 = nullptr;   // FP32-tier accumulators (FP32 accumulation)
+    float* d_Kp32 = nullptr;
+    bool last_mixed = false;   // whether the last build used the FP32 accumulators
     double* d_scalar = nullptr;  // small scratch scalars (8 doubles)
     unsigned long long* d_counters = nullptr;  // [class pair][precision][prim, contracted]
     long long bytes_h2d = 0;                   // bytes uploaded by engine creation

@@ -23,8 +23,9 @@ struct ShellPairDev {
     double Qmax;           // max primitive-pair Schwarz bound (reference definition)
     double Qs;             // sum of primitive-pair bounds (bounds the contracted integral)
     double pad;
+    float fABx, fABy, fABz, fQmax;  // FP32-tier copies (no conversions in FP32 kernels)
 };
-static_assert(sizeof(ShellPairDev) == 80, "ShellPairDev layout");
+static_assert(sizeof(ShellPairDev) == 96, "ShellPairDev layout");
 
 // One primitive pair of a shell pair.  K carries the contraction coefficients,
 // the component-independent part of the primitive norms, exp(-ab/p |AB|^2)
@@ -51,6 +52,8 @@ struct FockClassLaunch {
     const void* density;           // D' (double* or float*), N x N
     double* J;                     // J' accumulator
     double* K;                     // K' accumulator
+    float* J32;                    // FP32-tier accumulators
+    float* K32;
     const long long* off;          // nentry+1 prefix offsets
     const int* entry_bra;          // global bra pair index per entry
     const int* entry_lo;           // first ket (class-relative) per entry

@@ -111,6 +111,7 @@ __device__ long long block_scan_exclusive(long long v, long long* smem, long lon
 struct PlanArgs {
     const int* entry_bra;
     const int* entry_cnt;
+    const int* entry_lo0;       // class-relative first ket of the entry's group
     const double* pair_qs;
     const int* cp_entry_begin;  // per class pair
     const int* cp_nentry;
@@ -139,15 +140,16 @@ __global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
         if (i < ne) {
             const int e = eb + i;
             const int cnt = a.entry_cnt[e];
+            const int k0 = kb + a.entry_lo0[e];
             const double qb = a.pair_qs[a.entry_bra[e]] * dm;
-            int lo = 0, hi = cnt;  // first ket with qb*Qs_ket < thr
+            int lo = 0, hi = cnt;  // first ket of the group with qb*Qs_ket < thr
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (qb * a.pair_qs[kb + mid] >= a.mixed_threshold) lo = mid + 1; else hi = mid;
+                if (qb * a.pair_qs[k0 + mid] >= a.mixed_threshold) lo = mid + 1; else hi = mid;
             }
             c64 = lo;
             c32 = cnt - lo;
-            a.lo32[e] = lo;
+            a.lo32[e] = a.entry_lo0[e] + lo;
         }
         long long t64, t32;
         const long long x64 = block_scan_exclusive(c64, smem, t64);
@@ -162,6 +164,7 @@ __global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
 }
 
 __global__ void finish_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
+                              const float* __restrict__ Jp32, const float* __restrict__ Kp32,
                               const double* __restrict__ s, const double* __restrict__ H, int n,
                               double* __restrict__ J, double* __restrict__ K, double* __restrict__ F)
 {
@@ -171,8 +174,13 @@ __global__ void finish_kernel(const double* __restrict__ Jp, const double* __res
         const int i = static_cast<int>(k / n), j = static_cast<int>(k % n);
         const long long kt = static_cast<long long>(j) * n + i;
         const double ss = s[i] * s[j];
-        const double jv = 2.0 * (Jp[k] + Jp[kt]) * ss;
-        const double kv = (Kp[k] + Kp[kt]) * ss;
+        double jsum = Jp[k] + Jp[kt], ksum = Kp[k] + Kp[kt];
+        if (Jp32) {
+            jsum += static_cast<double>(Jp32[k]) + static_cast<double>(Jp32[kt]);
+            ksum += static_cast<double>(Kp32[k]) + static_cast<double>(Kp32[kt]);
+        }
+        const double jv = 2.0 * jsum * ss;
+        const double kv = ksum * ss;
         if (J) J[k] = jv;
         if (K) K[k] = kv;
         if (F) F[k] = H[k] + jv - 0.5 * kv;
@@ -195,6 +203,8 @@ FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off,
     L.density = fp32 ? static_cast<const void*>(e.d_Dp32) : static_cast<const void*>(e.d_Dp64);
     L.J = e.d_Jp;
     L.K = e.d_Kp;
+    L.J32 = e.d_Jp32;
+    L.K32 = e.d_Kp32;
     L.off = off + cp.entry_begin + cpi;
     L.entry_bra = e.d_entry_bra + cp.entry_begin;
     L.entry_lo = lo + cp.entry_begin;
@@ -226,6 +236,11 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
     if (st) return st;
     GB_CUDA_TRY(cudaMemsetAsync(e.d_Jp, 0, nn * sizeof(double), s));
     GB_CUDA_TRY(cudaMemsetAsync(e.d_Kp, 0, nn * sizeof(double), s));
+    e.last_mixed = mixed;
+    if (mixed) {
+        GB_CUDA_TRY(cudaMemsetAsync(e.d_Jp32, 0, nn * sizeof(float), s));
+        GB_CUDA_TRY(cudaMemsetAsync(e.d_Kp32, 0, nn * sizeof(float), s));
+    }
     const int ncp = static_cast<int>(e.class_pairs.size());
     if (!mixed) {
         for (int c = 0; c < ncp; ++c) {
@@ -235,7 +250,7 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
             const PairClass& Y = e.pair_classes[cp.Y];
             FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
             if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
-            f(false, make_launch(e, c, false, e.d_off_static, e.d_entry_zero), grid_for(cp.n_survivors, e.num_sms), s);
+            f(false, make_launch(e, c, false, e.d_off_static, e.d_entry_lo0), grid_for(cp.n_survivors, e.num_sms), s);
             GB_LAUNCH_CHECK();
         }
     } else {
@@ -244,6 +259,7 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
         PlanArgs a;
         a.entry_bra = e.d_entry_bra;
         a.entry_cnt = e.d_entry_cnt;
+        a.entry_lo0 = e.d_entry_lo0;
         a.pair_qs = e.d_pair_qs;
         a.cp_entry_begin = e.d_cp_meta;
         a.cp_nentry = e.d_cp_meta + ncp;
@@ -266,7 +282,7 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
             FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
             if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
             const int grid = grid_for(cp.n_survivors, e.num_sms);
-            f(false, make_launch(e, c, false, e.plan.off64, e.d_entry_zero), grid, s);
+            f(false, make_launch(e, c, false, e.plan.off64, e.d_entry_lo0), grid, s);
             GB_LAUNCH_CHECK();
             f(true, make_launch(e, c, true, e.plan.off32, e.plan.lo32), grid, s);
             GB_LAUNCH_CHECK();
@@ -274,7 +290,8 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
     }
     if (d_J || d_K) {
         const int grid = static_cast<int>(std::min<long long>((static_cast<long long>(nn) + 255) / 256, 4096));
-        finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, nullptr, e.num_basis, d_J, d_K, nullptr);
+        finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, mixed ? e.d_Jp32 : nullptr, mixed ? e.d_Kp32 : nullptr,
+                                           e.d_scale, nullptr, e.num_basis, d_J, d_K, nullptr);
         GB_LAUNCH_CHECK();
     }
     return HF_OK;
@@ -285,7 +302,9 @@ int finish_fock(Engine& e, const double* d_H, const double* d_J, const double* d
     (void)d_J; (void)d_K;
     const long long nn = static_cast<long long>(e.num_basis) * e.num_basis;
     const int grid = static_cast<int>(std::min<long long>((nn + 255) / 256, 4096));
-    finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, d_H, e.num_basis, nullptr, nullptr, d_F);
+    finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, e.last_mixed ? e.d_Jp32 : nullptr,
+                                       e.last_mixed ? e.d_Kp32 : nullptr, e.d_scale, d_H, e.num_basis, nullptr, nullptr,
+                                       d_F);
     GB_LAUNCH_CHECK();
     return HF_OK;
 }
@@ -363,7 +382,7 @@ int hf_compute_eri_matrix(hf_engine* eng, double* d_eri, void* stream)
         const PairClass& Y = e.pair_classes[cp.Y];
         EriLauncher f = eri_launcher(X.la, X.lb, Y.la, Y.lb);
         if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
-        f(make_launch(e, c, false, e.d_off_static, e.d_entry_zero), e.d_scale, d_eri, grid_for(cp.n_survivors, e.num_sms),
+        f(make_launch(e, c, false, e.d_off_static, e.d_entry_lo0), e.d_scale, d_eri, grid_for(cp.n_survivors, e.num_sms),
           s);
         GB_LAUNCH_CHECK();
     }

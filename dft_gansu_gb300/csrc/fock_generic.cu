@@ -117,22 +117,23 @@ __device__ int quartet_column(const ShellPairDev& bp, const ShellPairDev& kp, in
     T fx[kEI * kEI * kET], fy[kEI * kEI * kET], fz[kEI * kEI * kET];
     T Fs[kLT + 1], r[kHR], xh[kHAB];
     int count = 0;
-    const T qket_max = static_cast<T>(kp.Qmax);
+    const typename TierTypes<T>::Geom gb_(bp), gk_(kp);
+    const T qket_max = gk_.qmax;
     for (int ip = 0; ip < bp.pp_n; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
         if (pb.Q * qket_max < thr) continue;
         const T oo2p = T(0.5) * pb.invp;
-        hermite_e_rt<T>(la, lb, pb.PAx, pb.PAx + static_cast<T>(bp.ABx), oo2p, ex);
-        hermite_e_rt<T>(la, lb, pb.PAy, pb.PAy + static_cast<T>(bp.ABy), oo2p, ey);
-        hermite_e_rt<T>(la, lb, pb.PAz, pb.PAz + static_cast<T>(bp.ABz), oo2p, ez);
+        hermite_e_rt<T>(la, lb, pb.PAx, pb.PAx + gb_.x, oo2p, ex);
+        hermite_e_rt<T>(la, lb, pb.PAy, pb.PAy + gb_.y, oo2p, ey);
+        hermite_e_rt<T>(la, lb, pb.PAz, pb.PAz + gb_.z, oo2p, ez);
         for (int jq = 0; jq < kp.pp_n; ++jq) {
             const PP pk = pp[kp.pp_off + jq];
             if (pb.Q * pk.Q < thr) continue;
             ++count;
             const T oo2q = T(0.5) * pk.invp;
-            hermite_e_rt<T>(lc, ld, pk.PAx, pk.PAx + static_cast<T>(kp.ABx), oo2q, fx);
-            hermite_e_rt<T>(lc, ld, pk.PAy, pk.PAy + static_cast<T>(kp.ABy), oo2q, fy);
-            hermite_e_rt<T>(lc, ld, pk.PAz, pk.PAz + static_cast<T>(kp.ABz), oo2q, fz);
+            hermite_e_rt<T>(lc, ld, pk.PAx, pk.PAx + gk_.x, oo2q, fx);
+            hermite_e_rt<T>(lc, ld, pk.PAy, pk.PAy + gk_.y, oo2q, fy);
+            hermite_e_rt<T>(lc, ld, pk.PAz, pk.PAz + gk_.z, oo2q, fz);
             const T rr = fast_rsqrt(pb.p + pk.p);
             const T rho = pb.p * pk.p * (rr * rr);
             const T X = pb.Px - pk.Px, Y = pb.Py - pk.Py, Z = pb.Pz - pk.Pz;
@@ -189,6 +190,8 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
     const long long nwarps = ((total + 31) >> 5) * ncd;
     const long long warp_stride = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
     const T* __restrict__ Dp = static_cast<const T*>(L.density);
+    T* __restrict__ Jp = TierTypes<T>::J(L);
+    T* __restrict__ Kp = TierTypes<T>::K(L);
     const int N = L.num_basis;
     long long prim_quartets = 0, contracted = 0;
     T I[kNAB];
@@ -233,17 +236,17 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
         if (uniform_bra) {
             for (int ab = 0; ab < na0 * nb0; ++ab) {
                 const T s = warp_sum(dcd * I[ab] * fsym);
-                if (lane == 0) atomicAdd(&L.J[(bfA0 + ab / nb0) * N + bfB0 + ab % nb0], static_cast<double>(s));
+                if (lane == 0) atomicAdd(&Jp[(bfA0 + ab / nb0) * N + bfB0 + ab % nb0], s);
             }
         } else if (active) {
             for (int ab = 0; ab < na * nb; ++ab)
-                atomicAdd(&L.J[(bp.bfA + ab / nb) * N + bp.bfB + ab % nb], static_cast<double>(dcd * I[ab] * fsym));
+                atomicAdd(&Jp[(bp.bfA + ab / nb) * N + bp.bfB + ab % nb], dcd * I[ab] * fsym);
         }
         if (!active) continue;
         T jcd = T(0);
         for (int ia = 0; ia < na; ++ia)
             for (int ib = 0; ib < nb; ++ib) jcd += Dp[(bp.bfA + ia) * N + bp.bfB + ib] * I[ia * nb + ib];
-        atomicAdd(&L.J[c * N + d], static_cast<double>(jcd * fsym));
+        atomicAdd(&Jp[c * N + d], jcd * fsym);
         for (int ia = 0; ia < na; ++ia) {
             const int a = bp.bfA + ia;
             T kac = T(0), kad = T(0);
@@ -252,8 +255,8 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
                 kac += Dp[b * N + d] * I[ia * nb + ib];
                 kad += Dp[b * N + c] * I[ia * nb + ib];
             }
-            atomicAdd(&L.K[a * N + c], static_cast<double>(kac * fsym));
-            atomicAdd(&L.K[a * N + d], static_cast<double>(kad * fsym));
+            atomicAdd(&Kp[a * N + c], kac * fsym);
+            atomicAdd(&Kp[a * N + d], kad * fsym);
         }
         for (int ib = 0; ib < nb; ++ib) {
             const int b = bp.bfB + ib;
@@ -263,8 +266,8 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
                 kbd += Dp[a * N + c] * I[ia * nb + ib];
                 kbc += Dp[a * N + d] * I[ia * nb + ib];
             }
-            atomicAdd(&L.K[b * N + d], static_cast<double>(kbd * fsym));
-            atomicAdd(&L.K[b * N + c], static_cast<double>(kbc * fsym));
+            atomicAdd(&Kp[b * N + d], kbd * fsym);
+            atomicAdd(&Kp[b * N + c], kbc * fsym);
         }
     }
     unsigned long long pq = static_cast<unsigned long long>(prim_quartets);

@@ -74,6 +74,33 @@ __device__ __forceinline__ T warp_sum(T v)
 __device__ __forceinline__ double fast_rsqrt(double x) { return rsqrt(x); }
 __device__ __forceinline__ float fast_rsqrt(float x) { return rsqrtf(x); }
 
+// Pair geometry in the arithmetic type of the tier (A-B and the largest
+// primitive bound), read without conversions.
+struct PairGeom64 {
+    double x, y, z, qmax;
+    __device__ __forceinline__ explicit PairGeom64(const ShellPairDev& p) : x(p.ABx), y(p.ABy), z(p.ABz), qmax(p.Qmax) {}
+};
+struct PairGeom32 {
+    float x, y, z, qmax;
+    __device__ __forceinline__ explicit PairGeom32(const ShellPairDev& p)
+        : x(p.fABx), y(p.fABy), z(p.fABz), qmax(p.fQmax) {}
+};
+template <class T>
+struct TierTypes;
+template <>
+struct TierTypes<double> {
+    using Geom = PairGeom64;
+    __device__ __forceinline__ static double* J(const FockClassLaunch& L) { return L.J; }
+    __device__ __forceinline__ static double* K(const FockClassLaunch& L) { return L.K; }
+};
+template <>
+struct TierTypes<float> {
+    using Geom = PairGeom32;
+    // the FP32 tier accumulates in FP32 (merged into FP64 by the finishing kernel)
+    __device__ __forceinline__ static float* J(const FockClassLaunch& L) { return L.J32; }
+    __device__ __forceinline__ static float* K(const FockClassLaunch& L) { return L.K32; }
+};
+
 // Accumulates the ket component pairs [CD0, CD1) of the contracted quartet
 // (AB|CD)' into I[ab][cd - CD0], over the primitive quartets that pass the
 // primitive Schwarz test.  Returns the number of primitive quartets.
@@ -87,9 +114,10 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
     constexpr int NB = ncart(LB), ND = ncart(LD);
     constexpr int LAB = LA + LB, LCD = LC + LD, LT = LAB + LCD;
     int count = 0;
-    const T qket_max = static_cast<T>(kp.Qmax);
-    const T abx = static_cast<T>(bp.ABx), aby = static_cast<T>(bp.ABy), abz = static_cast<T>(bp.ABz);
-    const T cdx = static_cast<T>(kp.ABx), cdy = static_cast<T>(kp.ABy), cdz = static_cast<T>(kp.ABz);
+    const typename TierTypes<T>::Geom gb_(bp), gk_(kp);
+    const T qket_max = gk_.qmax;
+    const T abx = gb_.x, aby = gb_.y, abz = gb_.z;
+    const T cdx = gk_.x, cdy = gk_.y, cdz = gk_.z;
     for (int ip = 0; ip < bp.pp_n; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
         if (pb.Q * qket_max < thr) continue;
@@ -221,8 +249,8 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
             static_cast<T>(L.schwarz_threshold), I);
     }
 
-    double* __restrict__ Jp = L.J;
-    double* __restrict__ Kp = L.K;
+    T* __restrict__ Jp = TierTypes<T>::J(L);
+    T* __restrict__ Kp = TierTypes<T>::K(L);
     const int bra0 = __shfl_sync(0xffffffffu, q.bra, 0);
     const bool uniform_bra = __all_sync(0xffffffffu, (!q.active) || q.bra == bra0) && bra0 >= 0;
     // J'_ab += sum_cd D'_cd v  (a partial sum when the thread holds a component chunk)
@@ -240,9 +268,9 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
             s *= fsym;
             if (uniform_bra) {
                 s = warp_sum(s);
-                if (lane == 0) atomicAdd(&Jp[(bfA0 + ab / NB) * N + bfB0 + ab % NB], static_cast<double>(s));
+                if (lane == 0) atomicAdd(&Jp[(bfA0 + ab / NB) * N + bfB0 + ab % NB], s);
             } else if (q.active) {
-                atomicAdd(&Jp[(bfA + ab / NB) * N + bfB + ab % NB], static_cast<double>(s));
+                atomicAdd(&Jp[(bfA + ab / NB) * N + bfB + ab % NB], s);
             }
         }
     }
@@ -258,7 +286,7 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
         T s = T(0);
 #pragma unroll
         for (int ab = 0; ab < NA * NB; ++ab) s += dab[ab] * I[ab][cd - CD0];
-        atomicAdd(&Jp[(bfC + cd / ND) * N + bfD + cd % ND], static_cast<double>(s * fsym));
+        atomicAdd(&Jp[(bfC + cd / ND) * N + bfD + cd % ND], s * fsym);
     }
     // K'_ac += sum_bd D'_bd v ; K'_ad += sum_bc D'_bc v
 #pragma unroll
@@ -275,7 +303,7 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
                     if (cd < CD0 || cd >= CD1) continue;
                     s += Dp[(bfB + ib) * N + bfD + id] * I[ia * NB + ib][cd - CD0];
                 }
-            atomicAdd(&Kp[(bfA + ia) * N + bfC + ic], static_cast<double>(s * fsym));
+            atomicAdd(&Kp[(bfA + ia) * N + bfC + ic], s * fsym);
         }
 #pragma unroll
         for (int id = 0; id < ND; ++id) {
@@ -292,7 +320,7 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
                     if (cd < CD0 || cd >= CD1) continue;
                     s += Dp[(bfB + ib) * N + bfC + ic] * I[ia * NB + ib][cd - CD0];
                 }
-            atomicAdd(&Kp[(bfA + ia) * N + bfD + id], static_cast<double>(s * fsym));
+            atomicAdd(&Kp[(bfA + ia) * N + bfD + id], s * fsym);
         }
     }
     // K'_bd += sum_ac D'_ac v ; K'_bc += sum_ad D'_ad v
@@ -313,7 +341,7 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
                     if (cd < CD0 || cd >= CD1) continue;
                     s += Dp[(bfA + ia) * N + bfC + ic] * I[ia * NB + ib][cd - CD0];
                 }
-            atomicAdd(&Kp[(bfB + ib) * N + bfD + id], static_cast<double>(s * fsym));
+            atomicAdd(&Kp[(bfB + ib) * N + bfD + id], s * fsym);
         }
 #pragma unroll
         for (int ic = 0; ic < NC; ++ic) {
@@ -327,7 +355,7 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
                     if (cd < CD0 || cd >= CD1) continue;
                     s += Dp[(bfA + ia) * N + bfD + id] * I[ia * NB + ib][cd - CD0];
                 }
-            atomicAdd(&Kp[(bfB + ib) * N + bfC + ic], static_cast<double>(s * fsym));
+            atomicAdd(&Kp[(bfB + ib) * N + bfC + ic], s * fsym);
         }
     }
 }

@@ -86,6 +86,7 @@ __global__ void sub_kernel(const double* __restrict__ A, const double* __restric
 
 // G (+)= s (2 (J' + J'^T) - 1/2 (K' + K'^T)) s ; F = H + G
 __global__ void fock_from_jk_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
+                                    const float* __restrict__ Jp32, const float* __restrict__ Kp32,
                                     const double* __restrict__ s, const double* __restrict__ H, int n, int accumulate,
                                     double* __restrict__ G, double* __restrict__ F)
 {
@@ -94,7 +95,12 @@ __global__ void fock_from_jk_kernel(const double* __restrict__ Jp, const double*
          k += static_cast<long long>(gridDim.x) * blockDim.x) {
         const int i = static_cast<int>(k / n), j = static_cast<int>(k % n);
         const long long kt = static_cast<long long>(j) * n + i;
-        const double g = (2.0 * (Jp[k] + Jp[kt]) - 0.5 * (Kp[k] + Kp[kt])) * s[i] * s[j];
+        double jsum = Jp[k] + Jp[kt], ksum = Kp[k] + Kp[kt];
+        if (Jp32) {
+            jsum += static_cast<double>(Jp32[k]) + static_cast<double>(Jp32[kt]);
+            ksum += static_cast<double>(Kp32[k]) + static_cast<double>(Kp32[kt]);
+        }
+        const double g = (2.0 * jsum - 0.5 * ksum) * s[i] * s[j];
         const double gn = accumulate ? G[k] + g : g;
         G[k] = gn;
         F[k] = H[k] + gn;
@@ -403,7 +409,9 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
             const int prec = (opt.precision == HF_PRECISION_MIXED) ? opt.full_build_precision : opt.precision;
             if ((r = build_jk(e, w.D, nullptr, nullptr, prec, opt.mixed_threshold, s))) return r;
         }
-        fock_from_jk_kernel<<<grid_nn(nn), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, w.H, n, incremental ? 1 : 0, w.G, w.F);
+        fock_from_jk_kernel<<<grid_nn(nn), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.last_mixed ? e.d_Jp32 : nullptr,
+                                                         e.last_mixed ? e.d_Kp32 : nullptr, e.d_scale, w.H, n,
+                                                         incremental ? 1 : 0, w.G, w.F);
         GB_LAUNCH_CHECK();
         GB_CUDA_TRY(cudaMemcpyAsync(w.Dprev, w.D, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
         cudaEventRecord(f1, s);
