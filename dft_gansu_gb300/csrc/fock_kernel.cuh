@@ -41,14 +41,16 @@ struct FockTypes<float> {
     using PP = PrimPair32;
 };
 
-// Threads per contracted quartet: 1, or one per ket component pair when the
-// block of ncart^4 integrals (or the d x d Hermite tables of a (dd| bra)
-// exceed the register budget of the type; those classes run generic.
+// Threads per contracted quartet: 1 (fully unrolled kernel), or one per ket
+// component pair (generic kernel) for the classes whose unrolled form would
+// spill heavily: measured with -Xptxas -v, FP64 blocks above 162 integrals or a
+// (dd| bra with ket components (10 KB of spills), FP32 blocks above 324.
 template <class T, int LA, int LB, int LC, int LD>
 struct FockSplit {
     static constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
-    static constexpr int kLimit = sizeof(T) == 8 ? 36 : 81;
-    static constexpr bool kLarge = (NAB * NCD > kLimit) || (LA == 2 && LB == 2);
+    static constexpr bool kDDBra = (LA == 2 && LB == 2);
+    static constexpr bool kLarge =
+        sizeof(T) == 8 ? ((NAB * NCD > 162) || (kDDBra && NCD > 1)) : (NAB * NCD > 324);
     static constexpr int value = kLarge ? NCD : 1;
 };
 
