@@ -44,13 +44,14 @@ struct FockTypes<float> {
 // Threads per contracted quartet: 1 (fully unrolled kernel), or one per ket
 // component pair (generic kernel) for the classes whose unrolled form would
 // spill heavily: measured with -Xptxas -v, FP64 blocks above 162 integrals or a
-// (dd| bra with ket components (10 KB of spills), FP32 blocks above 324.
+// (dd| bra with ket components (10 KB of spills), FP32 blocks above 162
+// ((dp|dp) and (dd|pp) spill about 3 KB and ran slower than the generic path).
 template <class T, int LA, int LB, int LC, int LD>
 struct FockSplit {
     static constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
     static constexpr bool kDDBra = (LA == 2 && LB == 2);
     static constexpr bool kLarge =
-        sizeof(T) == 8 ? ((NAB * NCD > 162) || (kDDBra && NCD > 1)) : (NAB * NCD > 324);
+        sizeof(T) == 8 ? ((NAB * NCD > 162) || (kDDBra && NCD > 1)) : (NAB * NCD > 162);
     static constexpr int value = kLarge ? NCD : 1;
 };
 
