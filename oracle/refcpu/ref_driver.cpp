@@ -10,6 +10,10 @@
  *   - computeCoreHamiltonianMatrix src/gpu_manager.cu:333-404 (+ the upper->lower
  *     copy that Matrix_Symmetrization does, src/int1e.cu:67-84)
  *   - makeShellPairTypeInfo       src/gpu_manager.cu:413-432
+ *   - computeAuxiliarySchwarzUpperBounds, computeTwoCenterERIs,
+ *     computeThreeCenterERIs      src/gpu_manager.cu:1963-2210 (pair indices in
+ *     the order of the Schwarz kernels; the reference sorts them by bound,
+ *     src/eri.cu:119-236, which changes only the summation order)
  * The Boys table is the reference's own (src/boys/boys_30720.h, loaded the
  * same way as src/hf.cu:74-77).
  *
@@ -24,6 +28,8 @@
 #include "types.hpp"
 #include "int2e.hpp"
 #include "int1e.hpp"
+#include "int2c2e.hpp"
+#include "int3c2e.hpp"
 #include "boys/boys_30720.h"
 
 thread_local RefcpuDim3 threadIdx{0, 0, 0};
@@ -51,6 +57,29 @@ int index_2to1_horizontal(int i, int j, const int n)
 {
     if (i > j) std::swap(i, j);
     return j - static_cast<int>(i * (i - 2 * n + 1) / 2);
+}
+
+std::vector<PrimitiveShell> make_prims(int n, const double* exps, const double* coefs, const double* xyz,
+                                       const int* shell_type, const long long* basis_index, const int* atom_index)
+{
+    std::vector<PrimitiveShell> prims(n);
+    for (int i = 0; i < n; ++i) {
+        prims[i].exponent = exps[i];
+        prims[i].coefficient = coefs[i];
+        prims[i].coordinate = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+        prims[i].shell_type = shell_type[i];
+        prims[i].basis_index = static_cast<size_t>(basis_index[i]);
+        prims[i].atom_index = atom_index[i];
+    }
+    return prims;
+}
+
+std::vector<ShellTypeInfo> type_infos(const std::vector<PrimitiveShell>& prims)
+{
+    std::vector<ShellTypeInfo> sti(prims.back().shell_type + 1, {0, 0});
+    for (auto& p : prims) sti[p.shell_type].count++;
+    for (size_t i = 1; i < sti.size(); ++i) sti[i].start_index = sti[i - 1].start_index + sti[i - 1].count;
+    return sti;
 }
 
 }  // namespace
@@ -156,6 +185,79 @@ int refcpu_integrals(int nprim, const double* exps, const double* coefs, const d
                 H[i * N + j] = H[j * N + i];
             }
     }
+    return 0;
+}
+
+/* The reference's RI integrals: metric V[P*naux+Q] = (P|Q), three-centre
+ * T[(P*nbf + mu)*nbf + nu] = (mu nu|P), and the auxiliary Schwarz bounds. */
+int refcpu_ri_integrals(int nprim, const double* exps, const double* coefs, const double* xyz, const int* shell_type,
+                        const long long* basis_index, const int* atom_index, const double* cgto, int nbf,
+                        int naprim, const double* aexps, const double* acoefs, const double* axyz,
+                        const int* ashell_type, const long long* abasis_index, const int* aatom_index,
+                        const double* acgto, int naux, double thr, double* V, double* T, double* aux_bounds)
+{
+    std::vector<PrimitiveShell> prims = make_prims(nprim, exps, coefs, xyz, shell_type, basis_index, atom_index);
+    std::vector<PrimitiveShell> aprims = make_prims(naprim, aexps, acoefs, axyz, ashell_type, abasis_index, aatom_index);
+    std::vector<ShellTypeInfo> sti = type_infos(prims), asti = type_infos(aprims);
+    const int ntype = static_cast<int>(sti.size()), natype = static_cast<int>(asti.size());
+    const double* boys = gansu::h_boys_grid;
+
+    // AO primitive-pair Schwarz bounds and the pair index lists in the same order
+    std::vector<ShellPairTypeInfo> spti(ntype * (ntype + 1) / 2);
+    size_t npairs = 0;
+    for (int s0 = 0; s0 < ntype; ++s0)
+        for (int s1 = s0; s1 < ntype; ++s1) {
+            size_t nb = (s0 == s1) ? static_cast<size_t>(sti[s0].count) * (sti[s0].count + 1) / 2
+                                   : static_cast<size_t>(sti[s0].count) * sti[s1].count;
+            spti[index_2to1_horizontal(s0, s1, ntype)] = {nb, npairs};
+            npairs += nb;
+        }
+    std::vector<double> bounds(npairs, 0.0);
+    std::vector<size_t2> pair_idx(npairs);
+    for (int s0 = 0; s0 < ntype; ++s0)
+        for (int s1 = s0; s1 < ntype; ++s1) {
+            const size_t head = spti[index_2to1_horizontal(s0, s1, ntype)].start_index;
+            const size_t nb = spti[index_2to1_horizontal(s0, s1, ntype)].count;
+            auto k = gpu::get_schwarz_kernel(s0, s1);
+            run_threads(nb, [&] { k(prims.data(), cgto, sti[s0], sti[s1], head, nb, boys, bounds.data()); });
+            for (size_t id = 0; id < nb; ++id) {
+                if (s0 == s1) {
+                    const size_t r2 = static_cast<size_t>(std::floor((std::sqrt(8.0 * id + 1) - 1) / 2));
+                    pair_idx[head + id] = {id - r2 * (r2 + 1) / 2, r2};
+                } else {
+                    pair_idx[head + id] = {id / sti[s1].count, id % sti[s1].count};
+                }
+            }
+        }
+    // auxiliary bounds
+    std::vector<double> abounds(naprim, 0.0);
+    for (int s0 = 0; s0 < natype; ++s0) {
+        auto k = gpu::get_schwarz_aux_kernel(s0);
+        const size_t head = asti[s0].start_index, nb = asti[s0].count;
+        run_threads(nb, [&] { k(aprims.data(), acgto, asti[s0], head, nb, boys, abounds.data()); });
+    }
+    if (aux_bounds) std::memcpy(aux_bounds, abounds.data(), sizeof(double) * naprim);
+    // two-centre metric
+    std::memset(V, 0, sizeof(double) * naux * naux);
+    for (int a = 0; a < natype; ++a)
+        for (int b = a; b < natype; ++b) {
+            const int np = (a == b) ? asti[a].count * (asti[a].count + 1) / 2 : asti[a].count * asti[b].count;
+            auto k = gpu::get_2center_kernel(a, b);
+            run_threads(np, [&] { k(V, aprims.data(), acgto, asti[a], asti[b], np, abounds.data(), thr, naux, boys); });
+        }
+    // three-centre tensor
+    std::memset(T, 0, sizeof(double) * static_cast<size_t>(naux) * nbf * nbf);
+    for (int a = 0; a < ntype; ++a)
+        for (int b = a; b < ntype; ++b)
+            for (int c = 0; c < natype; ++c) {
+                const size_t head = spti[index_2to1_horizontal(a, b, ntype)].start_index;
+                const int64_t ntask = static_cast<int64_t>(spti[index_2to1_horizontal(a, b, ntype)].count) * asti[c].count;
+                auto k = gpu::get_3center_kernel(a, b, c);
+                run_threads(ntask, [&] {
+                    k(T, prims.data(), aprims.data(), cgto, acgto, sti[a], sti[b], asti[c], ntask, nbf,
+                      &pair_idx[head], &bounds[head], abounds.data(), thr, naux, boys);
+                });
+            }
     return 0;
 }
 
