@@ -220,6 +220,29 @@ class Engine:
               "hf_compute_fock_diis")
         return F
 
+    def energy_weighted_density(self, coefficients, orbital_energies, num_occupied: int, stream=None):
+        W = self._empty(self.N, self.N)
+        check(lib().hf_energy_weighted_density(self._h, _ptr(coefficients), _ptr(orbital_energies), int(num_occupied),
+                                               _ptr(W), _stream(stream)), "hf_energy_weighted_density")
+        return W
+
+    def gradient(self, density, energy_weighted_density, stream=None):
+        """Analytic nuclear gradient (natom, 3) in Eh/bohr and its device time in ms."""
+        g = np.zeros(3 * self.mol.num_atoms)
+        ms = C.c_double()
+        check(lib().hf_rhf_gradient(self._h, _ptr(density), _ptr(energy_weighted_density),
+                                    g.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ms), _stream(stream)),
+              "hf_rhf_gradient")
+        return g.reshape(-1, 3), ms.value
+
+    def energy_and_gradient(self, num_electrons: int, options: dict | None = None):
+        """Forward (SCF energy) and backward (analytic gradient) pair."""
+        r = self.rhf_scf(num_electrons, options, want_matrices=True)
+        W = self.energy_weighted_density(r["coefficients"], r["orbital_energies"], num_electrons // 2)
+        g, ms = self.gradient(r["density"], W)
+        r["gradient"], r["gradient_ms"] = g, ms
+        return r
+
     def rhf_scf(self, num_electrons: int, options: dict | None = None, want_matrices: bool = False):
         opt = ScfOptions()
         lib().hf_scf_options_default(C.byref(opt))

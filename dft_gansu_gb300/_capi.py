@@ -109,6 +109,8 @@ SIGNATURES = {
     "hf_compute_diis_error": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_diis": (_I, [_P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_diis_noalloc": (_I, [_P, _P, _P, _I, _I, _P]),
+    "hf_energy_weighted_density": (_I, [_P, _P, _P, _I, _P, _P]),
+    "hf_rhf_gradient": (_I, [_P, _P, _P, C.POINTER(_D), C.POINTER(_D), _P]),
     "hf_scf_options_default": (None, [C.POINTER(ScfOptions)]),
     "hf_rhf_scf": (_I, [_P, _I, C.POINTER(ScfOptions), C.POINTER(ScfResult), _P, _P, _P, _P]),
 }

@@ -87,6 +87,8 @@ struct Engine {
     float* d_Jp32 = nullptr;   // FP32-tier accumulators (FP32 accumulation)
     float* d_Kp32 = nullptr;
     bool last_mixed = false;   // whether the last build used the FP32 accumulators
+    double* d_grad = nullptr;     // 3 * natom gradient accumulators (allocated on first use)
+    int* d_shell_atom = nullptr;  // contracted shell -> atom
     double* d_scalar = nullptr;  // small scratch scalars (8 doubles)
     unsigned long long* d_counters = nullptr;  // [class pair][precision][prim, contracted]
     long long bytes_h2d = 0;                   // bytes uploaded by engine creation
@@ -125,6 +127,10 @@ int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s);
 
 // one_electron.cu
 int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s);
+
+// grad.cu
+int energy_weighted_density(Engine& e, const double* d_C, const double* d_eps, int nocc, double* d_W, cudaStream_t s);
+int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad, cudaStream_t s, float* ms_out);
 
 // host MD helpers (engine.cu)
 void host_boys_table(std::vector<double>& table);

@@ -1,0 +1,538 @@
+// Analytic RHF nuclear gradient (no counterpart in the reference, whose
+// "geometry optimisation" is an energy-only coordinate search,
+// include/builder.hpp:108-275).
+//
+//   dE/dR = sum D dH/dR - sum W dS/dR + sum_{unique quartets} f G_abcd d(ab|cd)/dR + dV_nn/dR
+//   G_abcd = 4 D_ab D_cd - D_ac D_bd - D_ad D_bc            (8 permutations folded)
+//   W      = 2 sum_occ eps_i C_i C_i^T                     (energy-weighted density)
+//
+// Derivatives of a Cartesian Gaussian with respect to its centre,
+//   d/dA_x phi_a = 2 alpha phi_{a+1x} - a_x phi_{a-1x},
+// turn every derivative integral into integrals of shifted angular momentum,
+// evaluated with the same McMurchie-Davidson Hermite expansions as the Fock
+// build (md_math.cuh); nothing is stored: Hermite intermediates are rebuilt
+// for every primitive quartet.  The two-electron term differentiates the bra
+// centres A, B and the ket centre C; D follows from translational invariance
+// (dA + dB + dC + dD = 0).  One thread handles one ket component pair (c,d)
+// of one contracted quartet (the quartet lists of the Fock build), so the
+// density weights of a column fit in registers.
+#include <cmath>
+#include <vector>
+
+#include "engine.hpp"
+#include "fock_kernel.cuh"
+
+namespace gb {
+namespace {
+
+constexpr int kGI = kMaxL + 2;             // E table dimension (l + 1 shift)
+constexpr int kGT = 2 * (kMaxL + 1) + 1;   // t range
+constexpr int kGE = kGI * kGI * kGT;
+constexpr int kGL = 4 * kMaxL + 1;         // highest R order
+constexpr int kGR = nherm(kGL);
+constexpr int kGX = nherm(2 * kMaxL + 1);  // bra Hermite entries with one extra order
+constexpr int kGNAB = ncart(kMaxL) * ncart(kMaxL);
+constexpr int kGradThreads = 64;
+
+__device__ __forceinline__ int gidx(int t, int u, int v)
+{
+    const int k = t + u + v, m = k - t;
+    return k * (k + 1) * (k + 2) / 6 + m * (m + 1) / 2 + v;
+}
+
+__device__ __forceinline__ void grad_e_table(int l1, int l2, double xpa, double xpb, double oo2p, double* e)
+{
+    e[0] = 1.0;
+    for (int i = 0; i <= l1; ++i)
+        for (int j = 0; j <= l2; ++j) {
+            if (i == 0 && j == 0) continue;
+            for (int t = 0; t <= i + j; ++t) {
+                double v;
+                if (i > 0) {
+                    v = (t <= i - 1 + j) ? xpa * e[((i - 1) * kGI + j) * kGT + t] : 0.0;
+                    if (t > 0) v += oo2p * e[((i - 1) * kGI + j) * kGT + t - 1];
+                    if (t + 1 <= i - 1 + j) v += (t + 1) * e[((i - 1) * kGI + j) * kGT + t + 1];
+                } else {
+                    v = (t <= j - 1) ? xpb * e[(j - 1) * kGT + t] : 0.0;
+                    if (t > 0) v += oo2p * e[(j - 1) * kGT + t - 1];
+                    if (t + 1 <= j - 1) v += (t + 1) * e[(j - 1) * kGT + t + 1];
+                }
+                e[(i * kGI + j) * kGT + t] = v;
+            }
+        }
+}
+
+__device__ __forceinline__ void grad_boys(int n, double x, const double* table, double* F)
+{
+#define GB_B(N)                              \
+    case N: {                                \
+        double f[N + 1];                     \
+        boys_fp64<N>(x, table, f);           \
+        for (int i = 0; i <= N; ++i) F[i] = f[i]; \
+        break;                               \
+    }
+    switch (n) {
+        GB_B(0) GB_B(1) GB_B(2) GB_B(3) GB_B(4) GB_B(5) GB_B(6) GB_B(7) GB_B(8) GB_B(9)
+    default: break;
+    }
+#undef GB_B
+}
+
+__device__ __forceinline__ void grad_r_table(int L, const double* Fs, double X, double Y, double Z, double* r)
+{
+    r[0] = Fs[L];
+    for (int n = L - 1; n >= 0; --n) {
+        for (int k = L - n; k >= 1; --k)
+            for (int t = k; t >= 0; --t)
+                for (int u = k - t; u >= 0; --u) {
+                    const int v = k - t - u;
+                    double val;
+                    if (t > 0) {
+                        val = X * r[gidx(t - 1, u, v)];
+                        if (t > 1) val += (t - 1) * r[gidx(t - 2, u, v)];
+                    } else if (u > 0) {
+                        val = Y * r[gidx(0, u - 1, v)];
+                        if (u > 1) val += (u - 1) * r[gidx(0, u - 2, v)];
+                    } else {
+                        val = Z * r[gidx(0, 0, v - 1)];
+                        if (v > 1) val += (v - 1) * r[gidx(0, 0, v - 2)];
+                    }
+                    r[gidx(t, u, v)] = val;
+                }
+        r[0] = Fs[n];
+    }
+}
+
+// ket contraction of one ket component (c + sh along axis ax, d) into the bra
+// Hermite index up to order lmax: x[tuv] = sum (-1)^{tau+nu+phi} E^{cd} R
+__device__ __forceinline__ void ket_contract(int lmax, const int c[3], const int d[3], const double* fx,
+                                             const double* fy, const double* fz, const double* r, double* x)
+{
+    const double* ex = fx + (c[0] * kGI + d[0]) * kGT;
+    const double* ey = fy + (c[1] * kGI + d[1]) * kGT;
+    const double* ez = fz + (c[2] * kGI + d[2]) * kGT;
+    for (int t = 0; t <= lmax; ++t)
+        for (int u = 0; u + t <= lmax; ++u)
+            for (int v = 0; v + u + t <= lmax; ++v) {
+                double s = 0.0;
+                for (int tau = 0; tau <= c[0] + d[0]; ++tau)
+                    for (int nu = 0; nu <= c[1] + d[1]; ++nu) {
+                        const double exy = ex[tau] * ey[nu];
+                        for (int phi = 0; phi <= c[2] + d[2]; ++phi) {
+                            const double w = exy * ez[phi] * r[gidx(t + tau, u + nu, v + phi)];
+                            s += ((tau + nu + phi) & 1) ? -w : w;
+                        }
+                    }
+                x[gidx(t, u, v)] = s;
+            }
+}
+
+// sum_tuv E^{a'b'}_tuv x[tuv] for bra exponents a', b' (per axis)
+__device__ __forceinline__ double bra_contract(const int a[3], const int b[3], const double* ex, const double* ey,
+                                               const double* ez, const double* x)
+{
+    const double* px = ex + (a[0] * kGI + b[0]) * kGT;
+    const double* py = ey + (a[1] * kGI + b[1]) * kGT;
+    const double* pz = ez + (a[2] * kGI + b[2]) * kGT;
+    double s = 0.0;
+    for (int t = 0; t <= a[0] + b[0]; ++t)
+        for (int u = 0; u <= a[1] + b[1]; ++u) {
+            const double exy = px[t] * py[u];
+            for (int v = 0; v <= a[2] + b[2]; ++v) s += exy * pz[v] * x[gidx(t, u, v)];
+        }
+    return s;
+}
+
+struct GradLaunch {
+    FockClassLaunch L;       // FP64 work list, pairs, primitive pairs, Boys table, D' (FP64)
+    const int* shell_atom;   // contracted shell -> atom
+    double* grad;            // 3 * natom accumulators
+};
+
+__global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch G, int ncd)
+{
+    const FockClassLaunch& L = G.L;
+    const long long total = L.off[L.nentry];
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((total + 31) >> 5) * ncd;
+    const long long warp_stride = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+    const double* __restrict__ Dp = static_cast<const double*>(L.density);
+    const PrimPair64* __restrict__ pp = static_cast<const PrimPair64*>(L.prim_pairs);
+    const double* __restrict__ boys = static_cast<const double*>(L.boys_table);
+    const int N = L.num_basis;
+    const double thr = L.schwarz_threshold;
+    double ex[kGE], ey[kGE], ez[kGE], fx[kGE], fy[kGE], fz[kGE];
+    double Fs[kGL + 1], r[kGR], x0[kGX], xp[3][kGX], xm[3][kGX];
+    double wcol[kGNAB];
+
+    for (long long wid = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; wid < nwarps;
+         wid += warp_stride) {
+        const int cdi = static_cast<int>(wid % ncd);
+        const long long w = (wid / ncd) * 32 + lane;
+        if (w >= total) continue;
+        const int e = find_entry(L.off, L.nentry, w);
+        const int bra = __ldg(L.entry_bra + e);
+        const int ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(w - __ldg(L.off + e));
+        const ShellPairDev bp = L.pairs[bra];
+        const ShellPairDev kp = L.pairs[ket];
+        const int la = bp.la, lb = bp.lb, lc = kp.la, ld = kp.lb;
+        const int na = ncart(la), nb = ncart(lb), nd = ncart(ld);
+        const int lab = la + lb, lt = lab + lc + ld + 1;
+        const int ic = cdi / nd, id = cdi % nd;
+        const int c[3] = {cart_exp(lc, ic, 0), cart_exp(lc, ic, 1), cart_exp(lc, ic, 2)};
+        const int d[3] = {cart_exp(ld, id, 0), cart_exp(ld, id, 1), cart_exp(ld, id, 2)};
+        const int cf = kp.bfA + ic, df = kp.bfB + id;
+        double fsym = 1.0;
+        if (bp.A == bp.B) fsym *= 0.5;
+        if (kp.A == kp.B) fsym *= 0.5;
+        if (bra == ket) fsym *= 0.5;
+        // density weights of this (c,d) column: f (4 D_ab D_cd - D_ac D_bd - D_ad D_bc)
+        const double dcd = Dp[cf * N + df];
+        bool any = false;
+        for (int ia = 0; ia < na; ++ia)
+            for (int ib = 0; ib < nb; ++ib) {
+                const int a = bp.bfA + ia, b = bp.bfB + ib;
+                const double v = fsym * (4.0 * Dp[a * N + b] * dcd - Dp[a * N + cf] * Dp[b * N + df] -
+                                         Dp[a * N + df] * Dp[b * N + cf]);
+                wcol[ia * nb + ib] = v;
+                any |= (v != 0.0);
+            }
+        if (!any) continue;
+        double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+        for (int ip = 0; ip < bp.pp_n; ++ip) {
+            const PrimPair64 pb = pp[bp.pp_off + ip];
+            if (pb.Q * kp.Qmax < thr) continue;
+            const double alpha2 = 2.0 * (pb.p - pb.b), beta2 = 2.0 * pb.b;
+            const double oo2p = 0.5 * pb.invp;
+            grad_e_table(la + 1, lb + 1, pb.PAx, pb.PAx + bp.ABx, oo2p, ex);
+            grad_e_table(la + 1, lb + 1, pb.PAy, pb.PAy + bp.ABy, oo2p, ey);
+            grad_e_table(la + 1, lb + 1, pb.PAz, pb.PAz + bp.ABz, oo2p, ez);
+            for (int jq = 0; jq < kp.pp_n; ++jq) {
+                const PrimPair64 pk = pp[kp.pp_off + jq];
+                if (pb.Q * pk.Q < thr) continue;
+                const double gamma2 = 2.0 * (pk.p - pk.b);
+                const double oo2q = 0.5 * pk.invp;
+                grad_e_table(lc + 1, ld, pk.PAx, pk.PAx + kp.ABx, oo2q, fx);
+                grad_e_table(lc + 1, ld, pk.PAy, pk.PAy + kp.ABy, oo2q, fy);
+                grad_e_table(lc + 1, ld, pk.PAz, pk.PAz + kp.ABz, oo2q, fz);
+                const double rr = rsqrt(pb.p + pk.p);
+                const double rho = pb.p * pk.p * rr * rr;
+                const double X = pb.Px - pk.Px, Y = pb.Py - pk.Py, Z = pb.Pz - pk.Pz;
+                grad_boys(lt, rho * (X * X + Y * Y + Z * Z), boys, Fs);
+                double scale = pb.KoP * pk.KoP * rr;
+                for (int n = 0; n <= lt; ++n) { Fs[n] *= scale; scale *= -2.0 * rho; }
+                grad_r_table(lt, Fs, X, Y, Z, r);
+                ket_contract(lab + 1, c, d, fx, fy, fz, r, x0);
+                for (int k = 0; k < 3; ++k) {
+                    int cp[3] = {c[0], c[1], c[2]};
+                    cp[k] += 1;
+                    ket_contract(lab, cp, d, fx, fy, fz, r, xp[k]);
+                    if (c[k] > 0) {
+                        cp[k] -= 2;
+                        ket_contract(lab, cp, d, fx, fy, fz, r, xm[k]);
+                    }
+                }
+                for (int ia = 0; ia < na; ++ia)
+                    for (int ib = 0; ib < nb; ++ib) {
+                        const double wv = wcol[ia * nb + ib];
+                        if (wv == 0.0) continue;
+                        const int a[3] = {cart_exp(la, ia, 0), cart_exp(la, ia, 1), cart_exp(la, ia, 2)};
+                        const int b[3] = {cart_exp(lb, ib, 0), cart_exp(lb, ib, 1), cart_exp(lb, ib, 2)};
+                        for (int k = 0; k < 3; ++k) {
+                            int s[3] = {a[0], a[1], a[2]};
+                            s[k] += 1;
+                            double dA = alpha2 * bra_contract(s, b, ex, ey, ez, x0);
+                            if (a[k] > 0) {
+                                s[k] -= 2;
+                                dA -= a[k] * bra_contract(s, b, ex, ey, ez, x0);
+                            }
+                            int t2[3] = {b[0], b[1], b[2]};
+                            t2[k] += 1;
+                            double dB = beta2 * bra_contract(a, t2, ex, ey, ez, x0);
+                            if (b[k] > 0) {
+                                t2[k] -= 2;
+                                dB -= b[k] * bra_contract(a, t2, ex, ey, ez, x0);
+                            }
+                            double dC = gamma2 * bra_contract(a, b, ex, ey, ez, xp[k]);
+                            if (c[k] > 0) dC -= c[k] * bra_contract(a, b, ex, ey, ez, xm[k]);
+                            gA[k] += wv * dA;
+                            gB[k] += wv * dB;
+                            gC[k] += wv * dC;
+                        }
+                    }
+            }
+        }
+        const int atA = G.shell_atom[bp.A], atB = G.shell_atom[bp.B], atC = G.shell_atom[kp.A],
+                  atD = G.shell_atom[kp.B];
+        for (int k = 0; k < 3; ++k) {
+            atomicAdd(&G.grad[3 * atA + k], gA[k]);
+            atomicAdd(&G.grad[3 * atB + k], gB[k]);
+            atomicAdd(&G.grad[3 * atC + k], gC[k]);
+            atomicAdd(&G.grad[3 * atD + k], -(gA[k] + gB[k] + gC[k]));
+        }
+    }
+}
+
+// One-electron part per shell pair: sum over the (a,b) block and its mirror of
+// D_ab d(T+V)_ab/dR - W_ab dS_ab/dR, including the Hellmann-Feynman term of
+// each nucleus C (dV/dC_x = Z (2 pi / p) K sum_tuv E_tuv R_{t+1,u,v}).
+template <int LA, int LB>
+__global__ void __launch_bounds__(128)
+grad_one_electron_kernel(const ShellPairDev* __restrict__ pairs, int begin, int count,
+                         const PrimPair64* __restrict__ pp, const double* __restrict__ boys,
+                         const double* __restrict__ atoms, int natom, const int* __restrict__ shell_atom,
+                         const double* __restrict__ scale, const double* __restrict__ D,
+                         const double* __restrict__ W, int n, double kfold, double* __restrict__ grad)
+{
+    constexpr int NA = ncart(LA), NB = ncart(LB), L = LA + LB + 1;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= count) return;
+    const ShellPairDev sp = pairs[begin + idx];
+    // density weights in the unnormalised space: factor 2 for the mirror block
+    const double mirror = (sp.A == sp.B) ? 1.0 : 2.0;
+    double dw[NA][NB], ww[NA][NB];
+    for (int ia = 0; ia < NA; ++ia)
+        for (int ib = 0; ib < NB; ++ib) {
+            const int a = sp.bfA + ia, b = sp.bfB + ib;
+            const double ss = scale[a] * scale[b] * mirror;
+            dw[ia][ib] = D[a * n + b] * ss;
+            ww[ia][ib] = W[a * n + b] * ss;
+        }
+    double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0};
+    const int atA = shell_atom[sp.A], atB = shell_atom[sp.B];
+    for (int ip = 0; ip < sp.pp_n; ++ip) {
+        const PrimPair64 q = pp[sp.pp_off + ip];
+        const double p = q.p, bexp = q.b, aexp = p - bexp, oo2p = 0.5 * q.invp;
+        const double k1 = q.K / kfold;
+        HermiteE<double, LA + 1, LB + 2> Ex, Ey, Ez;
+        Ex.build(q.PAx, q.PAx + sp.ABx, oo2p);
+        Ey.build(q.PAy, q.PAy + sp.ABy, oo2p);
+        Ez.build(q.PAz, q.PAz + sp.ABz, oo2p);
+        const double sq = sqrt(kPi / p);
+        // overlap and kinetic 1D factors for i <= LA+1, j <= LB
+        auto s1 = [&](const HermiteE<double, LA + 1, LB + 2>& E, int i, int j) { return E.e[i][j][0] * sq; };
+        auto t1 = [&](const HermiteE<double, LA + 1, LB + 2>& E, int i, int j) {
+            double tt = 4.0 * bexp * bexp * E.e[i][j + 2][0] - 2.0 * bexp * (2 * j + 1) * E.e[i][j][0];
+            if (j >= 2) tt += j * (j - 1) * E.e[i][j - 2][0];
+            return -0.5 * tt * sq;
+        };
+        for (int ia = 0; ia < NA; ++ia)
+            for (int ib = 0; ib < NB; ++ib) {
+                int a[3] = {cart_exp(LA, ia, 0), cart_exp(LA, ia, 1), cart_exp(LA, ia, 2)};
+                const int b[3] = {cart_exp(LB, ib, 0), cart_exp(LB, ib, 1), cart_exp(LB, ib, 2)};
+                const HermiteE<double, LA + 1, LB + 2>* E3[3] = {&Ex, &Ey, &Ez};
+                for (int k = 0; k < 3; ++k) {
+                    // d/dA_k of S and T: shift a along k
+                    double dS = 0.0, dT = 0.0;
+                    for (int sgn = 0; sgn < 2; ++sgn) {
+                        int ak = a[k] + (sgn == 0 ? 1 : -1);
+                        if (ak < 0) continue;
+                        const double c = (sgn == 0) ? 2.0 * aexp : -static_cast<double>(a[k]);
+                        int aa[3] = {a[0], a[1], a[2]};
+                        aa[k] = ak;
+                        const double sx = s1(*E3[0], aa[0], b[0]), sy = s1(*E3[1], aa[1], b[1]), sz = s1(*E3[2], aa[2], b[2]);
+                        const double tx = t1(*E3[0], aa[0], b[0]), ty = t1(*E3[1], aa[1], b[1]), tz = t1(*E3[2], aa[2], b[2]);
+                        dS += c * sx * sy * sz;
+                        dT += c * (tx * sy * sz + sx * ty * sz + sx * sy * tz);
+                    }
+                    const double g = k1 * (dw[ia][ib] * dT - ww[ia][ib] * dS);
+                    gA[k] += g;
+                    gB[k] -= g;  // S and T depend on A - B only
+                }
+            }
+        // nuclear attraction: basis centres (shift of a) and the operator centre
+        for (int cidx = 0; cidx < natom; ++cidx) {
+            const double X = q.Px - atoms[4 * cidx], Y = q.Py - atoms[4 * cidx + 1], Z = q.Pz - atoms[4 * cidx + 2];
+            double Fs[L + 1];
+            boys_fp64<L>(p * (X * X + Y * Y + Z * Z), boys, Fs);
+            double sc = -atoms[4 * cidx + 3] * 2.0 * kPi / p * k1;
+            for (int m = 0; m <= L; ++m) { Fs[m] *= sc; sc *= -2.0 * p; }
+            HermiteR<double, L> R;
+            R.build(Fs, X, Y, Z);
+            double gCn[3] = {0, 0, 0};
+            for (int ia = 0; ia < NA; ++ia)
+                for (int ib = 0; ib < NB; ++ib) {
+                    const int a[3] = {cart_exp(LA, ia, 0), cart_exp(LA, ia, 1), cart_exp(LA, ia, 2)};
+                    const int b[3] = {cart_exp(LB, ib, 0), cart_exp(LB, ib, 1), cart_exp(LB, ib, 2)};
+                    const double dwv = dw[ia][ib];
+                    if (dwv == 0.0) continue;
+                    for (int k = 0; k < 3; ++k) {
+                        double dA = 0.0;
+                        for (int sgn = 0; sgn < 2; ++sgn) {
+                            int aa[3] = {a[0], a[1], a[2]};
+                            aa[k] += (sgn == 0 ? 1 : -1);
+                            if (aa[k] < 0) continue;
+                            const double c = (sgn == 0) ? 2.0 * aexp : -static_cast<double>(a[k]);
+                            double acc = 0.0;
+                            for (int t = 0; t <= aa[0] + b[0]; ++t)
+                                for (int u = 0; u <= aa[1] + b[1]; ++u)
+                                    for (int v = 0; v <= aa[2] + b[2]; ++v)
+                                        acc += Ex.e[aa[0]][b[0]][t] * Ey.e[aa[1]][b[1]][u] * Ez.e[aa[2]][b[2]][v] *
+                                               R.r[t][u][v];
+                            dA += c * acc;
+                        }
+                        // operator centre: d/dC_k R_tuv(P - C) = -R_{tuv + 1_k}
+                        double dC = 0.0;
+                        for (int t = 0; t <= a[0] + b[0]; ++t)
+                            for (int u = 0; u <= a[1] + b[1]; ++u)
+                                for (int v = 0; v <= a[2] + b[2]; ++v) {
+                                    const double ev = Ex.e[a[0]][b[0]][t] * Ey.e[a[1]][b[1]][u] * Ez.e[a[2]][b[2]][v];
+                                    const double rv = (k == 0) ? R.r[t + 1][u][v] : (k == 1) ? R.r[t][u + 1][v] : R.r[t][u][v + 1];
+                                    dC -= ev * rv;
+                                }
+                        gA[k] += dwv * dA;
+                        gB[k] -= dwv * (dA + dC);
+                        gCn[k] += dwv * dC;
+                    }
+                }
+            for (int k = 0; k < 3; ++k)
+                if (gCn[k] != 0.0) atomicAdd(&grad[3 * cidx + k], gCn[k]);
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        atomicAdd(&grad[3 * atA + k], gA[k]);
+        atomicAdd(&grad[3 * atB + k], gB[k]);
+    }
+}
+
+// W = 2 sum_{i < nocc} eps_i C_i C_i^T (C row-major, columns = orbitals)
+__global__ void energy_weighted_density_kernel(const double* __restrict__ C, const double* __restrict__ eps, int n,
+                                               int nocc, double* __restrict__ W)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long i = k / n, j = k % n;
+        double s = 0.0;
+        for (int o = 0; o < nocc; ++o) s += eps[o] * C[i * n + o] * C[j * n + o];
+        W[k] = 2.0 * s;
+    }
+}
+
+}  // namespace
+
+int energy_weighted_density(Engine& e, const double* d_C, const double* d_eps, int nocc, double* d_W, cudaStream_t s)
+{
+    const long long nn = static_cast<long long>(e.num_basis) * e.num_basis;
+    energy_weighted_density_kernel<<<static_cast<int>(std::min<long long>((nn + 255) / 256, 4096)), 256, 0, s>>>(
+        d_C, d_eps, e.num_basis, nocc, d_W);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad, cudaStream_t s, float* ms_out)
+{
+    const int natom = e.num_atoms;
+    if (!e.d_grad) {
+        if (cudaMalloc(&e.d_grad, sizeof(double) * 3 * natom) != cudaSuccess ||
+            cudaMalloc(&e.d_shell_atom, sizeof(int) * e.num_shells) != cudaSuccess)
+            return set_error("cudaMalloc of gradient buffers failed"), HF_ERR_OUT_OF_MEMORY;
+        std::vector<int> sa(e.num_shells);
+        for (int i = 0; i < e.num_shells; ++i) sa[i] = e.shells[i].atom;
+        GB_CUDA_TRY(cudaMemcpy(e.d_shell_atom, sa.data(), sizeof(int) * e.num_shells, cudaMemcpyHostToDevice));
+    }
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    cudaEventRecord(t0, s);
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_grad, 0, sizeof(double) * 3 * natom, s));
+    int st = scale_density(e, d_D, false, s);
+    if (st) return st;
+    // two-electron part over the FP64 quartet lists of every class
+    for (int c = 0; c < static_cast<int>(e.class_pairs.size()); ++c) {
+        const ClassPair& cp = e.class_pairs[c];
+        if (cp.n_survivors == 0) continue;
+        const PairClass& Y = e.pair_classes[cp.Y];
+        GradLaunch G;
+        G.L.pairs = e.d_pairs;
+        G.L.prim_pairs = e.d_pp64;
+        G.L.boys_table = e.d_boys64;
+        G.L.density = e.d_Dp64;
+        G.L.J = nullptr;
+        G.L.K = nullptr;
+        G.L.J32 = nullptr;
+        G.L.K32 = nullptr;
+        G.L.off = e.d_off_static + cp.entry_begin + c;
+        G.L.entry_bra = e.d_entry_bra + cp.entry_begin;
+        G.L.entry_lo = e.d_entry_lo0 + cp.entry_begin;
+        G.L.nentry = cp.nentry;
+        G.L.ket_base = Y.begin;
+        G.L.num_basis = e.num_basis;
+        G.L.schwarz_threshold = e.schwarz_threshold;
+        G.L.counters = e.d_counters;
+        G.shell_atom = e.d_shell_atom;
+        G.grad = e.d_grad;
+        const int ncd = ncart(Y.la) * ncart(Y.lb);
+        const long long warps = ((cp.n_survivors + 31) / 32) * ncd;
+        const int grid = static_cast<int>(std::max<long long>(
+            1, std::min<long long>((warps * 32 + kGradThreads - 1) / kGradThreads, static_cast<long long>(e.num_sms) * 32)));
+        grad_eri_kernel<<<grid, kGradThreads, 0, s>>>(G, ncd);
+        GB_LAUNCH_CHECK();
+    }
+    // one-electron part
+    const double kfold = std::sqrt(2.0 * std::pow(kPi, 2.5));
+    for (const PairClass& pc : e.pair_classes) {
+        if (pc.count == 0) continue;
+        const int grid = (pc.count + 127) / 128;
+#define GB_G1(a, b)                                                                                                 \
+    if (pc.la == a && pc.lb == b)                                                                                   \
+        grad_one_electron_kernel<a, b><<<grid, 128, 0, s>>>(e.d_pairs, pc.begin, pc.count, e.d_pp64, e.d_boys64,    \
+                                                            e.d_atoms, e.num_atoms, e.d_shell_atom, e.d_scale, d_D, \
+                                                            d_W, e.num_basis, kfold, e.d_grad);
+        GB_G1(0, 0) GB_G1(1, 0) GB_G1(1, 1) GB_G1(2, 0) GB_G1(2, 1) GB_G1(2, 2)
+#undef GB_G1
+        GB_LAUNCH_CHECK();
+    }
+    cudaEventRecord(t1, s);
+    GB_CUDA_TRY(cudaMemcpyAsync(h_grad, e.d_grad, sizeof(double) * 3 * natom, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (ms_out) *ms_out = ms;
+    // nuclear repulsion: d/dR_A sum_{A<B} Z_A Z_B / |R_A - R_B|
+    for (int A = 0; A < natom; ++A)
+        for (int B = 0; B < natom; ++B) {
+            if (A == B) continue;
+            const double dx = e.atoms[A].x - e.atoms[B].x, dy = e.atoms[A].y - e.atoms[B].y,
+                         dz = e.atoms[A].z - e.atoms[B].z;
+            const double r2 = dx * dx + dy * dy + dz * dz, r = std::sqrt(r2);
+            const double f = -static_cast<double>(e.atoms[A].atomic_number) * e.atoms[B].atomic_number / (r2 * r);
+            h_grad[3 * A] += f * dx;
+            h_grad[3 * A + 1] += f * dy;
+            h_grad[3 * A + 2] += f * dz;
+        }
+    return HF_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int hf_energy_weighted_density(hf_engine* eng, const double* d_coefficients, const double* d_orbital_energies,
+                               int num_occupied, double* d_out, void* stream)
+{
+    clear_error();
+    if (!eng || !d_coefficients || !d_orbital_energies || !d_out || num_occupied <= 0)
+        return set_error("null argument or non-positive num_occupied"), HF_ERR_INVALID_ARGUMENT;
+    return energy_weighted_density(*reinterpret_cast<Engine*>(eng), d_coefficients, d_orbital_energies, num_occupied,
+                                   d_out, static_cast<cudaStream_t>(stream));
+}
+
+int hf_rhf_gradient(hf_engine* eng, const double* d_density, const double* d_energy_weighted_density,
+                    double* h_gradient, double* gradient_ms, void* stream)
+{
+    clear_error();
+    if (!eng || !d_density || !d_energy_weighted_density || !h_gradient)
+        return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    float ms = 0.f;
+    const int st = rhf_gradient(*reinterpret_cast<Engine*>(eng), d_density, d_energy_weighted_density, h_gradient,
+                                static_cast<cudaStream_t>(stream), &ms);
+    if (gradient_ms) *gradient_ms = ms;
+    return st;
+}
+
+}  // extern "C"

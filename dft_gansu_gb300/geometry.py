@@ -37,6 +37,12 @@ def _unit(v):
 
 def alkane(n_carbon: int = 10, jitter: float = 0.02, seed: int = 0, cc: float = 1.54, ch: float = 1.09):
     """Zig-zag n-alkane C_n H_{2n+2} with tetrahedral angles (bohr)."""
+    if n_carbon == 1:  # methane: four H on the tetrahedron vertices
+        t = ch / math.sqrt(3.0)
+        coords = np.array([[0.0, 0.0, 0.0], [t, t, t], [t, -t, -t], [-t, t, -t], [-t, -t, t]])
+        if jitter:
+            coords = coords + np.random.default_rng(seed).normal(0.0, jitter, coords.shape)
+        return _to_atoms(["C", "H", "H", "H", "H"], coords)
     half = TETRA / 2.0
     carbons = np.array([[i * cc * math.sin(half), (i % 2) * cc * math.cos(half), 0.0] for i in range(n_carbon)])
     symbols, coords = [], []

@@ -212,6 +212,24 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt, hf_
                double* d_density_out, double* d_fock_out, double* d_orbital_energies_out,
                double* d_coefficients_out);
 
+/* ------------------------------------------------------------- gradient */
+/* Energy-weighted density W = 2 sum_{i < num_occupied} eps_i C_i C_i^T from the
+ * SCF's coefficients (row-major, orbitals as columns) and orbital energies.
+ * No reference counterpart (the reference has no analytic gradient). */
+int hf_energy_weighted_density(hf_engine* eng, const double* d_coefficients, const double* d_orbital_energies,
+                               int num_occupied, double* d_out, void* stream);
+
+/* Analytic RHF nuclear gradient dE/dR (3 * num_atoms doubles, host, bohr,
+ * Eh/bohr) from the converged density D and energy-weighted density W:
+ * sum D dH - sum W dS + derivative ERIs contracted with the two-particle
+ * density (Hermite intermediates recomputed, FP64) + nuclear repulsion.
+ * The backward half of the energy/gradient pair that feeds a geometry
+ * optimiser (the reference only has an energy-only coordinate search,
+ * include/builder.hpp:108-275).  gradient_ms (may be NULL) receives the
+ * device time. */
+int hf_rhf_gradient(hf_engine* eng, const double* d_density, const double* d_energy_weighted_density,
+                    double* h_gradient, double* gradient_ms, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

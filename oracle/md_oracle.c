@@ -9,7 +9,7 @@
  *     their sources (oracle/refcpu/, built into oracle/_ref/), element by
  *     element for S, H, the primitive Schwarz bounds and the full ERI tensor;
  *   - against the reference's own linear-algebra known answers
- *     (test/test_gpu_manager.cu) for the SCF pieces in oracle/scf_oracle.py.
+ *     (test/test_gpu_manager.cu) for the SCF pieces in oracle/oracle.py.
  *
  * What it restates (reference file:line):
  *   Boys function F_n(x) = int_0^1 t^{2n} exp(-x t^2) dt      include/boys.hpp:32-182
@@ -25,6 +25,16 @@
  *   screening of a primitive quartet by Q_ab*Q_cd < thr        src/int2e.cu:1677-1680
  *   Fock F_ij = H_ij + sum_kl D_kl[(ij|kl) - 1/2 (ik|jl)]      src/gpu_kernels.cu:230-287
  *   S, T (kinetic) and V (nuclear attraction) matrices         src/gpu_manager.cu:333-404
+ *   RI: auxiliary functions are contracted shells of their own basis file,
+ *     normalised like orbital shells; (mu nu|P) and (P|Q) are four-centre
+ *     integrals with an exponent-0 unit s function as partner
+ *                                                              src/int3c2e.cu:1102-1330,
+ *                                                              src/int2c2e.cu:468-690
+ *     auxiliary Cartesian order loop_to_ang_RI (f differs)     include/int2c2e.hpp:39-47
+ *     auxiliary primitive bound sqrt(max_comp g_P^2 N^2 c^2 (P|P)), with the
+ *     auxiliary CGTO factor                                    src/schwarz.txt:480-682
+ *     screening Q_ab*Q_P < thr (3c) and Q_P*Q_Q < thr (2c)     src/int3c2e.cu, src/int2c2e.cu
+ *     (P|mu nu) written to both (mu,nu) and (nu,mu)            include/int3c2e.hpp:150-154
  *
  * Cartesian component order within a shell follows include/types.hpp:197-228.
  */
@@ -181,8 +191,21 @@ typedef struct {
 } or_basis;
 
 /* reference calcNorm: 2^L / sqrt((2l-1)!!(2m-1)!!(2n-1)!!) (2/pi)^{3/4} a^{(2L+3)/4} */
+/* Cartesian order of auxiliary shells (include/int2c2e.hpp:39-47): the same
+ * as or_cart except for f. */
+static const int or_cart_ri[OR_LMAX + 1][15][3] = {
+    {{0, 0, 0}},
+    {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},
+    {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}},
+    {{3, 0, 0}, {0, 3, 0}, {0, 0, 3}, {2, 1, 0}, {2, 0, 1}, {0, 2, 1}, {1, 2, 0}, {0, 1, 2}, {1, 0, 2}, {1, 1, 1}},
+    {{4, 0, 0}, {0, 4, 0}, {0, 0, 4}, {3, 1, 0}, {3, 0, 1}, {0, 3, 1}, {1, 3, 0}, {0, 1, 3}, {1, 0, 3},
+     {2, 2, 0}, {2, 0, 2}, {0, 2, 2}, {2, 1, 1}, {1, 2, 1}, {1, 1, 2}}};
+
+/* Normalisation of a primitive Cartesian; an exponent of exactly 0 marks the
+ * unit s function that turns a four-centre integral into a 3c/2c one. */
 static double or_prim_norm(double a, int l, int m, int n)
 {
+    if (a == 0.0) return 1.0;
     int L = l + m + n;
     return pow(2.0, L) / sqrt(or_dfact(2 * l - 1) * or_dfact(2 * m - 1) * or_dfact(2 * n - 1)) *
            pow(2.0 / OR_PI, 0.75) * pow(a, (2.0 * L + 3.0) / 4.0);
@@ -206,10 +229,12 @@ double oracle_cgto_factor(int L, int nprim, const double* alpha, const double* c
 
 /* Primitive quartet integrals over normalised primitive Cartesians (prim
  * norms included, coefficients and CGTO factors not), out[a][b][c][d]. */
-static void or_prim_quartet(int la, int lb, int lc, int ld,
-                            double a, double b, double c, double d,
-                            const double* A, const double* B, const double* C, const double* D,
-                            double* out)
+typedef const int (*or_order)[15][3];
+
+static void or_prim_quartet_o(int la, int lb, int lc, int ld,
+                              double a, double b, double c, double d,
+                              const double* A, const double* B, const double* C, const double* D,
+                              or_order oa, or_order ob, or_order oc, or_order od, double* out)
 {
     const int RD = OR_RDIM;
     const double p = a + b, q = c + d, alpha = p * q / (p + q);
@@ -230,8 +255,8 @@ static void or_prim_quartet(int la, int lb, int lc, int ld,
         for (int ib = 0; ib < nb; ++ib)
             for (int ic = 0; ic < nc; ++ic)
                 for (int id = 0; id < nd; ++id) {
-                    const int* ea = or_cart[la][ia]; const int* eb = or_cart[lb][ib];
-                    const int* ec = or_cart[lc][ic]; const int* ed = or_cart[ld][id];
+                    const int* ea = oa[la][ia]; const int* eb = ob[lb][ib];
+                    const int* ec = oc[lc][ic]; const int* ed = od[ld][id];
                     double s = 0.0;
                     for (int t = 0; t <= ea[0] + eb[0]; ++t)
                         for (int u = 0; u <= ea[1] + eb[1]; ++u)
@@ -252,6 +277,14 @@ static void or_prim_quartet(int la, int lb, int lc, int ld,
                     out[((ia * nb + ib) * nc + ic) * nd + id] = pref * s * nrm;
                 }
     free(R);
+}
+
+static void or_prim_quartet(int la, int lb, int lc, int ld,
+                            double a, double b, double c, double d,
+                            const double* A, const double* B, const double* C, const double* D,
+                            double* out)
+{
+    or_prim_quartet_o(la, lb, lc, ld, a, b, c, d, A, B, C, D, or_cart, or_cart, or_cart, or_cart, out);
 }
 
 /* Primitive-pair Schwarz bound, reference definition: sqrt(max over Cartesian
@@ -550,5 +583,110 @@ int oracle_one_electron(int nshell, const int* l, const int* nprim, const int* p
                 }
             free(R);
         }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ RI */
+
+/* Auxiliary primitive bounds (src/schwarz.txt:480-682), one per auxiliary
+ * primitive in the order of the auxiliary primitive list. */
+static void or_aux_bounds(const or_basis* ax, double* out)
+{
+    for (int P = 0; P < ax->nshell; ++P) {
+        const int lp = ax->l[P], np = or_ncart(lp);
+        double buf[15 * 15];
+        for (int i = 0; i < ax->nprim[P]; ++i) {
+            const int pi = ax->prim_off[P] + i;
+            const double g = ax->alpha[pi], c = ax->coef[pi];
+            or_prim_quartet_o(lp, 0, lp, 0, g, 0.0, g, 0.0, &ax->xyz[3 * P], &ax->xyz[3 * P], &ax->xyz[3 * P],
+                              &ax->xyz[3 * P], or_cart_ri, or_cart, or_cart_ri, or_cart, buf);
+            double mx = 0.0;
+            for (int k = 0; k < np; ++k) {
+                const double f = ax->cgto[ax->bf_off[P] + k];
+                const double v = f * f * c * c * buf[k * np + k];
+                if (fabs(v) > fabs(mx)) mx = v;
+            }
+            out[pi] = sqrt(mx);
+        }
+    }
+}
+
+/* RI metric V[P*naux+Q] = (P|Q) and three-centre T[(P*nbf+mu)*nbf+nu] = (mu nu|P)
+ * with the reference's primitive screening; aux_bounds (may be NULL) receives
+ * the auxiliary primitive bounds. */
+int oracle_ri_integrals(int nshell, const int* l, const int* nprim, const int* prim_off, const int* bf_off,
+                        const double* xyz, const double* alpha, const double* coef, const double* cgto, int nbf,
+                        int ashell, const int* al, const int* anprim, const int* aprim_off, const int* abf_off,
+                        const double* axyz, const double* aalpha, const double* acoef, const double* acgto,
+                        int naux, double thr, double* V, double* T, double* aux_bounds)
+{
+    or_basis bs, ax;
+    or_make_basis(&bs, nshell, l, nprim, prim_off, bf_off, xyz, alpha, coef, cgto, nbf);
+    or_make_basis(&ax, ashell, al, anprim, aprim_off, abf_off, axyz, aalpha, acoef, acgto, naux);
+    int naprim = 0;
+    for (int P = 0; P < ashell; ++P) naprim += anprim[P];
+    double* QP = (double*)malloc(sizeof(double) * (naprim > 0 ? naprim : 1));
+    or_aux_bounds(&ax, QP);
+    if (aux_bounds) memcpy(aux_bounds, QP, sizeof(double) * naprim);
+    int* off;
+    double* Q = or_all_bounds(&bs, &off);
+    const size_t N = (size_t)nbf, M = (size_t)naux;
+    if (V) {
+        memset(V, 0, sizeof(double) * M * M);
+#pragma omp parallel for collapse(2) schedule(dynamic)
+        for (int P = 0; P < ashell; ++P)
+            for (int R = 0; R < ashell; ++R) {
+                const int lp = al[P], lr = al[R], np = or_ncart(lp), nr = or_ncart(lr);
+                double blk[15 * 15], tmp[15 * 15];
+                memset(blk, 0, sizeof(blk));
+                for (int i = 0; i < anprim[P]; ++i)
+                    for (int k = 0; k < anprim[R]; ++k) {
+                        const int pi = aprim_off[P] + i, pk = aprim_off[R] + k;
+                        if (QP[pi] * QP[pk] < thr) continue;
+                        or_prim_quartet_o(lp, 0, lr, 0, aalpha[pi], 0.0, aalpha[pk], 0.0, &axyz[3 * P], &axyz[3 * P],
+                                          &axyz[3 * R], &axyz[3 * R], or_cart_ri, or_cart, or_cart_ri, or_cart, tmp);
+                        for (int e = 0; e < np * nr; ++e) blk[e] += acoef[pi] * acoef[pk] * tmp[e];
+                    }
+                for (int ip = 0; ip < np; ++ip)
+                    for (int ir = 0; ir < nr; ++ir)
+                        V[(size_t)(abf_off[P] + ip) * M + abf_off[R] + ir] =
+                            blk[ip * nr + ir] * acgto[abf_off[P] + ip] * acgto[abf_off[R] + ir];
+            }
+    }
+    if (T) {
+        memset(T, 0, sizeof(double) * M * N * N);
+#pragma omp parallel for collapse(2) schedule(dynamic)
+        for (int A = 0; A < nshell; ++A)
+            for (int B = 0; B < nshell; ++B) {
+                const int la = l[A], lb = l[B], na = or_ncart(la), nb = or_ncart(lb);
+                double blk[15 * 15 * 15], tmp[15 * 15 * 15];
+                for (int P = 0; P < ashell; ++P) {
+                    const int lp = al[P], np = or_ncart(lp);
+                    memset(blk, 0, sizeof(double) * na * nb * np);
+                    for (int i = 0; i < nprim[A]; ++i)
+                        for (int j = 0; j < nprim[B]; ++j) {
+                            const int pa = prim_off[A] + i, pb = prim_off[B] + j;
+                            const double qab = Q[off[A * nshell + B] + i * nprim[B] + j];
+                            for (int k = 0; k < anprim[P]; ++k) {
+                                const int pk = aprim_off[P] + k;
+                                if (qab * QP[pk] < thr) continue;
+                                or_prim_quartet_o(la, lb, lp, 0, alpha[pa], alpha[pb], aalpha[pk], 0.0, &xyz[3 * A],
+                                                  &xyz[3 * B], &axyz[3 * P], &axyz[3 * P], or_cart, or_cart, or_cart_ri,
+                                                  or_cart, tmp);
+                                const double cf = coef[pa] * coef[pb] * acoef[pk];
+                                for (int e = 0; e < na * nb * np; ++e) blk[e] += cf * tmp[e];
+                            }
+                        }
+                    for (int ia = 0; ia < na; ++ia)
+                        for (int ib = 0; ib < nb; ++ib)
+                            for (int ip = 0; ip < np; ++ip) {
+                                const size_t mu = bf_off[A] + ia, nu = bf_off[B] + ib, r = abf_off[P] + ip;
+                                T[(r * N + mu) * N + nu] =
+                                    blk[(ia * nb + ib) * np + ip] * cgto[mu] * cgto[nu] * acgto[r];
+                            }
+                }
+            }
+    }
+    free(QP); free(Q); free(off);
     return 0;
 }

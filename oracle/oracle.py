@@ -29,6 +29,7 @@ from dataclasses import dataclass, field
 from pathlib import Path
 
 import numpy as np
+import scipy.linalg
 
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
@@ -360,6 +361,47 @@ def rhf_from_basis(b: Basis, thr_schwarz=1e-12, stored=True, **kw):
     return rhf(S, H, fock, b.num_electrons // 2, nuclear_repulsion(b.atoms), **kw)
 
 
+# ------------------------------------------------------------ RI
+def ri_integrals(b: Basis, aux: Basis, thr=1e-12):
+    """Metric V (naux x naux), three-centre T (naux x N x N) and the auxiliary
+    primitive bounds, restated from src/int2c2e.cu, src/int3c2e.cu and
+    src/schwarz.txt:480-682 (md_oracle.c: oracle_ri_integrals)."""
+    M, N = aux.nbf, b.nbf
+    V, T = np.zeros((M, M)), np.zeros((M, N, N))
+    qp = np.zeros(len(aux.alpha))
+    _lib().oracle_ri_integrals(*b.cargs(), *aux.cargs(), C.c_double(thr), _dp(V), _dp(T), _dp(qp))
+    return V, T, qp
+
+
+def ri_factor(V, T):
+    """B = L^-1 T with V = L L^T (src/gpu_manager.cu:1448-1526: potrf, then a
+    lower-triangular solve on the naux x N^2 matrix)."""
+    L = np.linalg.cholesky(V)
+    M = T.shape[0]
+    return scipy.linalg.solve_triangular(L, T.reshape(M, -1), lower=True).reshape(T.shape)
+
+
+def ri_jk(B, D):
+    """J = sum_P B_P (B_P . D), K = sum_P B_P D B_P^T (src/gpu_manager.cu:1543-1632)."""
+    W = np.einsum("pij,ij->p", B, D)
+    J = np.einsum("p,pij->ij", W, B)
+    K = np.einsum("pik,kl,pjl->ij", B, D, B, optimize=True)
+    return J, K
+
+
+def rhf_ri_from_basis(b: Basis, aux: Basis, thr_schwarz=1e-12, **kw):
+    """RI-RHF with the reference's SCF loop (ERI_RI_RHF, include/rhf.hpp:644-691)."""
+    S, T1, V1 = one_electron(b)
+    H = T1 + V1
+    V, T, _ = ri_integrals(b, aux, thr_schwarz)
+    B = ri_factor(V, T)
+
+    def fock(D):
+        J, K = ri_jk(B, D)
+        return H + J - 0.5 * K
+    return rhf(S, H, fock, b.num_electrons // 2, nuclear_repulsion(b.atoms), **kw)
+
+
 # -------------------------------------------------- reference on the CPU
 def refcpu_integrals(b: Basis, thr=1e-12, want_eri=True):
     """S, H, primitive Schwarz bounds (reference layout) and the ERI tensor as
@@ -384,3 +426,22 @@ def refcpu_integrals(b: Basis, thr=1e-12, want_eri=True):
                             _ip(z), _dp(axyz), float(thr), _dp(S), _dp(H), _dp(eri) if want_eri else None,
                             _dp(bounds), C.byref(nb))
     return {"S": S, "H": H, "eri": eri, "bounds": bounds[: nb.value], "primitives": rows}
+
+
+def refcpu_ri_integrals(b: Basis, aux: Basis, thr=1e-12):
+    """(P|Q), (mu nu|P) and the auxiliary primitive bounds from the reference's
+    own RI kernels run on the CPU (bounds in the reference's primitive order)."""
+    def cols(bb):
+        rows = bb.reference_primitives()
+        return (len(rows), np.array([r[1] for r in rows]), np.array([r[2] for r in rows]),
+                np.ascontiguousarray(np.array([r[3] for r in rows])), np.array([r[0] for r in rows], np.int32),
+                np.array([r[4] for r in rows], np.int64), np.array([r[5] for r in rows], np.int32))
+    n, e, c, x, st, bi, ai = cols(b)
+    an, ae, ac, ax, ast, abi, aai = cols(aux)
+    M, N = aux.nbf, b.nbf
+    V, T, qp = np.zeros((M, M)), np.zeros((M, N, N)), np.zeros(an)
+    ll = lambda a: a.ctypes.data_as(C.POINTER(C.c_longlong))
+    _ref().refcpu_ri_integrals(n, _dp(e), _dp(c), _dp(x), _ip(st), ll(bi), _ip(ai), _dp(b.cgto), N,
+                               an, _dp(ae), _dp(ac), _dp(ax), _ip(ast), ll(abi), _ip(aai), _dp(aux.cgto), M,
+                               C.c_double(thr), _dp(V), _dp(T), _dp(qp))
+    return V, T, qp

@@ -1,10 +1,11 @@
 """Generates the golden fixtures in tests/golden/ from the reference's own
-integral kernels (oracle/refcpu: src/int2e.cu and src/int1e.cu of the
-reference compiled for the CPU) on the inputs below.  Needs the reference
+integral kernels (oracle/refcpu: src/int2e.cu, src/int1e.cu, src/int2c2e.cu
+and src/int3c2e.cu of the reference compiled for the CPU) on the inputs below.  Needs the reference
 tree (GANSU_REFERENCE, default /root/reference); the fixtures themselves are
 committed so that the tests need neither the reference nor this script.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # all fixtures
+    python tests/golden/make_golden.py --ri     # the RI fixtures only
 """
 import sys
 from pathlib import Path
@@ -52,5 +53,45 @@ def main():
         print(f"{name}: N={N} E={scf['total_energy']:.10f} iters={scf['iterations']}")
 
 
+RI_CASES = {
+    "ri_water_sto-3g": (geometry.water(), "sto-3g", True),
+    "ri_water_cc-pvdz": (geometry.water(), "cc-pvdz", False),
+    "ri_methane_cc-pvdz": (geometry.alkane(1, jitter=0.03, seed=4), "cc-pvdz", False),
+}
+
+
+def main_ri():
+    """(P|Q), (mu nu|P), auxiliary bounds and the RI-SCF energy on the
+    reference's own RI integrals (auxiliary basis cc-pVDZ-RIFIT)."""
+    O.build_refcpu()
+    rng = np.random.default_rng(1)
+    for name, (atoms, gbs, full) in RI_CASES.items():
+        b = O.make_basis(atoms, BASIS / f"{gbs}.gbs")
+        ax = O.make_basis(atoms, BASIS / "cc-pvdz-rifit.gbs")
+        V, T, qp = O.refcpu_ri_integrals(b, ax, thr=1e-12)
+        r = O.refcpu_integrals(b, thr=1e-12, want_eri=False)
+        B = O.ri_factor(V, T)
+        H = r["H"]
+
+        def fock(D):
+            J, K = O.ri_jk(B, D)
+            return H + J - 0.5 * K
+        scf = O.rhf(r["S"], H, fock, b.num_electrons // 2, O.nuclear_repulsion(atoms), thr=1e-10)
+        out = {"atoms": np.array(atoms), "V": V, "aux_bounds": qp, "energy_total": scf["total_energy"],
+               "iterations": scf["iterations"], "T_sum": T.sum(), "T_abs_sum": np.abs(T).sum(),
+               "T_sq_sum": (T * T).sum()}
+        if full:
+            out["T"] = T
+        else:
+            M, N = ax.nbf, b.nbf
+            idx = np.stack([rng.integers(0, M, 4000), rng.integers(0, N, 4000), rng.integers(0, N, 4000)], 1)
+            out["T_idx"] = idx
+            out["T_val"] = T[idx[:, 0], idx[:, 1], idx[:, 2]]
+        np.savez_compressed(Path(__file__).parent / f"{name}.npz", **out)
+        print(f"{name}: N={b.nbf} naux={ax.nbf} E_RI={scf['total_energy']:.10f} iters={scf['iterations']}")
+
+
 if __name__ == "__main__":
-    main()
+    if "--ri" not in sys.argv:
+        main()
+    main_ri()

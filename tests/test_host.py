@@ -123,6 +123,9 @@ def test_geometries():
     assert abs(cc - 1.54) < 1e-9
     hs = [np.linalg.norm(x[i] - x[j]) for i in range(10) for j in range(10, 32) if np.linalg.norm(x[i] - x[j]) < 1.2]
     assert len(hs) == 22 and np.allclose(hs, 1.09)
+    ch4 = np.array([a[1:] for a in geometry.alkane(1, jitter=0.0)]) / geometry.ANGSTROM_TO_BOHR
+    assert [a[0] for a in geometry.alkane(1)] == [6, 1, 1, 1, 1]
+    assert np.allclose(np.linalg.norm(ch4[1:] - ch4[0], axis=1), 1.09)
     c = np.array([a[1:] for a in geometry.c60(jitter=0.0)]) / geometry.ANGSTROM_TO_BOHR
     d = np.linalg.norm(c[:, None] - c[None], axis=-1)
     bonds = np.sort(d[(d > 0.1) & (d < 1.6)])

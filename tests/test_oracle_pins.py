@@ -1,8 +1,10 @@
 """The oracle is pinned before it is trusted.
 
 1. Against golden fixtures produced by the reference's OWN integral kernels
-   (src/int2e.cu, src/int1e.cu compiled for the CPU; tests/golden/make_golden.py):
-   S, H, primitive Schwarz bounds, ERI elements and checksums, SCF energy.
+   (src/int2e.cu, src/int1e.cu, src/int2c2e.cu, src/int3c2e.cu compiled for the
+   CPU; tests/golden/make_golden.py): S, H, primitive Schwarz bounds, ERI
+   elements and checksums, SCF energy; RI metric, three-centre integrals,
+   auxiliary bounds and the RI-SCF energy.
 2. Live against those kernels when the reference tree is mounted (oracle/_ref).
 3. Boys function against 40-digit quadrature of its definition (mpmath).
 4. The reference's linear-algebra known answers (test/test_gpu_manager.cu) for
@@ -113,3 +115,50 @@ def test_diis_bordered_solve_is_affine():
     F = O.diis_extrapolate(errs, focks)
     # coefficients sum to one: extrapolating constant matrices gives a constant
     assert np.allclose(F, F[0, 0])
+
+
+RI_CASES = ["ri_water_sto-3g", "ri_water_cc-pvdz", "ri_methane_cc-pvdz"]
+
+
+def _ri_basis(case):
+    g = np.load(GOLD / f"{case}.npz")
+    gbs = case.split("_", 2)[2]
+    atoms = [(int(a[0]), a[1], a[2], a[3]) for a in g["atoms"]]
+    return g, O.make_basis(atoms, BASIS / f"{gbs}.gbs"), O.make_basis(atoms, BASIS / "cc-pvdz-rifit.gbs")
+
+
+@pytest.mark.parametrize("case", RI_CASES)
+def test_oracle_ri_integrals_match_reference_kernels(case):
+    g, b, ax = _ri_basis(case)
+    V, T, qp = O.ri_integrals(b, ax, 1e-12)
+    assert np.abs(V - g["V"]).max() < 1e-12 * max(1.0, np.abs(g["V"]).max())
+    if "T" in g:
+        assert np.abs(T - g["T"]).max() < 1e-12
+    else:
+        idx = g["T_idx"]
+        assert np.abs(T[idx[:, 0], idx[:, 1], idx[:, 2]] - g["T_val"]).max() < 1e-12
+    assert abs(T.sum() - g["T_sum"]) < 1e-10 * max(1.0, abs(float(g["T_sum"])))
+    assert abs((T * T).sum() - g["T_sq_sum"]) < 1e-10 * float(g["T_sq_sum"])
+    # the reference sorts auxiliary primitives by bound inside each type; compare as multisets
+    np.testing.assert_allclose(np.sort(qp), np.sort(g["aux_bounds"]), rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("case", RI_CASES[:2])
+def test_oracle_ri_scf_energy_matches_reference_integrals(case):
+    g, b, ax = _ri_basis(case)
+    res = O.rhf_ri_from_basis(b, ax, thr=1e-10)
+    assert res["converged"]
+    assert abs(res["total_energy"] - float(g["energy_total"])) < 1e-8
+
+
+def test_oracle_ri_live_against_reference_kernels():
+    if not O.refcpu_available():
+        pytest.skip("reference tree not mounted")
+    from dft_gansu_gb300 import geometry
+    atoms = [(z, x + 0.02 * i, y, w - 0.01 * i) for i, (z, x, y, w) in enumerate(geometry.water())]
+    b = O.make_basis(atoms, BASIS / "6-31g_st.gbs")
+    ax = O.make_basis(atoms, BASIS / "cc-pvdz-rifit.gbs")
+    V, T, _ = O.ri_integrals(b, ax, 1e-10)
+    Vr, Tr, _ = O.refcpu_ri_integrals(b, ax, 1e-10)
+    assert np.abs(V - Vr).max() < 1e-12 * np.abs(Vr).max()
+    assert np.abs(T - Tr).max() < 1e-12
