@@ -12,7 +12,7 @@ from pathlib import Path
 
 import numpy as np
 
-from ._capi import (HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
+from ._capi import (HF_ERI_DIRECT, HF_ERI_RI, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
                     check, lib)
 
 BASIS_DIR = Path(__file__).resolve().parent / "basis"
@@ -20,7 +20,7 @@ ANGSTROM_TO_BOHR = 1.8897259886
 
 __all__ = [
     "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
-    "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "basis_path",
+    "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "basis_path",
 ]
 
 
@@ -235,6 +235,40 @@ class Engine:
               "hf_rhf_gradient")
         return g.reshape(-1, 3), ms.value
 
+    # ------------------------------------------------------------ RI
+    def set_auxiliary_basis(self, aux: "Molecular"):
+        """Attach the auxiliary basis (Molecular(atoms, auxiliary_gbsfilename))."""
+        check(lib().hf_engine_set_auxiliary_basis(self._h, aux._prims, aux.num_primitives, aux._cgto, aux.num_basis),
+              "hf_engine_set_auxiliary_basis")
+        self.aux = aux
+        self.naux = aux.num_basis
+
+    def two_center_eris(self, stream=None):
+        V = self._empty(self.naux, self.naux)
+        check(lib().hf_compute_two_center_eris(self._h, _ptr(V), _stream(stream)), "hf_compute_two_center_eris")
+        return V
+
+    def three_center_eris(self, stream=None):
+        T = self._empty(self.naux, self.N, self.N)
+        check(lib().hf_compute_three_center_eris(self._h, _ptr(T), _stream(stream)), "hf_compute_three_center_eris")
+        return T
+
+    def ri_intermediate_b(self, want: bool = True, stream=None):
+        B = self._empty(self.naux, self.N, self.N) if want else None
+        check(lib().hf_compute_ri_intermediate_b(self._h, _ptr(B), _stream(stream)), "hf_compute_ri_intermediate_b")
+        return B
+
+    def jk_ri(self, density, stream=None):
+        J, K = self._empty(self.N, self.N), self._empty(self.N, self.N)
+        check(lib().hf_compute_jk_ri(self._h, _ptr(density), _ptr(J), _ptr(K), _stream(stream)), "hf_compute_jk_ri")
+        return J, K
+
+    def fock_ri(self, density, core_hamiltonian, stream=None):
+        F = self._empty(self.N, self.N)
+        check(lib().hf_compute_fock_ri_rhf(self._h, _ptr(density), _ptr(core_hamiltonian), _ptr(F), _stream(stream)),
+              "hf_compute_fock_ri_rhf")
+        return F
+
     def energy_and_gradient(self, num_electrons: int, options: dict | None = None):
         """Forward (SCF energy) and backward (analytic gradient) pair."""
         r = self.rhf_scf(num_electrons, options, want_matrices=True)
@@ -274,7 +308,7 @@ _DEFAULTS = {
 }
 _SHORT = {"-m": "method", "-v": "verbose", "-p": "parameter_file", "-x": "xyzfilename", "-g": "gbsfilename",
           "-ag": "auxiliary_gbsfilename", "-c": "charge"}
-_KEEP_CASE = {"xyzfilename", "gbsfilename", "parameter_file"}
+_KEEP_CASE = {"xyzfilename", "gbsfilename", "parameter_file", "auxiliary_gbsfilename"}
 
 
 class ParameterManager:
@@ -325,8 +359,10 @@ class ParameterManager:
 
 
 class RHF:
-    """Mirror of gansu::RHF (include/rhf.hpp, src/rhf.cu) for the direct and
-    stored ERI methods: ``solve()`` runs the SCF on the GPU."""
+    """Mirror of gansu::RHF (include/rhf.hpp, src/rhf.cu) for the direct,
+    stored and ri ERI methods: ``solve()`` runs the SCF on the GPU.  ``stored``
+    and ``direct`` both run the fused direct build (no N^4 tensor); ``ri``
+    builds Molecular(atoms, auxiliary_gbsfilename) as src/rhf.cu:76-79 does."""
 
     def __init__(self, molecular: Molecular, parameters: ParameterManager):
         if molecular.num_alpha_spins != molecular.num_beta_spins:
@@ -334,13 +370,18 @@ class RHF:
         self.mol = molecular
         self.params = parameters
         method = parameters["eri_method"]
-        if method not in ("stored", "direct"):
+        if method not in ("stored", "direct", "ri"):
             raise ValueError(f"Invalid ERI method name: {method}")
         if parameters["convergence_method"] != "diis":
             raise ValueError("only the DIIS convergence method is provided by this engine")
         if parameters["initial_guess"] != "core":
             raise ValueError("only the core-Hamiltonian initial guess is provided by this engine")
         self.engine = Engine(molecular, parameters.get("schwarz_screening_threshold", float))
+        self.eri_method = HF_ERI_RI if method == "ri" else HF_ERI_DIRECT
+        if method == "ri":
+            atoms = [(a.atomic_number, a.x, a.y, a.z) for a in molecular._atoms]
+            self.auxiliary = Molecular(atoms, parameters["auxiliary_gbsfilename"])
+            self.engine.set_auxiliary_basis(self.auxiliary)
         self.result = None
 
     def solve(self) -> float:
@@ -354,6 +395,7 @@ class RHF:
             "mixed_threshold": p.get("mixed_threshold", float),
             "incremental": int(p.get("incremental_fock", bool)),
             "verbose": p.get("verbose", int),
+            "eri_method": self.eri_method,
         }
         self.result = self.engine.rhf_scf(self.mol.num_electrons, opts, want_matrices=True)
         return self.result["total_energy"]

@@ -22,6 +22,8 @@ HF_ERR_NOT_SPD = 7
 
 HF_PRECISION_FP64 = 0
 HF_PRECISION_MIXED = 1
+HF_ERI_DIRECT = 0
+HF_ERI_RI = 1
 
 
 class PrimitiveShell(C.Structure):
@@ -58,6 +60,7 @@ class ScfOptions(C.Structure):
         ("full_build_precision", C.c_int),
         ("eigensolver", C.c_int),
         ("verbose", C.c_int),
+        ("eri_method", C.c_int),
     ]
 
 
@@ -111,6 +114,12 @@ SIGNATURES = {
     "hf_compute_fock_diis_noalloc": (_I, [_P, _P, _P, _I, _I, _P]),
     "hf_energy_weighted_density": (_I, [_P, _P, _P, _I, _P, _P]),
     "hf_rhf_gradient": (_I, [_P, _P, _P, C.POINTER(_D), C.POINTER(_D), _P]),
+    "hf_engine_set_auxiliary_basis": (_I, [_P, _P, _I, _P, _I]),
+    "hf_compute_two_center_eris": (_I, [_P, _P, _P]),
+    "hf_compute_three_center_eris": (_I, [_P, _P, _P]),
+    "hf_compute_ri_intermediate_b": (_I, [_P, _P, _P]),
+    "hf_compute_fock_ri_rhf": (_I, [_P, _P, _P, _P, _P]),
+    "hf_compute_jk_ri": (_I, [_P, _P, _P, _P, _P]),
     "hf_scf_options_default": (None, [C.POINTER(ScfOptions)]),
     "hf_rhf_scf": (_I, [_P, _I, C.POINTER(ScfOptions), C.POINTER(ScfResult), _P, _P, _P, _P]),
 }

@@ -100,6 +100,40 @@ double prim_pair_bound_t(const PrimPair64& pp, double abx, double aby, double ab
     return std::sqrt(mx);
 }
 
+template <class T>
+T* dev_upload(const std::vector<T>& v, int& status)
+{
+    T* d = nullptr;
+    const size_t n = std::max<size_t>(v.size(), 1);
+    cudaError_t e = cudaMalloc(&d, n * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        status = (e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;
+        return nullptr;
+    }
+    if (!v.empty()) {
+        e = cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            set_error(std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+            status = HF_ERR_CUDA;
+        }
+    }
+    return d;
+}
+
+template <class T>
+int dev_alloc(T*& p, size_t n)
+{
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return (e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;
+    }
+    return HF_OK;
+}
+
+}  // namespace
+
 double prim_pair_bound(int la, int lb, const PrimPair64& pp, double abx, double aby, double abz, const double* boys)
 {
     switch (la * 3 + lb) {
@@ -141,39 +175,16 @@ PrimPair64 make_prim_pair(double a, double ca, const double* A, double b, double
     return r;
 }
 
-template <class T>
-T* dev_upload(const std::vector<T>& v, int& status)
+double aux_prim_bound(int l, const PrimPair64& q, const double* boys)
 {
-    T* d = nullptr;
-    const size_t n = std::max<size_t>(v.size(), 1);
-    cudaError_t e = cudaMalloc(&d, n * sizeof(T));
-    if (e != cudaSuccess) {
-        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        status = (e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;
-        return nullptr;
+    switch (l) {
+    case 0: return prim_pair_bound_t<0, 0>(q, 0.0, 0.0, 0.0, boys);
+    case 1: return prim_pair_bound_t<1, 0>(q, 0.0, 0.0, 0.0, boys);
+    case 2: return prim_pair_bound_t<2, 0>(q, 0.0, 0.0, 0.0, boys);
+    case 3: return prim_pair_bound_t<3, 0>(q, 0.0, 0.0, 0.0, boys);
+    default: return 0.0;
     }
-    if (!v.empty()) {
-        e = cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) {
-            set_error(std::string("cudaMemcpy: ") + cudaGetErrorString(e));
-            status = HF_ERR_CUDA;
-        }
-    }
-    return d;
 }
-
-template <class T>
-int dev_alloc(T*& p, size_t n)
-{
-    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
-    if (e != cudaSuccess) {
-        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        return (e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;
-    }
-    return HF_OK;
-}
-
-}  // namespace
 
 Engine::~Engine()
 {
@@ -182,6 +193,7 @@ Engine::~Engine()
                     plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_Jp32, d_Kp32, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
                     scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
                     scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j, d_grad, d_shell_atom};
+    ri_destroy(ri);
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (scf.syevj_params) cusolverDnDestroySyevjInfo(scf.syevj_params);

@@ -45,6 +45,8 @@ struct MixedPlan {
     int* lo32 = nullptr;
 };
 
+struct RiState;  // ri.hpp
+
 struct Engine {
     int num_basis = 0, num_shells = 0, num_atoms = 0, num_prims = 0;
     double schwarz_threshold = 1e-12;
@@ -93,6 +95,8 @@ struct Engine {
     unsigned long long* d_counters = nullptr;  // [class pair][precision][prim, contracted]
     long long bytes_h2d = 0;                   // bytes uploaded by engine creation
 
+    RiState* ri = nullptr;  // auxiliary basis and B tensor (RI), attached on request
+
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
     int num_sms = 152;
@@ -134,5 +138,12 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
 
 // host MD helpers (engine.cu)
 void host_boys_table(std::vector<double>& table);
+double prim_pair_bound(int la, int lb, const PrimPair64& pp, double abx, double aby, double abz, const double* boys);
+double aux_prim_bound(int l, const PrimPair64& q, const double* boys);  // unit partner, no CGTO factor
+double scaled_coef(double c, double a, int L);
+PrimPair64 make_prim_pair(double a, double ca, const double* A, double b, double cb, const double* B);
+
+// ri.cu
+void ri_destroy(RiState* r);
 
 }  // namespace gb

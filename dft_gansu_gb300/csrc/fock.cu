@@ -120,6 +120,7 @@ struct PlanArgs {
     const double* dmax;
     double factor;              // c_max^4
     double mixed_threshold;
+    double skip_threshold;      // quartets with Qs_ab*Qs_cd*c_max^4*max|D| below this are dropped
     long long* off64;
     long long* off32;
     int* lo32;
@@ -148,7 +149,14 @@ __global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
                 if (qb * a.pair_qs[k0 + mid] >= a.mixed_threshold) lo = mid + 1; else hi = mid;
             }
             c64 = lo;
-            c32 = cnt - lo;
+            // density-weighted screening: the tail whose bound times max|D| is below the
+            // Schwarz threshold contributes nothing measurable (it matters for dD builds)
+            int hi2 = cnt, lo2 = lo;
+            while (lo2 < hi2) {
+                const int mid = (lo2 + hi2) >> 1;
+                if (qb * a.pair_qs[k0 + mid] >= a.skip_threshold) lo2 = mid + 1; else hi2 = mid;
+            }
+            c32 = lo2 - lo;
             a.lo32[e] = a.entry_lo0[e] + lo;
         }
         long long t64, t32;
@@ -269,6 +277,7 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
         const double c2 = e.cgto_max * e.cgto_max;
         a.factor = c2 * c2;
         a.mixed_threshold = mixed_thr;
+        a.skip_threshold = std::min(e.schwarz_threshold, mixed_thr);
         a.off64 = e.plan.off64;
         a.off32 = e.plan.off32;
         a.lo32 = e.plan.lo32;

@@ -1,0 +1,58 @@
+// RI (density fitting) state attached to an Engine.
+#pragma once
+#include "engine.hpp"
+
+namespace gb {
+
+constexpr int kMaxAuxL = 3;  // auxiliary shells up to f (cc-pVDZ-RIFIT for H..Ar)
+
+// One contracted auxiliary shell; its primitives are PrimPair64 records of
+// (gamma, unit s) pairs: p = gamma, K = scaled coefficient * sqrt(2 pi^{5/2}),
+// P = centre, PA = 0, Q = reference auxiliary bound.
+struct AuxShellDev {
+    double x, y, z;
+    int l, bf, p_off, np;
+};
+
+struct RiState {
+    int naux = 0;
+    int class_begin[kMaxAuxL + 1] = {0, 0, 0, 0};  // auxiliary shells sorted by l
+    int class_count[kMaxAuxL + 1] = {0, 0, 0, 0};
+    std::vector<AuxShellDev> shells;
+    AuxShellDev* d_aux = nullptr;
+    PrimPair64* d_aux_pp = nullptr;
+    ShellPairDev* d_aux_pairs = nullptr;  // (P, unit) bra pairs for the metric
+    double* d_aux_scale = nullptr;        // s_P = auxiliary CGTO factor * component factor
+
+    bool have_b = false, have_full = false;
+    double* d_V = nullptr;   // metric, then its Cholesky factor (column-major lower)
+    double* d_Bp = nullptr;  // B packed: naux x N(N+1)/2, row-major
+    double* d_B = nullptr;   // B full: [P][mu][nu] (the reference layout), expanded on first use by K
+    double* d_Dt = nullptr;  // packed density with doubled off-diagonal
+    double* d_W = nullptr;   // naux
+    double* d_X = nullptr;   // K intermediate: N x (naux r), row-major
+    size_t x_len = 0;
+    double* d_J = nullptr;
+    double* d_K = nullptr;
+    double* d_Y = nullptr;     // density factor
+    double* d_evec = nullptr;  // density eigenvectors (arbitrary-D K)
+    double* d_eval = nullptr;
+    double* d_work = nullptr;  // cuSOLVER workspace
+    size_t work_len = 0;
+    int* d_info = nullptr;
+};
+
+int ri_set_auxiliary(Engine& e, const hf_primitive_shell* prims, int nprim, const double* cgto, int naux);
+int ri_metric(Engine& e, double* d_V, cudaStream_t s);
+int ri_three_center_packed(Engine& e, double* d_T, cudaStream_t s);
+int ri_expand(Engine& e, const double* d_packed, long long rows, double* d_full, cudaStream_t s);
+int ri_build_b(Engine& e, cudaStream_t s);
+int ri_require_b(Engine& e, cudaStream_t s);
+int ri_j(Engine& e, const double* d_D, double* d_J, cudaStream_t s);
+int ri_k_occupied(Engine& e, const double* d_C, int nocc, double* d_K, cudaStream_t s);
+int ri_k_density(Engine& e, const double* d_D, double* d_K, cudaStream_t s);
+int ri_fock_from_jk(Engine& e, const double* d_H, const double* d_J, const double* d_K, double* d_G, bool accumulate,
+                    double* d_F, cudaStream_t s);
+int ri_work_buffers(Engine& e, double** J, double** K);
+
+}  // namespace gb

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "ri.hpp"
 
 namespace gb {
 
@@ -321,6 +322,7 @@ void hf_scf_options_default(hf_scf_options* o)
     o->incremental = 0;
     o->rebuild_every = 0;
     o->full_build_precision = HF_PRECISION_FP64;
+    o->eri_method = HF_ERI_DIRECT;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -369,6 +371,14 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         return set_error("diis_size must be in [1, 16]"), HF_ERR_INVALID_ARGUMENT;
     if (opt.precision != HF_PRECISION_FP64 && opt.precision != HF_PRECISION_MIXED)
         return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI)
+        return set_error("unknown eri_method"), HF_ERR_INVALID_ARGUMENT;
+    const bool use_ri = opt.eri_method == HF_ERI_RI;
+    if (use_ri && !e.ri)
+        return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
+               HF_ERR_INVALID_ARGUMENT;
+    if (use_ri && opt.precision != HF_PRECISION_FP64)
+        return set_error("the RI backend runs in FP64 only"), HF_ERR_INVALID_ARGUMENT;
     const int m = opt.diis_size;
     int st = ensure_scf(e, m);
     if (st) return st;
@@ -398,6 +408,18 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     // one Fock build: F = H + G(D), full or incremental
     auto fock_build = [&](bool first) -> int {
         cudaEventRecord(f0, s);
+        if (use_ri) {
+            // J from the packed B and D; K from the occupied orbitals (D = 2 C_occ C_occ^T)
+            double *J, *K;
+            int r;
+            if ((r = ri_work_buffers(e, &J, &K))) return r;
+            if ((r = ri_j(e, w.D, J, s))) return r;
+            if ((r = ri_k_occupied(e, w.C, nocc, K, s))) return r;
+            if ((r = ri_fock_from_jk(e, w.H, J, K, nullptr, false, w.F, s))) return r;
+            cudaEventRecord(f1, s);
+            ++fock_builds;
+            return HF_OK;
+        }
         const bool incremental = opt.incremental && !first &&
                                  !(opt.rebuild_every > 0 && fock_builds % opt.rebuild_every == 0);
         int r;
@@ -426,7 +448,8 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     };
 
     const auto t_setup = std::chrono::steady_clock::now();
-    // core Hamiltonian, X, core guess
+    // core Hamiltonian, X, core guess (and the RI B tensor)
+    if (use_ri && (st = ri_require_b(e, s))) return st;
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
     transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);

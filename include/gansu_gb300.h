@@ -171,6 +171,40 @@ int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d
 int hf_compute_fock_diis_noalloc(const double* d_errors, const double* d_focks, double* d_new_fock, int num_prev,
                                  int num_basis, void* stream);
 
+/* -------------------------------------------------------------------- RI */
+/* Attaches the auxiliary basis of eri_method = ri: the primitives of
+ * Molecular(atoms, auxiliary_gbsfilename) (src/rhf.cu:76-79; the ERI_RI
+ * constructor, src/eri.cu:119-132), same layout and normalisation as the AO
+ * primitives, auxiliary shells up to f.  Replaces any earlier auxiliary basis
+ * and drops a B tensor built from it. */
+int hf_engine_set_auxiliary_basis(hf_engine* eng, const hf_primitive_shell* aux_prims, int num_aux_primitives,
+                                  const double* aux_cgto_norm, int num_aux_basis);
+
+/* Replaces gpu::computeTwoCenterERIs (src/gpu_manager.cu:1963-2041): the RI
+ * metric (P|Q), row-major naux x naux, screened by Q_P * Q_Q < thr. */
+int hf_compute_two_center_eris(hf_engine* eng, double* d_metric, void* stream);
+
+/* Replaces gpu::computeThreeCenterERIs (src/gpu_manager.cu:2048-2141):
+ * (mu nu|P) at d_three_center[(P * N + mu) * N + nu] (both triangles),
+ * screened by Q_mu_nu * Q_P < thr.  Allocates a packed temporary. */
+int hf_compute_three_center_eris(hf_engine* eng, double* d_three_center, void* stream);
+
+/* Replaces gpu::compute_RI_IntermediateMatrixB (src/gpu_manager.cu:1448-1526):
+ * metric, Cholesky V = L L^T (HF_ERR_NOT_SPD if it fails), three-centre
+ * integrals, B = L^-1 (mu nu|P).  B stays on the engine for the RI Fock
+ * builds; when d_b_out is non-NULL it also receives B in the reference layout
+ * [P][mu][nu] (naux * N * N doubles). */
+int hf_compute_ri_intermediate_b(hf_engine* eng, double* d_b_out, void* stream);
+
+/* Replaces gpu::computeFockMatrix_RI_RHF (src/gpu_manager.cu:1543-1632):
+ * F = H + J - K/2 with J = sum_P B_P (B_P . D) and K = sum_P B_P D B_P^T for a
+ * symmetric D (K from an eigen-factorisation of D).  Builds B on first use. */
+int hf_compute_fock_ri_rhf(hf_engine* eng, const double* d_density, const double* d_core_hamiltonian,
+                           double* d_fock, void* stream);
+
+/* The J and K of hf_compute_fock_ri_rhf separately (N x N each). */
+int hf_compute_jk_ri(hf_engine* eng, const double* d_density, double* d_J, double* d_K, void* stream);
+
 /* ------------------------------------------------------------------- SCF */
 typedef struct {
     int max_iter;                   /* reference default 100 */
@@ -184,7 +218,14 @@ typedef struct {
     int full_build_precision;       /* precision of full (non-incremental) builds under the mixed tier */
     int eigensolver;                /* 0: cuSOLVER syevd (divide and conquer), 1: syevj (Jacobi) */
     int verbose;                    /* print per-iteration lines like the reference */
+    int eri_method;                 /* HF_ERI_DIRECT or HF_ERI_RI (eri_method = direct / ri, src/rhf.cu:72-88) */
 } hf_scf_options;
+
+/* Two-electron backend of the SCF. */
+enum {
+    HF_ERI_DIRECT = 0,  /* fused direct J/K build every iteration */
+    HF_ERI_RI = 1       /* density fitting; needs hf_engine_set_auxiliary_basis */
+};
 
 typedef struct {
     double electronic_energy;       /* 1/2 sum D (H + F) */
