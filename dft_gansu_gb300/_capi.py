@@ -120,6 +120,7 @@ SIGNATURES = {
     "hf_compute_ri_intermediate_b": (_I, [_P, _P, _P]),
     "hf_compute_fock_ri_rhf": (_I, [_P, _P, _P, _P, _P]),
     "hf_compute_jk_ri": (_I, [_P, _P, _P, _P, _P]),
+    "hf_split_bf16_matmul": (_I, [_P, _P, _P, _I, _I, _I, _I, _P]),
     "hf_scf_options_default": (None, [C.POINTER(ScfOptions)]),
     "hf_rhf_scf": (_I, [_P, _I, C.POINTER(ScfOptions), C.POINTER(ScfResult), _P, _P, _P, _P]),
 }

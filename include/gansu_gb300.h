@@ -205,6 +205,16 @@ int hf_compute_fock_ri_rhf(hf_engine* eng, const double* d_density, const double
 /* The J and K of hf_compute_fock_ri_rhf separately (N x N each). */
 int hf_compute_jk_ri(hf_engine* eng, const double* d_density, double* d_J, double* d_K, void* stream);
 
+/* Split-BF16 tensor-core GEMM (no reference counterpart: the tcgen05 building
+ * block of the RI mixed tier, exposed for testing).  A is m x k, B is n x k,
+ * row-major FP64; both are split into BF16 hi/lo planes and
+ * A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T accumulates in FP32 in TMEM.
+ * mode 0: C (m x n) = A B^T, stored through the BF16 hi/lo output planes;
+ * mode 1: C (m x m) = A A^T (B unused; upper tiles, mirrored);
+ * mode 2: C (m x m) = A B^T + B A^T.  Allocates temporaries; synchronises. */
+int hf_split_bf16_matmul(const double* d_a, const double* d_b, double* d_c, int m, int n, int k, int mode,
+                         void* stream);
+
 /* ------------------------------------------------------------------- SCF */
 typedef struct {
     int max_iter;                   /* reference default 100 */
