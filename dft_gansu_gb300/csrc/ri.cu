@@ -33,6 +33,7 @@
 
 #include "engine.hpp"
 #include "ri.hpp"
+#include "tc_gemm.hpp"
 
 namespace gb {
 
@@ -349,7 +350,9 @@ void ri_destroy(RiState* r)
     if (!r) return;
     void* ptrs[] = {r->d_aux, r->d_aux_pp, r->d_aux_pairs, r->d_aux_scale, r->d_V, r->d_Bp, r->d_B,
                     r->d_Dt, r->d_W, r->d_X, r->d_J, r->d_K, r->d_Y, r->d_evec, r->d_eval, r->d_work,
-                    r->d_info};
+                    r->d_info, r->d_Bh, r->d_Bl, r->d_Yh, r->d_Yl, r->d_Y2h, r->d_Y2l, r->d_Xh, r->d_Xl,
+                    r->d_X2h, r->d_X2l, r->d_Kacc, r->d_Cprev, r->d_T1, r->d_M, r->d_U, r->d_U2, r->d_Ca,
+                    r->d_flag};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete r;
@@ -696,6 +699,337 @@ int ri_work_buffers(Engine& e, double** J, double** K)
     if ((st = ri_alloc(r.d_J, nn)) || (st = ri_alloc(r.d_K, nn))) return st;
     *J = r.d_J;
     *K = r.d_K;
+    return HF_OK;
+}
+
+
+// ------------------------------------------------------------------ mixed tier
+namespace {
+
+// B planes: row (P, mu) of the full B, columns nu (zero padded to kpad), split into BF16 hi/lo
+__global__ void b_planes_kernel(const double* __restrict__ Bp, int naux, int n, long long kpad,
+                                __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo)
+{
+    const long long npk = static_cast<long long>(n) * (n + 1) / 2;
+    const long long total = static_cast<long long>(naux) * n * kpad;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < total;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long row = k / kpad, c = k % kpad;
+        const long long P = row / n;
+        const int mu = static_cast<int>(row % n);
+        double v = 0.0;
+        if (c < n) v = Bp[P * npk + tri(mu, static_cast<int>(c))];
+        const float x = static_cast<float>(v);
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        hi[k] = h;
+        lo[k] = __float2bfloat16_rn(static_cast<float>(v - static_cast<double>(__bfloat162float(h))));
+    }
+}
+
+// factor planes Y^T[i][nu] = C[nu * ldc + i] + sgn * C2[nu * ld2 + i] for i < r, nu < n (pitch kpad)
+__global__ void factor_planes_kernel(const double* __restrict__ C, int ldc, const double* __restrict__ C2, int ld2,
+                                     double sgn, int r, int n, long long kpad, __nv_bfloat16* __restrict__ hi,
+                                     __nv_bfloat16* __restrict__ lo)
+{
+    const long long total = static_cast<long long>(r) * kpad;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < total;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int i = static_cast<int>(k / kpad);
+        const long long nu = k % kpad;
+        double v = 0.0;
+        if (nu < n) {
+            v = C[nu * ldc + i];
+            if (C2) v += sgn * C2[nu * ld2 + i];
+        }
+        const float x = static_cast<float>(v);
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        hi[k] = h;
+        lo[k] = __float2bfloat16_rn(static_cast<float>(v - static_cast<double>(__bfloat162float(h))));
+    }
+}
+
+__global__ void copy_cols_kernel(const double* __restrict__ C, int ldc, int n, int r, double* __restrict__ out)
+{
+    const long long total = static_cast<long long>(n) * r;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < total;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        out[k] = C[(k / r) * ldc + (k % r)];
+}
+
+// U2 = (3 I - U^T U) / 2 stored in place of the product buffer P (r x r)
+__global__ void ns_step_kernel(double* __restrict__ P, int r)
+{
+    const long long rr = static_cast<long long>(r) * r;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < rr;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const bool diag = (k / r) == (k % r);
+        P[k] = 0.5 * ((diag ? 3.0 : 0.0) - P[k]);
+    }
+}
+
+// max |U^T U - I| (P = U^T U) into out (single block)
+__global__ void orth_residual_kernel(const double* __restrict__ P, int r, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    double m = 0.0;
+    const long long rr = static_cast<long long>(r) * r;
+    for (long long k = threadIdx.x; k < rr; k += blockDim.x) {
+        const double v = P[k] - (((k / r) == (k % r)) ? 1.0 : 0.0);
+        m = fmax(m, fabs(v));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) *out = m;
+    }
+}
+
+// row-major C (m x n) = alpha op(A) op(B) + beta C
+cublasStatus_t gemm_rm(cublasHandle_t h, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
+                       const double* B, int ldb, double beta, double* C, int ldc)
+{
+    return cublasDgemm(h, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N, n, m, k, &alpha, B, ldb, A,
+                       lda, &beta, C, ldc);
+}
+
+template <class T>
+int ri_alloc_zero(T*& p, size_t n, cudaStream_t s)
+{
+    if (p) return HF_OK;
+    int st = ri_alloc(p, n);
+    if (st) return st;
+    GB_CUDA_TRY(cudaMemsetAsync(p, 0, std::max<size_t>(n, 1) * sizeof(T), s));
+    return HF_OK;
+}
+
+}  // namespace
+
+int ri_prepare_planes(Engine& e, int nocc, cudaStream_t s)
+{
+    RiState& r = *e.ri;
+    const int n = e.num_basis, M = r.naux;
+    const long long kpad = (n + 63) / 64 * 64;
+    int st;
+    if (!r.d_Bh) {
+        r.kpad_n = kpad;
+        const size_t plane = static_cast<size_t>(M) * n * kpad;
+        if ((st = ri_alloc(r.d_Bh, plane)) || (st = ri_alloc(r.d_Bl, plane))) return st;
+        b_planes_kernel<<<grid_for(static_cast<long long>(plane), 256, e.num_sms), 256, 0, s>>>(r.d_Bp, M, n, kpad,
+                                                                                              r.d_Bh, r.d_Bl);
+        GB_LAUNCH_CHECK();
+    }
+    if (nocc > r.r_cap) {
+        // factor planes and X planes sized for nocc rows
+        for (void* p : {static_cast<void*>(r.d_Yh), static_cast<void*>(r.d_Yl), static_cast<void*>(r.d_Y2h),
+                        static_cast<void*>(r.d_Y2l), static_cast<void*>(r.d_Xh), static_cast<void*>(r.d_Xl),
+                        static_cast<void*>(r.d_X2h), static_cast<void*>(r.d_X2l), static_cast<void*>(r.d_Cprev),
+                        static_cast<void*>(r.d_T1), static_cast<void*>(r.d_M), static_cast<void*>(r.d_U),
+                        static_cast<void*>(r.d_U2), static_cast<void*>(r.d_Ca)})
+            if (p) cudaFree(p);
+        r.d_Yh = r.d_Yl = r.d_Y2h = r.d_Y2l = r.d_Xh = r.d_Xl = r.d_X2h = r.d_X2l = nullptr;
+        r.d_Cprev = r.d_T1 = r.d_M = r.d_U = r.d_U2 = r.d_Ca = nullptr;
+        r.r_cap = nocc;
+        r.r_blk = (nocc + 63) / 64 * 64;
+        const size_t yplane = static_cast<size_t>(nocc) * kpad;
+        const size_t xplane = static_cast<size_t>(n) * M * r.r_blk;
+        if ((st = ri_alloc(r.d_Yh, yplane)) || (st = ri_alloc(r.d_Yl, yplane)) || (st = ri_alloc(r.d_Y2h, yplane)) ||
+            (st = ri_alloc(r.d_Y2l, yplane)))
+            return st;
+        // padding columns of the X planes (i >= nocc) stay zero: the GEMM writes only i < nocc
+        if ((st = ri_alloc_zero(r.d_Xh, xplane, s)) || (st = ri_alloc_zero(r.d_Xl, xplane, s)) ||
+            (st = ri_alloc_zero(r.d_X2h, xplane, s)) || (st = ri_alloc_zero(r.d_X2l, xplane, s)))
+            return st;
+        const size_t nr = static_cast<size_t>(n) * nocc, rr = static_cast<size_t>(nocc) * nocc;
+        if ((st = ri_alloc(r.d_Cprev, nr)) || (st = ri_alloc(r.d_T1, nr)) || (st = ri_alloc(r.d_Ca, nr)) ||
+            (st = ri_alloc(r.d_M, rr)) || (st = ri_alloc(r.d_U, rr)) || (st = ri_alloc(r.d_U2, rr)))
+            return st;
+    }
+    if ((st = ri_alloc_zero(r.d_flag, 1, s)) || (st = ri_alloc(r.d_Kacc, static_cast<size_t>(n) * n))) return st;
+    return HF_OK;
+}
+
+// X planes (N x naux r_blk) from the factor planes: X[mu][(P, i)] = sum_nu B_P[mu][nu] Y[nu][i]
+static int ri_x_planes(Engine& e, const __nv_bfloat16* yh, const __nv_bfloat16* yl, int nocc, __nv_bfloat16* xh,
+                       __nv_bfloat16* xl, cudaStream_t s)
+{
+    RiState& r = *e.ri;
+    const int n = e.num_basis;
+    SplitGemmArgs a{};
+    a.a_hi = r.d_Bh; a.a_lo = r.d_Bl;
+    a.b_hi = yh; a.b_lo = yl;
+    a.a_rows = static_cast<long long>(r.naux) * n;
+    a.b_rows = nocc;
+    a.kpad = r.kpad_n;
+    a.mode = kSplitStore;
+    a.out_hi = xh; a.out_lo = xl;
+    a.rows_per_block = n;
+    a.ld_out = static_cast<long long>(r.naux) * r.r_blk;
+    a.block_cols = r.r_blk;
+    a.col_off = 0;
+    a.scale = 1.0f;
+    a.error_flag = r.d_flag;
+    return split_bf16_gemm(a, e.num_sms, s);
+}
+
+static int ri_k_from_x(Engine& e, const __nv_bfloat16* xh, const __nv_bfloat16* xl, const __nv_bfloat16* x2h,
+                       const __nv_bfloat16* x2l, int mode, double alpha, double* d_K, cudaStream_t s)
+{
+    RiState& r = *e.ri;
+    const int n = e.num_basis;
+    SplitGemmArgs a{};
+    a.a_hi = xh; a.a_lo = xl;
+    a.b_hi = x2h; a.b_lo = x2l;
+    a.a_rows = n;
+    a.b_rows = n;
+    a.kpad = static_cast<long long>(r.naux) * r.r_blk;
+    a.mode = mode;
+    const long long tiles = (n + 127) / 128;
+    const long long ntile = (mode == kSymmetricAdd) ? tiles * (tiles + 1) / 2 : tiles * tiles;
+    const long long nkb = a.kpad / 64;
+    a.split_k = static_cast<int>(std::max<long long>(1, std::min<long long>(nkb, (2LL * e.num_sms + ntile - 1) / ntile)));
+    a.K = d_K;
+    a.ldk = n;
+    a.alpha = alpha;
+    a.error_flag = r.d_flag;
+    return split_bf16_gemm(a, e.num_sms, s);
+}
+
+int ri_k_tc_full(Engine& e, const double* d_C, int ldc, int nocc, double* d_K, cudaStream_t s)
+{
+    RiState& r = *e.ri;
+    const int n = e.num_basis;
+    int st;
+    if ((st = ri_prepare_planes(e, nocc, s))) return st;
+    factor_planes_kernel<<<grid_for(static_cast<long long>(nocc) * r.kpad_n, 256, e.num_sms), 256, 0, s>>>(
+        d_C, ldc, nullptr, 0, 0.0, nocc, n, r.kpad_n, r.d_Yh, r.d_Yl);
+    GB_LAUNCH_CHECK();
+    if ((st = ri_x_planes(e, r.d_Yh, r.d_Yl, nocc, r.d_Xh, r.d_Xl, s))) return st;
+    GB_CUDA_TRY(cudaMemsetAsync(d_K, 0, sizeof(double) * n * n, s));
+    // D = 2 C_occ C_occ^T
+    return ri_k_from_x(e, r.d_Xh, r.d_Xl, r.d_Xh, r.d_Xl, kSymmetricAdd, 2.0, d_K, s);
+}
+
+int ri_save_occupied(Engine& e, const double* d_C, int ldc, int nocc, cudaStream_t s)
+{
+    RiState& r = *e.ri;
+    int st = ri_prepare_planes(e, nocc, s);
+    if (st) return st;
+    copy_cols_kernel<<<grid_for(static_cast<long long>(e.num_basis) * nocc, 256, e.num_sms), 256, 0, s>>>(
+        d_C, ldc, e.num_basis, nocc, r.d_Cprev);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+// K(D_new) - K(D_old) with D = 2 C_occ C_occ^T: the old orbitals are rotated onto the new ones
+// (U = polar factor of C_old^T S C_new, Newton-Schulz), then with A = C_new - C_old U and
+// S = C_new + C_old U, D_new - D_old = A S^T + S A^T exactly and
+// K(dD) = sum_P (B_P A)(B_P S)^T + transpose, whose low-precision error scales with |A|.
+int ri_k_tc_delta(Engine& e, const double* d_C, int ldc, int nocc, const double* d_S, double* d_K, bool* aligned,
+                  cudaStream_t s)
+{
+    RiState& r = *e.ri;
+    const int n = e.num_basis, k = nocc;
+    int st;
+    if ((st = ri_prepare_planes(e, nocc, s))) return st;
+    cublasSetStream(e.cublas, s);
+    // new occupied block (N x k, pitch k) into Ca
+    copy_cols_kernel<<<grid_for(static_cast<long long>(n) * k, 256, e.num_sms), 256, 0, s>>>(d_C, ldc, n, k, r.d_Ca);
+    GB_LAUNCH_CHECK();
+    // M = C_old^T S C_new
+    if (gemm_rm(e.cublas, false, false, n, k, n, 1.0, d_S, n, r.d_Ca, k, 0.0, r.d_T1, k) != CUBLAS_STATUS_SUCCESS ||
+        gemm_rm(e.cublas, true, false, k, k, n, 1.0, r.d_Cprev, k, r.d_T1, k, 0.0, r.d_M, k) != CUBLAS_STATUS_SUCCESS)
+        return set_error("cublasDgemm (RI alignment) failed"), HF_ERR_SOLVER;
+    // Newton-Schulz: U <- U (3 I - U^T U) / 2, from U = M (singular values in (0, 1])
+    GB_CUDA_TRY(cudaMemcpyAsync(r.d_U, r.d_M, sizeof(double) * k * k, cudaMemcpyDeviceToDevice, s));
+    double res = 1.0;
+    *aligned = false;
+    for (int it = 0; it < 60; ++it) {
+        if (gemm_rm(e.cublas, true, false, k, k, k, 1.0, r.d_U, k, r.d_U, k, 0.0, r.d_U2, k) != CUBLAS_STATUS_SUCCESS)
+            return set_error("cublasDgemm (Newton-Schulz) failed"), HF_ERR_SOLVER;
+        if (it % 4 == 3) {
+            orth_residual_kernel<<<1, 256, 0, s>>>(r.d_U2, k, e.d_scalar + 6);
+            GB_LAUNCH_CHECK();
+            GB_CUDA_TRY(cudaMemcpyAsync(&res, e.d_scalar + 6, sizeof(double), cudaMemcpyDeviceToHost, s));
+            GB_CUDA_TRY(cudaStreamSynchronize(s));
+            if (res < 1e-13) { *aligned = true; break; }
+        }
+        ns_step_kernel<<<grid_for(static_cast<long long>(k) * k, 256, e.num_sms), 256, 0, s>>>(r.d_U2, k);
+        GB_LAUNCH_CHECK();
+        if (gemm_rm(e.cublas, false, false, k, k, k, 1.0, r.d_U, k, r.d_U2, k, 0.0, r.d_M, k) != CUBLAS_STATUS_SUCCESS)
+            return set_error("cublasDgemm (Newton-Schulz) failed"), HF_ERR_SOLVER;
+        std::swap(r.d_U, r.d_M);
+    }
+    if (!*aligned) return HF_OK;  // caller falls back to a full build
+    // C_old U into T1
+    if (gemm_rm(e.cublas, false, false, n, k, k, 1.0, r.d_Cprev, k, r.d_U, k, 0.0, r.d_T1, k) != CUBLAS_STATUS_SUCCESS)
+        return set_error("cublasDgemm (RI alignment) failed"), HF_ERR_SOLVER;
+    // A = C_new - C_old U, S = C_new + C_old U as factor planes
+    const long long work = static_cast<long long>(k) * r.kpad_n;
+    factor_planes_kernel<<<grid_for(work, 256, e.num_sms), 256, 0, s>>>(r.d_Ca, k, r.d_T1, k, -1.0, k, n, r.kpad_n,
+                                                                       r.d_Yh, r.d_Yl);
+    GB_LAUNCH_CHECK();
+    factor_planes_kernel<<<grid_for(work, 256, e.num_sms), 256, 0, s>>>(r.d_Ca, k, r.d_T1, k, 1.0, k, n, r.kpad_n,
+                                                                       r.d_Y2h, r.d_Y2l);
+    GB_LAUNCH_CHECK();
+    if ((st = ri_x_planes(e, r.d_Yh, r.d_Yl, k, r.d_Xh, r.d_Xl, s))) return st;
+    if ((st = ri_x_planes(e, r.d_Y2h, r.d_Y2l, k, r.d_X2h, r.d_X2l, s))) return st;
+    GB_CUDA_TRY(cudaMemsetAsync(d_K, 0, sizeof(double) * n * n, s));
+    return ri_k_from_x(e, r.d_Xh, r.d_Xl, r.d_X2h, r.d_X2l, kSymmetrizedAdd, 1.0, d_K, s);
+}
+
+int ri_check_flag(Engine& e)
+{
+    if (!e.ri || !e.ri->d_flag) return HF_OK;
+    int f = 0;
+    GB_CUDA_TRY(cudaMemcpy(&f, e.ri->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (f) return set_error("tensor-core GEMM pipeline wait timed out"), HF_ERR_CUDA;
+    return HF_OK;
+}
+
+
+namespace {
+__global__ void absmax_diff_kernel(const double* __restrict__ A, const double* __restrict__ B, long long nn,
+                                   double* __restrict__ out)
+{
+    __shared__ double red[32];
+    double m = 0.0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) m = fmax(m, fabs(A[k] - B[k]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) *out = m;
+    }
+}
+
+__global__ void add_inplace_kernel(double* __restrict__ A, const double* __restrict__ B, long long nn)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        A[k] += B[k];
+}
+}  // namespace
+
+int ri_absmax_diff(Engine& e, const double* d_A, const double* d_B, double* h_out, cudaStream_t s)
+{
+    const long long nn = static_cast<long long>(e.num_basis) * e.num_basis;
+    absmax_diff_kernel<<<1, 1024, 0, s>>>(d_A, d_B, nn, e.d_scalar + 7);
+    GB_LAUNCH_CHECK();
+    GB_CUDA_TRY(cudaMemcpyAsync(h_out, e.d_scalar + 7, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return HF_OK;
+}
+
+int ri_add_inplace(Engine& e, double* d_A, const double* d_B, cudaStream_t s)
+{
+    const long long nn = static_cast<long long>(e.num_basis) * e.num_basis;
+    add_inplace_kernel<<<grid_for(nn, 256, e.num_sms), 256, 0, s>>>(d_A, d_B, nn);
+    GB_LAUNCH_CHECK();
     return HF_OK;
 }
 

@@ -1,5 +1,7 @@
 // RI (density fitting) state attached to an Engine.
 #pragma once
+#include <cuda_bf16.h>
+
 #include "engine.hpp"
 
 namespace gb {
@@ -40,6 +42,18 @@ struct RiState {
     double* d_work = nullptr;  // cuSOLVER workspace
     size_t work_len = 0;
     int* d_info = nullptr;
+
+    // mixed tier: B as BF16 hi/lo planes [(P, mu)][nu] (row pitch kpad_n), tensor-core K
+    __nv_bfloat16 *d_Bh = nullptr, *d_Bl = nullptr;
+    long long kpad_n = 0;
+    __nv_bfloat16 *d_Yh = nullptr, *d_Yl = nullptr, *d_Y2h = nullptr, *d_Y2l = nullptr;  // factor planes (r x kpad_n)
+    __nv_bfloat16 *d_Xh = nullptr, *d_Xl = nullptr, *d_X2h = nullptr, *d_X2l = nullptr;  // N x (naux r_blk)
+    int r_blk = 0;            // columns per auxiliary function in the X planes (multiple of 64)
+    int r_cap = 0;            // factor rows the plane buffers hold
+    double* d_Kacc = nullptr; // accumulated K of the incremental builds
+    double* d_Cprev = nullptr;  // occupied orbitals of the last build (N x r, row-major)
+    double *d_T1 = nullptr, *d_M = nullptr, *d_U = nullptr, *d_U2 = nullptr, *d_Ca = nullptr;  // alignment work
+    int* d_flag = nullptr;    // tensor-core pipeline error flag
 };
 
 int ri_set_auxiliary(Engine& e, const hf_primitive_shell* prims, int nprim, const double* cgto, int naux);
@@ -54,5 +68,15 @@ int ri_k_density(Engine& e, const double* d_D, double* d_K, cudaStream_t s);
 int ri_fock_from_jk(Engine& e, const double* d_H, const double* d_J, const double* d_K, double* d_G, bool accumulate,
                     double* d_F, cudaStream_t s);
 int ri_work_buffers(Engine& e, double** J, double** K);
+
+// mixed tier (tensor cores)
+int ri_prepare_planes(Engine& e, int nocc, cudaStream_t s);
+int ri_k_tc_full(Engine& e, const double* d_C, int ldc, int nocc, double* d_K, cudaStream_t s);
+int ri_k_tc_delta(Engine& e, const double* d_C, int ldc, int nocc, const double* d_S, double* d_K, bool* aligned,
+                  cudaStream_t s);
+int ri_save_occupied(Engine& e, const double* d_C, int ldc, int nocc, cudaStream_t s);
+int ri_check_flag(Engine& e);
+int ri_absmax_diff(Engine& e, const double* d_A, const double* d_B, double* h_out, cudaStream_t s);
+int ri_add_inplace(Engine& e, double* d_A, const double* d_B, cudaStream_t s);
 
 }  // namespace gb

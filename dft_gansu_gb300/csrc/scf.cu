@@ -377,8 +377,6 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     if (use_ri && !e.ri)
         return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
                HF_ERR_INVALID_ARGUMENT;
-    if (use_ri && opt.precision != HF_PRECISION_FP64)
-        return set_error("the RI backend runs in FP64 only"), HF_ERR_INVALID_ARGUMENT;
     const int m = opt.diis_size;
     int st = ensure_scf(e, m);
     if (st) return st;
@@ -405,17 +403,50 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     double* h_energy = nullptr;
     cudaMallocHost(&h_energy, sizeof(double));
 
+    bool ri_anchored = false;  // mixed RI: an FP64 K build has been taken
+    int ri_anchor_builds = 0;
     // one Fock build: F = H + G(D), full or incremental
     auto fock_build = [&](bool first) -> int {
         cudaEventRecord(f0, s);
         if (use_ri) {
-            // J from the packed B and D; K from the occupied orbitals (D = 2 C_occ C_occ^T)
+            // J (FP64) from the packed B and D.  K: FP64 from the occupied orbitals
+            // (D = 2 C_occ C_occ^T); under the mixed tier, split-BF16 tensor-core builds
+            // until max|dD| < mixed_threshold, then one FP64 anchor build, then
+            // incremental K(dD) from rotation-aligned orbital differences.
             double *J, *K;
             int r;
             if ((r = ri_work_buffers(e, &J, &K))) return r;
             if ((r = ri_j(e, w.D, J, s))) return r;
-            if ((r = ri_k_occupied(e, w.C, nocc, K, s))) return r;
-            if ((r = ri_fock_from_jk(e, w.H, J, K, nullptr, false, w.F, s))) return r;
+            if (opt.precision == HF_PRECISION_FP64) {
+                if ((r = ri_k_occupied(e, w.C, nocc, K, s))) return r;
+                if ((r = ri_fock_from_jk(e, w.H, J, K, nullptr, false, w.F, s))) return r;
+            } else {
+                double dmax = 1.0;
+                if (!first && (r = ri_absmax_diff(e, w.D, w.Dprev, &dmax, s))) return r;
+                double* Kacc = nullptr;
+                if ((r = ri_prepare_planes(e, nocc, s))) return r;
+                Kacc = e.ri->d_Kacc;
+                bool done = false;
+                if (ri_anchored) {
+                    bool aligned = false;
+                    if ((r = ri_k_tc_delta(e, w.C, n, nocc, w.S, K, &aligned, s))) return r;
+                    if (aligned) {
+                        if ((r = ri_add_inplace(e, Kacc, K, s))) return r;
+                        done = true;
+                    }
+                } else if (first || dmax >= opt.mixed_threshold) {
+                    if ((r = ri_k_tc_full(e, w.C, n, nocc, Kacc, s))) return r;
+                    done = true;
+                }
+                if (!done) {  // FP64 anchor build
+                    if ((r = ri_k_occupied(e, w.C, nocc, Kacc, s))) return r;
+                    ri_anchored = true;
+                    ++ri_anchor_builds;
+                }
+                if ((r = ri_save_occupied(e, w.C, n, nocc, s))) return r;
+                if ((r = ri_fock_from_jk(e, w.H, J, Kacc, nullptr, false, w.F, s))) return r;
+                GB_CUDA_TRY(cudaMemcpyAsync(w.Dprev, w.D, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            }
             cudaEventRecord(f1, s);
             ++fock_builds;
             return HF_OK;
@@ -488,7 +519,10 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
             std::printf("---- Iteration: %d ----  Energy: %.17g Total energy: %.17g Difference: %.17g\n", iter, energy,
                         energy + res->nuclear_repulsion, diff);
         if (!std::isfinite(energy)) return set_error("SCF energy is not finite"), HF_ERR_NOT_CONVERGED;
-        if (diff < opt.convergence_threshold) { converged = true; break; }
+        if (diff < opt.convergence_threshold) {
+            // mixed RI: energies before the FP64 anchor carry the BF16x3 error of whole K builds
+            if (!(use_ri && opt.precision == HF_PRECISION_MIXED && !ri_anchored)) { converged = true; break; }
+        }
         ++iter;
         prev = energy;
         // DIIS update (Convergence_RHF_DIIS::get_new_fock_matrix)
@@ -504,6 +538,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     }
     cudaEventRecord(l1, s);
     GB_CUDA_TRY(cudaEventSynchronize(l1));
+    if (use_ri && (st = ri_check_flag(e))) return st;
     {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, l0, l1);

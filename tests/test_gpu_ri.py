@@ -120,3 +120,28 @@ def test_ri_without_auxiliary_basis_is_an_error(built_library, cuda):
     eng = gg.Engine(mol, 1e-12)
     with pytest.raises(gg.HFError):
         eng.rhf_scf(mol.num_electrons, {"eri_method": gg.HF_ERI_RI})
+
+
+@pytest.mark.parametrize("case", RI_CASES[1:])
+def test_mixed_ri_scf_matches_fp64_ri(built_library, cuda, case):
+    # split-BF16 tensor-core K until max|dD| < 1e-2, one FP64 anchor, then aligned K(dD) increments
+    g, eng, _, _ = _setup(case)
+    r64 = eng.rhf_scf(eng.mol.num_electrons, {"convergence_threshold": 1e-10, "eri_method": gg.HF_ERI_RI})
+    rmx = eng.rhf_scf(eng.mol.num_electrons, {"convergence_threshold": 1e-10, "eri_method": gg.HF_ERI_RI,
+                                              "precision": gg.HF_PRECISION_MIXED, "mixed_threshold": 1e-2})
+    assert r64["converged"] == 1 and rmx["converged"] == 1
+    assert abs(rmx["total_energy"] - r64["total_energy"]) < 1e-6
+    assert abs(rmx["total_energy"] - float(g["energy_total"])) < 1e-6
+
+
+def test_mixed_ri_scf_propane(built_library, cuda):
+    atoms = geometry.alkane(3, jitter=0.02, seed=11)
+    mol = gg.Molecular(atoms, gg.basis_path("cc-pvdz"))
+    eng = gg.Engine(mol, 1e-12)
+    eng.set_auxiliary_basis(gg.Molecular(atoms, gg.basis_path("cc-pvdz-rifit")))
+    base = {"convergence_threshold": 1e-9, "eri_method": gg.HF_ERI_RI}
+    r64 = eng.rhf_scf(mol.num_electrons, base)
+    for tau in (1e-1, 1e-2, 1e-3):
+        rmx = eng.rhf_scf(mol.num_electrons, dict(base, precision=gg.HF_PRECISION_MIXED, mixed_threshold=tau))
+        assert rmx["converged"] == 1
+        assert abs(rmx["total_energy"] - r64["total_energy"]) < 1e-6, tau
