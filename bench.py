@@ -30,6 +30,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "SCF ms/iter & gradient ms, mixed vs FP64 on 1 GB300 at |ΔE|≤1e-6 Eh"
 WORKLOAD = "RHF/6-31G* n-decane C10H22 (N=194 Cartesian, 238 primitive shells), zig-zag + N(0,0.02 A) jitter"
 MIXED_THRESHOLD = 0.1
+ANCHOR_THRESHOLD = 1e-2
 CONV = 1e-8
 
 
@@ -235,7 +236,7 @@ def run_ours(args, rank, world):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     opts_mixed = {"convergence_threshold": CONV, "precision": gg.HF_PRECISION_MIXED,
                   "mixed_threshold": args.mixed_threshold, "incremental": 1, "rebuild_every": 0,
-                  "full_build_precision": gg.HF_PRECISION_FP64}
+                  "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": args.anchor_threshold}
     opts_fp64 = {"convergence_threshold": CONV}
 
     def solve(opts):
@@ -341,8 +342,9 @@ def run_ours(args, rank, world):
             "metric": METRIC, "value": ms_mx, "unit": "ms/iter", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "seed": args.seed, "precision": "mixed (FP64 first build, then "
-                       f"incremental dD builds with FP32 quartets where Q_ab*Q_cd*max|dD| < {args.mixed_threshold})",
+            "config": {"workload": WORKLOAD, "seed": args.seed, "precision": "mixed (full builds with every quartet "
+                       f"FP32 while max|dD| >= {args.anchor_threshold}, one FP64 build, then incremental dD builds "
+                       f"with FP32 quartets where Q_ab*Q_cd*max|dD| < {args.mixed_threshold})",
                        "convergence": CONV, "l2": "flushed (512 MB write) before every step",
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "fp64_ms_per_iter": ms_64, "mixed_speedup_vs_fp64": ms_64 / ms_mx,
@@ -371,16 +373,23 @@ def run_ours(args, rank, world):
 
 
 def run_c60_ri(args, rank, world):
-    """RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT on C60 (N=900, naux=3960 Cartesian): the
-    B-tensor build, then SCF ms/iter in FP64 and in the mixed tier (split-BF16
-    tcgen05 K with an FP64 anchor and aligned K(dD) increments)."""
+    """RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT on C60 (N=900, naux=3960 Cartesian), or on
+    n-decane (N=260, naux=990) with --workload decane_ri: the B-tensor build, then
+    SCF ms/iter in FP64 and in the mixed tier (split-BF16 tcgen05 K with an FP64
+    anchor and aligned K(dD) increments)."""
     import torch
     import dft_gansu_gb300 as gg
     from dft_gansu_gb300 import geometry
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    atoms = geometry.c60(jitter=0.01, seed=args.seed)
+    if args.workload == "decane_ri":
+        atoms = geometry.alkane(10, jitter=0.02, seed=args.seed)
+        label = "RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT n-decane (N=260, naux=990 Cartesian), zig-zag + N(0,0.02 A) jitter"
+    else:
+        atoms = geometry.c60(jitter=0.01, seed=args.seed)
+        label = ("RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT C60 (N=900, naux=3960 Cartesian), "
+                 "truncated icosahedron 1.40/1.45 A + N(0,0.01 A) jitter")
     mol = gg.Molecular(atoms, gg.basis_path("cc-pvdz"))
     aux = gg.Molecular(atoms, gg.basis_path("cc-pvdz-rifit"))
     eng = gg.Engine(mol, 1e-12)
@@ -395,7 +404,7 @@ def run_c60_ri(args, rank, world):
     nel = mol.num_electrons
     tau = args.ri_threshold
     opts_mx = {"convergence_threshold": CONV, "eri_method": gg.HF_ERI_RI, "precision": gg.HF_PRECISION_MIXED,
-               "mixed_threshold": tau}
+               "anchor_threshold": tau}
     opts_64 = {"convergence_threshold": CONV, "eri_method": gg.HF_ERI_RI}
     for _ in range(args.warmup):
         eng.rhf_scf(nel, opts_mx)
@@ -410,12 +419,11 @@ def run_c60_ri(args, rank, world):
             "warmup": args.warmup, "ms_per_step": statistics.mean(r["scf_ms_total"] for r in mx),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64+bf16x3",
             "data": "synthetic",
-            "config": {"workload": "RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT C60 (N=900, naux=3960 Cartesian), "
-                                   "truncated icosahedron 1.40/1.45 A + N(0,0.01 A) jitter",
+            "config": {"workload": label,
                        "seed": args.seed, "convergence": CONV,
                        "precision": f"mixed: split-BF16x3 tcgen05 K until max|dD| < {tau}, one FP64 anchor K, "
                                     "then K(dD) from aligned orbital differences; J FP64",
-                       "l2": "inputs (B planes 13.7 GB) larger than L2", "parallelism": "1 GPU"},
+                       "l2": "inputs (the B planes) larger than L2", "parallelism": "1 GPU"},
             "fp64_ms_per_iter": ms_64, "mixed_speedup_vs_fp64": ms_64 / ms_mx,
             "delta_E_mixed_vs_fp64": max(abs(r["total_energy"] - r64["total_energy"]) for r in mx),
             "energy_fp64": r64["total_energy"], "iterations": {"mixed": mx[0]["iterations"], "fp64": r64["iterations"]},
@@ -440,16 +448,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--mixed-threshold", type=float, default=MIXED_THRESHOLD)
+    ap.add_argument("--anchor-threshold", type=float, default=ANCHOR_THRESHOLD)
     ap.add_argument("--sample-stride", type=int, default=4)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-gradient", action="store_true")
-    ap.add_argument("--workload", default="decane", choices=["decane", "c60_ri"])
+    ap.add_argument("--workload", default="decane", choices=["decane", "c60_ri", "decane_ri"])
     ap.add_argument("--ri-threshold", type=float, default=1e-2)
     args = ap.parse_args()
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         return run_reference(args, rank, world)
-    if args.workload == "c60_ri":
+    if args.workload in ("c60_ri", "decane_ri"):
         return run_c60_ri(args, rank, world)
     return run_ours(args, rank, world)
 

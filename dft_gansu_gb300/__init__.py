@@ -12,7 +12,7 @@ from pathlib import Path
 
 import numpy as np
 
-from ._capi import (HF_ERI_DIRECT, HF_ERI_RI, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
+from ._capi import (HF_ERR_NOT_CONVERGED, HF_ERI_DIRECT, HF_ERI_RI, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
                     check, lib)
 
 BASIS_DIR = Path(__file__).resolve().parent / "basis"
@@ -21,6 +21,7 @@ ANGSTROM_TO_BOHR = 1.8897259886
 __all__ = [
     "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
     "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "basis_path",
+    "optimize_geometry", "energy_and_gradient_at",
 ]
 
 
@@ -426,3 +427,84 @@ class HFBuilder:
         mol = Molecular.from_files(parameters["xyzfilename"], parameters["gbsfilename"],
                                    parameters.get("charge", int), parameters.get("beta_to_alpha", int))
         return RHF(mol, parameters)
+
+    @staticmethod
+    def buildOtimizer(parameters: ParameterManager) -> float:
+        """Geometry optimisation with the analytic gradient; same entry point and
+        return value (the final total energy) as gansu::HFBuilder::buildOtimizer
+        (include/builder.hpp:108-275), which instead searches each coordinate of
+        atoms 1.. with energy-only step halving.  The first atom stays fixed as
+        there.  BFGS on the Cartesian coordinates with a backtracking line search;
+        converged when max|gradient| < 1e-4 Eh/bohr and |dE| < 1e-6 Eh."""
+        if parameters["method"] != "rhf":
+            raise ValueError("geometry optimisation is provided for RHF")
+        mol = Molecular.from_files(parameters["xyzfilename"], parameters["gbsfilename"],
+                                   parameters.get("charge", int), parameters.get("beta_to_alpha", int))
+        atoms = [(a.atomic_number, a.x, a.y, a.z) for a in mol._atoms]
+        opts = {"convergence_threshold": min(parameters.get("convergence_energy_threshold", float), 1e-9),
+                "max_iter": parameters.get("maxiter", int)}
+        energy, _, _ = optimize_geometry(atoms, parameters["gbsfilename"], opts,
+                                         charge=parameters.get("charge", int),
+                                         schwarz=parameters.get("schwarz_screening_threshold", float))
+        return energy
+
+
+def energy_and_gradient_at(atoms, gbs_filename: str, scf_options: dict | None = None, charge: int = 0,
+                           schwarz: float = 1e-12):
+    """Total energy (Eh) and analytic gradient (natom x 3, Eh/bohr) of one geometry."""
+    mol = Molecular(atoms, gbs_filename, charge)
+    eng = Engine(mol, schwarz)
+    try:
+        r = eng.energy_and_gradient(mol.num_electrons, scf_options)
+        if r["converged"] != 1:
+            raise HFError(HF_ERR_NOT_CONVERGED, "energy_and_gradient_at", "SCF did not converge")
+        return r["total_energy"], np.array(r["gradient"])
+    finally:
+        eng.close()
+
+
+def optimize_geometry(atoms, gbs_filename: str, scf_options: dict | None = None, charge: int = 0,
+                      schwarz: float = 1e-12, gtol: float = 1e-4, etol: float = 1e-6, max_steps: int = 100,
+                      fixed_first_atom: bool = True):
+    """BFGS minimisation of the RHF energy over Cartesian coordinates (bohr).
+    Returns (energy, atoms, history of (energy, max|g|))."""
+    Z = [int(a[0]) for a in atoms]
+    x = np.array([a[1:] for a in atoms], dtype=float).ravel()
+    mask = np.ones_like(x)
+    if fixed_first_atom:
+        mask[:3] = 0.0
+
+    def evaluate(xv):
+        e, g = energy_and_gradient_at([(z, *xv[3 * i:3 * i + 3]) for i, z in enumerate(Z)], gbs_filename,
+                                      scf_options, charge, schwarz)
+        return e, g.ravel() * mask
+
+    e, g = evaluate(x)
+    Hinv = np.eye(x.size) * 0.5  # initial inverse Hessian (bohr^2/Eh), a stiff-bond guess
+    history = [(e, float(np.abs(g).max()))]
+    for _ in range(max_steps):
+        if np.abs(g).max() < gtol:
+            break
+        p = -Hinv @ g
+        step = np.abs(p).max()
+        if step > 0.3:  # trust radius in bohr
+            p *= 0.3 / step
+        t, e_new, g_new = 1.0, None, None
+        for _ls in range(20):
+            e_new, g_new = evaluate(x + t * p)
+            if e_new <= e + 1e-4 * t * float(g @ p):
+                break
+            t *= 0.5
+        s_vec, y_vec = t * p, g_new - g
+        x, de, e, g = x + s_vec, e_new - e, e_new, g_new
+        history.append((e, float(np.abs(g).max())))
+        sy = float(s_vec @ y_vec)
+        if sy > 1e-12:
+            rho = 1.0 / sy
+            I = np.eye(x.size)
+            Hinv = (I - rho * np.outer(s_vec, y_vec)) @ Hinv @ (I - rho * np.outer(y_vec, s_vec)) + \
+                rho * np.outer(s_vec, s_vec)
+        if np.abs(g).max() < gtol and abs(de) < etol:
+            break
+    final = [(z, *x[3 * i:3 * i + 3]) for i, z in enumerate(Z)]
+    return e, final, history

@@ -61,6 +61,7 @@ class ScfOptions(C.Structure):
         ("eigensolver", C.c_int),
         ("verbose", C.c_int),
         ("eri_method", C.c_int),
+        ("anchor_threshold", C.c_double),
     ]
 
 

@@ -192,7 +192,8 @@ Engine::~Engine()
                     d_entry_bra, d_entry_cnt, d_entry_lo0, d_pair_qs, d_off_static, d_cp_meta, plan.off64, plan.off32,
                     plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_Jp32, d_Kp32, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
                     scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
-                    scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j, d_grad, d_shell_atom};
+                    scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j, d_grad, d_shell_atom,
+                    d_shell_info, d_block_dmax};
     ri_destroy(ri);
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -284,6 +285,8 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
                     t.sp = ShellPairDev{};
                     t.sp.A = A; t.sp.B = B; t.sp.bfA = sa.bf; t.sp.bfB = sb.bf;
                     t.sp.la = la; t.sp.lb = lb;
+                    t.sp.mbase = 0;
+                    t.sp.mn = num_basis;
                     t.sp.ABx = Ac[0] - Bc[0]; t.sp.ABy = Ac[1] - Bc[1]; t.sp.ABz = Ac[2] - Bc[2];
                     double qs = 0.0, qm = 0.0;
                     for (int i = 0; i < sa.nprim; ++i)

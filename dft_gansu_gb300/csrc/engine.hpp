@@ -91,6 +91,8 @@ struct Engine {
     bool last_mixed = false;   // whether the last build used the FP32 accumulators
     double* d_grad = nullptr;     // 3 * natom gradient accumulators (allocated on first use)
     int* d_shell_atom = nullptr;  // contracted shell -> atom
+    int2* d_shell_info = nullptr;   // per shell: first basis function, number of components
+    float* d_block_dmax = nullptr;  // per shell block max |D| of the density being built (mixed plan)
     double* d_scalar = nullptr;  // small scratch scalars (8 doubles)
     unsigned long long* d_counters = nullptr;  // [class pair][precision][prim, contracted]
     long long bytes_h2d = 0;                   // bytes uploaded by engine creation

@@ -22,7 +22,8 @@ struct ShellPairDev {
     double ABx, ABy, ABz;  // A - B
     double Qmax;           // max primitive-pair Schwarz bound (reference definition)
     double Qs;             // sum of primitive-pair bounds (bounds the contracted integral)
-    double pad;
+    int mbase;             // molecule block: D/J/K element (a, b) of this pair's molecule is at
+    int mn;                //   mbase + a * mn + b (a single molecule: mbase = 0, mn = N)
     float fABx, fABy, fABz, fQmax;  // FP32-tier copies (no conversions in FP32 kernels)
 };
 static_assert(sizeof(ShellPairDev) == 96, "ShellPairDev layout");
@@ -62,6 +63,9 @@ struct FockClassLaunch {
     int num_basis;
     double schwarz_threshold;
     unsigned long long* counters;  // [0] primitive quartets, [1] contracted quartets
+    const float* block_dmax;       // incremental builds: max |dD| per shell block [A * nshell + B], or null
+    int nshell;
+    double skip_cut;               // skip when Qs_ab * Qs_cd * block max < skip_cut
 };
 
 }  // namespace gb

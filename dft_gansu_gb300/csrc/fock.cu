@@ -66,6 +66,22 @@ __global__ void scale_density_kernel(const double* __restrict__ D, const double*
     }
 }
 
+// max |D| over each shell block, both orders: out[A * ns + B] (shell first function and size in info)
+__global__ void block_absmax_kernel(const double* __restrict__ D, const int2* __restrict__ info, int ns, int n,
+                                    float* __restrict__ out)
+{
+    const long long total = static_cast<long long>(ns) * ns;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < total;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int A = static_cast<int>(k / ns), B = static_cast<int>(k % ns);
+        const int2 a = info[A], b = info[B];
+        double m = 0.0;
+        for (int i = 0; i < a.y; ++i)
+            for (int j = 0; j < b.y; ++j) m = fmax(m, fabs(D[static_cast<long long>(a.x + i) * n + b.x + j]));
+        out[k] = static_cast<float>(m);
+    }
+}
+
 __global__ void absmax_kernel(const double* __restrict__ A, long long n, double* __restrict__ out)
 {
     __shared__ double red[32];
@@ -221,6 +237,9 @@ FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off,
     L.num_basis = e.num_basis;
     L.schwarz_threshold = e.schwarz_threshold;
     L.counters = e.d_counters + 2 * (2 * cpi + (fp32 ? 1 : 0));
+    L.block_dmax = nullptr;
+    L.nshell = e.num_shells;
+    L.skip_cut = 0.0;
     return L;
 }
 
@@ -283,6 +302,20 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
         a.lo32 = e.plan.lo32;
         mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
         GB_LAUNCH_CHECK();
+        // per-shell-block maxima of the (difference) density for the per-quartet screen
+        if (!e.d_block_dmax) {
+            std::vector<int2> info(e.num_shells);
+            for (int i = 0; i < e.num_shells; ++i) info[i] = make_int2(e.shells[i].bf, ncart(e.shells[i].l));
+            GB_CUDA_TRY(cudaMalloc(&e.d_shell_info, sizeof(int2) * e.num_shells));
+            GB_CUDA_TRY(cudaMalloc(&e.d_block_dmax, sizeof(float) * e.num_shells * e.num_shells));
+            GB_CUDA_TRY(cudaMemcpy(e.d_shell_info, info.data(), sizeof(int2) * e.num_shells, cudaMemcpyHostToDevice));
+        }
+        {
+            const long long nsq = static_cast<long long>(e.num_shells) * e.num_shells;
+            const int g = static_cast<int>(std::min<long long>((nsq + 255) / 256, 4096));
+            block_absmax_kernel<<<g, 256, 0, s>>>(d_D, e.d_shell_info, e.num_shells, e.num_basis, e.d_block_dmax);
+            GB_LAUNCH_CHECK();
+        }
         for (int c = 0; c < ncp; ++c) {
             const ClassPair& cp = e.class_pairs[c];
             if (cp.n_survivors == 0) continue;
@@ -291,9 +324,13 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
             FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
             if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
             const int grid = grid_for(cp.n_survivors, e.num_sms);
-            f(false, make_launch(e, c, false, e.plan.off64, e.d_entry_lo0), grid, s);
+            FockClassLaunch l64 = make_launch(e, c, false, e.plan.off64, e.d_entry_lo0);
+            FockClassLaunch l32 = make_launch(e, c, true, e.plan.off32, e.plan.lo32);
+            l64.block_dmax = l32.block_dmax = e.d_block_dmax;
+            l64.skip_cut = l32.skip_cut = a.skip_threshold / a.factor;  // Qs Qs c_max^4 max|dD| < thr
+            f(false, l64, grid, s);
             GB_LAUNCH_CHECK();
-            f(true, make_launch(e, c, true, e.plan.off32, e.plan.lo32), grid, s);
+            f(true, l32, grid, s);
             GB_LAUNCH_CHECK();
         }
     }

@@ -189,10 +189,6 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((total + 31) >> 5) * ncd;
     const long long warp_stride = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
-    const T* __restrict__ Dp = static_cast<const T*>(L.density);
-    T* __restrict__ Jp = TierTypes<T>::J(L);
-    T* __restrict__ Kp = TierTypes<T>::K(L);
-    const int N = L.num_basis;
     long long prim_quartets = 0, contracted = 0;
     T I[kNAB];
 
@@ -200,7 +196,7 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
          wid += warp_stride) {
         const int cd = static_cast<int>(wid % ncd);
         const long long w = (wid / ncd) * 32 + lane;
-        const bool active = w < total;
+        bool active = w < total;
         int bra = -1, ket = -1;
         ShellPairDev bp{}, kp{};
         T fsym = T(0);
@@ -208,6 +204,12 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
             const int e = find_entry(L.off, L.nentry, w);
             bra = __ldg(L.entry_bra + e);
             ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(w - __ldg(L.off + e));
+            if (negligible_quartet(L, bra, ket)) {
+                active = false;
+                bra = ket = -1;
+            }
+        }
+        if (active) {
             bp = L.pairs[bra];
             kp = L.pairs[ket];
             fsym = T(1);
@@ -223,6 +225,11 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
         } else {
             for (int ab = 0; ab < kNAB; ++ab) I[ab] = T(0);
         }
+        // molecule block of this quartet (bra and ket pairs share it)
+        const int N = active ? bp.mn : L.num_basis;
+        const T* __restrict__ Dp = static_cast<const T*>(L.density) + (active ? bp.mbase : 0);
+        T* __restrict__ Jp = TierTypes<T>::J(L) + (active ? bp.mbase : 0);
+        T* __restrict__ Kp = TierTypes<T>::K(L) + (active ? bp.mbase : 0);
         const int na = ncart(bp.la), nb = ncart(bp.lb), nc = ncart(kp.la), nd = ncart(kp.lb);
         const int ic = cd / (nd > 0 ? nd : 1), id = cd % (nd > 0 ? nd : 1);
         const int c = kp.bfA + ic, d = kp.bfB + id;
@@ -232,11 +239,13 @@ __global__ void __launch_bounds__(kFockThreads) fock_generic_kernel(const FockCl
         const bool uniform_bra = __all_sync(0xffffffffu, (!active) || bra == bra0) && bra0 >= 0;
         const int na0 = __shfl_sync(0xffffffffu, na, 0), nb0 = __shfl_sync(0xffffffffu, nb, 0);
         const int bfA0 = __shfl_sync(0xffffffffu, bp.bfA, 0), bfB0 = __shfl_sync(0xffffffffu, bp.bfB, 0);
+        const int N0 = __shfl_sync(0xffffffffu, N, 0), mbase0 = __shfl_sync(0xffffffffu, active ? bp.mbase : 0, 0);
+        T* __restrict__ Jp0 = TierTypes<T>::J(L) + mbase0;
         const T dcd = active ? Dp[c * N + d] : T(0);
         if (uniform_bra) {
             for (int ab = 0; ab < na0 * nb0; ++ab) {
                 const T s = warp_sum(dcd * I[ab] * fsym);
-                if (lane == 0) atomicAdd(&Jp[(bfA0 + ab / nb0) * N + bfB0 + ab % nb0], s);
+                if (lane == 0) atomicAdd(&Jp0[(bfA0 + ab / nb0) * N0 + bfB0 + ab % nb0], s);
             }
         } else if (active) {
             for (int ab = 0; ab < na * nb; ++ab)

@@ -220,6 +220,22 @@ struct QuartetRef {
     bool active;
 };
 
+// Density-weighted screening of one contracted quartet (incremental builds):
+// true when Qs_ab Qs_cd times the largest |dD| over the six shell blocks the
+// quartet reads (AB, CD, AC, AD, BC, BD) is below the cut.
+__device__ __forceinline__ bool negligible_quartet(const FockClassLaunch& L, int bra, int ket)
+{
+    if (!L.block_dmax) return false;
+    const ShellPairDev* __restrict__ P = L.pairs;
+    const int A = P[bra].A, B = P[bra].B, C = P[ket].A, D = P[ket].B;
+    const int ns = L.nshell;
+    const float* __restrict__ bd = L.block_dmax;
+    const float dm = fmaxf(fmaxf(__ldg(bd + A * ns + B), __ldg(bd + C * ns + D)),
+                           fmaxf(fmaxf(__ldg(bd + A * ns + C), __ldg(bd + A * ns + D)),
+                                 fmaxf(__ldg(bd + B * ns + C), __ldg(bd + B * ns + D))));
+    return P[bra].Qs * P[ket].Qs * static_cast<double>(dm) < L.skip_cut;
+}
+
 // Evaluates and digests ket components [CD0, CD1) of one quartet per lane.
 template <class T, int LA, int LB, int LC, int LD, int CD0, int CD1>
 __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const QuartetRef q, int lane,
@@ -228,8 +244,8 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
     using PP = typename FockTypes<T>::PP;
     constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
     constexpr int NCH = CD1 - CD0;
-    const T* __restrict__ Dp = static_cast<const T*>(L.density);
-    const int N = L.num_basis;
+    int N = L.num_basis;
+    int mbase = 0;
 
     T I[NA * NB][NCH];
 #pragma unroll
@@ -243,6 +259,8 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
         const ShellPairDev bp = L.pairs[q.bra];
         const ShellPairDev kp = L.pairs[q.ket];
         bfA = bp.bfA; bfB = bp.bfB; bfC = kp.bfA; bfD = kp.bfB;
+        mbase = bp.mbase;  // bra and ket pairs belong to the same molecule
+        N = bp.mn;
         fsym = T(1);
         if (bp.A == bp.B) fsym *= T(0.5);
         if (kp.A == kp.B) fsym *= T(0.5);
@@ -252,8 +270,9 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
             static_cast<T>(L.schwarz_threshold), I);
     }
 
-    T* __restrict__ Jp = TierTypes<T>::J(L);
-    T* __restrict__ Kp = TierTypes<T>::K(L);
+    const T* __restrict__ Dp = static_cast<const T*>(L.density) + mbase;
+    T* __restrict__ Jp = TierTypes<T>::J(L) + mbase;
+    T* __restrict__ Kp = TierTypes<T>::K(L) + mbase;
     const int bra0 = __shfl_sync(0xffffffffu, q.bra, 0);
     const bool uniform_bra = __all_sync(0xffffffffu, (!q.active) || q.bra == bra0) && bra0 >= 0;
     // J'_ab += sum_cd D'_cd v  (a partial sum when the thread holds a component chunk)
@@ -263,6 +282,8 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
         for (int cd = CD0; cd < CD1; ++cd)
             dcd[cd - CD0] = q.active ? Dp[(bfC + cd / ND) * N + bfD + cd % ND] : T(0);
         const int bfA0 = __shfl_sync(0xffffffffu, bfA, 0), bfB0 = __shfl_sync(0xffffffffu, bfB, 0);
+        const int N0 = __shfl_sync(0xffffffffu, N, 0), mbase0 = __shfl_sync(0xffffffffu, mbase, 0);
+        T* __restrict__ Jp0 = TierTypes<T>::J(L) + mbase0;
 #pragma unroll
         for (int ab = 0; ab < NA * NB; ++ab) {
             T s = T(0);
@@ -271,7 +292,7 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
             s *= fsym;
             if (uniform_bra) {
                 s = warp_sum(s);
-                if (lane == 0) atomicAdd(&Jp[(bfA0 + ab / NB) * N + bfB0 + ab % NB], s);
+                if (lane == 0) atomicAdd(&Jp0[(bfA0 + ab / NB) * N0 + bfB0 + ab % NB], s);
             } else if (q.active) {
                 atomicAdd(&Jp[(bfA + ab / NB) * N + bfB + ab % NB], s);
             }
@@ -383,7 +404,12 @@ fock_direct_kernel(const FockClassLaunch launch)
             const int e = find_entry(launch.off, launch.nentry, w);
             q.bra = __ldg(launch.entry_bra + e);
             q.ket = launch.ket_base + __ldg(launch.entry_lo + e) + static_cast<int>(w - __ldg(launch.off + e));
-            ++contracted;
+            if (negligible_quartet(launch, q.bra, q.ket)) {
+                q.active = false;  // screened lanes look like lanes past the end (bra = -1)
+                q.bra = q.ket = -1;
+            } else {
+                ++contracted;
+            }
         }
         process_quartet<T, LA, LB, LC, LD, 0, NCD>(launch, q, lane, prim_quartets);
     }

@@ -127,22 +127,6 @@ __device__ __forceinline__ void ket_contract(int lmax, const int c[3], const int
             }
 }
 
-// sum_tuv E^{a'b'}_tuv x[tuv] for bra exponents a', b' (per axis)
-__device__ __forceinline__ double bra_contract(const int a[3], const int b[3], const double* ex, const double* ey,
-                                               const double* ez, const double* x)
-{
-    const double* px = ex + (a[0] * kGI + b[0]) * kGT;
-    const double* py = ey + (a[1] * kGI + b[1]) * kGT;
-    const double* pz = ez + (a[2] * kGI + b[2]) * kGT;
-    double s = 0.0;
-    for (int t = 0; t <= a[0] + b[0]; ++t)
-        for (int u = 0; u <= a[1] + b[1]; ++u) {
-            const double exy = px[t] * py[u];
-            for (int v = 0; v <= a[2] + b[2]; ++v) s += exy * pz[v] * x[gidx(t, u, v)];
-        }
-    return s;
-}
-
 struct GradLaunch {
     FockClassLaunch L;       // FP64 work list, pairs, primitive pairs, Boys table, D' (FP64)
     const int* shell_atom;   // contracted shell -> atom
@@ -198,15 +182,56 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
                 any |= (v != 0.0);
             }
         if (!any) continue;
-        double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+        // Bra side in Hermite space: per bra primitive pair, the weighted Hermite densities
+        //   H0[tuv]   = sum_ab w_ab E^{ab}_tuv
+        //   HA_k[tuv] = sum_ab w_ab (2 alpha E^{a+1_k, b}_tuv - a_k E^{a-1_k, b}_tuv)
+        // are built once and reused for every ket primitive pair, so the inner loop does
+        // not grow with the number of bra components.  Then
+        //   dA_k = sum HA_k x0,  dP_k = sum H0 x0[tuv + 1_k] (= dA_k + dB_k),
+        //   dC_k = sum H0 (2 gamma x[c + 1_k] - c_k x[c - 1_k]).
+        double gA[3] = {0, 0, 0}, gP[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+        double H0[kGX], HA[3][kGX];
         for (int ip = 0; ip < bp.pp_n; ++ip) {
             const PrimPair64 pb = pp[bp.pp_off + ip];
             if (pb.Q * kp.Qmax < thr) continue;
-            const double alpha2 = 2.0 * (pb.p - pb.b), beta2 = 2.0 * pb.b;
+            const double alpha2 = 2.0 * (pb.p - pb.b);
             const double oo2p = 0.5 * pb.invp;
-            grad_e_table(la + 1, lb + 1, pb.PAx, pb.PAx + bp.ABx, oo2p, ex);
-            grad_e_table(la + 1, lb + 1, pb.PAy, pb.PAy + bp.ABy, oo2p, ey);
-            grad_e_table(la + 1, lb + 1, pb.PAz, pb.PAz + bp.ABz, oo2p, ez);
+            grad_e_table(la + 1, lb, pb.PAx, pb.PAx + bp.ABx, oo2p, ex);
+            grad_e_table(la + 1, lb, pb.PAy, pb.PAy + bp.ABy, oo2p, ey);
+            grad_e_table(la + 1, lb, pb.PAz, pb.PAz + bp.ABz, oo2p, ez);
+            const int nh = nherm(lab + 1);
+            for (int h = 0; h < nh; ++h) { H0[h] = 0.0; HA[0][h] = 0.0; HA[1][h] = 0.0; HA[2][h] = 0.0; }
+            for (int ia = 0; ia < na; ++ia)
+                for (int ib = 0; ib < nb; ++ib) {
+                    const double wv = wcol[ia * nb + ib];
+                    if (wv == 0.0) continue;
+                    const int a[3] = {cart_exp(la, ia, 0), cart_exp(la, ia, 1), cart_exp(la, ia, 2)};
+                    const int b[3] = {cart_exp(lb, ib, 0), cart_exp(lb, ib, 1), cart_exp(lb, ib, 2)};
+                    // per-axis factors: e0 = E^{a b}, e1 = 2 alpha E^{a+1, b} - a E^{a-1, b}
+                    double e0[3][kGT], e1[3][kGT];
+                    const double* tab[3] = {ex, ey, ez};
+                    for (int k = 0; k < 3; ++k) {
+                        const double* row0 = tab[k] + (a[k] * kGI + b[k]) * kGT;
+                        const double* rowp = tab[k] + ((a[k] + 1) * kGI + b[k]) * kGT;
+                        const double* rowm = tab[k] + ((a[k] > 0 ? a[k] - 1 : 0) * kGI + b[k]) * kGT;
+                        for (int t = 0; t <= a[k] + b[k] + 1; ++t) {
+                            e0[k][t] = (t <= a[k] + b[k]) ? row0[t] : 0.0;
+                            double v = alpha2 * rowp[t];
+                            if (a[k] > 0 && t <= a[k] + b[k] - 1) v -= a[k] * rowm[t];
+                            e1[k][t] = v;
+                        }
+                    }
+                    for (int t = 0; t <= a[0] + b[0] + 1; ++t)
+                        for (int u = 0; u <= a[1] + b[1] + 1; ++u)
+                            for (int v = 0; v <= a[2] + b[2] + 1; ++v) {
+                                if (t + u + v > lab + 1) continue;
+                                const int h = gidx(t, u, v);
+                                HA[0][h] += wv * e1[0][t] * e0[1][u] * e0[2][v];
+                                HA[1][h] += wv * e0[0][t] * e1[1][u] * e0[2][v];
+                                HA[2][h] += wv * e0[0][t] * e0[1][u] * e1[2][v];
+                                H0[h] += wv * e0[0][t] * e0[1][u] * e0[2][v];
+                            }
+                }
             for (int jq = 0; jq < kp.pp_n; ++jq) {
                 const PrimPair64 pk = pp[kp.pp_off + jq];
                 if (pb.Q * pk.Q < thr) continue;
@@ -232,36 +257,29 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
                         ket_contract(lab, cp, d, fx, fy, fz, r, xm[k]);
                     }
                 }
-                for (int ia = 0; ia < na; ++ia)
-                    for (int ib = 0; ib < nb; ++ib) {
-                        const double wv = wcol[ia * nb + ib];
-                        if (wv == 0.0) continue;
-                        const int a[3] = {cart_exp(la, ia, 0), cart_exp(la, ia, 1), cart_exp(la, ia, 2)};
-                        const int b[3] = {cart_exp(lb, ib, 0), cart_exp(lb, ib, 1), cart_exp(lb, ib, 2)};
-                        for (int k = 0; k < 3; ++k) {
-                            int s[3] = {a[0], a[1], a[2]};
-                            s[k] += 1;
-                            double dA = alpha2 * bra_contract(s, b, ex, ey, ez, x0);
-                            if (a[k] > 0) {
-                                s[k] -= 2;
-                                dA -= a[k] * bra_contract(s, b, ex, ey, ez, x0);
+                for (int t = 0; t <= lab + 1; ++t)
+                    for (int u = 0; u + t <= lab + 1; ++u)
+                        for (int v = 0; v + u + t <= lab + 1; ++v) {
+                            const int h = gidx(t, u, v);
+                            const double x = x0[h];
+                            gA[0] += HA[0][h] * x;
+                            gA[1] += HA[1][h] * x;
+                            gA[2] += HA[2][h] * x;
+                            if (t + u + v > lab) continue;
+                            const double h0 = H0[h];
+                            gP[0] += h0 * x0[gidx(t + 1, u, v)];
+                            gP[1] += h0 * x0[gidx(t, u + 1, v)];
+                            gP[2] += h0 * x0[gidx(t, u, v + 1)];
+                            for (int k = 0; k < 3; ++k) {
+                                double dc = gamma2 * xp[k][h];
+                                if (c[k] > 0) dc -= c[k] * xm[k][h];
+                                gC[k] += h0 * dc;
                             }
-                            int t2[3] = {b[0], b[1], b[2]};
-                            t2[k] += 1;
-                            double dB = beta2 * bra_contract(a, t2, ex, ey, ez, x0);
-                            if (b[k] > 0) {
-                                t2[k] -= 2;
-                                dB -= b[k] * bra_contract(a, t2, ex, ey, ez, x0);
-                            }
-                            double dC = gamma2 * bra_contract(a, b, ex, ey, ez, xp[k]);
-                            if (c[k] > 0) dC -= c[k] * bra_contract(a, b, ex, ey, ez, xm[k]);
-                            gA[k] += wv * dA;
-                            gB[k] += wv * dB;
-                            gC[k] += wv * dC;
                         }
-                    }
             }
         }
+        double gB[3];
+        for (int k = 0; k < 3; ++k) gB[k] = gP[k] - gA[k];
         const int atA = G.shell_atom[bp.A], atB = G.shell_atom[bp.B], atC = G.shell_atom[kp.A],
                   atD = G.shell_atom[kp.B];
         for (int k = 0; k < 3; ++k) {
@@ -460,6 +478,9 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
         G.L.num_basis = e.num_basis;
         G.L.schwarz_threshold = e.schwarz_threshold;
         G.L.counters = e.d_counters;
+        G.L.block_dmax = nullptr;
+        G.L.nshell = e.num_shells;
+        G.L.skip_cut = 0.0;
         G.shell_atom = e.d_shell_atom;
         G.grad = e.d_grad;
         const int ncd = ncart(Y.la) * ncart(Y.lb);

@@ -409,6 +409,8 @@ int ri_set_auxiliary(Engine& e, const hf_primitive_shell* prims, int nprim, cons
         ShellPairDev sp{};
         sp.A = i; sp.B = -1; sp.bfA = shells[i].bf; sp.bfB = 0;
         sp.la = shells[i].l; sp.lb = 0;
+        sp.mbase = 0;
+        sp.mn = naux;
         sp.pp_off = shells[i].p_off; sp.pp_n = shells[i].np;
         double qm = 0.0, qs = 0.0;
         for (int k = 0; k < shells[i].np; ++k) { qm = std::max(qm, pp[shells[i].p_off + k].Q); qs += pp[shells[i].p_off + k].Q; }

@@ -323,6 +323,7 @@ void hf_scf_options_default(hf_scf_options* o)
     o->rebuild_every = 0;
     o->full_build_precision = HF_PRECISION_FP64;
     o->eri_method = HF_ERI_DIRECT;
+    o->anchor_threshold = 0.0;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -403,15 +404,20 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     double* h_energy = nullptr;
     cudaMallocHost(&h_energy, sizeof(double));
 
+    // Mixed tier with anchor_threshold > 0: full low-precision builds (direct: every
+    // quartet FP32; RI: split-BF16 K) while max|dD| >= anchor_threshold, then one FP64
+    // build (the anchor), then incremental builds.  With anchor_threshold <= 0 the
+    // first build is the anchor.  The SCF may not converge before the anchor.
+    const bool mixed_tier = opt.precision == HF_PRECISION_MIXED;
+    bool anchored = !(mixed_tier && opt.anchor_threshold > 0.0);
     bool ri_anchored = false;  // mixed RI: an FP64 K build has been taken
-    int ri_anchor_builds = 0;
     // one Fock build: F = H + G(D), full or incremental
     auto fock_build = [&](bool first) -> int {
         cudaEventRecord(f0, s);
         if (use_ri) {
             // J (FP64) from the packed B and D.  K: FP64 from the occupied orbitals
             // (D = 2 C_occ C_occ^T); under the mixed tier, split-BF16 tensor-core builds
-            // until max|dD| < mixed_threshold, then one FP64 anchor build, then
+            // until max|dD| < anchor_threshold, then one FP64 anchor build, then
             // incremental K(dD) from rotation-aligned orbital differences.
             double *J, *K;
             int r;
@@ -434,14 +440,14 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
                         if ((r = ri_add_inplace(e, Kacc, K, s))) return r;
                         done = true;
                     }
-                } else if (first || dmax >= opt.mixed_threshold) {
+                } else if (!anchored && (first || dmax >= opt.anchor_threshold)) {
                     if ((r = ri_k_tc_full(e, w.C, n, nocc, Kacc, s))) return r;
                     done = true;
                 }
                 if (!done) {  // FP64 anchor build
                     if ((r = ri_k_occupied(e, w.C, nocc, Kacc, s))) return r;
                     ri_anchored = true;
-                    ++ri_anchor_builds;
+                    anchored = true;
                 }
                 if ((r = ri_save_occupied(e, w.C, n, nocc, s))) return r;
                 if ((r = ri_fock_from_jk(e, w.H, J, Kacc, nullptr, false, w.F, s))) return r;
@@ -451,9 +457,28 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
             ++fock_builds;
             return HF_OK;
         }
+        int r;
+        if (!anchored) {
+            // before the anchor: full builds with every quartet in the FP32 tier, or the
+            // FP64 anchor build once max|dD| falls below anchor_threshold
+            double dmax = 1.0;
+            if (!first && (r = ri_absmax_diff(e, w.D, w.Dprev, &dmax, s))) return r;
+            const bool low = first || dmax >= opt.anchor_threshold;
+            if ((r = build_jk(e, w.D, nullptr, nullptr, low ? HF_PRECISION_MIXED : HF_PRECISION_FP64,
+                              std::numeric_limits<double>::infinity(), s)))
+                return r;
+            if (!low) anchored = true;
+            fock_from_jk_kernel<<<grid_nn(nn), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.last_mixed ? e.d_Jp32 : nullptr,
+                                                             e.last_mixed ? e.d_Kp32 : nullptr, e.d_scale, w.H, n, 0,
+                                                             w.G, w.F);
+            GB_LAUNCH_CHECK();
+            GB_CUDA_TRY(cudaMemcpyAsync(w.Dprev, w.D, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            cudaEventRecord(f1, s);
+            ++fock_builds;
+            return HF_OK;
+        }
         const bool incremental = opt.incremental && !first &&
                                  !(opt.rebuild_every > 0 && fock_builds % opt.rebuild_every == 0);
-        int r;
         if (incremental) {
             sub_kernel<<<grid_nn(nn), 256, 0, s>>>(w.D, w.Dprev, nn, w.dD);
             GB_LAUNCH_CHECK();
@@ -521,7 +546,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         if (!std::isfinite(energy)) return set_error("SCF energy is not finite"), HF_ERR_NOT_CONVERGED;
         if (diff < opt.convergence_threshold) {
             // mixed RI: energies before the FP64 anchor carry the BF16x3 error of whole K builds
-            if (!(use_ri && opt.precision == HF_PRECISION_MIXED && !ri_anchored)) { converged = true; break; }
+            if (anchored) { converged = true; break; }
         }
         ++iter;
         prev = energy;

@@ -229,6 +229,9 @@ typedef struct {
     int eigensolver;                /* 0: cuSOLVER syevd (divide and conquer), 1: syevj (Jacobi) */
     int verbose;                    /* print per-iteration lines like the reference */
     int eri_method;                 /* HF_ERI_DIRECT or HF_ERI_RI (eri_method = direct / ri, src/rhf.cu:72-88) */
+    double anchor_threshold;        /* mixed tier: low-precision full builds (direct: all quartets FP32; RI:
+                                       split-BF16 K) while max|dD| >= this, then one FP64 build, then
+                                       incremental builds; 0 = the first build is the FP64 one */
 } hf_scf_options;
 
 /* Two-electron backend of the SCF. */

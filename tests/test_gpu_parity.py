@@ -240,3 +240,19 @@ def test_edge_cases(built_library, cuda):
     np.testing.assert_allclose(_np(J), np.einsum("ijkl,kl->ij", eri, D), atol=1e-11)
     np.testing.assert_allclose(_np(K), np.einsum("ikjl,kl->ij", eri, D), atol=1e-11)
     assert engf.stats()["num_quartets"] < eng.stats()["num_quartets"] * 10 ** 6
+
+
+@pytest.mark.parametrize("anchor,tau", [(1e-2, 0.1), (1e-1, 1.0)])
+def test_scf_mixed_anchored_decane(built_library, cuda, anchor, tau):
+    # all-FP32 full builds while max|dD| >= anchor, one FP64 build, then FP32-tier dD builds
+    atoms = geometry.alkane(10, jitter=0.02, seed=0)
+    mol, eng = _engine(atoms, "6-31g_st")
+    r64 = eng.rhf_scf(mol.num_electrons, {"convergence_threshold": 1e-8}, want_matrices=True)
+    rmx = eng.rhf_scf(mol.num_electrons, {"convergence_threshold": 1e-8, "precision": gg.HF_PRECISION_MIXED,
+                                          "mixed_threshold": tau, "incremental": 1, "anchor_threshold": anchor},
+                      want_matrices=True)
+    assert rmx["converged"] == 1
+    assert abs(rmx["total_energy"] - r64["total_energy"]) < 1e-6
+    np.testing.assert_allclose(_np(rmx["orbital_energies"]), _np(r64["orbital_energies"]), atol=1e-5)
+    # exactly one full FP64 build's worth of FP64 quartets: the anchor
+    assert rmx["fp64_quartets"] <= r64["fp64_quartets"] / (r64["iterations"] + 1) * 1.5

@@ -128,7 +128,7 @@ def test_mixed_ri_scf_matches_fp64_ri(built_library, cuda, case):
     g, eng, _, _ = _setup(case)
     r64 = eng.rhf_scf(eng.mol.num_electrons, {"convergence_threshold": 1e-10, "eri_method": gg.HF_ERI_RI})
     rmx = eng.rhf_scf(eng.mol.num_electrons, {"convergence_threshold": 1e-10, "eri_method": gg.HF_ERI_RI,
-                                              "precision": gg.HF_PRECISION_MIXED, "mixed_threshold": 1e-2})
+                                              "precision": gg.HF_PRECISION_MIXED, "anchor_threshold": 1e-2})
     assert r64["converged"] == 1 and rmx["converged"] == 1
     assert abs(rmx["total_energy"] - r64["total_energy"]) < 1e-6
     assert abs(rmx["total_energy"] - float(g["energy_total"])) < 1e-6
@@ -142,6 +142,6 @@ def test_mixed_ri_scf_propane(built_library, cuda):
     base = {"convergence_threshold": 1e-9, "eri_method": gg.HF_ERI_RI}
     r64 = eng.rhf_scf(mol.num_electrons, base)
     for tau in (1e-1, 1e-2, 1e-3):
-        rmx = eng.rhf_scf(mol.num_electrons, dict(base, precision=gg.HF_PRECISION_MIXED, mixed_threshold=tau))
+        rmx = eng.rhf_scf(mol.num_electrons, dict(base, precision=gg.HF_PRECISION_MIXED, anchor_threshold=tau))
         assert rmx["converged"] == 1
         assert abs(rmx["total_energy"] - r64["total_energy"]) < 1e-6, tau
