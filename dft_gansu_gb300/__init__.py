@@ -21,7 +21,7 @@ ANGSTROM_TO_BOHR = 1.8897259886
 __all__ = [
     "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
     "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "basis_path",
-    "optimize_geometry", "energy_and_gradient_at",
+    "optimize_geometry", "energy_and_gradient_at", "Batch",
 ]
 
 
@@ -310,6 +310,59 @@ _DEFAULTS = {
 _SHORT = {"-m": "method", "-v": "verbose", "-p": "parameter_file", "-x": "xyzfilename", "-g": "gbsfilename",
           "-ag": "auxiliary_gbsfilename", "-c": "charge"}
 _KEEP_CASE = {"xyzfilename", "gbsfilename", "parameter_file", "auxiliary_gbsfilename"}
+
+
+class Batch:
+    """Many independent molecules in one engine (hf_engine_create_batch) and
+    their RHF in lockstep (hf_batch_rhf_scf).  Molecules are ordered by
+    (N, electrons) inside, so that equal sizes form batched linear-algebra
+    groups; results come back in the caller's order."""
+
+    def __init__(self, molecules, schwarz_screening_threshold: float = 1e-12):
+        self.molecules = list(molecules)
+        n = len(self.molecules)
+        self.order = sorted(range(n), key=lambda i: (self.molecules[i].num_basis, self.molecules[i].num_electrons))
+        ms = [self.molecules[i] for i in self.order]
+        P = C.c_void_p * n
+        I = C.c_int * n
+        h = C.c_void_p()
+        check(lib().hf_engine_create_batch(
+            n, P(*[C.cast(m._prims, C.c_void_p) for m in ms]), I(*[m.num_primitives for m in ms]),
+            P(*[C.cast(m._cgto, C.c_void_p) for m in ms]), I(*[m.num_basis for m in ms]),
+            P(*[C.cast(m._atoms, C.c_void_p) for m in ms]), I(*[m.num_atoms for m in ms]),
+            float(schwarz_screening_threshold), C.byref(h)), "hf_engine_create_batch")
+        self._h = h
+        self._sorted = ms
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hf_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def rhf_scf(self, options: dict | None = None):
+        """Returns (per-molecule result dicts in the caller's order, batch ms, batch iterations)."""
+        opt = ScfOptions()
+        lib().hf_scf_options_default(C.byref(opt))
+        for k, v in (options or {}).items():
+            setattr(opt, k, v)
+        n = len(self._sorted)
+        res = (ScfResult * n)()
+        ne = (C.c_int * n)(*[m.num_electrons for m in self._sorted])
+        ms, it = C.c_double(), C.c_int()
+        st = lib().hf_batch_rhf_scf(self._h, ne, C.byref(opt), res, C.byref(ms), C.byref(it))
+        if st not in (0, 4):
+            check(st, "hf_batch_rhf_scf")
+        out = [None] * n
+        for k, i in enumerate(self.order):
+            out[i] = {f: getattr(res[k], f) for f, _ in ScfResult._fields_}
+            out[i]["status"] = st
+        return out, ms.value, it.value
 
 
 class ParameterManager:

@@ -30,7 +30,7 @@ FOCK_CLASSES = [
     (2, 2, 2, 0), (2, 2, 2, 1), (2, 2, 2, 2),
 ]
 
-CUDA_SOURCES = ["engine.cu", "fock.cu", "fock_generic.cu", "one_electron.cu", "scf.cu", "peaks.cu", "diis_noalloc.cu", "grad.cu", "ri.cu", "tc_gemm.cu"]
+CUDA_SOURCES = ["engine.cu", "fock.cu", "fock_generic.cu", "one_electron.cu", "scf.cu", "peaks.cu", "diis_noalloc.cu", "grad.cu", "ri.cu", "tc_gemm.cu", "batch.cu"]
 CXX_SOURCES = ["molecule.cpp", "errors.cpp"]
 
 

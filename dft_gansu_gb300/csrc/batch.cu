@@ -1,0 +1,470 @@
+// Batched RHF over many independent molecules (no reference counterpart: the
+// reference runs RHF::solve once per molecule, src/hf.cu:245-314).
+//
+// All molecules live in one engine (build_engine with several inputs): shell
+// pairs and quartet work lists never mix molecules, and every N x N matrix of
+// molecule m is a block of the block layout (BlockMap).  One SCF iteration for
+// the whole batch is:
+//   * per group of equal-size molecules (molecules are sorted by (N, nocc)):
+//     F' = X^T F X, eigenvectors (cuSOLVER batched syev), C = X V, D = 2 C_occ C_occ^T
+//     as strided-batched DGEMMs over the group's contiguous blocks;
+//   * one Fock build over all molecules (the same class kernels and work lists
+//     as a single molecule: one launch per quartet class covers the batch);
+//   * per-molecule energies in one kernel, read back once;
+//   * DIIS for every molecule: error F D S - S D F by batched DGEMMs, then one
+//     kernel with a CTA per molecule that updates that molecule's B matrix,
+//     solves the bordered system and extrapolates F.
+// The SCF semantics per molecule are those of the single-molecule loop (core
+// guess, cyclic DIIS from the second stored pair, |dE| convergence); a
+// converged molecule keeps iterating with the batch, its result is the one at
+// its first convergence.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <limits>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+
+namespace gb {
+
+int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s);
+
+namespace {
+
+constexpr int kBatchDiis = 16;
+
+struct Group {
+    int first, count;  // molecules [first, first + count) of the sorted order
+    int n, nocc;
+    long long base;    // block offset of the first molecule
+};
+
+struct BatchState {
+    int m = 8;
+    double *S = nullptr, *H = nullptr, *X = nullptr, *F = nullptr, *D = nullptr, *C = nullptr, *Fp = nullptr,
+           *T1 = nullptr, *T2 = nullptr, *eps = nullptr, *Es = nullptr, *Fs = nullptr, *B = nullptr,
+           *energy = nullptr, *work = nullptr;
+    int* info = nullptr;
+    size_t work_bytes = 0;
+    std::vector<void*> owned;
+    ~BatchState()
+    {
+        for (void* p : owned) cudaFree(p);
+    }
+    template <class T>
+    int alloc(T*& p, size_t n)
+    {
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            set_error(std::string("cudaMalloc (batch): ") + cudaGetErrorString(e));
+            return HF_ERR_OUT_OF_MEMORY;
+        }
+        owned.push_back(p);
+        return HF_OK;
+    }
+};
+
+int grid_of(long long n) { return static_cast<int>(std::max<long long>(1, std::min<long long>((n + 255) / 256, 8192))); }
+
+// X = U s^{-1/2} per block (eigenvalues below 1e-6 -> 0), from column-major eigenvectors W
+__global__ void batch_transform_kernel(const double* __restrict__ W, const double* __restrict__ evals,
+                                       const long long* __restrict__ ebase, const BlockMap M, double* __restrict__ X)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int m = block_of(M, k);
+        const int n = M.n[m];
+        const long long base = M.base[m], r = k - base;
+        const int i = static_cast<int>(r / n), c = static_cast<int>(r % n);
+        const double v = evals[ebase[m] + c];
+        const double d = (v < 1e-6) ? 0.0 : 1.0 / sqrt(v);
+        X[k] = W[base + static_cast<long long>(c) * n + i] * d;
+    }
+}
+
+// G = 2 (J' + J'^T) s s - (K' + K'^T) s s / 2, F = H + G, per block
+__global__ void batch_fock_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
+                                  const double* __restrict__ s, const double* __restrict__ H, const BlockMap M,
+                                  double* __restrict__ F)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int m = block_of(M, k);
+        const int n = M.n[m], g0 = M.bf0[m];
+        const long long base = M.base[m], r = k - base;
+        const int i = static_cast<int>(r / n), j = static_cast<int>(r % n);
+        const long long kt = base + static_cast<long long>(j) * n + i;
+        const double ss = s[g0 + i] * s[g0 + j];
+        F[k] = H[k] + (2.0 * (Jp[k] + Jp[kt]) - 0.5 * (Kp[k] + Kp[kt])) * ss;
+    }
+}
+
+// E_m = 1/2 sum D (H + F) over block m: one CTA per molecule
+__global__ void batch_energy_kernel(const double* __restrict__ D, const double* __restrict__ H,
+                                    const double* __restrict__ F, const BlockMap M, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    const int m = blockIdx.x;
+    const long long base = M.base[m], nn = static_cast<long long>(M.n[m]) * M.n[m];
+    double s = 0.0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) s += D[base + k] * (H[base + k] + F[base + k]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) out[m] = 0.5 * s;
+    }
+}
+
+// E = T - T^T per block
+__global__ void batch_antisym_kernel(const double* __restrict__ T, const BlockMap M, double* __restrict__ E)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int m = block_of(M, k);
+        const int n = M.n[m];
+        const long long base = M.base[m], r = k - base;
+        const int i = static_cast<int>(r / n), j = static_cast<int>(r % n);
+        E[k] = T[k] - T[base + static_cast<long long>(j) * n + i];
+    }
+}
+
+// One CTA per molecule: new row/column `slot` of its DIIS B matrix from the stored
+// errors, then (nprev > 1) the bordered solve and F = sum c_i F_i.
+__global__ void batch_diis_kernel(const double* __restrict__ Es, const double* __restrict__ Fs, long long nelem,
+                                  const BlockMap M, int slot, int nprev, double* __restrict__ Bm,
+                                  double* __restrict__ F)
+{
+    __shared__ double red[32];
+    __shared__ double coef[kBatchDiis];
+    const int m = blockIdx.x;
+    const long long base = M.base[m], nn = static_cast<long long>(M.n[m]) * M.n[m];
+    double* B = Bm + static_cast<long long>(m) * kBatchDiis * kBatchDiis;
+    const double* en = Es + static_cast<long long>(slot) * nelem + base;
+    for (int j = 0; j < nprev; ++j) {
+        const double* ej = Es + static_cast<long long>(j) * nelem + base;
+        double s = 0.0;
+        for (long long k = threadIdx.x; k < nn; k += blockDim.x) s += en[k] * ej[k];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += red[w];
+            B[slot * kBatchDiis + j] = t;
+            B[j * kBatchDiis + slot] = t;
+        }
+        __syncthreads();
+    }
+    if (nprev < 2) return;
+    if (threadIdx.x == 0) {
+        // bordered system [B -1; -1 0] c = [0 .. 0 -1], partial pivoting
+        const int n = nprev + 1;
+        double A[kBatchDiis + 1][kBatchDiis + 2];
+        for (int i = 0; i < n; ++i) {
+            for (int j = 0; j < n; ++j) {
+                if (i < nprev && j < nprev) A[i][j] = B[i * kBatchDiis + j];
+                else if (i == nprev && j == nprev) A[i][j] = 0.0;
+                else A[i][j] = -1.0;
+            }
+            A[i][n] = (i == nprev) ? -1.0 : 0.0;
+        }
+        for (int c = 0; c < n; ++c) {
+            int piv = c;
+            for (int r = c + 1; r < n; ++r)
+                if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
+            if (A[piv][c] == 0.0) continue;
+            if (piv != c)
+                for (int k = 0; k <= n; ++k) { const double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
+            for (int r = c + 1; r < n; ++r) {
+                const double f = A[r][c] / A[c][c];
+                for (int k = c; k <= n; ++k) A[r][k] -= f * A[c][k];
+            }
+        }
+        double x[kBatchDiis + 1];
+        for (int r = n - 1; r >= 0; --r) {
+            double s = A[r][n];
+            for (int k = r + 1; k < n; ++k) s -= A[r][k] * x[k];
+            x[r] = (A[r][r] != 0.0) ? s / A[r][r] : 0.0;
+        }
+        for (int i = 0; i < nprev; ++i) coef[i] = x[i];
+    }
+    __syncthreads();
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) {
+        double s = 0.0;
+        for (int i = 0; i < nprev; ++i) s += coef[i] * Fs[static_cast<long long>(i) * nelem + base + k];
+        F[base + k] = s;
+    }
+}
+
+// row-major strided-batched C = alpha op(A) op(B) + beta C over n x n blocks (k inner)
+cublasStatus_t gemm_batched(cublasHandle_t h, bool ta, bool tb, int n, int k, double alpha, const double* A, int lda,
+                            const double* B, int ldb, double beta, double* C, int count)
+{
+    const long long st = static_cast<long long>(n) * n;
+    return cublasDgemmStridedBatched(h, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N, n, n, k, &alpha,
+                                     B, ldb, st, A, lda, st, &beta, C, n, st, count);
+}
+
+struct Batch {
+    Engine* e;
+    BatchState w;
+    std::vector<Group> groups;
+    std::vector<long long> ebase;  // eigenvalue offsets per molecule
+    long long* d_ebase = nullptr;
+    cusolverDnParams_t params = nullptr;
+    ~Batch()
+    {
+        if (d_ebase) cudaFree(d_ebase);
+        if (params) cusolverDnDestroyParams(params);
+    }
+};
+
+// eigenvectors (in place, column-major) and eigenvalues of every block of A, group by group
+int batch_syev(Batch& b, double* A, double* evals, cudaStream_t s)
+{
+    Engine& e = *b.e;
+    cusolverDnSetStream(e.cusolver, s);
+    for (const Group& g : b.groups) {
+        double* Ag = A + g.base;
+        double* Wg = evals + b.ebase[g.first];
+        size_t dbytes = 0, hbytes = 0;
+        cusolverStatus_t q = cusolverDnXsyevBatched_bufferSize(e.cusolver, b.params, CUSOLVER_EIG_MODE_VECTOR,
+                                                               CUBLAS_FILL_MODE_LOWER, g.n, CUDA_R_64F, Ag, g.n,
+                                                               CUDA_R_64F, Wg, CUDA_R_64F, &dbytes, &hbytes, g.count);
+        bool batched = (q == CUSOLVER_STATUS_SUCCESS) && hbytes <= (1u << 20);
+        if (batched) {
+            if (dbytes > b.w.work_bytes) {
+                double* nw = nullptr;
+                if (b.w.alloc(nw, dbytes / sizeof(double) + 1)) return HF_ERR_OUT_OF_MEMORY;
+                b.w.work = nw;
+                b.w.work_bytes = dbytes;
+            }
+            std::vector<char> hwork(std::max<size_t>(hbytes, 1));
+            q = cusolverDnXsyevBatched(e.cusolver, b.params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g.n,
+                                       CUDA_R_64F, Ag, g.n, CUDA_R_64F, Wg, CUDA_R_64F, b.w.work, dbytes,
+                                       hwork.data(), hbytes, b.w.info, g.count);
+            batched = (q == CUSOLVER_STATUS_SUCCESS);
+        }
+        if (batched) continue;
+        // one divide-and-conquer solve per molecule
+        int lwork = 0;
+        if (cusolverDnDsyevd_bufferSize(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g.n, Ag, g.n, Wg,
+                                        &lwork) != CUSOLVER_STATUS_SUCCESS)
+            return set_error("cusolverDnDsyevd_bufferSize failed"), HF_ERR_SOLVER;
+        if (static_cast<size_t>(lwork) * sizeof(double) > b.w.work_bytes) {
+            double* nw = nullptr;
+            if (b.w.alloc(nw, static_cast<size_t>(lwork) + 1)) return HF_ERR_OUT_OF_MEMORY;
+            b.w.work = nw;
+            b.w.work_bytes = static_cast<size_t>(lwork) * sizeof(double);
+        }
+        for (int i = 0; i < g.count; ++i) {
+            const long long off = static_cast<long long>(i) * g.n * g.n;
+            if (cusolverDnDsyevd(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g.n, Ag + off, g.n,
+                                 Wg + static_cast<long long>(i) * g.n, b.w.work, lwork, b.w.info) !=
+                CUSOLVER_STATUS_SUCCESS)
+                return set_error("cusolverDnDsyevd (batch) failed"), HF_ERR_SOLVER;
+        }
+    }
+    return HF_OK;
+}
+
+// C and D from F for every molecule: F' = X^T F X, eigenvectors V, C = X V, D = 2 C_occ C_occ^T
+int batch_density(Batch& b, const double* F, cudaStream_t s)
+{
+    Engine& e = *b.e;
+    BatchState& w = b.w;
+    cublasSetStream(e.cublas, s);
+    for (const Group& g : b.groups) {
+        const long long o = g.base;
+        if (gemm_batched(e.cublas, false, false, g.n, g.n, 1.0, F + o, g.n, w.X + o, g.n, 0.0, w.T1 + o, g.count) ||
+            gemm_batched(e.cublas, true, false, g.n, g.n, 1.0, w.X + o, g.n, w.T1 + o, g.n, 0.0, w.Fp + o, g.count))
+            return set_error("cublasDgemmStridedBatched (F') failed"), HF_ERR_SOLVER;
+    }
+    int st = batch_syev(b, w.Fp, w.eps, s);
+    if (st) return st;
+    for (const Group& g : b.groups) {
+        const long long o = g.base;
+        // V as row-major is V^T (column-major eigenvectors): C = X (V^T)^T
+        if (gemm_batched(e.cublas, false, true, g.n, g.n, 1.0, w.X + o, g.n, w.Fp + o, g.n, 0.0, w.C + o, g.count) ||
+            gemm_batched(e.cublas, false, true, g.n, g.nocc, 2.0, w.C + o, g.n, w.C + o, g.n, 0.0, w.D + o, g.count))
+            return set_error("cublasDgemmStridedBatched (C, D) failed"), HF_ERR_SOLVER;
+    }
+    return HF_OK;
+}
+
+int batch_fock(Batch& b, cudaStream_t s)
+{
+    Engine& e = *b.e;
+    int st = build_jk(e, b.w.D, nullptr, nullptr, HF_PRECISION_FP64, 0.0, s);
+    if (st) return st;
+    batch_fock_kernel<<<grid_of(e.nelem), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, b.w.H, e.block_map(), b.w.F);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+}  // namespace
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int hf_engine_create_batch(int num_molecules, const hf_primitive_shell* const* prims, const int* num_primitives,
+                           const double* const* cgto_norm, const int* num_basis, const hf_atom* const* atoms,
+                           const int* num_atoms, double schwarz_threshold, hf_engine** out)
+{
+    clear_error();
+    if (num_molecules <= 0 || !prims || !num_primitives || !cgto_norm || !num_basis || !atoms || !num_atoms || !out)
+        return set_error("hf_engine_create_batch: null argument"), HF_ERR_INVALID_ARGUMENT;
+    std::vector<MolInput> mols(num_molecules);
+    for (int m = 0; m < num_molecules; ++m)
+        mols[m] = MolInput{prims[m], num_primitives[m], cgto_norm[m], num_basis[m], atoms[m], num_atoms[m]};
+    return build_engine(mols.data(), num_molecules, schwarz_threshold, out);
+}
+
+int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_options* opt_in, hf_scf_result* results,
+                     double* batch_scf_ms, int* batch_iterations)
+{
+    clear_error();
+    if (!eng || !num_electrons || !results) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    hf_scf_options opt;
+    if (opt_in) opt = *opt_in; else hf_scf_options_default(&opt);
+    if (opt.diis_size < 1 || opt.diis_size > kBatchDiis)
+        return set_error("diis_size must be in [1, 16]"), HF_ERR_INVALID_ARGUMENT;
+    const int nmol = e.nmol;
+    Batch b;
+    b.e = &e;
+    // groups of consecutive molecules with equal (N, nocc)
+    for (int m = 0; m < nmol; ++m) {
+        const int ne = num_electrons[m];
+        if (ne <= 0 || (ne & 1) || ne / 2 > e.mol_n[m])
+            return set_error("molecule " + std::to_string(m) + ": RHF needs an even electron count <= 2N"),
+                   HF_ERR_INVALID_ARGUMENT;
+        if (!b.groups.empty() && b.groups.back().n == e.mol_n[m] && b.groups.back().nocc == ne / 2 &&
+            b.groups.back().first + b.groups.back().count == m)
+            b.groups.back().count++;
+        else
+            b.groups.push_back(Group{m, 1, e.mol_n[m], ne / 2, e.mol_base[m]});
+    }
+    b.ebase.assign(nmol + 1, 0);
+    for (int m = 0; m < nmol; ++m) b.ebase[m + 1] = b.ebase[m] + e.mol_n[m];
+    cudaStream_t s = nullptr;
+    const long long ne = e.nelem;
+    BatchState& w = b.w;
+    int st;
+    if ((st = w.alloc(w.S, ne)) || (st = w.alloc(w.H, ne)) || (st = w.alloc(w.X, ne)) || (st = w.alloc(w.F, ne)) ||
+        (st = w.alloc(w.D, ne)) || (st = w.alloc(w.C, ne)) || (st = w.alloc(w.Fp, ne)) || (st = w.alloc(w.T1, ne)) ||
+        (st = w.alloc(w.T2, ne)) || (st = w.alloc(w.eps, b.ebase[nmol])) ||
+        (st = w.alloc(w.Es, static_cast<size_t>(opt.diis_size) * ne)) ||
+        (st = w.alloc(w.Fs, static_cast<size_t>(opt.diis_size) * ne)) ||
+        (st = w.alloc(w.B, static_cast<size_t>(nmol) * kBatchDiis * kBatchDiis)) || (st = w.alloc(w.energy, nmol)) ||
+        (st = w.alloc(w.info, std::max(nmol, 1))))
+        return st;
+    if (cudaMalloc(&b.d_ebase, sizeof(long long) * (nmol + 1)) != cudaSuccess)
+        return set_error("cudaMalloc failed"), HF_ERR_OUT_OF_MEMORY;
+    GB_CUDA_TRY(cudaMemcpy(b.d_ebase, b.ebase.data(), sizeof(long long) * (nmol + 1), cudaMemcpyHostToDevice));
+    if (cusolverDnCreateParams(&b.params) != CUSOLVER_STATUS_SUCCESS)
+        return set_error("cusolverDnCreateParams failed"), HF_ERR_SOLVER;
+    GB_CUDA_TRY(cudaMemsetAsync(w.B, 0, sizeof(double) * nmol * kBatchDiis * kBatchDiis, s));
+    std::vector<double> enuc(nmol, 0.0);
+    for (int m = 0; m < nmol; ++m)
+        for (int i = 0; i < e.mol_natom[m]; ++i)
+            for (int j = i + 1; j < e.mol_natom[m]; ++j) {
+                const hf_atom& A = e.atoms[e.mol_atom0[m] + i];
+                const hf_atom& B = e.atoms[e.mol_atom0[m] + j];
+                const double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+                enuc[m] += static_cast<double>(A.atomic_number) * B.atomic_number / std::sqrt(dx * dx + dy * dy + dz * dz);
+            }
+
+    cudaEvent_t l0, l1;
+    cudaEventCreate(&l0);
+    cudaEventCreate(&l1);
+    // setup: S, H, X = U s^-1/2, core guess
+    if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
+    GB_CUDA_TRY(cudaMemcpyAsync(w.Fp, w.S, sizeof(double) * ne, cudaMemcpyDeviceToDevice, s));
+    if ((st = batch_syev(b, w.Fp, w.eps, s))) return st;
+    batch_transform_kernel<<<grid_of(ne), 256, 0, s>>>(w.Fp, w.eps, b.d_ebase, e.block_map(), w.X);
+    GB_LAUNCH_CHECK();
+    if ((st = batch_density(b, w.H, s))) return st;
+    if ((st = batch_fock(b, s))) return st;
+
+    std::vector<double> E(nmol), prev(nmol, std::numeric_limits<double>::max());
+    std::vector<int> done_iter(nmol, -1);
+    std::vector<double> done_energy(nmol, 0.0);
+    const int m = opt.diis_size;
+    int iter = 0, diis_iter = 0, ndone = 0;
+    cudaEventRecord(l0, s);
+    while (iter < opt.max_iter) {
+        if ((st = batch_density(b, w.F, s))) return st;
+        if ((st = batch_fock(b, s))) return st;
+        batch_energy_kernel<<<nmol, 256, 0, s>>>(w.D, w.H, w.F, e.block_map(), w.energy);
+        GB_LAUNCH_CHECK();
+        GB_CUDA_TRY(cudaMemcpyAsync(E.data(), w.energy, sizeof(double) * nmol, cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int k = 0; k < nmol; ++k) {
+            if (!std::isfinite(E[k])) return set_error("batch SCF energy is not finite"), HF_ERR_NOT_CONVERGED;
+            if (done_iter[k] < 0 && std::fabs(E[k] - prev[k]) < opt.convergence_threshold) {
+                done_iter[k] = iter;
+                done_energy[k] = E[k];
+                ++ndone;
+            }
+        }
+        if (ndone == nmol) break;
+        ++iter;
+        prev = E;
+        // DIIS: e = F D S - S D F per molecule, stored with F in the ring
+        const int slot = diis_iter % m;
+        double* Es = w.Es + static_cast<long long>(slot) * ne;
+        for (const Group& g : b.groups) {
+            const long long o = g.base;
+            if (gemm_batched(e.cublas, false, false, g.n, g.n, 1.0, w.F + o, g.n, w.D + o, g.n, 0.0, w.T1 + o, g.count) ||
+                gemm_batched(e.cublas, false, false, g.n, g.n, 1.0, w.T1 + o, g.n, w.S + o, g.n, 0.0, w.T2 + o, g.count))
+                return set_error("cublasDgemmStridedBatched (DIIS) failed"), HF_ERR_SOLVER;
+        }
+        batch_antisym_kernel<<<grid_of(ne), 256, 0, s>>>(w.T2, e.block_map(), Es);
+        GB_LAUNCH_CHECK();
+        if (opt.diis_include_transform) {
+            for (const Group& g : b.groups) {
+                const long long o = g.base;
+                if (gemm_batched(e.cublas, true, false, g.n, g.n, 1.0, w.X + o, g.n, Es + o, g.n, 0.0, w.T1 + o, g.count) ||
+                    gemm_batched(e.cublas, false, false, g.n, g.n, 1.0, w.T1 + o, g.n, w.X + o, g.n, 0.0, Es + o, g.count))
+                    return set_error("cublasDgemmStridedBatched (DIIS transform) failed"), HF_ERR_SOLVER;
+            }
+        }
+        GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + static_cast<long long>(slot) * ne, w.F, sizeof(double) * ne,
+                                    cudaMemcpyDeviceToDevice, s));
+        const int nprev = std::min(diis_iter + 1, m);
+        batch_diis_kernel<<<nmol, 256, 0, s>>>(w.Es, w.Fs, ne, e.block_map(), slot, nprev, w.B, w.F);
+        GB_LAUNCH_CHECK();
+        ++diis_iter;
+    }
+    cudaEventRecord(l1, s);
+    GB_CUDA_TRY(cudaEventSynchronize(l1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, l0, l1);
+    cudaEventDestroy(l0);
+    cudaEventDestroy(l1);
+    if (batch_scf_ms) *batch_scf_ms = ms;
+    if (batch_iterations) *batch_iterations = iter;
+    for (int k = 0; k < nmol; ++k) {
+        hf_scf_result& r = results[k];
+        r = hf_scf_result{};
+        r.nuclear_repulsion = enuc[k];
+        r.converged = done_iter[k] >= 0 ? 1 : 0;
+        r.electronic_energy = r.converged ? done_energy[k] : E[k];
+        r.total_energy = r.electronic_energy + enuc[k];
+        r.iterations = r.converged ? done_iter[k] : iter;
+        r.scf_ms_total = ms;
+    }
+    return ndone == nmol ? HF_OK : (set_error("batch SCF: not every molecule converged"), HF_ERR_NOT_CONVERGED);
+}
+
+}  // extern "C"

@@ -193,7 +193,7 @@ Engine::~Engine()
                     plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_Jp32, d_Kp32, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
                     scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
                     scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j, d_grad, d_shell_atom,
-                    d_shell_info, d_block_dmax};
+                    d_shell_info, d_block_dmax, d_mol_base, d_mol_n, d_mol_bf0, d_mol_atoms, d_shell_mol};
     ri_destroy(ri);
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -202,39 +202,66 @@ Engine::~Engine()
     if (cusolver) cusolverDnDestroy(cusolver);
 }
 
-}  // namespace gb
 
-using namespace gb;
-
-extern "C" {
-
-int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const double* cgto_norm, int num_basis,
-                     const hf_atom* atoms, int num_atoms, double schwarz_threshold, hf_engine** out)
+// Builds an engine over one or several molecules.  Shells, pairs and quartet
+// work lists never mix molecules; matrices use the block layout of BlockMap.
+int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_engine** out)
 {
     clear_error();
-    if (!prims || !cgto_norm || !atoms || !out || num_primitives <= 0 || num_basis <= 0 || num_atoms <= 0)
-        return set_error("hf_engine_create: null pointer or empty input"), HF_ERR_INVALID_ARGUMENT;
+    if (!mols || nmol <= 0 || !out) return set_error("build_engine: no molecules"), HF_ERR_INVALID_ARGUMENT;
     *out = nullptr;
-    for (int i = 0; i < num_primitives; ++i) {
-        const auto& p = prims[i];
-        if (p.shell_type < 0 || p.shell_type > kMaxL)
-            return set_error("hf_engine_create: shell type " + std::to_string(p.shell_type) +
-                             " not supported (s, p, d shells)"),
-                   HF_ERR_INVALID_ARGUMENT;
-        if (p.basis_index + ncart(p.shell_type) > static_cast<size_t>(num_basis) || !(p.exponent > 0.0))
-            return set_error("hf_engine_create: primitive " + std::to_string(i) + " out of range"),
-                   HF_ERR_INVALID_ARGUMENT;
-        if (i > 0 && prims[i - 1].shell_type > p.shell_type)
-            return set_error("hf_engine_create: primitives must be sorted by shell type"), HF_ERR_INVALID_ARGUMENT;
+    int num_primitives = 0, num_basis = 0, num_atoms = 0;
+    for (int m = 0; m < nmol; ++m) {
+        const MolInput& M = mols[m];
+        if (!M.prims || !M.cgto || !M.atoms || M.nprim <= 0 || M.nbasis <= 0 || M.natom <= 0)
+            return set_error("hf_engine_create: null pointer or empty input"), HF_ERR_INVALID_ARGUMENT;
+        for (int i = 0; i < M.nprim; ++i) {
+            const auto& p = M.prims[i];
+            if (p.shell_type < 0 || p.shell_type > kMaxL)
+                return set_error("hf_engine_create: shell type " + std::to_string(p.shell_type) +
+                                 " not supported (s, p, d shells)"),
+                       HF_ERR_INVALID_ARGUMENT;
+            if (p.basis_index + ncart(p.shell_type) > static_cast<size_t>(M.nbasis) || !(p.exponent > 0.0) ||
+                p.atom_index < 0 || p.atom_index >= M.natom)
+                return set_error("hf_engine_create: primitive " + std::to_string(i) + " out of range"),
+                       HF_ERR_INVALID_ARGUMENT;
+            if (i > 0 && M.prims[i - 1].shell_type > p.shell_type)
+                return set_error("hf_engine_create: primitives must be sorted by shell type"), HF_ERR_INVALID_ARGUMENT;
+        }
+        num_primitives += M.nprim;
+        num_basis += M.nbasis;
+        num_atoms += M.natom;
     }
     auto e = std::make_unique<Engine>();
     e->num_basis = num_basis;
     e->num_atoms = num_atoms;
     e->num_prims = num_primitives;
     e->schwarz_threshold = schwarz_threshold;
-    e->prims.assign(prims, prims + num_primitives);
-    e->cgto.assign(cgto_norm, cgto_norm + num_basis);
-    e->atoms.assign(atoms, atoms + num_atoms);
+    e->nmol = nmol;
+    e->mol_base.assign(1, 0);
+    for (int m = 0; m < nmol; ++m) {
+        const MolInput& M = mols[m];
+        const int bf0 = static_cast<int>(e->cgto.size()), a0 = static_cast<int>(e->atoms.size());
+        e->mol_bf0.push_back(bf0);
+        e->mol_n.push_back(M.nbasis);
+        e->mol_atom0.push_back(a0);
+        e->mol_natom.push_back(M.natom);
+        e->mol_base.push_back(e->mol_base.back() + static_cast<long long>(M.nbasis) * M.nbasis);
+        for (int i = 0; i < M.nprim; ++i) {
+            hf_primitive_shell p = M.prims[i];
+            p.basis_index += static_cast<size_t>(bf0);
+            p.atom_index += a0;
+            e->prims.push_back(p);
+        }
+        e->cgto.insert(e->cgto.end(), M.cgto, M.cgto + M.nbasis);
+        e->atoms.insert(e->atoms.end(), M.atoms, M.atoms + M.natom);
+    }
+    e->nelem = e->mol_base.back();
+    std::vector<int> atom_mol(num_atoms);
+    for (int m = 0; m < nmol; ++m)
+        for (int a = 0; a < e->mol_natom[m]; ++a) atom_mol[e->mol_atom0[m] + a] = m;
+    const hf_primitive_shell* prims = e->prims.data();
+    const hf_atom* atoms = e->atoms.data();
     e->cgto_max = *std::max_element(e->cgto.begin(), e->cgto.end());
 
     // ---- contracted shells: group by (shell_type, basis_index)
@@ -250,6 +277,7 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
         const auto& p0 = prims[kv.second[0]];
         s.x = p0.x; s.y = p0.y; s.z = p0.z;
         s.atom = p0.atom_index;
+        s.mol = atom_mol[p0.atom_index];
         for (int idx : kv.second) {
             sh_alpha.push_back(prims[idx].exponent);
             sh_coef.push_back(scaled_coef(prims[idx].coefficient, prims[idx].exponent, s.l));
@@ -261,6 +289,9 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
     for (const Shell& s : e->shells)
         for (int i = 0; i < ncart(s.l); ++i) e->scale[s.bf + i] = e->cgto[s.bf + i] * component_factor(s.l, i);
 
+    std::vector<std::vector<int>> mol_shells(nmol);
+    for (int i = 0; i < e->num_shells; ++i) mol_shells[e->shells[i].mol].push_back(i);
+
     std::vector<double> boys;
     host_boys_table(boys);
 
@@ -271,11 +302,13 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
             struct Tmp {
                 ShellPairDev sp;
                 std::vector<PrimPair64> pp;
+                int mol;
             };
             std::vector<Tmp> tmp;
-            for (int A = 0; A < e->num_shells; ++A) {
+            for (int m = 0; m < nmol; ++m)
+            for (int A : mol_shells[m]) {
                 if (e->shells[A].l != la) continue;
-                for (int B = 0; B < e->num_shells; ++B) {
+                for (int B : mol_shells[m]) {
                     if (e->shells[B].l != lb) continue;
                     if (la == lb && B > A) continue;
                     const Shell& sa = e->shells[A];
@@ -283,10 +316,13 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
                     const double Ac[3] = {sa.x, sa.y, sa.z}, Bc[3] = {sb.x, sb.y, sb.z};
                     Tmp t;
                     t.sp = ShellPairDev{};
-                    t.sp.A = A; t.sp.B = B; t.sp.bfA = sa.bf; t.sp.bfB = sb.bf;
+                    t.sp.A = A; t.sp.B = B;
+                    t.sp.bfA = sa.bf - e->mol_bf0[m];  // molecule-local function indices
+                    t.sp.bfB = sb.bf - e->mol_bf0[m];
                     t.sp.la = la; t.sp.lb = lb;
-                    t.sp.mbase = 0;
-                    t.sp.mn = num_basis;
+                    t.sp.mbase = static_cast<int>(e->mol_base[m]);
+                    t.sp.mn = e->mol_n[m];
+                    t.mol = m;
                     t.sp.ABx = Ac[0] - Bc[0]; t.sp.ABy = Ac[1] - Bc[1]; t.sp.ABz = Ac[2] - Bc[2];
                     double qs = 0.0, qm = 0.0;
                     for (int i = 0; i < sa.nprim; ++i)
@@ -306,13 +342,16 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
             // groups of equal primitive-pair count (so the lanes of a warp run
             // the same primitive loops), each group sorted by Qs descending
             std::stable_sort(tmp.begin(), tmp.end(), [](const Tmp& a, const Tmp& b) {
+                if (a.mol != b.mol) return a.mol < b.mol;
                 if (a.pp.size() != b.pp.size()) return a.pp.size() > b.pp.size();
                 return a.sp.Qs > b.sp.Qs;
             });
             for (size_t k = 0; k < tmp.size(); ++k) {
                 Tmp& t = tmp[k];
-                if (k == 0 || tmp[k - 1].pp.size() != t.pp.size())
+                if (k == 0 || tmp[k - 1].pp.size() != t.pp.size() || tmp[k - 1].mol != t.mol) {
                     pc.groups.push_back({static_cast<int>(k), 0});
+                    pc.group_mol.push_back(t.mol);
+                }
                 pc.groups.back().second++;
                 t.sp.pp_off = static_cast<int>(e->pp64.size());
                 t.sp.pp_n = static_cast<int>(t.pp.size());
@@ -336,9 +375,15 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
             ClassPair cp{X, Y, static_cast<int>(e->entry_bra.size()), 0, 0};
             e->off_static.push_back(0);
             long long acc = 0;
+            // ket groups of each molecule (groups are sorted by molecule)
+            std::vector<int> gbeg(nmol + 1, 0);
+            for (size_t gi = 0; gi < py.groups.size(); ++gi) gbeg[py.group_mol[gi] + 1]++;
+            for (int m = 0; m < nmol; ++m) gbeg[m + 1] += gbeg[m];
             for (int i = 0; i < px.count; ++i) {
                 const double qi = e->pairs[px.begin + i].Qs;
-                for (const auto& g : py.groups) {
+                const int mi = e->shells[e->pairs[px.begin + i].A].mol;
+                for (int gi = gbeg[mi]; gi < gbeg[mi + 1]; ++gi) {
+                    const auto& g = py.groups[gi];
                     // kets of a group sorted by Qs descending: count those with qi*qj >= thr
                     int lo = 0, hi = g.second;
                     while (lo < hi) {
@@ -407,8 +452,19 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
         }
         e->d_cp_meta = dev_upload(meta, st);
     }
+    {
+        std::vector<int2> mol_atoms(nmol);
+        for (int m = 0; m < nmol; ++m) mol_atoms[m] = make_int2(e->mol_atom0[m], e->mol_natom[m]);
+        std::vector<int> shell_mol(e->num_shells);
+        for (int i = 0; i < e->num_shells; ++i) shell_mol[i] = e->shells[i].mol;
+        e->d_mol_base = dev_upload(e->mol_base, st);
+        e->d_mol_n = dev_upload(e->mol_n, st);
+        e->d_mol_bf0 = dev_upload(e->mol_bf0, st);
+        e->d_mol_atoms = dev_upload(mol_atoms, st);
+        e->d_shell_mol = dev_upload(shell_mol, st);
+    }
     if (st != HF_OK) return st;
-    const size_t nn = static_cast<size_t>(num_basis) * num_basis;
+    const size_t nn = static_cast<size_t>(e->nelem);
     const size_t noff = e->off_static.size();
     if ((st = dev_alloc(e->plan.off64, noff)) || (st = dev_alloc(e->plan.off32, noff)) ||
         (st = dev_alloc(e->plan.lo32, e->entry_bra.size())) || (st = dev_alloc(e->d_Dp64, nn)) ||
@@ -428,6 +484,19 @@ int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const 
         e->off_static.size() * sizeof(long long) + 4 * e->class_pairs.size() * sizeof(int));
     *out = reinterpret_cast<hf_engine*>(e.release());
     return HF_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int hf_engine_create(const hf_primitive_shell* prims, int num_primitives, const double* cgto_norm, int num_basis,
+                     const hf_atom* atoms, int num_atoms, double schwarz_threshold, hf_engine** out)
+{
+    const MolInput m{prims, num_primitives, cgto_norm, num_basis, atoms, num_atoms};
+    return build_engine(&m, 1, schwarz_threshold, out);
 }
 
 void hf_engine_destroy(hf_engine* eng) { delete reinterpret_cast<Engine*>(eng); }

@@ -20,16 +20,52 @@ constexpr int kNumClassPairs = kNumPairClasses * (kNumPairClasses + 1) / 2;
 constexpr int kCounterSlots = kNumClassPairs * 2 * 2;
 
 struct Shell {
-    int l, nprim, prim_off, bf, atom;
+    int l, nprim, prim_off, bf, atom;  // bf: global first function (sum of the earlier molecules' N + local)
+    int mol;                           // molecule of the shell (0 for a single-molecule engine)
     double x, y, z;
 };
+
+// Block layout of N x N matrices for one or several molecules: molecule m's
+// matrix occupies [base[m], base[m] + n[m]^2) row-major; a single molecule is
+// the plain N x N matrix.
+struct BlockMap {
+    const long long* base;  // nmol + 1 offsets
+    const int* n;
+    const int* bf0;         // first global function of each molecule
+    int nmol;
+    long long nelem;        // base[nmol]
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ int block_of(const BlockMap& M, long long k)
+{
+    int lo = 0, hi = M.nmol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (M.base[mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+#endif
 
 // (la, lb) pair classes with la >= lb, ordered (0,0),(1,0),(1,1),(2,0),(2,1),(2,2)
 struct PairClass {
     int la, lb;
     int begin, count;  // global pair index range
     std::vector<std::pair<int, int>> groups;  // (class-relative start, size) of equal primitive-pair count
+    std::vector<int> group_mol;               // molecule of each group (groups never span molecules)
 };
+
+// One molecule of an engine's input (reference layouts: gansu::PrimitiveShell, gansu::Atom).
+struct MolInput {
+    const hf_primitive_shell* prims;
+    int nprim;
+    const double* cgto;
+    int nbasis;
+    const hf_atom* atoms;
+    int natom;
+};
+int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_engine** out);
 
 // bra class X >= ket class Y
 struct ClassPair {
@@ -49,6 +85,17 @@ struct RiState;  // ri.hpp
 
 struct Engine {
     int num_basis = 0, num_shells = 0, num_atoms = 0, num_prims = 0;
+    // molecules (a batch engine holds several; a plain engine one)
+    int nmol = 1;
+    std::vector<int> mol_bf0, mol_n, mol_atom0, mol_natom;
+    std::vector<long long> mol_base;  // nmol + 1 block offsets of the block layout
+    long long nelem = 0;              // elements of one block-layout matrix (N^2 for one molecule)
+    long long* d_mol_base = nullptr;
+    int* d_mol_n = nullptr;
+    int* d_mol_bf0 = nullptr;
+    int2* d_mol_atoms = nullptr;      // first atom, number of atoms
+    int* d_shell_mol = nullptr;
+    BlockMap block_map() const { return BlockMap{d_mol_base, d_mol_n, d_mol_bf0, nmol, nelem}; }
     double schwarz_threshold = 1e-12;
     double cgto_max = 1.0;
 

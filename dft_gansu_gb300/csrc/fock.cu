@@ -53,14 +53,17 @@ namespace {
 
 constexpr int kPlanThreads = 256;
 
-__global__ void scale_density_kernel(const double* __restrict__ D, const double* __restrict__ s, int n,
+// D' = s D s per molecule block (global function g = bf0 + local index)
+__global__ void scale_density_kernel(const double* __restrict__ D, const double* __restrict__ s, const BlockMap M,
                                      double* __restrict__ Dp64, float* __restrict__ Dp32)
 {
-    const long long nn = static_cast<long long>(n) * n;
-    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
          k += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int i = static_cast<int>(k / n), j = static_cast<int>(k % n);
-        const double v = s[i] * D[k] * s[j];
+        const int m = block_of(M, k);
+        const int n = M.n[m], g0 = M.bf0[m];
+        const long long r = k - M.base[m];
+        const int i = static_cast<int>(r / n), j = static_cast<int>(r % n);
+        const double v = s[g0 + i] * D[k] * s[g0 + j];
         Dp64[k] = v;
         if (Dp32) Dp32[k] = static_cast<float>(v);
     }
@@ -189,15 +192,17 @@ __global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
 
 __global__ void finish_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
                               const float* __restrict__ Jp32, const float* __restrict__ Kp32,
-                              const double* __restrict__ s, const double* __restrict__ H, int n,
+                              const double* __restrict__ s, const double* __restrict__ H, const BlockMap M,
                               double* __restrict__ J, double* __restrict__ K, double* __restrict__ F)
 {
-    const long long nn = static_cast<long long>(n) * n;
-    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
          k += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int i = static_cast<int>(k / n), j = static_cast<int>(k % n);
-        const long long kt = static_cast<long long>(j) * n + i;
-        const double ss = s[i] * s[j];
+        const int m = block_of(M, k);
+        const int n = M.n[m], g0 = M.bf0[m];
+        const long long base = M.base[m], r = k - base;
+        const int i = static_cast<int>(r / n), j = static_cast<int>(r % n);
+        const long long kt = base + static_cast<long long>(j) * n + i;
+        const double ss = s[g0 + i] * s[g0 + j];
         double jsum = Jp[k] + Jp[kt], ksum = Kp[k] + Kp[kt];
         if (Jp32) {
             jsum += static_cast<double>(Jp32[k]) + static_cast<double>(Jp32[kt]);
@@ -247,9 +252,9 @@ FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off,
 
 int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s)
 {
-    const long long nn = static_cast<long long>(e.num_basis) * e.num_basis;
+    const long long nn = e.nelem;
     const int grid = static_cast<int>(std::min<long long>((nn + 255) / 256, 4096));
-    scale_density_kernel<<<grid, 256, 0, s>>>(d_D, e.d_scale, e.num_basis, e.d_Dp64, want_fp32 ? e.d_Dp32 : nullptr);
+    scale_density_kernel<<<grid, 256, 0, s>>>(d_D, e.d_scale, e.block_map(), e.d_Dp64, want_fp32 ? e.d_Dp32 : nullptr);
     GB_LAUNCH_CHECK();
     return HF_OK;
 }
@@ -257,7 +262,7 @@ int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s)
 int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
              cudaStream_t s, bool /*accumulate_counters*/)
 {
-    const size_t nn = static_cast<size_t>(e.num_basis) * e.num_basis;
+    const size_t nn = static_cast<size_t>(e.nelem);
     const bool mixed = (precision == HF_PRECISION_MIXED);
     int st = scale_density(e, d_D, mixed, s);
     if (st) return st;
@@ -303,14 +308,15 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
         mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
         GB_LAUNCH_CHECK();
         // per-shell-block maxima of the (difference) density for the per-quartet screen
-        if (!e.d_block_dmax) {
+        // (single-molecule engines: the table is num_shells^2)
+        if (e.nmol == 1 && !e.d_block_dmax) {
             std::vector<int2> info(e.num_shells);
             for (int i = 0; i < e.num_shells; ++i) info[i] = make_int2(e.shells[i].bf, ncart(e.shells[i].l));
             GB_CUDA_TRY(cudaMalloc(&e.d_shell_info, sizeof(int2) * e.num_shells));
             GB_CUDA_TRY(cudaMalloc(&e.d_block_dmax, sizeof(float) * e.num_shells * e.num_shells));
             GB_CUDA_TRY(cudaMemcpy(e.d_shell_info, info.data(), sizeof(int2) * e.num_shells, cudaMemcpyHostToDevice));
         }
-        {
+        if (e.nmol == 1) {
             const long long nsq = static_cast<long long>(e.num_shells) * e.num_shells;
             const int g = static_cast<int>(std::min<long long>((nsq + 255) / 256, 4096));
             block_absmax_kernel<<<g, 256, 0, s>>>(d_D, e.d_shell_info, e.num_shells, e.num_basis, e.d_block_dmax);
@@ -337,7 +343,7 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
     if (d_J || d_K) {
         const int grid = static_cast<int>(std::min<long long>((static_cast<long long>(nn) + 255) / 256, 4096));
         finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, mixed ? e.d_Jp32 : nullptr, mixed ? e.d_Kp32 : nullptr,
-                                           e.d_scale, nullptr, e.num_basis, d_J, d_K, nullptr);
+                                           e.d_scale, nullptr, e.block_map(), d_J, d_K, nullptr);
         GB_LAUNCH_CHECK();
     }
     return HF_OK;
@@ -346,10 +352,10 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
 int finish_fock(Engine& e, const double* d_H, const double* d_J, const double* d_K, double* d_F, cudaStream_t s)
 {
     (void)d_J; (void)d_K;
-    const long long nn = static_cast<long long>(e.num_basis) * e.num_basis;
+    const long long nn = e.nelem;
     const int grid = static_cast<int>(std::min<long long>((nn + 255) / 256, 4096));
     finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, e.last_mixed ? e.d_Jp32 : nullptr,
-                                       e.last_mixed ? e.d_Kp32 : nullptr, e.d_scale, d_H, e.num_basis, nullptr, nullptr,
+                                       e.last_mixed ? e.d_Kp32 : nullptr, e.d_scale, d_H, e.block_map(), nullptr, nullptr,
                                        d_F);
     GB_LAUNCH_CHECK();
     return HF_OK;
@@ -418,6 +424,7 @@ int hf_compute_eri_matrix(hf_engine* eng, double* d_eri, void* stream)
     clear_error();
     if (!eng || !d_eri) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
     Engine& e = *reinterpret_cast<Engine*>(eng);
+    if (e.nmol != 1) return set_error("hf_compute_eri_matrix: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t n = e.num_basis;
     GB_CUDA_TRY(cudaMemsetAsync(d_eri, 0, n * n * n * n * sizeof(double), s));

@@ -549,6 +549,8 @@ int hf_rhf_gradient(hf_engine* eng, const double* d_density, const double* d_ene
     clear_error();
     if (!eng || !d_density || !d_energy_weighted_density || !h_gradient)
         return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<Engine*>(eng)->nmol != 1)
+        return set_error("hf_rhf_gradient: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
     float ms = 0.f;
     const int st = rhf_gradient(*reinterpret_cast<Engine*>(eng), d_density, d_energy_weighted_density, h_gradient,
                                 static_cast<cudaStream_t>(stream), &ms);

@@ -21,14 +21,21 @@ constexpr int kOneThreads = 128;
 template <int LA, int LB>
 __global__ void __launch_bounds__(kOneThreads)
 one_electron_kernel(const ShellPairDev* __restrict__ pairs, int begin, int count, const PrimPair64* __restrict__ pp,
-                    const double* __restrict__ boys, const double* __restrict__ atoms, int natom,
-                    const double* __restrict__ scale, int n, double kfold, double* __restrict__ S,
-                    double* __restrict__ H)
+                    const double* __restrict__ boys, const double* __restrict__ atoms,
+                    const int* __restrict__ shell_mol, const int2* __restrict__ mol_atoms,
+                    const int* __restrict__ mol_bf0, const double* __restrict__ scale, double kfold,
+                    double* __restrict__ S, double* __restrict__ H)
 {
     constexpr int NA = ncart(LA), NB = ncart(LB), L = LA + LB;
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= count) return;
     const ShellPairDev sp = pairs[begin + idx];
+    // the pair's molecule: its atoms (nuclear attraction), first global function, matrix block
+    const int mol = shell_mol[sp.A];
+    const int2 arange = mol_atoms[mol];
+    const int g0 = mol_bf0[mol], n = sp.mn;
+    S += sp.mbase;
+    H += sp.mbase;
     double s_[NA][NB], t_[NA][NB], v_[NA][NB];
 #pragma unroll
     for (int i = 0; i < NA; ++i)
@@ -58,7 +65,7 @@ one_electron_kernel(const ShellPairDev* __restrict__ pairs, int begin, int count
                 s_[ia][ib] += k1 * sx * sy * sz;
                 t_[ia][ib] += k1 * (kin(Ex, ax, bx) * sy * sz + sx * kin(Ey, ay, by) * sz + sx * sy * kin(Ez, az, bz));
             }
-        for (int c = 0; c < natom; ++c) {
+        for (int c = arange.x; c < arange.x + arange.y; ++c) {
             const double X = q.Px - atoms[4 * c], Y = q.Py - atoms[4 * c + 1], Z = q.Pz - atoms[4 * c + 2];
             double Fs[L + 1];
             boys_fp64<L>(p * (X * X + Y * Y + Z * Z), boys, Fs);
@@ -96,7 +103,7 @@ one_electron_kernel(const ShellPairDev* __restrict__ pairs, int begin, int count
 #pragma unroll
         for (int ib = 0; ib < NB; ++ib) {
             const int a = sp.bfA + ia, bb = sp.bfB + ib;
-            const double ss = scale[a] * scale[bb];
+            const double ss = scale[g0 + a] * scale[g0 + bb];
             const double sv = s_[ia][ib] * ss, hv = (t_[ia][ib] + v_[ia][ib]) * ss;
             S[static_cast<long long>(a) * n + bb] = sv;
             S[static_cast<long long>(bb) * n + a] = sv;
@@ -116,8 +123,9 @@ int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s)
 #define GB_ONE(a, b)                                                                                           \
     if (pc.la == a && pc.lb == b)                                                                              \
         one_electron_kernel<a, b><<<grid, kOneThreads, 0, s>>>(e.d_pairs, pc.begin, pc.count, e.d_pp64,        \
-                                                               e.d_boys64, e.d_atoms, e.num_atoms, e.d_scale,  \
-                                                               e.num_basis, kfold, d_S, d_H);
+                                                               e.d_boys64, e.d_atoms, e.d_shell_mol,           \
+                                                               e.d_mol_atoms, e.d_mol_bf0, e.d_scale, kfold,   \
+                                                               d_S, d_H);
         GB_ONE(0, 0) GB_ONE(1, 0) GB_ONE(1, 1) GB_ONE(2, 0) GB_ONE(2, 1) GB_ONE(2, 2)
 #undef GB_ONE
         GB_LAUNCH_CHECK();

@@ -1047,6 +1047,8 @@ int hf_engine_set_auxiliary_basis(hf_engine* eng, const hf_primitive_shell* aux_
     clear_error();
     if (!eng || !aux_prims || !aux_cgto_norm || num_aux_primitives <= 0 || num_aux_basis <= 0)
         return set_error("null argument or empty auxiliary basis"), HF_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<Engine*>(eng)->nmol != 1)
+        return set_error("RI: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
     return ri_set_auxiliary(*reinterpret_cast<Engine*>(eng), aux_prims, num_aux_primitives, aux_cgto_norm,
                             num_aux_basis);
 }

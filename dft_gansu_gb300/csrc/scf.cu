@@ -361,6 +361,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     clear_error();
     if (!eng || !res) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
     Engine& e = *reinterpret_cast<Engine*>(eng);
+    if (e.nmol != 1) return set_error("hf_rhf_scf: a batch engine runs hf_batch_rhf_scf"), HF_ERR_INVALID_ARGUMENT;
     hf_scf_options opt;
     if (opt_in) opt = *opt_in; else hf_scf_options_default(&opt);
     if (num_electrons <= 0 || (num_electrons & 1))

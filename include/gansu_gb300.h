@@ -266,6 +266,27 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt, hf_
                double* d_density_out, double* d_fock_out, double* d_orbital_energies_out,
                double* d_coefficients_out);
 
+/* ---------------------------------------------------------------- batch */
+/* One engine over many independent molecules (no reference counterpart: the
+ * reference solves one molecule per HF object).  Molecule m is given as the
+ * arrays hf_engine_create takes.  Shell pairs and quartets never mix
+ * molecules; one launch per quartet class serves the whole batch.  Give
+ * molecules of equal size (and electron count) next to each other: each run
+ * of them is one group of batched linear algebra.  RI, the gradient and
+ * hf_rhf_scf are single-molecule; a batch engine's J/K/F outputs use the
+ * block layout (molecule m's N_m x N_m matrix after those of molecules < m). */
+int hf_engine_create_batch(int num_molecules, const hf_primitive_shell* const* prims, const int* num_primitives,
+                           const double* const* cgto_norm, const int* num_basis, const hf_atom* const* atoms,
+                           const int* num_atoms, double schwarz_threshold, hf_engine** out);
+
+/* RHF for every molecule of a batch engine, in lockstep iterations (replaces a
+ * loop of RHF::solve, src/hf.cu:245-314; FP64).  results[m] holds molecule m's
+ * energies and iteration count at its own convergence; batch_scf_ms (may be
+ * NULL) the device time of the batch loop and batch_iterations (may be NULL)
+ * its iteration count.  HF_ERR_NOT_CONVERGED if any molecule did not converge. */
+int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_options* opt, hf_scf_result* results,
+                     double* batch_scf_ms, int* batch_iterations);
+
 /* ------------------------------------------------------------- gradient */
 /* Energy-weighted density W = 2 sum_{i < num_occupied} eps_i C_i C_i^T from the
  * SCF's coefficients (row-major, orbitals as columns) and orbital energies.

@@ -1,0 +1,53 @@
+"""Batched RHF (hf_engine_create_batch + hf_batch_rhf_scf) against one engine
+and one SCF per molecule: every molecule's energy within 1e-8 Eh (the same FP64
+arithmetic; only atomic summation orders differ) and the batch converges."""
+import numpy as np
+import pytest
+
+import dft_gansu_gb300 as gg
+from dft_gansu_gb300 import geometry
+
+pytestmark = pytest.mark.gpu
+CONV = {"convergence_threshold": 1e-9}
+
+
+def _individual(atoms, gbs):
+    mol = gg.Molecular(atoms, gg.basis_path(gbs))
+    eng = gg.Engine(mol, 1e-12)
+    r = eng.rhf_scf(mol.num_electrons, CONV)
+    assert r["converged"] == 1
+    return r["total_energy"]
+
+
+def test_batch_matches_individual_runs(built_library, cuda):
+    clusters = geometry.water_cluster_set(10, nmax=4, seed=5)
+    mols = [gg.Molecular(c, gg.basis_path("6-31g")) for c in clusters]
+    batch = gg.Batch(mols)
+    res, ms, it = batch.rhf_scf(CONV)
+    assert ms > 0 and it > 0
+    for c, r in zip(clusters, res):
+        assert r["converged"] == 1
+        assert abs(r["total_energy"] - _individual(c, "6-31g")) < 1e-8
+
+
+def test_batch_of_one_and_mixed_basis(built_library, cuda):
+    atoms = geometry.water()
+    res, _, _ = gg.Batch([gg.Molecular(atoms, gg.basis_path("sto-3g"))]).rhf_scf(CONV)
+    assert abs(res[0]["total_energy"] - _individual(atoms, "sto-3g")) < 1e-9
+    # different basis sets and sizes in one batch, given out of order
+    mols = [gg.Molecular(geometry.alkane(3, seed=2), gg.basis_path("6-31g_st")),
+            gg.Molecular(atoms, gg.basis_path("sto-3g")),
+            gg.Molecular(atoms, gg.basis_path("6-31g_st"))]
+    res, _, _ = gg.Batch(mols).rhf_scf(CONV)
+    assert abs(res[0]["total_energy"] - _individual(geometry.alkane(3, seed=2), "6-31g_st")) < 1e-8
+    assert abs(res[1]["total_energy"] - _individual(atoms, "sto-3g")) < 1e-8
+    assert abs(res[2]["total_energy"] - _individual(atoms, "6-31g_st")) < 1e-8
+
+
+def test_batch_engine_rejects_single_molecule_entry_points(built_library, cuda):
+    mols = [gg.Molecular(geometry.water(), gg.basis_path("sto-3g")) for _ in range(2)]
+    b = gg.Batch(mols)
+    import ctypes as C
+    from dft_gansu_gb300._capi import ScfResult, lib
+    r = ScfResult()
+    assert lib().hf_rhf_scf(b._h, 10, None, C.byref(r), None, None, None, None) == 1
