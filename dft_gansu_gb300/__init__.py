@@ -227,14 +227,39 @@ class Engine:
                                                _ptr(W), _stream(stream)), "hf_energy_weighted_density")
         return W
 
-    def gradient(self, density, energy_weighted_density, stream=None):
-        """Analytic nuclear gradient (natom, 3) in Eh/bohr and its device time in ms."""
+    def gradient(self, density, energy_weighted_density, stream=None, mixed_threshold=None):
+        """Analytic nuclear gradient (natom, 3) in Eh/bohr and its device time in ms.
+        mixed_threshold: None for FP64, else the FP64/FP32 quartet cut."""
         g = np.zeros(3 * self.mol.num_atoms)
         ms = C.c_double()
-        check(lib().hf_rhf_gradient(self._h, _ptr(density), _ptr(energy_weighted_density),
-                                    g.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ms), _stream(stream)),
-              "hf_rhf_gradient")
+        gp = g.ctypes.data_as(C.POINTER(C.c_double))
+        if mixed_threshold is None:
+            check(lib().hf_rhf_gradient(self._h, _ptr(density), _ptr(energy_weighted_density), gp, C.byref(ms),
+                                        _stream(stream)), "hf_rhf_gradient")
+        else:
+            check(lib().hf_rhf_gradient_mixed(self._h, _ptr(density), _ptr(energy_weighted_density),
+                                              float(mixed_threshold), gp, C.byref(ms), _stream(stream)),
+                  "hf_rhf_gradient_mixed")
         return g.reshape(-1, 3), ms.value
+
+    def uhf_scf(self, num_alpha: int, num_beta: int, options: dict | None = None, want_matrices: bool = False):
+        """Unrestricted HF (hf_uhf_scf)."""
+        opt = ScfOptions()
+        lib().hf_scf_options_default(C.byref(opt))
+        for k, v in (options or {}).items():
+            setattr(opt, k, v)
+        res = ScfResult()
+        outs = [self._empty(self.N, self.N), self._empty(self.N, self.N), self._empty(self.N),
+                self._empty(self.N)] if want_matrices else [None] * 4
+        st = lib().hf_uhf_scf(self._h, int(num_alpha), int(num_beta), C.byref(opt), C.byref(res),
+                              *[_ptr(t) for t in outs])
+        out = {f: getattr(res, f) for f, _ in ScfResult._fields_}
+        out["status"] = st
+        if st not in (0, 4):
+            check(st, "hf_uhf_scf")
+        if want_matrices:
+            out["density_alpha"], out["density_beta"], out["orbital_energies_alpha"], out["orbital_energies_beta"] = outs
+        return out
 
     # ------------------------------------------------------------ RI
     def set_auxiliary_basis(self, aux: "Molecular"):

@@ -115,6 +115,7 @@ SIGNATURES = {
     "hf_compute_fock_diis_noalloc": (_I, [_P, _P, _P, _I, _I, _P]),
     "hf_energy_weighted_density": (_I, [_P, _P, _P, _I, _P, _P]),
     "hf_rhf_gradient": (_I, [_P, _P, _P, C.POINTER(_D), C.POINTER(_D), _P]),
+    "hf_rhf_gradient_mixed": (_I, [_P, _P, _P, _D, C.POINTER(_D), C.POINTER(_D), _P]),
     "hf_engine_set_auxiliary_basis": (_I, [_P, _P, _I, _P, _I]),
     "hf_compute_two_center_eris": (_I, [_P, _P, _P]),
     "hf_compute_three_center_eris": (_I, [_P, _P, _P]),
@@ -123,6 +124,7 @@ SIGNATURES = {
     "hf_compute_jk_ri": (_I, [_P, _P, _P, _P, _P]),
     "hf_split_bf16_matmul": (_I, [_P, _P, _P, _I, _I, _I, _I, _P]),
     "hf_engine_create_batch": (_I, [_I, _P, _P, _P, _P, _P, _P, _D, _P]),
+    "hf_uhf_scf": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
     "hf_batch_rhf_scf": (_I, [_P, _P, _P, _P, _P, _P]),
     "hf_scf_options_default": (None, [C.POINTER(ScfOptions)]),
     "hf_rhf_scf": (_I, [_P, _I, C.POINTER(ScfOptions), C.POINTER(ScfResult), _P, _P, _P, _P]),

@@ -177,13 +177,16 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
              cudaStream_t s, bool accumulate_counters = true);
 int finish_fock(Engine& e, const double* d_H, const double* d_J, const double* d_K, double* d_F, cudaStream_t s);
 int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s);
+// device split of the static quartet lists into FP64 prefix / FP32 rest (e.plan)
+int mixed_plan(Engine& e, const double* d_D, double factor, bool square, double tau, double skip, cudaStream_t s);
 
 // one_electron.cu
 int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s);
 
 // grad.cu
 int energy_weighted_density(Engine& e, const double* d_C, const double* d_eps, int nocc, double* d_W, cudaStream_t s);
-int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad, cudaStream_t s, float* ms_out);
+int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad, cudaStream_t s, float* ms_out,
+                 int precision = 0, double mixed_threshold = 0.0);
 
 // host MD helpers (engine.cu)
 void host_boys_table(std::vector<double>& table);

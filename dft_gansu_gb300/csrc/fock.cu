@@ -140,6 +140,7 @@ struct PlanArgs {
     double factor;              // c_max^4
     double mixed_threshold;
     double skip_threshold;      // quartets with Qs_ab*Qs_cd*c_max^4*max|D| below this are dropped
+    int square;                 // weight by max|D|^2 (gradient) instead of max|D| (Fock)
     long long* off64;
     long long* off32;
     int* lo32;
@@ -151,7 +152,8 @@ __global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
     __shared__ long long smem[32];
     const int cp = blockIdx.x;
     const int eb = a.cp_entry_begin[cp], ne = a.cp_nentry[cp], kb = a.cp_ket_base[cp], ob = a.cp_off_base[cp];
-    const double dm = *a.dmax * a.factor;
+    const double dmv = *a.dmax;
+    const double dm = (a.square ? dmv * dmv : dmv) * a.factor;
     long long base64 = 0, base32 = 0;
     if (threadIdx.x == 0) { a.off64[ob] = 0; a.off32[ob] = 0; }
     for (int start = 0; start < ne; start += blockDim.x) {
@@ -259,6 +261,43 @@ int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s)
     return HF_OK;
 }
 
+// Splits every class pair's static quartet list into an FP64 prefix and an FP32
+// remainder on the device: FP64 where Qs_bra*Qs_ket*factor*max|D| >= tau
+// (max|D|^2 with square), dropped below skip.  max|D| from an absmax of d_D.
+static int mixed_plan_args(Engine& e, const double* d_D, double factor, bool square, double tau, double skip,
+                           cudaStream_t s, PlanArgs* out)
+{
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    absmax_kernel<<<1, 1024, 0, s>>>(d_D, e.nelem, e.d_scalar);
+    GB_LAUNCH_CHECK();
+    PlanArgs a;
+    a.entry_bra = e.d_entry_bra;
+    a.entry_cnt = e.d_entry_cnt;
+    a.entry_lo0 = e.d_entry_lo0;
+    a.pair_qs = e.d_pair_qs;
+    a.cp_entry_begin = e.d_cp_meta;
+    a.cp_nentry = e.d_cp_meta + ncp;
+    a.cp_ket_base = e.d_cp_meta + 2 * ncp;
+    a.cp_off_base = e.d_cp_meta + 3 * ncp;
+    a.dmax = e.d_scalar;
+    a.factor = factor;
+    a.mixed_threshold = tau;
+    a.skip_threshold = skip;
+    a.square = square ? 1 : 0;
+    a.off64 = e.plan.off64;
+    a.off32 = e.plan.off32;
+    a.lo32 = e.plan.lo32;
+    mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
+    GB_LAUNCH_CHECK();
+    if (out) *out = a;
+    return HF_OK;
+}
+
+int mixed_plan(Engine& e, const double* d_D, double factor, bool square, double tau, double skip, cudaStream_t s)
+{
+    return mixed_plan_args(e, d_D, factor, square, tau, skip, s, nullptr);
+}
+
 int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
              cudaStream_t s, bool /*accumulate_counters*/)
 {
@@ -286,27 +325,10 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
             GB_LAUNCH_CHECK();
         }
     } else {
-        absmax_kernel<<<1, 1024, 0, s>>>(d_D, static_cast<long long>(nn), e.d_scalar);
-        GB_LAUNCH_CHECK();
-        PlanArgs a;
-        a.entry_bra = e.d_entry_bra;
-        a.entry_cnt = e.d_entry_cnt;
-        a.entry_lo0 = e.d_entry_lo0;
-        a.pair_qs = e.d_pair_qs;
-        a.cp_entry_begin = e.d_cp_meta;
-        a.cp_nentry = e.d_cp_meta + ncp;
-        a.cp_ket_base = e.d_cp_meta + 2 * ncp;
-        a.cp_off_base = e.d_cp_meta + 3 * ncp;
-        a.dmax = e.d_scalar;
         const double c2 = e.cgto_max * e.cgto_max;
-        a.factor = c2 * c2;
-        a.mixed_threshold = mixed_thr;
-        a.skip_threshold = std::min(e.schwarz_threshold, mixed_thr);
-        a.off64 = e.plan.off64;
-        a.off32 = e.plan.off32;
-        a.lo32 = e.plan.lo32;
-        mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
-        GB_LAUNCH_CHECK();
+        PlanArgs a;
+        int pst = mixed_plan_args(e, d_D, c2 * c2, false, mixed_thr, std::min(e.schwarz_threshold, mixed_thr), s, &a);
+        if (pst) return pst;
         // per-shell-block maxima of the (difference) density for the per-quartet screen
         // (single-molecule engines: the table is num_shells^2)
         if (e.nmol == 1 && !e.d_block_dmax) {

@@ -40,20 +40,21 @@ __device__ __forceinline__ int gidx(int t, int u, int v)
     return k * (k + 1) * (k + 2) / 6 + m * (m + 1) / 2 + v;
 }
 
-__device__ __forceinline__ void grad_e_table(int l1, int l2, double xpa, double xpb, double oo2p, double* e)
+template <class T>
+__device__ __forceinline__ void grad_e_table(int l1, int l2, T xpa, T xpb, T oo2p, T* e)
 {
-    e[0] = 1.0;
+    e[0] = T(1);
     for (int i = 0; i <= l1; ++i)
         for (int j = 0; j <= l2; ++j) {
             if (i == 0 && j == 0) continue;
             for (int t = 0; t <= i + j; ++t) {
-                double v;
+                T v;
                 if (i > 0) {
-                    v = (t <= i - 1 + j) ? xpa * e[((i - 1) * kGI + j) * kGT + t] : 0.0;
+                    v = (t <= i - 1 + j) ? xpa * e[((i - 1) * kGI + j) * kGT + t] : T(0);
                     if (t > 0) v += oo2p * e[((i - 1) * kGI + j) * kGT + t - 1];
                     if (t + 1 <= i - 1 + j) v += (t + 1) * e[((i - 1) * kGI + j) * kGT + t + 1];
                 } else {
-                    v = (t <= j - 1) ? xpb * e[(j - 1) * kGT + t] : 0.0;
+                    v = (t <= j - 1) ? xpb * e[(j - 1) * kGT + t] : T(0);
                     if (t > 0) v += oo2p * e[(j - 1) * kGT + t - 1];
                     if (t + 1 <= j - 1) v += (t + 1) * e[(j - 1) * kGT + t + 1];
                 }
@@ -62,12 +63,13 @@ __device__ __forceinline__ void grad_e_table(int l1, int l2, double xpa, double 
         }
 }
 
-__device__ __forceinline__ void grad_boys(int n, double x, const double* table, double* F)
+template <class T>
+__device__ __forceinline__ void grad_boys(int n, T x, const T* table, T* F)
 {
 #define GB_B(N)                              \
     case N: {                                \
-        double f[N + 1];                     \
-        boys_fp64<N>(x, table, f);           \
+        T f[N + 1];                          \
+        BoysEval<T>::template run<N>(x, table, f); \
         for (int i = 0; i <= N; ++i) F[i] = f[i]; \
         break;                               \
     }
@@ -78,7 +80,8 @@ __device__ __forceinline__ void grad_boys(int n, double x, const double* table, 
 #undef GB_B
 }
 
-__device__ __forceinline__ void grad_r_table(int L, const double* Fs, double X, double Y, double Z, double* r)
+template <class T>
+__device__ __forceinline__ void grad_r_table(int L, const T* Fs, T X, T Y, T Z, T* r)
 {
     r[0] = Fs[L];
     for (int n = L - 1; n >= 0; --n) {
@@ -86,7 +89,7 @@ __device__ __forceinline__ void grad_r_table(int L, const double* Fs, double X, 
             for (int t = k; t >= 0; --t)
                 for (int u = k - t; u >= 0; --u) {
                     const int v = k - t - u;
-                    double val;
+                    T val;
                     if (t > 0) {
                         val = X * r[gidx(t - 1, u, v)];
                         if (t > 1) val += (t - 1) * r[gidx(t - 2, u, v)];
@@ -105,21 +108,22 @@ __device__ __forceinline__ void grad_r_table(int L, const double* Fs, double X, 
 
 // ket contraction of one ket component (c + sh along axis ax, d) into the bra
 // Hermite index up to order lmax: x[tuv] = sum (-1)^{tau+nu+phi} E^{cd} R
-__device__ __forceinline__ void ket_contract(int lmax, const int c[3], const int d[3], const double* fx,
-                                             const double* fy, const double* fz, const double* r, double* x)
+template <class T>
+__device__ __forceinline__ void ket_contract(int lmax, const int c[3], const int d[3], const T* fx, const T* fy,
+                                             const T* fz, const T* r, T* x)
 {
-    const double* ex = fx + (c[0] * kGI + d[0]) * kGT;
-    const double* ey = fy + (c[1] * kGI + d[1]) * kGT;
-    const double* ez = fz + (c[2] * kGI + d[2]) * kGT;
+    const T* ex = fx + (c[0] * kGI + d[0]) * kGT;
+    const T* ey = fy + (c[1] * kGI + d[1]) * kGT;
+    const T* ez = fz + (c[2] * kGI + d[2]) * kGT;
     for (int t = 0; t <= lmax; ++t)
         for (int u = 0; u + t <= lmax; ++u)
             for (int v = 0; v + u + t <= lmax; ++v) {
-                double s = 0.0;
+                T s = T(0);
                 for (int tau = 0; tau <= c[0] + d[0]; ++tau)
                     for (int nu = 0; nu <= c[1] + d[1]; ++nu) {
-                        const double exy = ex[tau] * ey[nu];
+                        const T exy = ex[tau] * ey[nu];
                         for (int phi = 0; phi <= c[2] + d[2]; ++phi) {
-                            const double w = exy * ez[phi] * r[gidx(t + tau, u + nu, v + phi)];
+                            const T w = exy * ez[phi] * r[gidx(t + tau, u + nu, v + phi)];
                             s += ((tau + nu + phi) & 1) ? -w : w;
                         }
                     }
@@ -133,6 +137,7 @@ struct GradLaunch {
     double* grad;            // 3 * natom accumulators
 };
 
+template <class T>
 __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch G, int ncd)
 {
     const FockClassLaunch& L = G.L;
@@ -140,14 +145,15 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((total + 31) >> 5) * ncd;
     const long long warp_stride = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
-    const double* __restrict__ Dp = static_cast<const double*>(L.density);
-    const PrimPair64* __restrict__ pp = static_cast<const PrimPair64*>(L.prim_pairs);
-    const double* __restrict__ boys = static_cast<const double*>(L.boys_table);
+    using PP = typename FockTypes<T>::PP;
+    const T* __restrict__ Dp = static_cast<const T*>(L.density);
+    const PP* __restrict__ pp = static_cast<const PP*>(L.prim_pairs);
+    const T* __restrict__ boys = static_cast<const T*>(L.boys_table);
     const int N = L.num_basis;
-    const double thr = L.schwarz_threshold;
-    double ex[kGE], ey[kGE], ez[kGE], fx[kGE], fy[kGE], fz[kGE];
-    double Fs[kGL + 1], r[kGR], x0[kGX], xp[3][kGX], xm[3][kGX];
-    double wcol[kGNAB];
+    const T thr = static_cast<T>(L.schwarz_threshold);
+    T ex[kGE], ey[kGE], ez[kGE], fx[kGE], fy[kGE], fz[kGE];
+    T Fs[kGL + 1], r[kGR], x0[kGX], xp[3][kGX], xm[3][kGX];
+    T wcol[kGNAB];
 
     for (long long wid = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; wid < nwarps;
          wid += warp_stride) {
@@ -166,20 +172,28 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
         const int c[3] = {cart_exp(lc, ic, 0), cart_exp(lc, ic, 1), cart_exp(lc, ic, 2)};
         const int d[3] = {cart_exp(ld, id, 0), cart_exp(ld, id, 1), cart_exp(ld, id, 2)};
         const int cf = kp.bfA + ic, df = kp.bfB + id;
-        double fsym = 1.0;
-        if (bp.A == bp.B) fsym *= 0.5;
-        if (kp.A == kp.B) fsym *= 0.5;
-        if (bra == ket) fsym *= 0.5;
+        T fsym = T(1);
+        if (bp.A == bp.B) fsym *= T(0.5);
+        if (kp.A == kp.B) fsym *= T(0.5);
+        if (bra == ket) fsym *= T(0.5);
+        // bra/ket geometry in the tier's type
+        const T bABx = sizeof(T) == 4 ? static_cast<T>(bp.fABx) : static_cast<T>(bp.ABx);
+        const T bABy = sizeof(T) == 4 ? static_cast<T>(bp.fABy) : static_cast<T>(bp.ABy);
+        const T bABz = sizeof(T) == 4 ? static_cast<T>(bp.fABz) : static_cast<T>(bp.ABz);
+        const T kABx = sizeof(T) == 4 ? static_cast<T>(kp.fABx) : static_cast<T>(kp.ABx);
+        const T kABy = sizeof(T) == 4 ? static_cast<T>(kp.fABy) : static_cast<T>(kp.ABy);
+        const T kABz = sizeof(T) == 4 ? static_cast<T>(kp.fABz) : static_cast<T>(kp.ABz);
+        const T kQmax = sizeof(T) == 4 ? static_cast<T>(kp.fQmax) : static_cast<T>(kp.Qmax);
         // density weights of this (c,d) column: f (4 D_ab D_cd - D_ac D_bd - D_ad D_bc)
-        const double dcd = Dp[cf * N + df];
+        const T dcd = Dp[cf * N + df];
         bool any = false;
         for (int ia = 0; ia < na; ++ia)
             for (int ib = 0; ib < nb; ++ib) {
                 const int a = bp.bfA + ia, b = bp.bfB + ib;
-                const double v = fsym * (4.0 * Dp[a * N + b] * dcd - Dp[a * N + cf] * Dp[b * N + df] -
-                                         Dp[a * N + df] * Dp[b * N + cf]);
+                const T v = fsym * (T(4) * Dp[a * N + b] * dcd - Dp[a * N + cf] * Dp[b * N + df] -
+                                    Dp[a * N + df] * Dp[b * N + cf]);
                 wcol[ia * nb + ib] = v;
-                any |= (v != 0.0);
+                any |= (v != T(0));
             }
         if (!any) continue;
         // Bra side in Hermite space: per bra primitive pair, the weighted Hermite densities
@@ -189,35 +203,35 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
         // not grow with the number of bra components.  Then
         //   dA_k = sum HA_k x0,  dP_k = sum H0 x0[tuv + 1_k] (= dA_k + dB_k),
         //   dC_k = sum H0 (2 gamma x[c + 1_k] - c_k x[c - 1_k]).
-        double gA[3] = {0, 0, 0}, gP[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
-        double H0[kGX], HA[3][kGX];
+        T gA[3] = {0, 0, 0}, gP[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+        T H0[kGX], HA[3][kGX];
         for (int ip = 0; ip < bp.pp_n; ++ip) {
-            const PrimPair64 pb = pp[bp.pp_off + ip];
-            if (pb.Q * kp.Qmax < thr) continue;
-            const double alpha2 = 2.0 * (pb.p - pb.b);
-            const double oo2p = 0.5 * pb.invp;
-            grad_e_table(la + 1, lb, pb.PAx, pb.PAx + bp.ABx, oo2p, ex);
-            grad_e_table(la + 1, lb, pb.PAy, pb.PAy + bp.ABy, oo2p, ey);
-            grad_e_table(la + 1, lb, pb.PAz, pb.PAz + bp.ABz, oo2p, ez);
+            const PP pb = pp[bp.pp_off + ip];
+            if (pb.Q * kQmax < thr) continue;
+            const T alpha2 = T(2) * (pb.p - pb.b);
+            const T oo2p = T(0.5) * pb.invp;
+            grad_e_table<T>(la + 1, lb, pb.PAx, pb.PAx + bABx, oo2p, ex);
+            grad_e_table<T>(la + 1, lb, pb.PAy, pb.PAy + bABy, oo2p, ey);
+            grad_e_table<T>(la + 1, lb, pb.PAz, pb.PAz + bABz, oo2p, ez);
             const int nh = nherm(lab + 1);
-            for (int h = 0; h < nh; ++h) { H0[h] = 0.0; HA[0][h] = 0.0; HA[1][h] = 0.0; HA[2][h] = 0.0; }
+            for (int h = 0; h < nh; ++h) { H0[h] = T(0); HA[0][h] = T(0); HA[1][h] = T(0); HA[2][h] = T(0); }
             for (int ia = 0; ia < na; ++ia)
                 for (int ib = 0; ib < nb; ++ib) {
-                    const double wv = wcol[ia * nb + ib];
-                    if (wv == 0.0) continue;
+                    const T wv = wcol[ia * nb + ib];
+                    if (wv == T(0)) continue;
                     const int a[3] = {cart_exp(la, ia, 0), cart_exp(la, ia, 1), cart_exp(la, ia, 2)};
                     const int b[3] = {cart_exp(lb, ib, 0), cart_exp(lb, ib, 1), cart_exp(lb, ib, 2)};
                     // per-axis factors: e0 = E^{a b}, e1 = 2 alpha E^{a+1, b} - a E^{a-1, b}
-                    double e0[3][kGT], e1[3][kGT];
-                    const double* tab[3] = {ex, ey, ez};
+                    T e0[3][kGT], e1[3][kGT];
+                    const T* tab[3] = {ex, ey, ez};
                     for (int k = 0; k < 3; ++k) {
-                        const double* row0 = tab[k] + (a[k] * kGI + b[k]) * kGT;
-                        const double* rowp = tab[k] + ((a[k] + 1) * kGI + b[k]) * kGT;
-                        const double* rowm = tab[k] + ((a[k] > 0 ? a[k] - 1 : 0) * kGI + b[k]) * kGT;
+                        const T* row0 = tab[k] + (a[k] * kGI + b[k]) * kGT;
+                        const T* rowp = tab[k] + ((a[k] + 1) * kGI + b[k]) * kGT;
+                        const T* rowm = tab[k] + ((a[k] > 0 ? a[k] - 1 : 0) * kGI + b[k]) * kGT;
                         for (int t = 0; t <= a[k] + b[k] + 1; ++t) {
-                            e0[k][t] = (t <= a[k] + b[k]) ? row0[t] : 0.0;
-                            double v = alpha2 * rowp[t];
-                            if (a[k] > 0 && t <= a[k] + b[k] - 1) v -= a[k] * rowm[t];
+                            e0[k][t] = (t <= a[k] + b[k]) ? row0[t] : T(0);
+                            T v = alpha2 * rowp[t];
+                            if (a[k] > 0 && t <= a[k] + b[k] - 1) v -= T(a[k]) * rowm[t];
                             e1[k][t] = v;
                         }
                     }
@@ -233,60 +247,60 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
                             }
                 }
             for (int jq = 0; jq < kp.pp_n; ++jq) {
-                const PrimPair64 pk = pp[kp.pp_off + jq];
+                const PP pk = pp[kp.pp_off + jq];
                 if (pb.Q * pk.Q < thr) continue;
-                const double gamma2 = 2.0 * (pk.p - pk.b);
-                const double oo2q = 0.5 * pk.invp;
-                grad_e_table(lc + 1, ld, pk.PAx, pk.PAx + kp.ABx, oo2q, fx);
-                grad_e_table(lc + 1, ld, pk.PAy, pk.PAy + kp.ABy, oo2q, fy);
-                grad_e_table(lc + 1, ld, pk.PAz, pk.PAz + kp.ABz, oo2q, fz);
-                const double rr = rsqrt(pb.p + pk.p);
-                const double rho = pb.p * pk.p * rr * rr;
-                const double X = pb.Px - pk.Px, Y = pb.Py - pk.Py, Z = pb.Pz - pk.Pz;
-                grad_boys(lt, rho * (X * X + Y * Y + Z * Z), boys, Fs);
-                double scale = pb.KoP * pk.KoP * rr;
-                for (int n = 0; n <= lt; ++n) { Fs[n] *= scale; scale *= -2.0 * rho; }
-                grad_r_table(lt, Fs, X, Y, Z, r);
-                ket_contract(lab + 1, c, d, fx, fy, fz, r, x0);
+                const T gamma2 = T(2) * (pk.p - pk.b);
+                const T oo2q = T(0.5) * pk.invp;
+                grad_e_table<T>(lc + 1, ld, pk.PAx, pk.PAx + kABx, oo2q, fx);
+                grad_e_table<T>(lc + 1, ld, pk.PAy, pk.PAy + kABy, oo2q, fy);
+                grad_e_table<T>(lc + 1, ld, pk.PAz, pk.PAz + kABz, oo2q, fz);
+                const T rr = rsqrt(pb.p + pk.p);
+                const T rho = pb.p * pk.p * rr * rr;
+                const T X = pb.Px - pk.Px, Y = pb.Py - pk.Py, Z = pb.Pz - pk.Pz;
+                grad_boys<T>(lt, rho * (X * X + Y * Y + Z * Z), boys, Fs);
+                T scale = pb.KoP * pk.KoP * rr;
+                for (int n = 0; n <= lt; ++n) { Fs[n] *= scale; scale *= T(-2) * rho; }
+                grad_r_table<T>(lt, Fs, X, Y, Z, r);
+                ket_contract<T>(lab + 1, c, d, fx, fy, fz, r, x0);
                 for (int k = 0; k < 3; ++k) {
                     int cp[3] = {c[0], c[1], c[2]};
                     cp[k] += 1;
-                    ket_contract(lab, cp, d, fx, fy, fz, r, xp[k]);
+                    ket_contract<T>(lab, cp, d, fx, fy, fz, r, xp[k]);
                     if (c[k] > 0) {
                         cp[k] -= 2;
-                        ket_contract(lab, cp, d, fx, fy, fz, r, xm[k]);
+                        ket_contract<T>(lab, cp, d, fx, fy, fz, r, xm[k]);
                     }
                 }
                 for (int t = 0; t <= lab + 1; ++t)
                     for (int u = 0; u + t <= lab + 1; ++u)
                         for (int v = 0; v + u + t <= lab + 1; ++v) {
                             const int h = gidx(t, u, v);
-                            const double x = x0[h];
+                            const T x = x0[h];
                             gA[0] += HA[0][h] * x;
                             gA[1] += HA[1][h] * x;
                             gA[2] += HA[2][h] * x;
                             if (t + u + v > lab) continue;
-                            const double h0 = H0[h];
+                            const T h0 = H0[h];
                             gP[0] += h0 * x0[gidx(t + 1, u, v)];
                             gP[1] += h0 * x0[gidx(t, u + 1, v)];
                             gP[2] += h0 * x0[gidx(t, u, v + 1)];
                             for (int k = 0; k < 3; ++k) {
-                                double dc = gamma2 * xp[k][h];
-                                if (c[k] > 0) dc -= c[k] * xm[k][h];
+                                T dc = gamma2 * xp[k][h];
+                                if (c[k] > 0) dc -= T(c[k]) * xm[k][h];
                                 gC[k] += h0 * dc;
                             }
                         }
             }
         }
-        double gB[3];
+        T gB[3];
         for (int k = 0; k < 3; ++k) gB[k] = gP[k] - gA[k];
         const int atA = G.shell_atom[bp.A], atB = G.shell_atom[bp.B], atC = G.shell_atom[kp.A],
                   atD = G.shell_atom[kp.B];
         for (int k = 0; k < 3; ++k) {
-            atomicAdd(&G.grad[3 * atA + k], gA[k]);
-            atomicAdd(&G.grad[3 * atB + k], gB[k]);
-            atomicAdd(&G.grad[3 * atC + k], gC[k]);
-            atomicAdd(&G.grad[3 * atD + k], -(gA[k] + gB[k] + gC[k]));
+            atomicAdd(&G.grad[3 * atA + k], static_cast<double>(gA[k]));
+            atomicAdd(&G.grad[3 * atB + k], static_cast<double>(gB[k]));
+            atomicAdd(&G.grad[3 * atC + k], static_cast<double>(gC[k]));
+            atomicAdd(&G.grad[3 * atD + k], -static_cast<double>(gA[k] + gB[k] + gC[k]));
         }
     }
 }
@@ -438,7 +452,8 @@ int energy_weighted_density(Engine& e, const double* d_C, const double* d_eps, i
     return HF_OK;
 }
 
-int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad, cudaStream_t s, float* ms_out)
+int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad, cudaStream_t s, float* ms_out,
+                 int precision, double mixed_threshold)
 {
     const int natom = e.num_atoms;
     if (!e.d_grad) {
@@ -449,46 +464,61 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
         for (int i = 0; i < e.num_shells; ++i) sa[i] = e.shells[i].atom;
         GB_CUDA_TRY(cudaMemcpy(e.d_shell_atom, sa.data(), sizeof(int) * e.num_shells, cudaMemcpyHostToDevice));
     }
+    const bool mixed = precision == HF_PRECISION_MIXED;
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
     cudaEventRecord(t0, s);
     GB_CUDA_TRY(cudaMemsetAsync(e.d_grad, 0, sizeof(double) * 3 * natom, s));
-    int st = scale_density(e, d_D, false, s);
+    int st = scale_density(e, d_D, mixed, s);
     if (st) return st;
-    // two-electron part over the FP64 quartet lists of every class
+    if (mixed) {
+        // FP64 for the quartets with Qs_ab Qs_cd c_max^4 max|D|^2 >= mixed_threshold, FP32 for the rest
+        const double c2 = e.cgto_max * e.cgto_max;
+        if ((st = mixed_plan(e, d_D, c2 * c2, true, mixed_threshold, 0.0, s))) return st;
+    }
+    // two-electron part over the quartet lists of every class
     for (int c = 0; c < static_cast<int>(e.class_pairs.size()); ++c) {
         const ClassPair& cp = e.class_pairs[c];
         if (cp.n_survivors == 0) continue;
         const PairClass& Y = e.pair_classes[cp.Y];
-        GradLaunch G;
-        G.L.pairs = e.d_pairs;
-        G.L.prim_pairs = e.d_pp64;
-        G.L.boys_table = e.d_boys64;
-        G.L.density = e.d_Dp64;
-        G.L.J = nullptr;
-        G.L.K = nullptr;
-        G.L.J32 = nullptr;
-        G.L.K32 = nullptr;
-        G.L.off = e.d_off_static + cp.entry_begin + c;
-        G.L.entry_bra = e.d_entry_bra + cp.entry_begin;
-        G.L.entry_lo = e.d_entry_lo0 + cp.entry_begin;
-        G.L.nentry = cp.nentry;
-        G.L.ket_base = Y.begin;
-        G.L.num_basis = e.num_basis;
-        G.L.schwarz_threshold = e.schwarz_threshold;
-        G.L.counters = e.d_counters;
-        G.L.block_dmax = nullptr;
-        G.L.nshell = e.num_shells;
-        G.L.skip_cut = 0.0;
-        G.shell_atom = e.d_shell_atom;
-        G.grad = e.d_grad;
-        const int ncd = ncart(Y.la) * ncart(Y.lb);
-        const long long warps = ((cp.n_survivors + 31) / 32) * ncd;
-        const int grid = static_cast<int>(std::max<long long>(
-            1, std::min<long long>((warps * 32 + kGradThreads - 1) / kGradThreads, static_cast<long long>(e.num_sms) * 32)));
-        grad_eri_kernel<<<grid, kGradThreads, 0, s>>>(G, ncd);
-        GB_LAUNCH_CHECK();
+        for (int tier = 0; tier < (mixed ? 2 : 1); ++tier) {
+            const bool f32 = tier == 1;
+            GradLaunch G;
+            G.L.pairs = e.d_pairs;
+            G.L.prim_pairs = f32 ? static_cast<const void*>(e.d_pp32) : static_cast<const void*>(e.d_pp64);
+            G.L.boys_table = f32 ? static_cast<const void*>(e.d_boys32) : static_cast<const void*>(e.d_boys64);
+            G.L.density = f32 ? static_cast<const void*>(e.d_Dp32) : static_cast<const void*>(e.d_Dp64);
+            G.L.J = nullptr;
+            G.L.K = nullptr;
+            G.L.J32 = nullptr;
+            G.L.K32 = nullptr;
+            const long long* off = !mixed ? e.d_off_static : (f32 ? e.plan.off32 : e.plan.off64);
+            const int* lo = f32 ? e.plan.lo32 : e.d_entry_lo0;
+            G.L.off = off + cp.entry_begin + c;
+            G.L.entry_bra = e.d_entry_bra + cp.entry_begin;
+            G.L.entry_lo = lo + cp.entry_begin;
+            G.L.nentry = cp.nentry;
+            G.L.ket_base = Y.begin;
+            G.L.num_basis = e.num_basis;
+            G.L.schwarz_threshold = e.schwarz_threshold;
+            G.L.counters = e.d_counters;
+            G.L.block_dmax = nullptr;
+            G.L.nshell = e.num_shells;
+            G.L.skip_cut = 0.0;
+            G.shell_atom = e.d_shell_atom;
+            G.grad = e.d_grad;
+            const int ncd = ncart(Y.la) * ncart(Y.lb);
+            const long long warps = ((cp.n_survivors + 31) / 32) * ncd;
+            const int grid = static_cast<int>(std::max<long long>(
+                1, std::min<long long>((warps * 32 + kGradThreads - 1) / kGradThreads,
+                                       static_cast<long long>(e.num_sms) * 32)));
+            if (f32)
+                grad_eri_kernel<float><<<grid, kGradThreads, 0, s>>>(G, ncd);
+            else
+                grad_eri_kernel<double><<<grid, kGradThreads, 0, s>>>(G, ncd);
+            GB_LAUNCH_CHECK();
+        }
     }
     // one-electron part
     const double kfold = std::sqrt(2.0 * std::pow(kPi, 2.5));
@@ -554,6 +584,21 @@ int hf_rhf_gradient(hf_engine* eng, const double* d_density, const double* d_ene
     float ms = 0.f;
     const int st = rhf_gradient(*reinterpret_cast<Engine*>(eng), d_density, d_energy_weighted_density, h_gradient,
                                 static_cast<cudaStream_t>(stream), &ms);
+    if (gradient_ms) *gradient_ms = ms;
+    return st;
+}
+
+int hf_rhf_gradient_mixed(hf_engine* eng, const double* d_density, const double* d_energy_weighted_density,
+                          double mixed_threshold, double* h_gradient, double* gradient_ms, void* stream)
+{
+    clear_error();
+    if (!eng || !d_density || !d_energy_weighted_density || !h_gradient || !(mixed_threshold >= 0.0))
+        return set_error("null argument or negative threshold"), HF_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<Engine*>(eng)->nmol != 1)
+        return set_error("hf_rhf_gradient_mixed: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
+    float ms = 0.f;
+    const int st = rhf_gradient(*reinterpret_cast<Engine*>(eng), d_density, d_energy_weighted_density, h_gradient,
+                                static_cast<cudaStream_t>(stream), &ms, HF_PRECISION_MIXED, mixed_threshold);
     if (gradient_ms) *gradient_ms = ms;
     return st;
 }

@@ -178,6 +178,53 @@ __global__ void diis_combine_kernel(const double* __restrict__ Fs, const double*
     }
 }
 
+// D = factor sum_{o < nocc} C_o C_o^T (UHF spin densities use factor 1)
+__global__ void density_factor_kernel(const double* __restrict__ C, int n, int nocc, double factor,
+                                      double* __restrict__ D)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long i = k / n, j = k % n;
+        double s = 0.0;
+        for (int o = 0; o < nocc; ++o) s += C[i * n + o] * C[j * n + o];
+        D[k] = factor * s;
+    }
+}
+
+// UHF energy 1/2 sum [(Da + Db) H + Da Fa + Db Fb]
+__global__ void uhf_energy_kernel(const double* __restrict__ Da, const double* __restrict__ Db,
+                                  const double* __restrict__ H, const double* __restrict__ Fa,
+                                  const double* __restrict__ Fb, long long nn, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x)
+        s += (Da[k] + Db[k]) * H[k] + Da[k] * Fa[k] + Db[k] * Fb[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) *out = 0.5 * s;
+    }
+}
+
+// Fa = H + Ja + Jb - Ka, Fb = H + Ja + Jb - Kb
+__global__ void uhf_fock_kernel(const double* __restrict__ H, const double* __restrict__ Ja,
+                                const double* __restrict__ Jb, const double* __restrict__ Ka,
+                                const double* __restrict__ Kb, long long nn, double* __restrict__ Fa,
+                                double* __restrict__ Fb)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double h = H[k] + Ja[k] + Jb[k];
+        Fa[k] = h - Ka[k];
+        Fb[k] = h - Kb[k];
+    }
+}
+
 int grid_nn(long long nn) { return static_cast<int>(std::min<long long>((nn + 255) / 256, 8192)); }
 
 template <class T>
@@ -601,6 +648,142 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     }
     if (d_coefficients_out) GB_CUDA_TRY(cudaMemcpy(d_coefficients_out, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     return converged ? HF_OK : (set_error("SCF did not converge"), HF_ERR_NOT_CONVERGED);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options* opt_in, hf_scf_result* res,
+               double* d_density_a_out, double* d_density_b_out, double* d_orbital_energies_a_out,
+               double* d_orbital_energies_b_out)
+{
+    clear_error();
+    if (!eng || !res) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    if (e.nmol != 1) return set_error("hf_uhf_scf: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
+    hf_scf_options opt;
+    if (opt_in) opt = *opt_in; else hf_scf_options_default(&opt);
+    const int n = e.num_basis;
+    if (num_alpha < 0 || num_beta < 0 || num_alpha + num_beta == 0 || num_alpha > n || num_beta > n)
+        return set_error("hf_uhf_scf: bad alpha/beta electron counts"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.diis_size < 1 || opt.diis_size > kMaxDiis)
+        return set_error("diis_size must be in [1, 16]"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.precision != HF_PRECISION_FP64 && opt.precision != HF_PRECISION_MIXED)
+        return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
+    const int m = opt.diis_size;
+    int st = ensure_scf(e, m);
+    if (st) return st;
+    auto& w = e.scf;
+    const long long nn = static_cast<long long>(n) * n;
+    cudaStream_t s = nullptr;
+    cublasSetStream(e.cublas, s);
+    cusolverDnSetStream(e.cusolver, s);
+    // beta-spin buffers and the two J/K pairs (owned by this call)
+    std::vector<void*> owned;
+    auto buf = [&](double*& p, size_t count) -> int {
+        if (cudaMalloc(&p, count * sizeof(double)) != cudaSuccess)
+            return set_error("cudaMalloc (UHF) failed"), HF_ERR_OUT_OF_MEMORY;
+        owned.push_back(p);
+        return HF_OK;
+    };
+    double *Fb = nullptr, *Db = nullptr, *Ja = nullptr, *Ka = nullptr, *Jb = nullptr, *Kb = nullptr, *epsb = nullptr,
+           *Esb = nullptr, *Fsb = nullptr;
+    struct Free {
+        std::vector<void*>& v;
+        ~Free() { for (void* p : v) cudaFree(p); }
+    } guard{owned};
+    if ((st = buf(Fb, nn)) || (st = buf(Db, nn)) || (st = buf(Ja, nn)) || (st = buf(Ka, nn)) || (st = buf(Jb, nn)) ||
+        (st = buf(Kb, nn)) || (st = buf(epsb, n)) || (st = buf(Esb, nn * m)) || (st = buf(Fsb, nn * m)))
+        return st;
+    double* Fa = w.F;
+    double* Da = w.D;
+    *res = hf_scf_result{};
+    res->nuclear_repulsion = nuclear_repulsion(e);
+    GB_CUDA_TRY(cudaMemsetAsync(w.info, 0, 4 * sizeof(int), s));
+    double* h_energy = nullptr;
+    cudaMallocHost(&h_energy, sizeof(double));
+
+    auto densities = [&](const double* FA, const double* FB) -> int {
+        int r;
+        if ((r = coefficients(e, FA, s, opt.eigensolver))) return r;
+        density_factor_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, num_alpha, 1.0, Da);
+        GB_LAUNCH_CHECK();
+        if ((r = coefficients(e, FB, s, opt.eigensolver))) return r;
+        density_factor_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, num_beta, 1.0, Db);
+        GB_LAUNCH_CHECK();
+        GB_CUDA_TRY(cudaMemcpyAsync(epsb, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        return HF_OK;
+    };
+    auto fock = [&]() -> int {
+        int r;
+        if ((r = build_jk(e, Da, Ja, Ka, opt.precision, opt.mixed_threshold, s))) return r;
+        if ((r = build_jk(e, Db, Jb, Kb, opt.precision, opt.mixed_threshold, s))) return r;
+        uhf_fock_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, Ja, Jb, Ka, Kb, nn, Fa, Fb);
+        GB_LAUNCH_CHECK();
+        return HF_OK;
+    };
+    cudaEvent_t l0, l1;
+    cudaEventCreate(&l0);
+    cudaEventCreate(&l1);
+    // core Hamiltonian, X, core guess for both spins
+    if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
+    if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
+    transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
+    GB_LAUNCH_CHECK();
+    if ((st = densities(w.H, w.H))) return st;
+    if ((st = fock())) return st;
+    cudaEventRecord(l0, s);
+    double prev = std::numeric_limits<double>::max(), energy = 0.0;
+    int iter = 0, diis_iter = 0;
+    bool converged = false;
+    while (iter < opt.max_iter) {
+        if ((st = densities(Fa, Fb))) return st;
+        if ((st = fock())) return st;
+        uhf_energy_kernel<<<1, 1024, 0, s>>>(Da, Db, w.H, Fa, Fb, nn, e.d_scalar + 4);
+        GB_LAUNCH_CHECK();
+        GB_CUDA_TRY(cudaMemcpyAsync(h_energy, e.d_scalar + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
+        GB_CUDA_TRY(cudaStreamSynchronize(s));
+        energy = *h_energy;
+        if (!std::isfinite(energy)) return cudaFreeHost(h_energy), set_error("UHF energy is not finite"), HF_ERR_NOT_CONVERGED;
+        if (std::fabs(energy - prev) < opt.convergence_threshold) { converged = true; break; }
+        ++iter;
+        prev = energy;
+        // DIIS per spin on the same cyclic ring index (Convergence_UHF_DIIS, include/uhf.hpp:291-380)
+        const int slot = diis_iter % m;
+        const int nprev = std::min(diis_iter + 1, m);
+        if ((st = diis_error(e, w.S, w.X, Fa, Da, w.Es + slot * nn, opt.diis_include_transform != 0, s))) return st;
+        GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + slot * nn, Fa, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, Fa, s))) return st;
+        if ((st = diis_error(e, w.S, w.X, Fb, Db, Esb + slot * nn, opt.diis_include_transform != 0, s))) return st;
+        GB_CUDA_TRY(cudaMemcpyAsync(Fsb + slot * nn, Fb, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (nprev > 1 && (st = diis_extrapolate(e, Esb, Fsb, nprev, Fb, s))) return st;
+        ++diis_iter;
+    }
+    cudaEventRecord(l1, s);
+    GB_CUDA_TRY(cudaEventSynchronize(l1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, l0, l1);
+    cudaEventDestroy(l0);
+    cudaEventDestroy(l1);
+    cudaFreeHost(h_energy);
+    res->scf_ms_total = ms;
+    res->electronic_energy = energy;
+    res->total_energy = energy + res->nuclear_repulsion;
+    res->iterations = iter;
+    res->converged = converged ? 1 : 0;
+    if (d_density_a_out) GB_CUDA_TRY(cudaMemcpy(d_density_a_out, Da, nn * sizeof(double), cudaMemcpyDeviceToDevice));
+    if (d_density_b_out) GB_CUDA_TRY(cudaMemcpy(d_density_b_out, Db, nn * sizeof(double), cudaMemcpyDeviceToDevice));
+    // orbital energies of the final Fock matrices of both spins
+    if (d_orbital_energies_a_out) {
+        if ((st = coefficients(e, Fa, s, opt.eigensolver))) return st;
+        GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_a_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
+    }
+    if (d_orbital_energies_b_out) {
+        if ((st = coefficients(e, Fb, s, opt.eigensolver))) return st;
+        GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_b_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
+    }
+    return converged ? HF_OK : (set_error("UHF did not converge"), HF_ERR_NOT_CONVERGED);
 }
 
 }  // extern "C"

@@ -266,6 +266,17 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt, hf_
                double* d_density_out, double* d_fock_out, double* d_orbital_energies_out,
                double* d_coefficients_out);
 
+/* Unrestricted HF on the device (UHF::solve, src/uhf.cu; Convergence_UHF_DIIS,
+ * include/uhf.hpp:291-380): spin densities D_s = C_s,occ C_s,occ^T, Fock
+ * F_a = H + J(D_a + D_b) - K(D_a) (and b), energy 1/2 sum[(D_a + D_b) H + D_a F_a
+ * + D_b F_b], core guess for both spins, one DIIS ring per spin on the same
+ * cyclic index, |dE| convergence.  Two direct J/K builds per iteration.
+ * Outputs (may be NULL): spin densities and the orbital energies of the final
+ * Fock matrices. */
+int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options* opt, hf_scf_result* result,
+               double* d_density_a_out, double* d_density_b_out, double* d_orbital_energies_a_out,
+               double* d_orbital_energies_b_out);
+
 /* ---------------------------------------------------------------- batch */
 /* One engine over many independent molecules (no reference counterpart: the
  * reference solves one molecule per HF object).  Molecule m is given as the
@@ -304,6 +315,13 @@ int hf_energy_weighted_density(hf_engine* eng, const double* d_coefficients, con
  * device time. */
 int hf_rhf_gradient(hf_engine* eng, const double* d_density, const double* d_energy_weighted_density,
                     double* h_gradient, double* gradient_ms, void* stream);
+
+/* hf_rhf_gradient with the two-electron part split by bound: derivative
+ * integrals of quartets with Qs_ab Qs_cd c_max^4 max|D|^2 >= mixed_threshold in
+ * FP64, the rest in FP32 (FP32 Hermite tables and contraction, FP64 atomic
+ * accumulation into the gradient).  No reference counterpart. */
+int hf_rhf_gradient_mixed(hf_engine* eng, const double* d_density, const double* d_energy_weighted_density,
+                          double mixed_threshold, double* h_gradient, double* gradient_ms, void* stream);
 
 #ifdef __cplusplus
 }

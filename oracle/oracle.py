@@ -348,6 +348,55 @@ def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_tran
             "orbital_energies": eps, "density": D, "fock": F, "history": history}
 
 
+def uhf(S, H, jk, na, nb, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False):
+    """The reference UHF loop (src/uhf.cu, Convergence_UHF_DIIS include/uhf.hpp:291-380):
+    core guess for both spins, F_s = H + J(Da + Db) - K(D_s), one DIIS ring per spin."""
+    X = transform_matrix(S)
+    _, Cm = coefficients(H, X)
+    Da, Db = Cm[:, :na] @ Cm[:, :na].T, Cm[:, :nb] @ Cm[:, :nb].T
+
+    def fock(Da, Db):
+        Ja, Ka = jk(Da)
+        Jb, Kb = jk(Db)
+        return H + Ja + Jb - Ka, H + Ja + Jb - Kb
+    Fa, Fb = fock(Da, Db)
+    prev, energy, it, diis_it = np.finfo(float).max, 0.0, 0, 0
+    ring = {"a": ([None] * diis_size, [None] * diis_size), "b": ([None] * diis_size, [None] * diis_size)}
+    converged = False
+    while it < maxiter:
+        _, Ca = coefficients(Fa, X)
+        _, Cb = coefficients(Fb, X)
+        Da, Db = Ca[:, :na] @ Ca[:, :na].T, Cb[:, :nb] @ Cb[:, :nb].T
+        Fa, Fb = fock(Da, Db)
+        energy = 0.5 * (np.vdot(Da + Db, H) + np.vdot(Da, Fa) + np.vdot(Db, Fb))
+        if abs(energy - prev) < thr:
+            converged = True
+            break
+        it += 1
+        prev = energy
+        slot = diis_it % diis_size
+        nprev = min(diis_it + 1, diis_size)
+        out = []
+        for key, F, D in (("a", Fa, Da), ("b", Fb, Db)):
+            e = F @ D @ S - S @ D @ F
+            if include_transform:
+                e = X @ e @ X.T
+            errs, focks = ring[key]
+            errs[slot], focks[slot] = e, F.copy()
+            out.append(diis_extrapolate(errs[:nprev], focks[:nprev]) if nprev > 1 else F)
+        Fa, Fb = out
+        diis_it += 1
+    return {"electronic_energy": energy, "total_energy": energy + enuc, "iterations": it, "converged": converged,
+            "density_alpha": Da, "density_beta": Db}
+
+
+def uhf_from_basis(b: Basis, na: int, nb: int, thr_schwarz=1e-12, **kw):
+    S, T, V = one_electron(b)
+    eri = eri_tensor(b, thr_schwarz)
+    jk = lambda D: (np.einsum("ijkl,kl->ij", eri, D), np.einsum("ikjl,kl->ij", eri, D))
+    return uhf(S, T + V, jk, na, nb, nuclear_repulsion(b.atoms), **kw)
+
+
 def rhf_from_basis(b: Basis, thr_schwarz=1e-12, stored=True, **kw):
     S, T, V = one_electron(b)
     H = T + V

@@ -87,3 +87,17 @@ def test_gradient_invariances_decane(built_library, cuda):
     assert np.abs(g.sum(axis=0)).max() < 1e-7
     assert np.abs(np.cross(R, g).sum(axis=0)).max() < 1e-6
     assert np.abs(g).max() > 1e-4  # a jittered geometry is not a stationary point
+
+
+@pytest.mark.parametrize("gbs", ["6-31g_st", "cc-pvdz"])
+def test_mixed_gradient_matches_fp64(built_library, cuda, gbs):
+    # FP32 derivative integrals for the small-bound quartets: within 1e-5 Eh/bohr of FP64
+    atoms = geometry.alkane(4, jitter=0.02, seed=3)
+    mol = gg.Molecular(atoms, gg.basis_path(gbs))
+    eng = gg.Engine(mol, 1e-12)
+    r = eng.rhf_scf(mol.num_electrons, {"convergence_threshold": 1e-10}, want_matrices=True)
+    W = eng.energy_weighted_density(r["coefficients"], r["orbital_energies"], mol.num_electrons // 2)
+    g64, _ = eng.gradient(r["density"], W)
+    g32, _ = eng.gradient(r["density"], W, mixed_threshold=1e-3)
+    assert np.abs(g32 - g64).max() < 1e-5
+    assert np.abs(g32.sum(axis=0)).max() < 1e-6
