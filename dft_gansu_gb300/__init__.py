@@ -21,7 +21,7 @@ ANGSTROM_TO_BOHR = 1.8897259886
 __all__ = [
     "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
     "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "basis_path",
-    "optimize_geometry", "energy_and_gradient_at", "Batch",
+    "optimize_geometry", "energy_and_gradient_at", "Batch", "UHF",
 ]
 
 
@@ -453,8 +453,8 @@ class RHF:
             raise ValueError(f"Invalid ERI method name: {method}")
         if parameters["convergence_method"] != "diis":
             raise ValueError("only the DIIS convergence method is provided by this engine")
-        if parameters["initial_guess"] != "core":
-            raise ValueError("only the core-Hamiltonian initial guess is provided by this engine")
+        if parameters["initial_guess"] not in ("core", "gwh"):
+            raise ValueError("initial guesses provided by this engine: core, gwh")
         self.engine = Engine(molecular, parameters.get("schwarz_screening_threshold", float))
         self.eri_method = HF_ERI_RI if method == "ri" else HF_ERI_DIRECT
         if method == "ri":
@@ -475,6 +475,7 @@ class RHF:
             "incremental": int(p.get("incremental_fock", bool)),
             "verbose": p.get("verbose", int),
             "eri_method": self.eri_method,
+            "initial_guess": 1 if p["initial_guess"] == "gwh" else 0,
         }
         self.result = self.engine.rhf_scf(self.mol.num_electrons, opts, want_matrices=True)
         return self.result["total_energy"]
@@ -494,17 +495,48 @@ class RHF:
                 f"Converged: {bool(r['converged'])}\n")
 
 
+class UHF:
+    """Mirror of gansu::UHF (include/uhf.hpp, src/uhf.cu) with the direct ERI
+    method: ``solve()`` runs hf_uhf_scf for the molecule's alpha/beta counts."""
+
+    def __init__(self, molecular: Molecular, parameters: ParameterManager):
+        self.mol = molecular
+        self.params = parameters
+        if parameters["eri_method"] not in ("stored", "direct"):
+            raise ValueError(f"Invalid ERI method name for UHF: {parameters['eri_method']}")
+        if parameters["convergence_method"] != "diis":
+            raise ValueError("only the DIIS convergence method is provided by this engine")
+        self.engine = Engine(molecular, parameters.get("schwarz_screening_threshold", float))
+        self.result = None
+
+    def solve(self) -> float:
+        p = self.params
+        opts = {
+            "max_iter": p.get("maxiter", int),
+            "convergence_threshold": p.get("convergence_energy_threshold", float),
+            "diis_size": p.get("diis_size", int),
+            "diis_include_transform": int(p.get("diis_include_transform", bool)),
+            "verbose": p.get("verbose", int),
+        }
+        self.result = self.engine.uhf_scf(self.mol.num_alpha_spins, self.mol.num_beta_spins, opts,
+                                          want_matrices=True)
+        return self.result["total_energy"]
+
+    def get_total_energy(self) -> float:
+        return self.result["total_energy"]
+
+
 class HFBuilder:
     """Mirror of gansu::HFBuilder::buildHF (include/builder.hpp:43-106)."""
 
     @staticmethod
-    def buildHF(parameters: ParameterManager) -> RHF:
+    def buildHF(parameters: ParameterManager):
         method = parameters["method"]
-        if method != "rhf":
-            raise ValueError(f"method {method!r}: this engine provides RHF")
+        if method not in ("rhf", "uhf"):
+            raise ValueError(f"method {method!r}: this engine provides RHF and UHF")
         mol = Molecular.from_files(parameters["xyzfilename"], parameters["gbsfilename"],
                                    parameters.get("charge", int), parameters.get("beta_to_alpha", int))
-        return RHF(mol, parameters)
+        return RHF(mol, parameters) if method == "rhf" else UHF(mol, parameters)
 
     @staticmethod
     def buildOtimizer(parameters: ParameterManager) -> float:

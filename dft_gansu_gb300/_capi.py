@@ -24,6 +24,8 @@ HF_PRECISION_FP64 = 0
 HF_PRECISION_MIXED = 1
 HF_ERI_DIRECT = 0
 HF_ERI_RI = 1
+HF_GUESS_CORE = 0
+HF_GUESS_GWH = 1
 
 
 class PrimitiveShell(C.Structure):
@@ -62,6 +64,7 @@ class ScfOptions(C.Structure):
         ("verbose", C.c_int),
         ("eri_method", C.c_int),
         ("anchor_threshold", C.c_double),
+        ("initial_guess", C.c_int),
     ]
 
 

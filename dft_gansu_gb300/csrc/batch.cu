@@ -89,11 +89,12 @@ __global__ void batch_transform_kernel(const double* __restrict__ W, const doubl
 // G = 2 (J' + J'^T) s s - (K' + K'^T) s s / 2, F = H + G, per block
 __global__ void batch_fock_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
                                   const double* __restrict__ s, const double* __restrict__ H, const BlockMap M,
-                                  double* __restrict__ F)
+                                  const unsigned char* __restrict__ active, double* __restrict__ F)
 {
     for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
          k += static_cast<long long>(gridDim.x) * blockDim.x) {
         const int m = block_of(M, k);
+        if (active && !active[m]) continue;  // converged: F stays
         const int n = M.n[m], g0 = M.bf0[m];
         const long long base = M.base[m], r = k - base;
         const int i = static_cast<int>(r / n), j = static_cast<int>(r % n);
@@ -138,12 +139,13 @@ __global__ void batch_antisym_kernel(const double* __restrict__ T, const BlockMa
 // One CTA per molecule: new row/column `slot` of its DIIS B matrix from the stored
 // errors, then (nprev > 1) the bordered solve and F = sum c_i F_i.
 __global__ void batch_diis_kernel(const double* __restrict__ Es, const double* __restrict__ Fs, long long nelem,
-                                  const BlockMap M, int slot, int nprev, double* __restrict__ Bm,
-                                  double* __restrict__ F)
+                                  const BlockMap M, int slot, int nprev, const unsigned char* __restrict__ active,
+                                  double* __restrict__ Bm, double* __restrict__ F)
 {
     __shared__ double red[32];
     __shared__ double coef[kBatchDiis];
     const int m = blockIdx.x;
+    if (active && !active[m]) return;
     const long long base = M.base[m], nn = static_cast<long long>(M.n[m]) * M.n[m];
     double* B = Bm + static_cast<long long>(m) * kBatchDiis * kBatchDiis;
     const double* en = Es + static_cast<long long>(slot) * nelem + base;
@@ -212,6 +214,8 @@ cublasStatus_t gemm_batched(cublasHandle_t h, bool ta, bool tb, int n, int k, do
                                      B, ldb, st, A, lda, st, &beta, C, n, st, count);
 }
 
+constexpr int kSyevStreams = 8;
+
 struct Batch {
     Engine* e;
     BatchState w;
@@ -219,10 +223,26 @@ struct Batch {
     std::vector<long long> ebase;  // eigenvalue offsets per molecule
     long long* d_ebase = nullptr;
     cusolverDnParams_t params = nullptr;
+    // per-molecule divide-and-conquer solves spread over several streams
+    cudaStream_t streams[kSyevStreams] = {};
+    cusolverDnHandle_t handles[kSyevStreams] = {};
+    double* swork[kSyevStreams] = {};
+    int* sinfo[kSyevStreams] = {};
+    int swork_len = 0;
+    cudaEvent_t fork = nullptr, join[kSyevStreams] = {};
+    std::vector<unsigned char> active;  // molecules still iterating (host copy)
     ~Batch()
     {
         if (d_ebase) cudaFree(d_ebase);
         if (params) cusolverDnDestroyParams(params);
+        for (int i = 0; i < kSyevStreams; ++i) {
+            if (handles[i]) cusolverDnDestroy(handles[i]);
+            if (streams[i]) cudaStreamDestroy(streams[i]);
+            if (swork[i]) cudaFree(swork[i]);
+            if (sinfo[i]) cudaFree(sinfo[i]);
+            if (join[i]) cudaEventDestroy(join[i]);
+        }
+        if (fork) cudaEventDestroy(fork);
     }
 };
 
@@ -253,23 +273,44 @@ int batch_syev(Batch& b, double* A, double* evals, cudaStream_t s)
             batched = (q == CUSOLVER_STATUS_SUCCESS);
         }
         if (batched) continue;
-        // one divide-and-conquer solve per molecule
-        int lwork = 0;
-        if (cusolverDnDsyevd_bufferSize(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g.n, Ag, g.n, Wg,
-                                        &lwork) != CUSOLVER_STATUS_SUCCESS)
-            return set_error("cusolverDnDsyevd_bufferSize failed"), HF_ERR_SOLVER;
-        if (static_cast<size_t>(lwork) * sizeof(double) > b.w.work_bytes) {
-            double* nw = nullptr;
-            if (b.w.alloc(nw, static_cast<size_t>(lwork) + 1)) return HF_ERR_OUT_OF_MEMORY;
-            b.w.work = nw;
-            b.w.work_bytes = static_cast<size_t>(lwork) * sizeof(double);
+        // one divide-and-conquer solve per molecule, spread over kSyevStreams streams
+        if (!b.streams[0]) {
+            for (int k = 0; k < kSyevStreams; ++k) {
+                GB_CUDA_TRY(cudaStreamCreateWithFlags(&b.streams[k], cudaStreamNonBlocking));
+                if (cusolverDnCreate(&b.handles[k]) != CUSOLVER_STATUS_SUCCESS)
+                    return set_error("cusolverDnCreate failed"), HF_ERR_SOLVER;
+                cusolverDnSetStream(b.handles[k], b.streams[k]);
+                GB_CUDA_TRY(cudaEventCreateWithFlags(&b.join[k], cudaEventDisableTiming));
+                GB_CUDA_TRY(cudaMalloc(&b.sinfo[k], sizeof(int)));
+            }
+            GB_CUDA_TRY(cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming));
         }
+        int lwork = 0;
+        if (cusolverDnDsyevd_bufferSize(b.handles[0], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g.n, Ag, g.n,
+                                        Wg, &lwork) != CUSOLVER_STATUS_SUCCESS)
+            return set_error("cusolverDnDsyevd_bufferSize failed"), HF_ERR_SOLVER;
+        if (lwork > b.swork_len) {
+            for (int k = 0; k < kSyevStreams; ++k) {
+                if (b.swork[k]) cudaFree(b.swork[k]);
+                GB_CUDA_TRY(cudaMalloc(&b.swork[k], sizeof(double) * static_cast<size_t>(lwork)));
+            }
+            b.swork_len = lwork;
+        }
+        GB_CUDA_TRY(cudaEventRecord(b.fork, s));
+        const int used = std::min(kSyevStreams, g.count);
+        for (int k = 0; k < used; ++k) GB_CUDA_TRY(cudaStreamWaitEvent(b.streams[k], b.fork, 0));
         for (int i = 0; i < g.count; ++i) {
+            if (!b.active.empty() && !b.active[g.first + i]) continue;  // converged
+            const int k = i % kSyevStreams;
             const long long off = static_cast<long long>(i) * g.n * g.n;
-            if (cusolverDnDsyevd(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g.n, Ag + off, g.n,
-                                 Wg + static_cast<long long>(i) * g.n, b.w.work, lwork, b.w.info) !=
+            if (cusolverDnDsyevd(b.handles[k], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g.n, Ag + off, g.n,
+                                 Wg + static_cast<long long>(i) * g.n, b.swork[k], b.swork_len, b.sinfo[k]) !=
                 CUSOLVER_STATUS_SUCCESS)
                 return set_error("cusolverDnDsyevd (batch) failed"), HF_ERR_SOLVER;
+        }
+        for (int k = 0; k < used; ++k) {
+            GB_CUDA_TRY(cudaEventRecord(b.join[k], b.streams[k]));
+            GB_CUDA_TRY(cudaStreamWaitEvent(s, b.join[k], 0));
         }
     }
     return HF_OK;
@@ -304,7 +345,8 @@ int batch_fock(Batch& b, cudaStream_t s)
     Engine& e = *b.e;
     int st = build_jk(e, b.w.D, nullptr, nullptr, HF_PRECISION_FP64, 0.0, s);
     if (st) return st;
-    batch_fock_kernel<<<grid_of(e.nelem), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, b.w.H, e.block_map(), b.w.F);
+    batch_fock_kernel<<<grid_of(e.nelem), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, b.w.H, e.block_map(),
+                                                       e.d_mol_active, b.w.F);
     GB_LAUNCH_CHECK();
     return HF_OK;
 }
@@ -374,6 +416,16 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     if (cusolverDnCreateParams(&b.params) != CUSOLVER_STATUS_SUCCESS)
         return set_error("cusolverDnCreateParams failed"), HF_ERR_SOLVER;
     GB_CUDA_TRY(cudaMemsetAsync(w.B, 0, sizeof(double) * nmol * kBatchDiis * kBatchDiis, s));
+    // molecules still iterating: the Fock kernels, the F update, DIIS and the eigensolves skip the others
+    unsigned char* d_active = nullptr;
+    if (w.alloc(d_active, nmol)) return HF_ERR_OUT_OF_MEMORY;
+    b.active.assign(nmol, 1);
+    GB_CUDA_TRY(cudaMemcpyAsync(d_active, b.active.data(), nmol, cudaMemcpyHostToDevice, s));
+    struct ActiveGuard {
+        Engine& e;
+        ~ActiveGuard() { e.d_mol_active = nullptr; }
+    } active_guard{e};
+    e.d_mol_active = d_active;
     std::vector<double> enuc(nmol, 0.0);
     for (int m = 0; m < nmol; ++m)
         for (int i = 0; i < e.mol_natom[m]; ++i)
@@ -402,22 +454,39 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     const int m = opt.diis_size;
     int iter = 0, diis_iter = 0, ndone = 0;
     cudaEventRecord(l0, s);
+    cudaEvent_t p0, p1, p2;
+    cudaEventCreate(&p0);
+    cudaEventCreate(&p1);
+    cudaEventCreate(&p2);
+    double diag_ms = 0.0, fock_ms = 0.0;
     while (iter < opt.max_iter) {
+        cudaEventRecord(p0, s);
         if ((st = batch_density(b, w.F, s))) return st;
+        cudaEventRecord(p1, s);
         if ((st = batch_fock(b, s))) return st;
+        cudaEventRecord(p2, s);
         batch_energy_kernel<<<nmol, 256, 0, s>>>(w.D, w.H, w.F, e.block_map(), w.energy);
         GB_LAUNCH_CHECK();
         GB_CUDA_TRY(cudaMemcpyAsync(E.data(), w.energy, sizeof(double) * nmol, cudaMemcpyDeviceToHost, s));
         GB_CUDA_TRY(cudaStreamSynchronize(s));
+        {
+            float a = 0.f, c = 0.f;
+            cudaEventElapsedTime(&a, p0, p1);
+            cudaEventElapsedTime(&c, p1, p2);
+            diag_ms += a;
+            fock_ms += c;
+        }
         for (int k = 0; k < nmol; ++k) {
             if (!std::isfinite(E[k])) return set_error("batch SCF energy is not finite"), HF_ERR_NOT_CONVERGED;
             if (done_iter[k] < 0 && std::fabs(E[k] - prev[k]) < opt.convergence_threshold) {
                 done_iter[k] = iter;
                 done_energy[k] = E[k];
                 ++ndone;
+                b.active[k] = 0;
             }
         }
         if (ndone == nmol) break;
+        GB_CUDA_TRY(cudaMemcpyAsync(d_active, b.active.data(), nmol, cudaMemcpyHostToDevice, s));
         ++iter;
         prev = E;
         // DIIS: e = F D S - S D F per molecule, stored with F in the ring
@@ -442,7 +511,8 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
         GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + static_cast<long long>(slot) * ne, w.F, sizeof(double) * ne,
                                     cudaMemcpyDeviceToDevice, s));
         const int nprev = std::min(diis_iter + 1, m);
-        batch_diis_kernel<<<nmol, 256, 0, s>>>(w.Es, w.Fs, ne, e.block_map(), slot, nprev, w.B, w.F);
+        batch_diis_kernel<<<nmol, 256, 0, s>>>(w.Es, w.Fs, ne, e.block_map(), slot, nprev, e.d_mol_active, w.B,
+                                               w.F);
         GB_LAUNCH_CHECK();
         ++diis_iter;
     }
@@ -463,7 +533,12 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
         r.total_energy = r.electronic_energy + enuc[k];
         r.iterations = r.converged ? done_iter[k] : iter;
         r.scf_ms_total = ms;
+        r.diag_ms_total = diag_ms;
+        r.fock_ms_total = fock_ms;
     }
+    cudaEventDestroy(p0);
+    cudaEventDestroy(p1);
+    cudaEventDestroy(p2);
     return ndone == nmol ? HF_OK : (set_error("batch SCF: not every molecule converged"), HF_ERR_NOT_CONVERGED);
 }
 

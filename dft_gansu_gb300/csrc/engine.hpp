@@ -95,6 +95,7 @@ struct Engine {
     int* d_mol_bf0 = nullptr;
     int2* d_mol_atoms = nullptr;      // first atom, number of atoms
     int* d_shell_mol = nullptr;
+    unsigned char* d_mol_active = nullptr;  // batches: set while a batch SCF runs (null otherwise)
     BlockMap block_map() const { return BlockMap{d_mol_base, d_mol_n, d_mol_bf0, nmol, nelem}; }
     double schwarz_threshold = 1e-12;
     double cgto_max = 1.0;

@@ -66,6 +66,8 @@ struct FockClassLaunch {
     const float* block_dmax;       // incremental builds: max |dD| per shell block [A * nshell + B], or null
     int nshell;
     double skip_cut;               // skip when Qs_ab * Qs_cd * block max < skip_cut
+    const unsigned char* mol_active;  // batches: molecules still iterating (null = all)
+    const int* shell_mol;             // contracted shell -> molecule
 };
 
 }  // namespace gb

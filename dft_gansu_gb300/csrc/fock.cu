@@ -247,6 +247,8 @@ FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off,
     L.block_dmax = nullptr;
     L.nshell = e.num_shells;
     L.skip_cut = 0.0;
+    L.mol_active = e.d_mol_active;
+    L.shell_mol = e.d_shell_mol;
     return L;
 }
 

@@ -225,8 +225,10 @@ struct QuartetRef {
 // quartet reads (AB, CD, AC, AD, BC, BD) is below the cut.
 __device__ __forceinline__ bool negligible_quartet(const FockClassLaunch& L, int bra, int ket)
 {
-    if (!L.block_dmax) return false;
     const ShellPairDev* __restrict__ P = L.pairs;
+    // batches: quartets of molecules that have converged are not built again
+    if (L.mol_active && !L.mol_active[L.shell_mol[P[bra].A]]) return true;
+    if (!L.block_dmax) return false;
     const int A = P[bra].A, B = P[bra].B, C = P[ket].A, D = P[ket].B;
     const int ns = L.nshell;
     const float* __restrict__ bd = L.block_dmax;

@@ -131,6 +131,26 @@ __device__ __forceinline__ void ket_contract(int lmax, const int c[3], const int
             }
 }
 
+// one entry of the ket contraction: sum (-1)^{tau+nu+phi} E^{cd}_{tau nu phi} R_{t+tau, u+nu, v+phi}
+template <class T>
+__device__ __forceinline__ T ket_value(int t, int u, int v, const int c[3], const int d[3], const T* fx, const T* fy,
+                                       const T* fz, const T* r)
+{
+    const T* ex = fx + (c[0] * kGI + d[0]) * kGT;
+    const T* ey = fy + (c[1] * kGI + d[1]) * kGT;
+    const T* ez = fz + (c[2] * kGI + d[2]) * kGT;
+    T s = T(0);
+    for (int tau = 0; tau <= c[0] + d[0]; ++tau)
+        for (int nu = 0; nu <= c[1] + d[1]; ++nu) {
+            const T exy = ex[tau] * ey[nu];
+            for (int phi = 0; phi <= c[2] + d[2]; ++phi) {
+                const T w = exy * ez[phi] * r[gidx(t + tau, u + nu, v + phi)];
+                s += ((tau + nu + phi) & 1) ? -w : w;
+            }
+        }
+    return s;
+}
+
 struct GradLaunch {
     FockClassLaunch L;       // FP64 work list, pairs, primitive pairs, Boys table, D' (FP64)
     const int* shell_atom;   // contracted shell -> atom
@@ -151,8 +171,12 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
     const T* __restrict__ boys = static_cast<const T*>(L.boys_table);
     const int N = L.num_basis;
     const T thr = static_cast<T>(L.schwarz_threshold);
-    T ex[kGE], ey[kGE], ez[kGE], fx[kGE], fy[kGE], fz[kGE];
-    T Fs[kGL + 1], r[kGR], x0[kGX], xp[3][kGX], xm[3][kGX];
+    // one set of E tables: the bra's (used only to build H0/HA) and then each ket primitive pair's
+    T ex[kGE], ey[kGE], ez[kGE];
+    T* const fx = ex;
+    T* const fy = ey;
+    T* const fz = ez;
+    T Fs[kGL + 1], r[kGR];
     T wcol[kGNAB];
 
     for (long long wid = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; wid < nwarps;
@@ -261,32 +285,30 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
                 T scale = pb.KoP * pk.KoP * rr;
                 for (int n = 0; n <= lt; ++n) { Fs[n] *= scale; scale *= T(-2) * rho; }
                 grad_r_table<T>(lt, Fs, X, Y, Z, r);
-                ket_contract<T>(lab + 1, c, d, fx, fy, fz, r, x0);
-                for (int k = 0; k < 3; ++k) {
-                    int cp[3] = {c[0], c[1], c[2]};
-                    cp[k] += 1;
-                    ket_contract<T>(lab, cp, d, fx, fy, fz, r, xp[k]);
-                    if (c[k] > 0) {
-                        cp[k] -= 2;
-                        ket_contract<T>(lab, cp, d, fx, fy, fz, r, xm[k]);
-                    }
-                }
+                // contractions evaluated where they are used (no x arrays):
+                //   gA += HA x0,  gP += H0[tuv - 1_k] x0[tuv],  gC += H0 (2 gamma x[c+1_k] - c_k x[c-1_k])
                 for (int t = 0; t <= lab + 1; ++t)
                     for (int u = 0; u + t <= lab + 1; ++u)
                         for (int v = 0; v + u + t <= lab + 1; ++v) {
                             const int h = gidx(t, u, v);
-                            const T x = x0[h];
+                            const T x = ket_value<T>(t, u, v, c, d, fx, fy, fz, r);
                             gA[0] += HA[0][h] * x;
                             gA[1] += HA[1][h] * x;
                             gA[2] += HA[2][h] * x;
+                            if (t > 0) gP[0] += H0[gidx(t - 1, u, v)] * x;
+                            if (u > 0) gP[1] += H0[gidx(t, u - 1, v)] * x;
+                            if (v > 0) gP[2] += H0[gidx(t, u, v - 1)] * x;
                             if (t + u + v > lab) continue;
                             const T h0 = H0[h];
-                            gP[0] += h0 * x0[gidx(t + 1, u, v)];
-                            gP[1] += h0 * x0[gidx(t, u + 1, v)];
-                            gP[2] += h0 * x0[gidx(t, u, v + 1)];
+                            if (h0 == T(0)) continue;
                             for (int k = 0; k < 3; ++k) {
-                                T dc = gamma2 * xp[k][h];
-                                if (c[k] > 0) dc -= T(c[k]) * xm[k][h];
+                                int cp[3] = {c[0], c[1], c[2]};
+                                cp[k] += 1;
+                                T dc = gamma2 * ket_value<T>(t, u, v, cp, d, fx, fy, fz, r);
+                                if (c[k] > 0) {
+                                    cp[k] -= 2;
+                                    dc -= T(c[k]) * ket_value<T>(t, u, v, cp, d, fx, fy, fz, r);
+                                }
                                 gC[k] += h0 * dc;
                             }
                         }
@@ -506,6 +528,8 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
             G.L.block_dmax = nullptr;
             G.L.nshell = e.num_shells;
             G.L.skip_cut = 0.0;
+            G.L.mol_active = nullptr;
+            G.L.shell_mol = e.d_shell_mol;
             G.shell_atom = e.d_shell_atom;
             G.grad = e.d_grad;
             const int ncd = ncart(Y.la) * ncart(Y.lb);

@@ -225,6 +225,18 @@ __global__ void uhf_fock_kernel(const double* __restrict__ H, const double* __re
     }
 }
 
+// generalised Wolfsberg-Helmholz guess F_pq = c S_pq (H_pp + H_qq) / 2 for every p, q, c = 1.75
+// (the reference's computeInitialFockMatrix_GWH_kernel, src/gpu_kernels.cu:535-545, includes the diagonal)
+__global__ void gwh_kernel(const double* __restrict__ H, const double* __restrict__ S, int n, double* __restrict__ F)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long p = k / n, q = k % n;
+        F[k] = 1.75 * S[k] * (H[p * n + p] + H[q * n + q]) * 0.5;
+    }
+}
+
 int grid_nn(long long nn) { return static_cast<int>(std::min<long long>((nn + 255) / 256, 8192)); }
 
 template <class T>
@@ -371,6 +383,7 @@ void hf_scf_options_default(hf_scf_options* o)
     o->full_build_precision = HF_PRECISION_FP64;
     o->eri_method = HF_ERI_DIRECT;
     o->anchor_threshold = 0.0;
+    o->initial_guess = HF_GUESS_CORE;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -422,6 +435,8 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
     if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI)
         return set_error("unknown eri_method"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.initial_guess != HF_GUESS_CORE && opt.initial_guess != HF_GUESS_GWH)
+        return set_error("initial_guess: core or GWH"), HF_ERR_INVALID_ARGUMENT;
     const bool use_ri = opt.eri_method == HF_ERI_RI;
     if (use_ri && !e.ri)
         return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
@@ -558,7 +573,13 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
     transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
     GB_LAUNCH_CHECK();
-    if ((st = coefficients(e, w.H, s, opt.eigensolver))) return st;
+    if (opt.initial_guess == HF_GUESS_GWH) {
+        gwh_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, w.S, n, w.E);
+        GB_LAUNCH_CHECK();
+        if ((st = coefficients(e, w.E, s, opt.eigensolver))) return st;
+    } else if ((st = coefficients(e, w.H, s, opt.eigensolver))) {
+        return st;
+    }
     density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
     GB_LAUNCH_CHECK();
     if ((st = fock_build(true))) return st;
@@ -731,7 +752,13 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
     transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
     GB_LAUNCH_CHECK();
-    if ((st = densities(w.H, w.H))) return st;
+    if (opt.initial_guess == HF_GUESS_GWH) {
+        gwh_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, w.S, n, w.E);
+        GB_LAUNCH_CHECK();
+        if ((st = densities(w.E, w.E))) return st;
+    } else if ((st = densities(w.H, w.H))) {
+        return st;
+    }
     if ((st = fock())) return st;
     cudaEventRecord(l0, s);
     double prev = std::numeric_limits<double>::max(), energy = 0.0;

@@ -122,8 +122,18 @@ def water_cluster(n: int, rng, oh: float = 0.96, hoh: float = 104.5, min_oo: flo
         if any(np.linalg.norm(o - p) < min_oo for p in placed_o):
             continue
         w = mono @ _random_rotation(rng).T + o
-        if coords and min(np.linalg.norm(np.asarray(coords) - h, axis=1).min() for h in w) < 1.4:
-            continue
+        # intermolecular contacts no shorter than an H-bond: O...H >= 1.7 A, H...H >= 2.0 A
+        if coords:
+            old = np.asarray(coords)
+            old_h = np.array([i % 3 != 0 for i in range(len(old))])
+            too_close = False
+            for j, r in enumerate(w):
+                d = np.linalg.norm(old - r, axis=1)
+                if d.min() < 1.7 or (j > 0 and d[old_h].min() < 2.0):
+                    too_close = True
+                    break
+            if too_close:
+                continue
         placed_o.append(o)
         for s, r in zip(["O", "H", "H"], w):
             symbols.append(s)

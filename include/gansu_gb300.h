@@ -232,7 +232,14 @@ typedef struct {
     double anchor_threshold;        /* mixed tier: low-precision full builds (direct: all quartets FP32; RI:
                                        split-BF16 K) while max|dD| >= this, then one FP64 build, then
                                        incremental builds; 0 = the first build is the FP64 one */
+    int initial_guess;              /* HF_GUESS_CORE or HF_GUESS_GWH (initial_guess = core / gwh) */
 } hf_scf_options;
+
+/* Initial guess (InitialGuess_RHF_Core / _GWH, include/rhf.hpp:378-588). */
+enum {
+    HF_GUESS_CORE = 0,  /* diagonalise H */
+    HF_GUESS_GWH = 1    /* diagonalise 1.75 S_pq (H_pp + H_qq) / 2 (src/gpu_kernels.cu:535-545) */
+};
 
 /* Two-electron backend of the SCF. */
 enum {

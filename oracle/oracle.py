@@ -309,14 +309,23 @@ def diis_extrapolate(errs, focks):
             B[i, j] = np.vdot(errs[i], errs[j])
     rhs = np.zeros(m + 1)
     rhs[m] = -1.0
-    c = np.linalg.solve(B, rhs)
+    try:
+        c = np.linalg.solve(B, rhs)
+    except np.linalg.LinAlgError:  # exactly dependent error vectors (e.g. all zero): least squares
+        c = np.linalg.lstsq(B, rhs, rcond=None)[0]
     return sum(ci * Fi for ci, Fi in zip(c[:m], focks))
 
 
-def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False):
-    """The reference SCF loop (src/hf.cu:278-307) with the core guess and DIIS."""
+def gwh_guess(S, H):
+    """GWH guess F_pq = 1.75 S_pq (H_pp + H_qq) / 2, diagonal included (src/gpu_kernels.cu:535-545)."""
+    d = np.diag(H)
+    return 1.75 * S * (d[:, None] + d[None, :]) * 0.5
+
+
+def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False, guess="core"):
+    """The reference SCF loop (src/hf.cu:278-307) with the core (or GWH) guess and DIIS."""
     X = transform_matrix(S)
-    _, Cm = coefficients(H, X)
+    _, Cm = coefficients(gwh_guess(S, H) if guess == "gwh" else H, X)
     D = density(Cm, nocc)
     F = fock(D)
     prev, energy, it, diis_it = np.finfo(float).max, 0.0, 0, 0

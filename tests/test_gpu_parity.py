@@ -256,3 +256,15 @@ def test_scf_mixed_anchored_decane(built_library, cuda, anchor, tau):
     np.testing.assert_allclose(_np(rmx["orbital_energies"]), _np(r64["orbital_energies"]), atol=1e-5)
     # exactly one full FP64 build's worth of FP64 quartets: the anchor
     assert rmx["fp64_quartets"] <= r64["fp64_quartets"] / (r64["iterations"] + 1) * 1.5
+
+
+def test_gwh_guess_matches_oracle(built_library, cuda):
+    g, atoms, gbs = _case("water_6-31g_st")
+    mol, eng = _engine(atoms, gbs)
+    r = eng.rhf_scf(mol.num_electrons, {"convergence_threshold": 1e-10, "initial_guess": gg.HF_GUESS_GWH})
+    b = O.make_basis(atoms, gg.basis_path(gbs))
+    ro = O.rhf_from_basis(b, thr=1e-10, guess="gwh")
+    assert r["converged"] == 1 and ro["converged"]
+    assert abs(r["total_energy"] - ro["total_energy"]) < 1e-8
+    assert r["iterations"] == ro["iterations"]
+    assert abs(r["total_energy"] - float(g["energy_total"])) < 1e-8
