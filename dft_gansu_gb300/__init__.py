@@ -12,7 +12,8 @@ from pathlib import Path
 
 import numpy as np
 
-from ._capi import (HF_ERR_NOT_CONVERGED, HF_ERI_DIRECT, HF_ERI_RI, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
+from ._capi import (HF_EIGEN_PURIFICATION, HF_EIGEN_SYEVD, HF_GUESS_CORE, HF_GUESS_GWH, HF_ERR_NOT_CONVERGED,
+                    HF_ERI_DIRECT, HF_ERI_RI, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
                     check, lib)
 
 BASIS_DIR = Path(__file__).resolve().parent / "basis"
@@ -21,7 +22,8 @@ ANGSTROM_TO_BOHR = 1.8897259886
 __all__ = [
     "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
     "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "basis_path",
-    "optimize_geometry", "energy_and_gradient_at", "Batch", "UHF",
+    "optimize_geometry", "energy_and_gradient_at", "Batch", "UHF", "HF_EIGEN_PURIFICATION", "HF_EIGEN_SYEVD",
+    "HF_GUESS_CORE", "HF_GUESS_GWH",
 ]
 
 

@@ -26,6 +26,9 @@ HF_ERI_DIRECT = 0
 HF_ERI_RI = 1
 HF_GUESS_CORE = 0
 HF_GUESS_GWH = 1
+HF_EIGEN_SYEVD = 0
+HF_EIGEN_SYEVJ = 1
+HF_EIGEN_PURIFICATION = 2
 
 
 class PrimitiveShell(C.Structure):

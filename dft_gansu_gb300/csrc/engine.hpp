@@ -162,6 +162,7 @@ struct Engine {
         int lwork = 0, lwork_j = 0;
         double* work_j = nullptr;
         syevjInfo_t syevj_params = nullptr;
+        float *P32a = nullptr, *P32b = nullptr, *P32c = nullptr;  // purification (FP32 SP2) buffers
     } scf;
 
     ~Engine();

@@ -237,6 +237,101 @@ __global__ void gwh_kernel(const double* __restrict__ H, const double* __restric
     }
 }
 
+// ---- density by purification (eigensolver 2): no eigenvectors inside the SCF loop
+// Gershgorin interval [lo, hi] of the symmetric F' (one block)
+__global__ void gershgorin_kernel(const double* __restrict__ A, int n, double* __restrict__ out)
+{
+    __shared__ double rlo[32], rhi[32];
+    double lo = 1e300, hi = -1e300;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double r = 0.0;
+        for (int j = 0; j < n; ++j)
+            if (j != i) r += fabs(A[static_cast<long long>(i) * n + j]);
+        const double d = A[static_cast<long long>(i) * n + i];
+        lo = fmin(lo, d - r);
+        hi = fmax(hi, d + r);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) { rlo[threadIdx.x >> 5] = lo; rhi[threadIdx.x >> 5] = hi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) { lo = fmin(lo, rlo[w]); hi = fmax(hi, rhi[w]); }
+        out[0] = fmin(lo, rlo[0]);
+        out[1] = fmax(hi, rhi[0]);
+    }
+}
+
+// P0 = (hi I - F') / (hi - lo): eigenvalues in [0, 1], the lowest orbitals near 1
+__global__ void sp2_init_kernel(const double* __restrict__ Fp, int n, const double* __restrict__ bounds,
+                                float* __restrict__ P)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    const double lo = bounds[0], hi = bounds[1];
+    const double inv = 1.0 / (hi - lo);
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const bool diag = (k / n) == (k % n);
+        P[k] = static_cast<float>(((diag ? hi : 0.0) - Fp[k]) * inv);
+    }
+}
+
+// One SP2 step (Niklasson): Pn = P^2 or 2P - P^2, whichever trace is closer to nocc.
+// Every block reads both traces from the diagonals, so P, P2 and Pn are distinct buffers.
+__global__ void sp2_step_kernel(const float* __restrict__ P, const float* __restrict__ P2, int n, int nocc,
+                                float* __restrict__ Pn)
+{
+    __shared__ float r1[32], r2[32];
+    __shared__ int take_square;
+    float t1 = 0.f, t2 = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        t1 += P[static_cast<long long>(i) * n + i];
+        t2 += P2[static_cast<long long>(i) * n + i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+        t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+    }
+    if ((threadIdx.x & 31) == 0) { r1[threadIdx.x >> 5] = t1; r2[threadIdx.x >> 5] = t2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f, b = 0.f;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) { a += r1[w]; b += r2[w]; }
+        take_square = fabsf(b - nocc) < fabsf(2.f * a - b - nocc) ? 1 : 0;
+    }
+    __syncthreads();
+    const long long nn = static_cast<long long>(n) * n;
+    const bool sq = take_square != 0;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        Pn[k] = sq ? P2[k] : 2.f * P[k] - P2[k];
+}
+
+__global__ void scale_copy_kernel(const double* __restrict__ a, double f, long long nn, double* __restrict__ b)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        b[k] = f * a[k];
+}
+
+__global__ void widen_kernel(const float* __restrict__ a, long long nn, double* __restrict__ b)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        b[k] = static_cast<double>(a[k]);
+}
+
+// McWeeny step P = 3 P^2 - 2 P^3
+__global__ void mcweeny_kernel(const double* __restrict__ P2, const double* __restrict__ P3, long long nn,
+                               double* __restrict__ P)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        P[k] = 3.0 * P2[k] - 2.0 * P3[k];
+}
+
 int grid_nn(long long nn) { return static_cast<int>(std::min<long long>((nn + 255) / 256, 8192)); }
 
 template <class T>
@@ -313,6 +408,56 @@ int coefficients(Engine& e, const double* F, cudaStream_t s, int solver = 0)
     if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, w.X, w.T2))) return st;  // X^T F X
     if ((st = syevd(e, w.T2, s, solver))) return st;
     return gemm_rm(e.cublas, false, true, w.n, w.X, w.W, w.C);  // C = X C'
+}
+
+// D = 2 X P X^T with P the projector on the nocc lowest states of F' = X^T F X, by
+// purification: FP32 SP2 steps (cuBLAS SGEMM) from the Gershgorin-scaled F', then FP64
+// McWeeny steps to FP64 idempotency.  Equals the aufbau density of a diagonalisation
+// whenever the HOMO-LUMO gap is open.
+constexpr int kSp2Steps = 50;
+constexpr int kMcWeenySteps = 3;
+
+int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t s)
+{
+    auto& w = e.scf;
+    const int n = w.n;
+    const long long nn = static_cast<long long>(n) * n;
+    int st;
+    if (!w.P32a) {
+        if ((st = alloc(w.P32a, nn)) || (st = alloc(w.P32b, nn)) || (st = alloc(w.P32c, nn))) return st;
+    }
+    if ((st = gemm_rm(e.cublas, true, false, n, w.X, F, w.T1))) return st;    // X^T F
+    if ((st = gemm_rm(e.cublas, false, false, n, w.T1, w.X, w.T2))) return st; // F'
+    gershgorin_kernel<<<1, 1024, 0, s>>>(w.T2, n, e.d_scalar + 8);
+    GB_LAUNCH_CHECK();
+    sp2_init_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T2, n, e.d_scalar + 8, w.P32a);
+    GB_LAUNCH_CHECK();
+    float* P = w.P32a;
+    float* Pn = w.P32b;
+    float* P2 = w.P32c;
+    const float one = 1.f, zero = 0.f;
+    for (int k = 0; k < kSp2Steps; ++k) {
+        // P symmetric: the column-major product is P^2 as well
+        if (cublasSgemm(e.cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, P, n, P, n, &zero, P2, n) !=
+            CUBLAS_STATUS_SUCCESS)
+            return set_error("cublasSgemm (purification) failed"), HF_ERR_SOLVER;
+        sp2_step_kernel<<<grid_nn(nn), 256, 0, s>>>(P, P2, n, nocc, Pn);
+        GB_LAUNCH_CHECK();
+        std::swap(P, Pn);
+    }
+    widen_kernel<<<grid_nn(nn), 256, 0, s>>>(P, nn, w.W);
+    GB_LAUNCH_CHECK();
+    for (int k = 0; k < kMcWeenySteps; ++k) {
+        if ((st = gemm_rm(e.cublas, false, false, n, w.W, w.W, w.T1))) return st;  // P^2
+        if ((st = gemm_rm(e.cublas, false, false, n, w.T1, w.W, w.T2))) return st; // P^3
+        mcweeny_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T1, w.T2, nn, w.W);
+        GB_LAUNCH_CHECK();
+    }
+    if ((st = gemm_rm(e.cublas, false, false, n, w.X, w.W, w.T1))) return st;  // X P
+    if ((st = gemm_rm(e.cublas, false, true, n, w.T1, w.X, w.T2))) return st;  // X P X^T
+    scale_copy_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T2, 2.0, nn, D);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
 }
 
 int diis_error(Engine& e, const double* S, const double* X, const double* F, const double* D, double* E,
@@ -573,14 +718,23 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
     transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
     GB_LAUNCH_CHECK();
+    // purification needs no orbitals, but the RI K build uses the occupied ones
+    const bool purify = opt.eigensolver == HF_EIGEN_PURIFICATION && !use_ri;
+    auto density_from = [&](const double* Fm) -> int {
+        int r;
+        if (purify) return purify_density(e, Fm, nocc, w.D, s);
+        if ((r = coefficients(e, Fm, s, opt.eigensolver))) return r;
+        density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
+        GB_LAUNCH_CHECK();
+        return HF_OK;
+    };
     if (opt.initial_guess == HF_GUESS_GWH) {
         gwh_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, w.S, n, w.E);
         GB_LAUNCH_CHECK();
-        if ((st = coefficients(e, w.E, s, opt.eigensolver))) return st;
-    } else if ((st = coefficients(e, w.H, s, opt.eigensolver))) {
+        if ((st = density_from(w.E))) return st;
+    } else if ((st = density_from(w.H))) {
         return st;
     }
-    density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
     GB_LAUNCH_CHECK();
     if ((st = fock_build(true))) return st;
     fock_ms += elapsed(f0, f1);
@@ -595,9 +749,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     bool converged = false;
     while (iter < opt.max_iter) {
         cudaEventRecord(c0, s);
-        if ((st = coefficients(e, w.F, s, opt.eigensolver))) return st;
-        density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
-        GB_LAUNCH_CHECK();
+        if ((st = density_from(w.F))) return st;
         cudaEventRecord(c1, s);
         if ((st = fock_build(false))) return st;
         energy_kernel<<<1, 1024, 0, s>>>(w.D, w.H, w.F, nn, e.d_scalar + 4);
@@ -661,6 +813,10 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     res->fp64_quartets = static_cast<long long>(prim64);
     res->fp32_quartets = static_cast<long long>(prim32);
     if (info[0] != 0) return set_error("syevd reported info " + std::to_string(info[0])), HF_ERR_SOLVER;
+    if (purify && (d_orbital_energies_out || d_coefficients_out)) {
+        // purification kept no orbitals: one diagonalisation of the final Fock matrix
+        if ((st = coefficients(e, w.F, s, 0))) return st;
+    }
     if (d_density_out) GB_CUDA_TRY(cudaMemcpy(d_density_out, w.D, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     if (d_fock_out) GB_CUDA_TRY(cudaMemcpy(d_fock_out, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     if (d_orbital_energies_out) {

@@ -226,7 +226,7 @@ typedef struct {
     int incremental;                /* 1: build G(dD) and accumulate (mixed tier) */
     int rebuild_every;              /* full rebuild period for the incremental build, 0 = never */
     int full_build_precision;       /* precision of full (non-incremental) builds under the mixed tier */
-    int eigensolver;                /* 0: cuSOLVER syevd (divide and conquer), 1: syevj (Jacobi) */
+    int eigensolver;                /* HF_EIGEN_SYEVD, HF_EIGEN_SYEVJ or HF_EIGEN_PURIFICATION */
     int verbose;                    /* print per-iteration lines like the reference */
     int eri_method;                 /* HF_ERI_DIRECT or HF_ERI_RI (eri_method = direct / ri, src/rhf.cu:72-88) */
     double anchor_threshold;        /* mixed tier: low-precision full builds (direct: all quartets FP32; RI:
@@ -234,6 +234,18 @@ typedef struct {
                                        incremental builds; 0 = the first build is the FP64 one */
     int initial_guess;              /* HF_GUESS_CORE or HF_GUESS_GWH (initial_guess = core / gwh) */
 } hf_scf_options;
+
+/* Density from the Fock matrix inside the SCF loop.  The reference diagonalises
+ * (computeCoefficientMatrix, src/gpu_manager.cu:529-599); purification gives the
+ * same aufbau density when the HOMO-LUMO gap is open, without eigenvectors:
+ * FP32 SP2 steps then FP64 McWeeny steps; orbitals and orbital energies come
+ * from one diagonalisation of the final Fock matrix.  RI keeps syevd (its K
+ * build uses the occupied orbitals). */
+enum {
+    HF_EIGEN_SYEVD = 0,
+    HF_EIGEN_SYEVJ = 1,
+    HF_EIGEN_PURIFICATION = 2
+};
 
 /* Initial guess (InitialGuess_RHF_Core / _GWH, include/rhf.hpp:378-588). */
 enum {

@@ -268,3 +268,20 @@ def test_gwh_guess_matches_oracle(built_library, cuda):
     assert abs(r["total_energy"] - ro["total_energy"]) < 1e-8
     assert r["iterations"] == ro["iterations"]
     assert abs(r["total_energy"] - float(g["energy_total"])) < 1e-8
+
+
+def test_purification_density_matches_diagonalisation(built_library, cuda):
+    # FP32 SP2 + FP64 McWeeny inside the loop: same energies and iterations as syevd
+    atoms = geometry.alkane(10, jitter=0.02, seed=0)
+    mol, eng = _engine(atoms, "6-31g_st")
+    base = {"convergence_threshold": 1e-9}
+    rd = eng.rhf_scf(mol.num_electrons, base, want_matrices=True)
+    rp = eng.rhf_scf(mol.num_electrons, dict(base, eigensolver=gg.HF_EIGEN_PURIFICATION), want_matrices=True)
+    assert rp["converged"] == 1
+    assert abs(rp["total_energy"] - rd["total_energy"]) < 1e-9
+    assert abs(rp["iterations"] - rd["iterations"]) <= 1
+    np.testing.assert_allclose(_np(rp["density"]), _np(rd["density"]), atol=1e-6)
+    np.testing.assert_allclose(_np(rp["orbital_energies"]), _np(rd["orbital_energies"]), atol=1e-6)
+    rm = eng.rhf_scf(mol.num_electrons, dict(base, eigensolver=gg.HF_EIGEN_PURIFICATION, precision=gg.HF_PRECISION_MIXED,
+                                             mixed_threshold=0.1, incremental=1, anchor_threshold=1e-2))
+    assert rm["converged"] == 1 and abs(rm["total_energy"] - rd["total_energy"]) < 1e-6
