@@ -205,6 +205,100 @@ __global__ void batch_diis_kernel(const double* __restrict__ Es, const double* _
     }
 }
 
+// ---- purification over all molecules (eigensolver 2)
+// per-molecule Gershgorin interval of F' (one CTA per molecule)
+__global__ void batch_gershgorin_kernel(const double* __restrict__ A, const BlockMap M, double* __restrict__ bounds)
+{
+    __shared__ double rlo[32], rhi[32];
+    const int m = blockIdx.x, n = M.n[m];
+    const double* a = A + M.base[m];
+    double lo = 1e300, hi = -1e300;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double r = 0.0;
+        for (int j = 0; j < n; ++j)
+            if (j != i) r += fabs(a[static_cast<long long>(i) * n + j]);
+        const double d = a[static_cast<long long>(i) * n + i];
+        lo = fmin(lo, d - r);
+        hi = fmax(hi, d + r);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) { rlo[threadIdx.x >> 5] = lo; rhi[threadIdx.x >> 5] = hi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) { lo = fmin(lo, rlo[w]); hi = fmax(hi, rhi[w]); }
+        bounds[2 * m] = fmin(lo, rlo[0]);
+        bounds[2 * m + 1] = fmax(hi, rhi[0]);
+    }
+}
+
+__global__ void batch_sp2_init_kernel(const double* __restrict__ Fp, const double* __restrict__ bounds,
+                                      const BlockMap M, float* __restrict__ P)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int m = block_of(M, k);
+        const int n = M.n[m];
+        const long long r = k - M.base[m];
+        const double lo = bounds[2 * m], hi = bounds[2 * m + 1];
+        const bool diag = (r / n) == (r % n);
+        P[k] = static_cast<float>(((diag ? hi : 0.0) - Fp[k]) / (hi - lo));
+    }
+}
+
+// per molecule: take P^2 if its trace is nearer nocc than 2P - P^2's (one CTA per molecule)
+__global__ void batch_sp2_decide_kernel(const float* __restrict__ P, const float* __restrict__ P2, const BlockMap M,
+                                        const int* __restrict__ nocc, unsigned char* __restrict__ square)
+{
+    __shared__ float r1[32], r2[32];
+    const int m = blockIdx.x, n = M.n[m];
+    const long long base = M.base[m];
+    float t1 = 0.f, t2 = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        t1 += P[base + static_cast<long long>(i) * n + i];
+        t2 += P2[base + static_cast<long long>(i) * n + i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+        t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+    }
+    if ((threadIdx.x & 31) == 0) { r1[threadIdx.x >> 5] = t1; r2[threadIdx.x >> 5] = t2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f, b = 0.f;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) { a += r1[w]; b += r2[w]; }
+        const float no = static_cast<float>(nocc[m]);
+        square[m] = fabsf(b - no) < fabsf(2.f * a - b - no) ? 1 : 0;
+    }
+}
+
+__global__ void batch_sp2_update_kernel(const float* __restrict__ P, const float* __restrict__ P2, const BlockMap M,
+                                        const unsigned char* __restrict__ square, float* __restrict__ Pn)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int m = block_of(M, k);
+        Pn[k] = square[m] ? P2[k] : 2.f * P[k] - P2[k];
+    }
+}
+
+__global__ void batch_widen_kernel(const float* __restrict__ a, long long nn, double* __restrict__ b)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        b[k] = static_cast<double>(a[k]);
+}
+
+__global__ void batch_mcweeny_kernel(const double* __restrict__ P2, const double* __restrict__ P3, long long nn,
+                                     double* __restrict__ P)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        P[k] = 3.0 * P2[k] - 2.0 * P3[k];
+}
+
 // row-major strided-batched C = alpha op(A) op(B) + beta C over n x n blocks (k inner)
 cublasStatus_t gemm_batched(cublasHandle_t h, bool ta, bool tb, int n, int k, double alpha, const double* A, int lda,
                             const double* B, int ldb, double beta, double* C, int count)
@@ -231,10 +325,18 @@ struct Batch {
     int swork_len = 0;
     cudaEvent_t fork = nullptr, join[kSyevStreams] = {};
     std::vector<unsigned char> active;  // molecules still iterating (host copy)
+    bool purify = false;                // eigensolver 2: SP2 + McWeeny instead of batched syev
+    float *P32a = nullptr, *P32b = nullptr, *P32c = nullptr;
+    double* bounds = nullptr;
+    unsigned char* square = nullptr;
+    int* d_nocc = nullptr;
     ~Batch()
     {
         if (d_ebase) cudaFree(d_ebase);
         if (params) cusolverDnDestroyParams(params);
+        for (void* p : {static_cast<void*>(P32a), static_cast<void*>(P32b), static_cast<void*>(P32c),
+                        static_cast<void*>(bounds), static_cast<void*>(square), static_cast<void*>(d_nocc)})
+            if (p) cudaFree(p);
         for (int i = 0; i < kSyevStreams; ++i) {
             if (handles[i]) cusolverDnDestroy(handles[i]);
             if (streams[i]) cudaStreamDestroy(streams[i]);
@@ -317,6 +419,8 @@ int batch_syev(Batch& b, double* A, double* evals, cudaStream_t s)
 }
 
 // C and D from F for every molecule: F' = X^T F X, eigenvectors V, C = X V, D = 2 C_occ C_occ^T
+int batch_purify(Batch& b, cudaStream_t s);
+
 int batch_density(Batch& b, const double* F, cudaStream_t s)
 {
     Engine& e = *b.e;
@@ -328,6 +432,7 @@ int batch_density(Batch& b, const double* F, cudaStream_t s)
             gemm_batched(e.cublas, true, false, g.n, g.n, 1.0, w.X + o, g.n, w.T1 + o, g.n, 0.0, w.Fp + o, g.count))
             return set_error("cublasDgemmStridedBatched (F') failed"), HF_ERR_SOLVER;
     }
+    if (b.purify) return batch_purify(b, s);
     int st = batch_syev(b, w.Fp, w.eps, s);
     if (st) return st;
     for (const Group& g : b.groups) {
@@ -336,6 +441,59 @@ int batch_density(Batch& b, const double* F, cudaStream_t s)
         if (gemm_batched(e.cublas, false, true, g.n, g.n, 1.0, w.X + o, g.n, w.Fp + o, g.n, 0.0, w.C + o, g.count) ||
             gemm_batched(e.cublas, false, true, g.n, g.nocc, 2.0, w.C + o, g.n, w.C + o, g.n, 0.0, w.D + o, g.count))
             return set_error("cublasDgemmStridedBatched (C, D) failed"), HF_ERR_SOLVER;
+    }
+    return HF_OK;
+}
+
+// D = 2 X P X^T with P from FP32 SP2 steps on every molecule's F' (strided-batched SGEMM per
+// group, per-molecule trace decisions on the device) and FP64 McWeeny steps
+int batch_purify(Batch& b, cudaStream_t s)
+{
+    Engine& e = *b.e;
+    BatchState& w = b.w;
+    const long long ne = e.nelem;
+    const BlockMap M = e.block_map();
+    batch_gershgorin_kernel<<<e.nmol, 256, 0, s>>>(w.Fp, M, b.bounds);
+    GB_LAUNCH_CHECK();
+    batch_sp2_init_kernel<<<grid_of(ne), 256, 0, s>>>(w.Fp, b.bounds, M, b.P32a);
+    GB_LAUNCH_CHECK();
+    float* P = b.P32a;
+    float* Pn = b.P32b;
+    float* P2 = b.P32c;
+    const float one = 1.f, zero = 0.f;
+    for (int k = 0; k < 50; ++k) {
+        for (const Group& g : b.groups) {
+            const long long st = static_cast<long long>(g.n) * g.n;
+            if (cublasSgemmStridedBatched(e.cublas, CUBLAS_OP_N, CUBLAS_OP_N, g.n, g.n, g.n, &one, P + g.base, g.n, st,
+                                          P + g.base, g.n, st, &zero, P2 + g.base, g.n, st, g.count) !=
+                CUBLAS_STATUS_SUCCESS)
+                return set_error("cublasSgemmStridedBatched (purification) failed"), HF_ERR_SOLVER;
+        }
+        batch_sp2_decide_kernel<<<e.nmol, 256, 0, s>>>(P, P2, M, b.d_nocc, b.square);
+        GB_LAUNCH_CHECK();
+        batch_sp2_update_kernel<<<grid_of(ne), 256, 0, s>>>(P, P2, M, b.square, Pn);
+        GB_LAUNCH_CHECK();
+        std::swap(P, Pn);
+    }
+    batch_widen_kernel<<<grid_of(ne), 256, 0, s>>>(P, ne, w.Fp);
+    GB_LAUNCH_CHECK();
+    for (int k = 0; k < 3; ++k) {
+        for (const Group& g : b.groups) {
+            const long long o = g.base;
+            if (gemm_batched(e.cublas, false, false, g.n, g.n, 1.0, w.Fp + o, g.n, w.Fp + o, g.n, 0.0, w.T1 + o,
+                             g.count) ||
+                gemm_batched(e.cublas, false, false, g.n, g.n, 1.0, w.T1 + o, g.n, w.Fp + o, g.n, 0.0, w.T2 + o,
+                             g.count))
+                return set_error("cublasDgemmStridedBatched (McWeeny) failed"), HF_ERR_SOLVER;
+        }
+        batch_mcweeny_kernel<<<grid_of(ne), 256, 0, s>>>(w.T1, w.T2, ne, w.Fp);
+        GB_LAUNCH_CHECK();
+    }
+    for (const Group& g : b.groups) {
+        const long long o = g.base;
+        if (gemm_batched(e.cublas, false, false, g.n, g.n, 1.0, w.X + o, g.n, w.Fp + o, g.n, 0.0, w.T1 + o, g.count) ||
+            gemm_batched(e.cublas, false, true, g.n, g.n, 2.0, w.T1 + o, g.n, w.X + o, g.n, 0.0, w.D + o, g.count))
+            return set_error("cublasDgemmStridedBatched (X P X^T) failed"), HF_ERR_SOLVER;
     }
     return HF_OK;
 }
@@ -415,6 +573,18 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     GB_CUDA_TRY(cudaMemcpy(b.d_ebase, b.ebase.data(), sizeof(long long) * (nmol + 1), cudaMemcpyHostToDevice));
     if (cusolverDnCreateParams(&b.params) != CUSOLVER_STATUS_SUCCESS)
         return set_error("cusolverDnCreateParams failed"), HF_ERR_SOLVER;
+    if (opt.eigensolver == HF_EIGEN_PURIFICATION) {
+        b.purify = true;
+        std::vector<int> nocc(nmol);
+        for (int m2 = 0; m2 < nmol; ++m2) nocc[m2] = num_electrons[m2] / 2;
+        if (cudaMalloc(&b.P32a, sizeof(float) * ne) != cudaSuccess ||
+            cudaMalloc(&b.P32b, sizeof(float) * ne) != cudaSuccess ||
+            cudaMalloc(&b.P32c, sizeof(float) * ne) != cudaSuccess ||
+            cudaMalloc(&b.bounds, sizeof(double) * 2 * nmol) != cudaSuccess ||
+            cudaMalloc(&b.square, nmol) != cudaSuccess || cudaMalloc(&b.d_nocc, sizeof(int) * nmol) != cudaSuccess)
+            return set_error("cudaMalloc (batch purification) failed"), HF_ERR_OUT_OF_MEMORY;
+        GB_CUDA_TRY(cudaMemcpy(b.d_nocc, nocc.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
+    }
     GB_CUDA_TRY(cudaMemsetAsync(w.B, 0, sizeof(double) * nmol * kBatchDiis * kBatchDiis, s));
     // molecules still iterating: the Fock kernels, the F update, DIIS and the eigensolves skip the others
     unsigned char* d_active = nullptr;

@@ -51,3 +51,14 @@ def test_batch_engine_rejects_single_molecule_entry_points(built_library, cuda):
     from dft_gansu_gb300._capi import ScfResult, lib
     r = ScfResult()
     assert lib().hf_rhf_scf(b._h, 10, None, C.byref(r), None, None, None, None) == 1
+
+
+def test_batch_purification_matches_diagonalisation(built_library, cuda):
+    clusters = geometry.water_cluster_set(8, nmax=4, seed=9)
+    mols = [gg.Molecular(c, gg.basis_path("6-31g")) for c in clusters]
+    batch = gg.Batch(mols)
+    rd, _, _ = batch.rhf_scf(CONV)
+    rp, _, _ = batch.rhf_scf(dict(CONV, eigensolver=gg.HF_EIGEN_PURIFICATION))
+    for a, b in zip(rd, rp):
+        assert a["converged"] == 1 and b["converged"] == 1
+        assert abs(a["total_energy"] - b["total_energy"]) < 1e-8
