@@ -32,6 +32,7 @@ WORKLOAD = "RHF/6-31G* n-decane C10H22 (N=194 Cartesian, 238 primitive shells), 
 MIXED_THRESHOLD = 0.1
 ANCHOR_THRESHOLD = 1e-2
 CONV = 1e-8
+GUESSES = {"core": 0, "gwh": 1, "sad": 3}  # HF_GUESS_CORE / _GWH / _SAD
 
 
 # ----------------------------------------------------------------- model
@@ -238,6 +239,9 @@ def run_ours(args, rank, world):
                   "mixed_threshold": args.mixed_threshold, "incremental": 1, "rebuild_every": 0,
                   "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": args.anchor_threshold}
     opts_fp64 = {"convergence_threshold": CONV}
+    for o in (opts_mixed, opts_fp64):
+        o["initial_guess"] = GUESSES[args.guess or "core"]
+        o["eigensolver"] = gg.HF_EIGEN_PURIFICATION if args.eigensolver == "purification" else gg.HF_EIGEN_SYEVD
 
     def solve(opts):
         flush.zero_()
@@ -392,6 +396,7 @@ def run_ours(args, rank, world):
                        f"FP32 while max|dD| >= {args.anchor_threshold}, one FP64 build, then incremental dD builds "
                        f"with FP32 quartets where Q_ab*Q_cd*max|dD| < {args.mixed_threshold})",
                        "convergence": CONV, "l2": "flushed (512 MB write) before every step",
+                       "initial_guess": args.guess or "core", "eigensolver": args.eigensolver,
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "fp64_ms_per_iter": ms_64, "mixed_speedup_vs_fp64": ms_64 / ms_mx,
             "delta_E_mixed_vs_fp64": dE, "energy_fp64": fp64[0]["total_energy"],
@@ -498,15 +503,20 @@ def run_water_batch(args, rank, world):
     torch.cuda.set_device(dev)
     clusters = geometry.water_cluster_set(args.batch_size, nmax=16, seed=args.seed)
     gbs = gg.basis_path("6-31g")
-    conv = {"convergence_threshold": CONV}
+    guess = args.guess or "sad"
+    conv = {"convergence_threshold": CONV, "initial_guess": GUESSES[guess],
+            "eigensolver": gg.HF_EIGEN_PURIFICATION if args.eigensolver == "purification" else gg.HF_EIGEN_SYEVD}
     t0 = time.perf_counter()
     mols = [gg.Molecular(c, gbs) for c in clusters]
     batch = gg.Batch(mols)
+    batch_conv = dict(conv)
+    if guess == "sad":
+        batch_conv["guess_density_a"], batch_conv["guess_density_b"] = batch.sad_density()
     setup_s = time.perf_counter() - t0
     for _ in range(args.warmup):
-        batch.rhf_scf(conv)
+        batch.rhf_scf(batch_conv)
     with ClockSampler(dev) as clocks:
-        runs = [batch.rhf_scf(conv) for _ in range(args.steps)]
+        runs = [batch.rhf_scf(batch_conv) for _ in range(args.steps)]
     res, ms, it = runs[-1]
     ms_iter = statistics.mean(r[1] / max(r[2], 1) for r in runs)
     # individual FP64 runs (engine + SCF per molecule), device time of their SCF loops
@@ -529,6 +539,7 @@ def run_water_batch(args, rank, world):
             "config": {"workload": f"batched RHF/6-31G, {len(clusters)} water clusters (H2O)_n, n ~ U{{1..16}} "
                                    f"(sum N = {sum(m.num_basis for m in mols)}), O-H 0.96 A, HOH 104.5, O-O >= 2.7 A",
                        "seed": args.seed, "convergence": CONV, "waters": [min(sizes), max(sizes), sum(sizes)],
+                       "initial_guess": guess, "eigensolver": args.eigensolver,
                        "l2": "matrices and lists of all molecules (> L2) touched every iteration",
                        "parallelism": "1 GPU, all molecules in one engine"},
             "batch_ms_total": ms, "batch_iterations": it,
@@ -617,6 +628,9 @@ def main():
     ap.add_argument("--grad-threshold", type=float, default=1e-3)
     ap.add_argument("--batch-size", type=int, default=256)
     ap.add_argument("--ri-threshold", type=float, default=1e-2)
+    ap.add_argument("--guess", default=None, choices=["core", "gwh", "sad"],
+                    help="initial guess (default: core; water_batch: sad)")
+    ap.add_argument("--eigensolver", default="syevd", choices=["syevd", "purification"])
     args = ap.parse_args()
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":

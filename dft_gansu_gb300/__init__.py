@@ -12,7 +12,8 @@ from pathlib import Path
 
 import numpy as np
 
-from ._capi import (HF_EIGEN_PURIFICATION, HF_EIGEN_SYEVD, HF_GUESS_CORE, HF_GUESS_GWH, HF_ERR_NOT_CONVERGED,
+from ._capi import (HF_EIGEN_PURIFICATION, HF_EIGEN_SYEVD, HF_GUESS_CORE, HF_GUESS_DENSITY, HF_GUESS_GWH,
+                    HF_GUESS_SAD, HF_ERR_NOT_CONVERGED,
                     HF_ERI_DIRECT, HF_ERI_RI, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
                     check, lib)
 
@@ -23,7 +24,7 @@ __all__ = [
     "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
     "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "basis_path",
     "optimize_geometry", "energy_and_gradient_at", "Batch", "UHF", "HF_EIGEN_PURIFICATION", "HF_EIGEN_SYEVD",
-    "HF_GUESS_CORE", "HF_GUESS_GWH",
+    "HF_GUESS_CORE", "HF_GUESS_GWH", "HF_GUESS_DENSITY", "HF_GUESS_SAD", "ROHF", "ROHF_COUPLINGS",
 ]
 
 
@@ -49,6 +50,7 @@ class Molecular:
         check(lib().hf_molecule_from_atoms(arr, len(atoms), str(gbs_filename).encode(), charge, beta_to_alpha,
                                            C.byref(h)), "hf_molecule_from_atoms")
         self._init_from_handle(h)
+        self.gbs_filename = str(gbs_filename)
 
     @classmethod
     def from_files(cls, xyz_filename: str, gbs_filename: str, charge: int = 0, beta_to_alpha: int = 0):
@@ -57,6 +59,7 @@ class Molecular:
                                            beta_to_alpha, C.byref(h)), "hf_molecule_from_files")
         obj = cls.__new__(cls)
         obj._init_from_handle(h)
+        obj.gbs_filename = str(gbs_filename)
         return obj
 
     def _init_from_handle(self, h):
@@ -120,6 +123,37 @@ def _stream(stream) -> C.c_void_p:
     if stream is None:
         return C.c_void_p(0)
     return C.c_void_p(int(getattr(stream, "cuda_stream", stream)))
+
+
+def _scf_options(options: dict | None):
+    """hf_scf_options from a dict; guess_density_a/_b may be CUDA tensors (kept
+    alive by the returned list for the duration of the call)."""
+    opt = ScfOptions()
+    lib().hf_scf_options_default(C.byref(opt))
+    keep = []
+    for k, v in (options or {}).items():
+        if k in ("guess_density_a", "guess_density_b"):
+            if v is not None and not isinstance(v, int):
+                v = v.contiguous().double()
+                keep.append(v)
+                v = int(v.data_ptr())
+            setattr(opt, k, v)
+        else:
+            setattr(opt, k, v)
+    return opt, keep
+
+
+# ROHF coupling constants (A_cc, B_cc, A_oo, B_oo, A_vv, B_vv) by rohf_parameter_name (src/rohf.cu:30-39)
+ROHF_COUPLINGS = {
+    "roothaan": (-0.5, 1.5, 0.5, 0.5, 1.5, -0.5),
+    "mcweeny-diercksen": (1.0 / 3.0, 2.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0, 2.0 / 3.0, 1.0 / 3.0),
+    "davidson": (0.5, 1.0, 0.0, 1.0, 1.0, 0.0),
+    "guest-saunders": (0.5, 0.5, 0.5, 0.5, 0.5, 0.5),
+    "binkley-pople-dobosh": (0.5, 0.5, 1.0, 0.0, 0.0, 1.0),
+    "faegri-manne": (0.5, 0.5, 1.0, 0.0, 0.5, 0.5),
+    "goddard": (0.5, 0.5, 0.5, 0.0, 1.0, 0.0),
+    "plakhutin-gorelik-breslavskaya": (0.0, 1.0, 1.0, 0.0, 1.0, 0.0),
+}
 
 
 class Engine:
@@ -246,10 +280,7 @@ class Engine:
 
     def uhf_scf(self, num_alpha: int, num_beta: int, options: dict | None = None, want_matrices: bool = False):
         """Unrestricted HF (hf_uhf_scf)."""
-        opt = ScfOptions()
-        lib().hf_scf_options_default(C.byref(opt))
-        for k, v in (options or {}).items():
-            setattr(opt, k, v)
+        opt, _keep = _scf_options(self._with_guess(options))
         res = ScfResult()
         outs = [self._empty(self.N, self.N), self._empty(self.N, self.N), self._empty(self.N),
                 self._empty(self.N)] if want_matrices else [None] * 4
@@ -261,6 +292,40 @@ class Engine:
             check(st, "hf_uhf_scf")
         if want_matrices:
             out["density_alpha"], out["density_beta"], out["orbital_energies_alpha"], out["orbital_energies_beta"] = outs
+        return out
+
+    def sad_density(self, source: str = "auto"):
+        """SAD alpha and beta densities of the molecule (CUDA tensors, N x N)."""
+        from . import sad
+
+        a, b = sad.sad_guess(self.mol, self.mol.gbs_filename, source)
+        t = self.torch
+        return t.from_numpy(a).to("cuda"), t.from_numpy(b).to("cuda")
+
+    def _with_guess(self, options: dict | None) -> dict:
+        """initial_guess SAD without densities: assemble them from the atoms."""
+        options = dict(options or {})
+        if options.get("initial_guess") == HF_GUESS_SAD and options.get("guess_density_a") is None:
+            options["guess_density_a"], options["guess_density_b"] = self.sad_density()
+        return options
+
+    def rohf_scf(self, num_alpha: int, num_beta: int, options: dict | None = None, want_matrices: bool = False,
+                 coupling="roothaan"):
+        """Restricted open-shell HF (hf_rohf_scf); coupling: a rohf_parameter_name or six constants."""
+        opt, _keep = _scf_options(self._with_guess(options))
+        cp = ROHF_COUPLINGS[coupling] if isinstance(coupling, str) else tuple(float(c) for c in coupling)
+        cparr = (C.c_double * 6)(*cp)
+        res = ScfResult()
+        outs = [self._empty(self.N, self.N), self._empty(self.N, self.N), self._empty(self.N),
+                self._empty(self.N, self.N)] if want_matrices else [None] * 4
+        st = lib().hf_rohf_scf(self._h, int(num_alpha), int(num_beta), C.cast(cparr, C.c_void_p), C.byref(opt),
+                               C.byref(res), *[_ptr(t) for t in outs])
+        out = {f: getattr(res, f) for f, _ in ScfResult._fields_}
+        out["status"] = st
+        if st not in (0, 4):
+            check(st, "hf_rohf_scf")
+        if want_matrices:
+            out["density_alpha"], out["density_beta"], out["orbital_energies"], out["coefficients"] = outs
         return out
 
     # ------------------------------------------------------------ RI
@@ -306,10 +371,7 @@ class Engine:
         return r
 
     def rhf_scf(self, num_electrons: int, options: dict | None = None, want_matrices: bool = False):
-        opt = ScfOptions()
-        lib().hf_scf_options_default(C.byref(opt))
-        for k, v in (options or {}).items():
-            setattr(opt, k, v)
+        opt, _keep = _scf_options(self._with_guess(options))
         res = ScfResult()
         outs = [self._empty(self.N, self.N), self._empty(self.N, self.N), self._empty(self.N),
                 self._empty(self.N, self.N)] if want_matrices else [None] * 4
@@ -372,12 +434,26 @@ class Batch:
         except Exception:
             pass
 
+    def sad_density(self, source: str = "auto"):
+        """SAD alpha and beta densities of every molecule in the block layout (CUDA tensors)."""
+        import torch
+
+        from . import sad
+
+        pa, pb = [], []
+        for m in self._sorted:
+            a, b = sad.sad_guess(m, m.gbs_filename, source)
+            pa.append(a.ravel())
+            pb.append(b.ravel())
+        return torch.from_numpy(np.concatenate(pa)).to("cuda"), torch.from_numpy(np.concatenate(pb)).to("cuda")
+
     def rhf_scf(self, options: dict | None = None):
-        """Returns (per-molecule result dicts in the caller's order, batch ms, batch iterations)."""
-        opt = ScfOptions()
-        lib().hf_scf_options_default(C.byref(opt))
-        for k, v in (options or {}).items():
-            setattr(opt, k, v)
+        """Returns (per-molecule result dicts in the caller's order, batch ms, batch iterations).
+        initial_guess HF_GUESS_SAD without guess densities assembles them (sad_density)."""
+        options = dict(options or {})
+        if options.get("initial_guess") == HF_GUESS_SAD and options.get("guess_density_a") is None:
+            options["guess_density_a"], options["guess_density_b"] = self.sad_density()
+        opt, _keep = _scf_options(options)
         n = len(self._sorted)
         res = (ScfResult * n)()
         ne = (C.c_int * n)(*[m.num_electrons for m in self._sorted])
@@ -439,15 +515,15 @@ class ParameterManager:
                 self[k] = v
 
 
-class RHF:
-    """Mirror of gansu::RHF (include/rhf.hpp, src/rhf.cu) for the direct,
-    stored and ri ERI methods: ``solve()`` runs the SCF on the GPU.  ``stored``
-    and ``direct`` both run the fused direct build (no N^4 tensor); ``ri``
-    builds Molecular(atoms, auxiliary_gbsfilename) as src/rhf.cu:76-79 does."""
+_GUESSES = {"core": HF_GUESS_CORE, "gwh": HF_GUESS_GWH, "density": HF_GUESS_DENSITY, "sad": HF_GUESS_SAD}
+
+
+class _HFBase:
+    """The parts of gansu::HF (include/hf.hpp, src/hf.cu) shared by the RHF, UHF
+    and ROHF mirrors: parameter checks, the engine (and the auxiliary basis for
+    eri_method ri, src/rhf.cu:76-79), the SCF options and the guess densities."""
 
     def __init__(self, molecular: Molecular, parameters: ParameterManager):
-        if molecular.num_alpha_spins != molecular.num_beta_spins:
-            raise ValueError("In restricted Hartree Fock method, the number of alpha and beta electrons should be equal.")
         self.mol = molecular
         self.params = parameters
         method = parameters["eri_method"]
@@ -455,8 +531,11 @@ class RHF:
             raise ValueError(f"Invalid ERI method name: {method}")
         if parameters["convergence_method"] != "diis":
             raise ValueError("only the DIIS convergence method is provided by this engine")
-        if parameters["initial_guess"] not in ("core", "gwh"):
-            raise ValueError("initial guesses provided by this engine: core, gwh")
+        if parameters["initial_guess"] not in _GUESSES:
+            raise ValueError(f"Invalid initial guess method: {parameters['initial_guess']}")
+        if parameters["initial_guess"] == "sad" and not parameters["gbsfilename"] and \
+                not getattr(molecular, "gbs_filename", ""):
+            raise ValueError("The basis set file is not specified for SAD initial guess method.")
         self.engine = Engine(molecular, parameters.get("schwarz_screening_threshold", float))
         self.eri_method = HF_ERI_RI if method == "ri" else HF_ERI_DIRECT
         if method == "ri":
@@ -465,8 +544,11 @@ class RHF:
             self.engine.set_auxiliary_basis(self.auxiliary)
         self.result = None
 
-    def solve(self) -> float:
+    def _options(self, density_alpha=None, density_beta=None, force_density=False) -> dict:
         p = self.params
+        guess = p["initial_guess"]
+        if force_density:
+            guess = "density"
         opts = {
             "max_iter": p.get("maxiter", int),
             "convergence_threshold": p.get("convergence_energy_threshold", float),
@@ -474,13 +556,19 @@ class RHF:
             "diis_include_transform": int(p.get("diis_include_transform", bool)),
             "precision": HF_PRECISION_MIXED if p["precision"] == "mixed" else HF_PRECISION_FP64,
             "mixed_threshold": p.get("mixed_threshold", float),
-            "incremental": int(p.get("incremental_fock", bool)),
             "verbose": p.get("verbose", int),
             "eri_method": self.eri_method,
-            "initial_guess": 1 if p["initial_guess"] == "gwh" else 0,
+            "initial_guess": _GUESSES[guess],
         }
-        self.result = self.engine.rhf_scf(self.mol.num_electrons, opts, want_matrices=True)
-        return self.result["total_energy"]
+        if guess == "density":
+            if density_alpha is None or density_beta is None:
+                # guess_initial_fock_matrix falls back to the core guess (src/rhf.cu:129-132)
+                opts["initial_guess"] = HF_GUESS_CORE
+            else:
+                t = self.engine.torch
+                opts["guess_density_a"] = t.as_tensor(np.asarray(density_alpha, float).reshape(self.mol.num_basis, -1)).to("cuda")
+                opts["guess_density_b"] = t.as_tensor(np.asarray(density_beta, float).reshape(self.mol.num_basis, -1)).to("cuda")
+        return opts
 
     def get_total_energy(self) -> float:
         return self.result["total_energy"]
@@ -496,36 +584,80 @@ class RHF:
         return (f"Total energy: {r['total_energy']:.12f}\nIterations: {r['iterations']}\n"
                 f"Converged: {bool(r['converged'])}\n")
 
+    def export_sad_cache(self, filename: str = "temp_sad_cache.dat") -> None:
+        """HF::generate_sad_cache (include/hf.hpp:372-405) of the solved molecule."""
+        from . import sad
 
-class UHF:
-    """Mirror of gansu::UHF (include/uhf.hpp, src/uhf.cu) with the direct ERI
-    method: ``solve()`` runs hf_uhf_scf for the molecule's alpha/beta counts."""
+        Da, Db = self.export_density_matrix()
+        sad.export_sad_cache(filename, Da, Db)
+
+
+class RHF(_HFBase):
+    """Mirror of gansu::RHF (include/rhf.hpp, src/rhf.cu): ``solve()`` runs the
+    SCF on the GPU.  ``stored`` and ``direct`` both run the fused direct build
+    (no N^4 tensor); ``ri`` uses Molecular(atoms, auxiliary_gbsfilename).
+    Guesses core / gwh / density / sad (include/rhf.hpp:378-588)."""
 
     def __init__(self, molecular: Molecular, parameters: ParameterManager):
-        self.mol = molecular
-        self.params = parameters
-        if parameters["eri_method"] not in ("stored", "direct"):
-            raise ValueError(f"Invalid ERI method name for UHF: {parameters['eri_method']}")
-        if parameters["convergence_method"] != "diis":
-            raise ValueError("only the DIIS convergence method is provided by this engine")
-        self.engine = Engine(molecular, parameters.get("schwarz_screening_threshold", float))
-        self.result = None
+        if molecular.num_alpha_spins != molecular.num_beta_spins:
+            raise ValueError("In restricted Hartree Fock method, the number of alpha and beta electrons should be equal.")
+        super().__init__(molecular, parameters)
 
-    def solve(self) -> float:
-        p = self.params
-        opts = {
-            "max_iter": p.get("maxiter", int),
-            "convergence_threshold": p.get("convergence_energy_threshold", float),
-            "diis_size": p.get("diis_size", int),
-            "diis_include_transform": int(p.get("diis_include_transform", bool)),
-            "verbose": p.get("verbose", int),
-        }
+    def solve(self, density_matrix_alpha=None, density_matrix_beta=None, force_density: bool = False) -> float:
+        opts = self._options(density_matrix_alpha, density_matrix_beta, force_density)
+        opts["incremental"] = int(self.params.get("incremental_fock", bool))
+        self.result = self.engine.rhf_scf(self.mol.num_electrons, opts, want_matrices=True)
+        return self.result["total_energy"]
+
+    def export_density_matrix(self):
+        """alpha = beta = D/2 (RHF::export_density_matrix)."""
+        D = self.result["density"].double().cpu().numpy()
+        return 0.5 * D, 0.5 * D
+
+
+class UHF(_HFBase):
+    """Mirror of gansu::UHF (include/uhf.hpp, src/uhf.cu): ``solve()`` runs
+    hf_uhf_scf for the molecule's alpha/beta counts (direct or RI)."""
+
+    def solve(self, density_matrix_alpha=None, density_matrix_beta=None, force_density: bool = False) -> float:
+        opts = self._options(density_matrix_alpha, density_matrix_beta, force_density)
         self.result = self.engine.uhf_scf(self.mol.num_alpha_spins, self.mol.num_beta_spins, opts,
                                           want_matrices=True)
         return self.result["total_energy"]
 
-    def get_total_energy(self) -> float:
+    def export_density_matrix(self):
+        return (self.result["density_alpha"].double().cpu().numpy(),
+                self.result["density_beta"].double().cpu().numpy())
+
+
+class ROHF(_HFBase):
+    """Mirror of gansu::ROHF (include/rohf.hpp, src/rohf.cu): ``solve()`` runs
+    hf_rohf_scf with the coupling constants of rohf_parameter_name."""
+
+    def __init__(self, molecular: Molecular, parameters: ParameterManager):
+        name = parameters["rohf_parameter_name"]
+        if name not in ROHF_COUPLINGS:
+            raise ValueError(f"Invalid ROHF parameter name: {name}")
+        if molecular.num_alpha_spins > molecular.num_basis or molecular.num_beta_spins > molecular.num_basis:
+            raise ValueError("The number of alpha or beta electrons should be less than or equal to the number of "
+                             "basis functions.")
+        super().__init__(molecular, parameters)
+        self.coupling = ROHF_COUPLINGS[name]
+
+    def solve(self, density_matrix_alpha=None, density_matrix_beta=None, force_density: bool = False) -> float:
+        opts = self._options(density_matrix_alpha, density_matrix_beta, force_density)
+        self.result = self.engine.rohf_scf(self.mol.num_alpha_spins, self.mol.num_beta_spins, opts,
+                                           want_matrices=True, coupling=self.coupling)
         return self.result["total_energy"]
+
+    def export_density_matrix(self):
+        return (self.result["density_alpha"].double().cpu().numpy(),
+                self.result["density_beta"].double().cpu().numpy())
+
+    def get_total_spin(self) -> float:
+        """S(S+1) with S = (open orbitals)/2 (ROHF::get_total_spin)."""
+        no = self.mol.num_alpha_spins - self.mol.num_beta_spins
+        return (no / 2.0) * (no / 2.0 + 1.0)
 
 
 class HFBuilder:
@@ -534,11 +666,11 @@ class HFBuilder:
     @staticmethod
     def buildHF(parameters: ParameterManager):
         method = parameters["method"]
-        if method not in ("rhf", "uhf"):
-            raise ValueError(f"method {method!r}: this engine provides RHF and UHF")
+        if method not in ("rhf", "uhf", "rohf"):
+            raise ValueError(f"Invalid method: {method}")
         mol = Molecular.from_files(parameters["xyzfilename"], parameters["gbsfilename"],
                                    parameters.get("charge", int), parameters.get("beta_to_alpha", int))
-        return RHF(mol, parameters) if method == "rhf" else UHF(mol, parameters)
+        return {"rhf": RHF, "uhf": UHF, "rohf": ROHF}[method](mol, parameters)
 
     @staticmethod
     def buildOtimizer(parameters: ParameterManager) -> float:

@@ -26,6 +26,8 @@ HF_ERI_DIRECT = 0
 HF_ERI_RI = 1
 HF_GUESS_CORE = 0
 HF_GUESS_GWH = 1
+HF_GUESS_DENSITY = 2
+HF_GUESS_SAD = 3
 HF_EIGEN_SYEVD = 0
 HF_EIGEN_SYEVJ = 1
 HF_EIGEN_PURIFICATION = 2
@@ -68,6 +70,8 @@ class ScfOptions(C.Structure):
         ("eri_method", C.c_int),
         ("anchor_threshold", C.c_double),
         ("initial_guess", C.c_int),
+        ("guess_density_a", C.c_void_p),
+        ("guess_density_b", C.c_void_p),
     ]
 
 
@@ -131,6 +135,7 @@ SIGNATURES = {
     "hf_split_bf16_matmul": (_I, [_P, _P, _P, _I, _I, _I, _I, _P]),
     "hf_engine_create_batch": (_I, [_I, _P, _P, _P, _P, _P, _P, _D, _P]),
     "hf_uhf_scf": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "hf_rohf_scf": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "hf_batch_rhf_scf": (_I, [_P, _P, _P, _P, _P, _P]),
     "hf_scf_options_default": (None, [C.POINTER(ScfOptions)]),
     "hf_rhf_scf": (_I, [_P, _I, C.POINTER(ScfOptions), C.POINTER(ScfResult), _P, _P, _P, _P]),

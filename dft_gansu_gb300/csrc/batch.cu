@@ -14,10 +14,10 @@
 //   * DIIS for every molecule: error F D S - S D F by batched DGEMMs, then one
 //     kernel with a CTA per molecule that updates that molecule's B matrix,
 //     solves the bordered system and extrapolates F.
-// The SCF semantics per molecule are those of the single-molecule loop (core
-// guess, cyclic DIIS from the second stored pair, |dE| convergence); a
-// converged molecule keeps iterating with the batch, its result is the one at
-// its first convergence.
+// The SCF semantics per molecule are those of the single-molecule loop (core,
+// GWH, density or SAD guess, cyclic DIIS from the second stored pair, |dE|
+// convergence); a converged molecule drops out of the Fock build, the DIIS
+// update and the eigensolves, and its result is the one at its convergence.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -84,6 +84,29 @@ __global__ void batch_transform_kernel(const double* __restrict__ W, const doubl
         const double d = (v < 1e-6) ? 0.0 : 1.0 / sqrt(v);
         X[k] = W[base + static_cast<long long>(c) * n + i] * d;
     }
+}
+
+// GWH guess 1.75 S_pq (H_pp + H_qq) / 2 per block (src/gpu_kernels.cu:535-545)
+__global__ void batch_gwh_kernel(const double* __restrict__ H, const double* __restrict__ S, const BlockMap M,
+                                 double* __restrict__ F)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int m = block_of(M, k);
+        const int n = M.n[m];
+        const long long base = M.base[m], r = k - base;
+        const long long p = r / n, q = r % n;
+        F[k] = 1.75 * S[k] * (H[base + p * n + p] + H[base + q * n + q]) * 0.5;
+    }
+}
+
+// D = a (+ b) over the block layout
+__global__ void batch_sum_kernel(const double* __restrict__ a, const double* __restrict__ b, long long ne,
+                                 double* __restrict__ D)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < ne;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        D[k] = a[k] + (b ? b[k] : 0.0);
 }
 
 // G = 2 (J' + J'^T) s s - (K' + K'^T) s s / 2, F = H + G, per block
@@ -539,6 +562,11 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     if (opt_in) opt = *opt_in; else hf_scf_options_default(&opt);
     if (opt.diis_size < 1 || opt.diis_size > kBatchDiis)
         return set_error("diis_size must be in [1, 16]"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.initial_guess < HF_GUESS_CORE || opt.initial_guess > HF_GUESS_SAD)
+        return set_error("initial_guess: core, GWH, density or SAD"), HF_ERR_INVALID_ARGUMENT;
+    const bool density_guess = opt.initial_guess == HF_GUESS_DENSITY || opt.initial_guess == HF_GUESS_SAD;
+    if (density_guess && !opt.guess_density_a)
+        return set_error("initial_guess density/SAD needs guess_density_a (block layout)"), HF_ERR_INVALID_ARGUMENT;
     const int nmol = e.nmol;
     Batch b;
     b.e = &e;
@@ -609,14 +637,28 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     cudaEvent_t l0, l1;
     cudaEventCreate(&l0);
     cudaEventCreate(&l1);
-    // setup: S, H, X = U s^-1/2, core guess
+    // setup: S, H, X = U s^-1/2, guess (core, GWH, density, SAD as in hf_rhf_scf)
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
     GB_CUDA_TRY(cudaMemcpyAsync(w.Fp, w.S, sizeof(double) * ne, cudaMemcpyDeviceToDevice, s));
     if ((st = batch_syev(b, w.Fp, w.eps, s))) return st;
     batch_transform_kernel<<<grid_of(ne), 256, 0, s>>>(w.Fp, w.eps, b.d_ebase, e.block_map(), w.X);
     GB_LAUNCH_CHECK();
-    if ((st = batch_density(b, w.H, s))) return st;
-    if ((st = batch_fock(b, s))) return st;
+    if (density_guess) {
+        batch_sum_kernel<<<grid_of(ne), 256, 0, s>>>(opt.guess_density_a, opt.guess_density_b, ne, w.D);
+        GB_LAUNCH_CHECK();
+        if ((st = batch_fock(b, s))) return st;
+        if (opt.initial_guess == HF_GUESS_SAD && ((st = batch_density(b, w.F, s)) || (st = batch_fock(b, s))))
+            return st;
+    } else {
+        if (opt.initial_guess == HF_GUESS_GWH) {
+            batch_gwh_kernel<<<grid_of(ne), 256, 0, s>>>(w.H, w.S, e.block_map(), w.F);
+            GB_LAUNCH_CHECK();
+            if ((st = batch_density(b, w.F, s))) return st;
+        } else if ((st = batch_density(b, w.H, s))) {
+            return st;
+        }
+        if ((st = batch_fock(b, s))) return st;
+    }
 
     std::vector<double> E(nmol), prev(nmol, std::numeric_limits<double>::max());
     std::vector<int> done_iter(nmol, -1);

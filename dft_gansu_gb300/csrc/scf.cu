@@ -237,6 +237,106 @@ __global__ void gwh_kernel(const double* __restrict__ H, const double* __restric
     }
 }
 
+// out = fa a + fb b (b may be NULL)
+__global__ void combine_kernel(const double* __restrict__ a, double fa, const double* __restrict__ b, double fb,
+                               long long nn, double* __restrict__ out)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        out[k] = fa * a[k] + (b ? fb * b[k] : 0.0);
+}
+
+// InitialGuess_UHF::break_symmetry (include/uhf.hpp:429-436): the last basis function's
+// row and the last orbital's column of the beta coefficients set to zero
+__global__ void break_symmetry_kernel(double* __restrict__ C, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        C[static_cast<long long>(n - 1) * n + i] = 0.0;
+        C[static_cast<long long>(i) * n + (n - 1)] = 0.0;
+    }
+}
+
+// ---- ROHF (src/rohf.cu, src/gpu_kernels.cu:98-139, :351-498)
+// D_c = 2 sum_{o < nc} C_o C_o^T, D_o = sum_{nc <= o < nc + no} C_o C_o^T, D = D_c + D_o
+__global__ void rohf_density_kernel(const double* __restrict__ C, int n, int nc, int no, double* __restrict__ Dc,
+                                    double* __restrict__ Do, double* __restrict__ D)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long i = k / n, j = k % n;
+        double c = 0.0, o = 0.0;
+        for (int q = 0; q < nc; ++q) c += C[i * n + q] * C[j * n + q];
+        for (int q = nc; q < nc + no; ++q) o += C[i * n + q] * C[j * n + q];
+        Dc[k] = 2.0 * c;
+        Do[k] = o;
+        D[k] = 2.0 * c + o;
+    }
+}
+
+// F_c = H + J - K_c/2 - K_o/2, F_o = (H + J - K_c/2 - K_o)/2 with J = J(D_c) + J(D_o)
+__global__ void rohf_fock_kernel(const double* __restrict__ H, const double* __restrict__ Jc,
+                                 const double* __restrict__ Jo, const double* __restrict__ Kc,
+                                 const double* __restrict__ Ko, long long nn, double* __restrict__ Fc,
+                                 double* __restrict__ Fo)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double h = H[k] + Jc[k] + Jo[k] - 0.5 * Kc[k];
+        Fc[k] = h - 0.5 * Ko[k];
+        Fo[k] = 0.5 * (h - Ko[k]);
+    }
+}
+
+struct RohfCoupling {
+    double acc, bcc, aoo, boo, avv, bvv;
+};
+
+// unified Fock matrix in the MO basis from F_c^MO and F_o^MO, by the classes
+// (closed, open, virtual) of the two orbitals; element (i, j) is read at
+// (min, max) and mirrored (computeUnifiedFockMatrix_ROHF_kernel)
+__global__ void rohf_unified_kernel(const double* __restrict__ Fc, const double* __restrict__ Fo, RohfCoupling p,
+                                    int nc, int no, int n, double* __restrict__ R)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int r = static_cast<int>(k / n), c = static_cast<int>(k % n);
+        const int i = min(r, c), j = max(r, c);
+        const long long ij = static_cast<long long>(i) * n + j;
+        const double fc = Fc[ij], fo = Fo[ij];
+        const int ci = (i < nc) ? 0 : (i < nc + no ? 1 : 2);
+        const int cj = (j < nc) ? 0 : (j < nc + no ? 1 : 2);
+        double d;
+        if (ci == 0 && cj == 0) d = 2.0 * (p.acc * fo + p.bcc * (fc - fo));
+        else if (ci == 0 && cj == 1) d = 2.0 * (fc - fo);
+        else if (ci == 0) d = fc;
+        else if (ci == 1 && cj == 1) d = 2.0 * (p.aoo * fo + p.boo * (fc - fo));
+        else if (ci == 1) d = 2.0 * fo;
+        else d = 2.0 * (p.avv * fo + p.bvv * (fc - fo));
+        R[k] = d;
+    }
+}
+
+// ROHF energy 1/2 [<D_c, H + F_c> + <D_o, H> + 2 <D_o, F_o>]
+__global__ void rohf_energy_kernel(const double* __restrict__ Dc, const double* __restrict__ Do,
+                                   const double* __restrict__ H, const double* __restrict__ Fc,
+                                   const double* __restrict__ Fo, long long nn, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x)
+        s += Dc[k] * (H[k] + Fc[k]) + Do[k] * (H[k] + 2.0 * Fo[k]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) *out = 0.5 * s;
+    }
+}
+
 // ---- density by purification (eigensolver 2): no eigenvectors inside the SCF loop
 // Gershgorin interval [lo, hi] of the symmetric F' (one block)
 __global__ void gershgorin_kernel(const double* __restrict__ A, int n, double* __restrict__ out)
@@ -506,6 +606,19 @@ double nuclear_repulsion(const Engine& e)
     return v;
 }
 
+// J(D) and K(D) of one density (standard definitions, N x N each) through the
+// direct kernels or, with use_ri, the RI tensor (J from B, K from the density)
+int jk_of(Engine& e, bool use_ri, const double* D, double* J, double* K, int precision, double mixed_thr,
+          cudaStream_t s)
+{
+    if (!use_ri) return build_jk(e, D, J, K, precision, mixed_thr, s);
+    int r;
+    if ((r = ri_j(e, D, J, s))) return r;
+    return ri_k_density(e, D, K, s);
+}
+
+bool valid_guess(int g) { return g == HF_GUESS_CORE || g == HF_GUESS_GWH || g == HF_GUESS_DENSITY || g == HF_GUESS_SAD; }
+
 }  // namespace
 
 }  // namespace gb
@@ -580,8 +693,11 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
     if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI)
         return set_error("unknown eri_method"), HF_ERR_INVALID_ARGUMENT;
-    if (opt.initial_guess != HF_GUESS_CORE && opt.initial_guess != HF_GUESS_GWH)
-        return set_error("initial_guess: core or GWH"), HF_ERR_INVALID_ARGUMENT;
+    if (!valid_guess(opt.initial_guess))
+        return set_error("initial_guess: core, GWH, density or SAD"), HF_ERR_INVALID_ARGUMENT;
+    const bool density_guess = opt.initial_guess == HF_GUESS_DENSITY || opt.initial_guess == HF_GUESS_SAD;
+    if (density_guess && !opt.guess_density_a)
+        return set_error("initial_guess density/SAD needs guess_density_a"), HF_ERR_INVALID_ARGUMENT;
     const bool use_ri = opt.eri_method == HF_ERI_RI;
     if (use_ri && !e.ri)
         return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
@@ -728,16 +844,37 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         GB_LAUNCH_CHECK();
         return HF_OK;
     };
-    if (opt.initial_guess == HF_GUESS_GWH) {
-        gwh_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, w.S, n, w.E);
+    if (density_guess) {
+        // InitialGuess_RHF_Density: F = F(D_a + D_b); InitialGuess_RHF_SAD then C, D, F
+        // (include/rhf.hpp:440-456, :551-584).  The RI K of a density that is no
+        // aufbau projector comes from the density itself (not the occupied orbitals).
+        combine_kernel<<<grid_nn(nn), 256, 0, s>>>(opt.guess_density_a, 1.0, opt.guess_density_b, 1.0, nn, w.D);
         GB_LAUNCH_CHECK();
-        if ((st = density_from(w.E))) return st;
-    } else if ((st = density_from(w.H))) {
-        return st;
+        if (use_ri) {
+            double *J, *K;
+            if ((st = ri_require_b(e, s)) || (st = ri_work_buffers(e, &J, &K)) ||
+                (st = jk_of(e, true, w.D, J, K, HF_PRECISION_FP64, 0.0, s)) ||
+                (st = ri_fock_from_jk(e, w.H, J, K, nullptr, false, w.F, s)))
+                return st;
+            GB_CUDA_TRY(cudaMemcpyAsync(w.Dprev, w.D, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        } else if ((st = fock_build(true))) {
+            return st;
+        }
+        if (opt.initial_guess == HF_GUESS_SAD) {
+            if ((st = density_from(w.F))) return st;
+            if ((st = fock_build(true))) return st;
+        }
+    } else {
+        if (opt.initial_guess == HF_GUESS_GWH) {
+            gwh_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, w.S, n, w.E);
+            GB_LAUNCH_CHECK();
+            if ((st = density_from(w.E))) return st;
+        } else if ((st = density_from(w.H))) {
+            return st;
+        }
+        if ((st = fock_build(true))) return st;
     }
-    GB_LAUNCH_CHECK();
-    if ((st = fock_build(true))) return st;
-    fock_ms += elapsed(f0, f1);
+    if (!(density_guess && use_ri && opt.initial_guess == HF_GUESS_DENSITY)) fock_ms += elapsed(f0, f1);
     res->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_setup).count();
 
     cudaEvent_t l0, l1;
@@ -848,6 +985,17 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         return set_error("diis_size must be in [1, 16]"), HF_ERR_INVALID_ARGUMENT;
     if (opt.precision != HF_PRECISION_FP64 && opt.precision != HF_PRECISION_MIXED)
         return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
+    if (!valid_guess(opt.initial_guess))
+        return set_error("initial_guess: core, GWH, density or SAD"), HF_ERR_INVALID_ARGUMENT;
+    const bool density_guess = opt.initial_guess == HF_GUESS_DENSITY || opt.initial_guess == HF_GUESS_SAD;
+    if (density_guess && !opt.guess_density_a)
+        return set_error("initial_guess density/SAD needs guess_density_a"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI)
+        return set_error("unknown eri_method"), HF_ERR_INVALID_ARGUMENT;
+    const bool use_ri = opt.eri_method == HF_ERI_RI;
+    if (use_ri && !e.ri)
+        return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
+               HF_ERR_INVALID_ARGUMENT;
     const int m = opt.diis_size;
     int st = ensure_scf(e, m);
     if (st) return st;
@@ -856,6 +1004,7 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     cudaStream_t s = nullptr;
     cublasSetStream(e.cublas, s);
     cusolverDnSetStream(e.cusolver, s);
+    if (use_ri && (st = ri_require_b(e, s))) return st;
     // beta-spin buffers and the two J/K pairs (owned by this call)
     std::vector<void*> owned;
     auto buf = [&](double*& p, size_t count) -> int {
@@ -881,12 +1030,17 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     double* h_energy = nullptr;
     cudaMallocHost(&h_energy, sizeof(double));
 
-    auto densities = [&](const double* FA, const double* FB) -> int {
+    // spin densities from FA and FB; break = the guess's beta symmetry break
+    auto densities = [&](const double* FA, const double* FB, bool brk) -> int {
         int r;
         if ((r = coefficients(e, FA, s, opt.eigensolver))) return r;
         density_factor_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, num_alpha, 1.0, Da);
         GB_LAUNCH_CHECK();
         if ((r = coefficients(e, FB, s, opt.eigensolver))) return r;
+        if (brk) {
+            break_symmetry_kernel<<<(n + 255) / 256, 256, 0, s>>>(w.C, n);
+            GB_LAUNCH_CHECK();
+        }
         density_factor_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, num_beta, 1.0, Db);
         GB_LAUNCH_CHECK();
         GB_CUDA_TRY(cudaMemcpyAsync(epsb, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -894,8 +1048,8 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     };
     auto fock = [&]() -> int {
         int r;
-        if ((r = build_jk(e, Da, Ja, Ka, opt.precision, opt.mixed_threshold, s))) return r;
-        if ((r = build_jk(e, Db, Jb, Kb, opt.precision, opt.mixed_threshold, s))) return r;
+        if ((r = jk_of(e, use_ri, Da, Ja, Ka, opt.precision, opt.mixed_threshold, s))) return r;
+        if ((r = jk_of(e, use_ri, Db, Jb, Kb, opt.precision, opt.mixed_threshold, s))) return r;
         uhf_fock_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, Ja, Jb, Ka, Kb, nn, Fa, Fb);
         GB_LAUNCH_CHECK();
         return HF_OK;
@@ -903,16 +1057,26 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     cudaEvent_t l0, l1;
     cudaEventCreate(&l0);
     cudaEventCreate(&l1);
-    // core Hamiltonian, X, core guess for both spins
+    // core Hamiltonian, X, guess (InitialGuess_UHF_Core / _GWH / _Density / _SAD,
+    // include/uhf.hpp:484-620): orbitals for both spins with the beta symmetry break
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
     transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
     GB_LAUNCH_CHECK();
-    if (opt.initial_guess == HF_GUESS_GWH) {
+    if (density_guess) {
+        // D_a, D_b given (D_b NULL: both halves of D_a); F, C, break, D, F
+        combine_kernel<<<grid_nn(nn), 256, 0, s>>>(opt.guess_density_a, opt.guess_density_b ? 1.0 : 0.5, nullptr,
+                                                    0.0, nn, Da);
+        combine_kernel<<<grid_nn(nn), 256, 0, s>>>(opt.guess_density_b ? opt.guess_density_b : opt.guess_density_a,
+                                                    opt.guess_density_b ? 1.0 : 0.5, nullptr, 0.0, nn, Db);
+        GB_LAUNCH_CHECK();
+        if ((st = fock())) return st;
+        if ((st = densities(Fa, Fb, true))) return st;
+    } else if (opt.initial_guess == HF_GUESS_GWH) {
         gwh_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, w.S, n, w.E);
         GB_LAUNCH_CHECK();
-        if ((st = densities(w.E, w.E))) return st;
-    } else if ((st = densities(w.H, w.H))) {
+        if ((st = densities(w.E, w.E, true))) return st;
+    } else if ((st = densities(w.H, w.H, true))) {
         return st;
     }
     if ((st = fock())) return st;
@@ -921,7 +1085,7 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     int iter = 0, diis_iter = 0;
     bool converged = false;
     while (iter < opt.max_iter) {
-        if ((st = densities(Fa, Fb))) return st;
+        if ((st = densities(Fa, Fb, false))) return st;
         if ((st = fock())) return st;
         uhf_energy_kernel<<<1, 1024, 0, s>>>(Da, Db, w.H, Fa, Fb, nn, e.d_scalar + 4);
         GB_LAUNCH_CHECK();
@@ -967,6 +1131,197 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_b_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
     }
     return converged ? HF_OK : (set_error("UHF did not converge"), HF_ERR_NOT_CONVERGED);
+}
+
+
+int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupling, const hf_scf_options* opt_in,
+                hf_scf_result* res, double* d_density_a_out, double* d_density_b_out, double* d_orbital_energies_out,
+                double* d_coefficients_out)
+{
+    clear_error();
+    if (!eng || !res) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    if (e.nmol != 1) return set_error("hf_rohf_scf: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
+    hf_scf_options opt;
+    if (opt_in) opt = *opt_in; else hf_scf_options_default(&opt);
+    const int n = e.num_basis;
+    if (num_beta < 0 || num_alpha < num_beta || num_alpha == 0 || num_alpha > n)
+        return set_error("hf_rohf_scf: needs 0 <= num_beta <= num_alpha <= N, num_alpha > 0"),
+               HF_ERR_INVALID_ARGUMENT;
+    if (opt.diis_size < 1 || opt.diis_size > kMaxDiis)
+        return set_error("diis_size must be in [1, 16]"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.precision != HF_PRECISION_FP64 && opt.precision != HF_PRECISION_MIXED)
+        return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
+    if (!valid_guess(opt.initial_guess))
+        return set_error("initial_guess: core, GWH, density or SAD"), HF_ERR_INVALID_ARGUMENT;
+    const bool density_guess = opt.initial_guess == HF_GUESS_DENSITY || opt.initial_guess == HF_GUESS_SAD;
+    if (density_guess && (!opt.guess_density_a || !opt.guess_density_b))
+        return set_error("ROHF initial_guess density/SAD needs guess_density_a and _b"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI)
+        return set_error("unknown eri_method"), HF_ERR_INVALID_ARGUMENT;
+    const bool use_ri = opt.eri_method == HF_ERI_RI;
+    if (use_ri && !e.ri)
+        return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
+               HF_ERR_INVALID_ARGUMENT;
+    // Roothaan's constants by default (rohf_parameter_name = roothaan, src/rohf.cu:31)
+    RohfCoupling cp{-0.5, 1.5, 0.5, 0.5, 1.5, -0.5};
+    if (coupling) cp = RohfCoupling{coupling[0], coupling[1], coupling[2], coupling[3], coupling[4], coupling[5]};
+    const int nc = num_beta, no = num_alpha - num_beta;
+    const int m = opt.diis_size;
+    int st = ensure_scf(e, m);
+    if (st) return st;
+    auto& w = e.scf;
+    const long long nn = static_cast<long long>(n) * n;
+    cudaStream_t s = nullptr;
+    cublasSetStream(e.cublas, s);
+    cusolverDnSetStream(e.cusolver, s);
+    if (use_ri && (st = ri_require_b(e, s))) return st;
+    std::vector<void*> owned;
+    struct Free {
+        std::vector<void*>& v;
+        ~Free() { for (void* p : v) cudaFree(p); }
+    } guard{owned};
+    auto buf = [&](double*& p, size_t count) -> int {
+        if (cudaMalloc(&p, count * sizeof(double)) != cudaSuccess)
+            return set_error("cudaMalloc (ROHF) failed"), HF_ERR_OUT_OF_MEMORY;
+        owned.push_back(p);
+        return HF_OK;
+    };
+    double *Dc = nullptr, *Do = nullptr, *Fc = nullptr, *Fo = nullptr, *Jc = nullptr, *Kc = nullptr, *Jo = nullptr,
+           *Ko = nullptr, *R = nullptr;
+    if ((st = buf(Dc, nn)) || (st = buf(Do, nn)) || (st = buf(Fc, nn)) || (st = buf(Fo, nn)) || (st = buf(Jc, nn)) ||
+        (st = buf(Kc, nn)) || (st = buf(Jo, nn)) || (st = buf(Ko, nn)) || (st = buf(R, nn)))
+        return st;
+    *res = hf_scf_result{};
+    res->nuclear_repulsion = nuclear_repulsion(e);
+    GB_CUDA_TRY(cudaMemsetAsync(w.info, 0, 4 * sizeof(int), s));
+    double* h_energy = nullptr;
+    cudaMallocHost(&h_energy, sizeof(double));
+    struct FreeHost {
+        double* p;
+        ~FreeHost() { cudaFreeHost(p); }
+    } host_guard{h_energy};
+
+    auto density = [&]() -> int {
+        rohf_density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nc, no, Dc, Do, w.D);
+        GB_LAUNCH_CHECK();
+        return HF_OK;
+    };
+    // F_c, F_o from D_c, D_o; the unified F = S C R C^T S from the current orbitals C
+    auto fock = [&]() -> int {
+        int r;
+        if ((r = jk_of(e, use_ri, Dc, Jc, Kc, opt.precision, opt.mixed_threshold, s))) return r;
+        if (no > 0) {
+            if ((r = jk_of(e, use_ri, Do, Jo, Ko, opt.precision, opt.mixed_threshold, s))) return r;
+        } else {
+            GB_CUDA_TRY(cudaMemsetAsync(Jo, 0, nn * sizeof(double), s));
+            GB_CUDA_TRY(cudaMemsetAsync(Ko, 0, nn * sizeof(double), s));
+        }
+        rohf_fock_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, Jc, Jo, Kc, Ko, nn, Fc, Fo);
+        GB_LAUNCH_CHECK();
+        // C^T F_c C and C^T F_o C (Jc, Jo reused as the MO-basis matrices)
+        if ((r = gemm_rm(e.cublas, true, false, n, w.C, Fc, w.T1)) ||
+            (r = gemm_rm(e.cublas, false, false, n, w.T1, w.C, Jc)) ||
+            (r = gemm_rm(e.cublas, true, false, n, w.C, Fo, w.T1)) ||
+            (r = gemm_rm(e.cublas, false, false, n, w.T1, w.C, Jo)))
+            return r;
+        rohf_unified_kernel<<<grid_nn(nn), 256, 0, s>>>(Jc, Jo, cp, nc, no, n, R);
+        GB_LAUNCH_CHECK();
+        // T1 = S C, T2 = T1 R, F = T2 T1^T
+        if ((r = gemm_rm(e.cublas, false, false, n, w.S, w.C, w.T1)) ||
+            (r = gemm_rm(e.cublas, false, false, n, w.T1, R, w.T2)) ||
+            (r = gemm_rm(e.cublas, false, true, n, w.T2, w.T1, w.F)))
+            return r;
+        return HF_OK;
+    };
+    // core Hamiltonian, X, guess (InitialGuess_ROHF_Core / _GWH / _Density / _SAD,
+    // include/rohf.hpp:416-600).  For the density guesses the first unified Fock
+    // matrix is formed with the core-guess orbitals.
+    if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
+    if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
+    transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
+    GB_LAUNCH_CHECK();
+    if (density_guess) {
+        if ((st = coefficients(e, w.H, s, opt.eigensolver))) return st;
+        combine_kernel<<<grid_nn(nn), 256, 0, s>>>(opt.guess_density_b, 2.0, nullptr, 0.0, nn, Dc);
+        combine_kernel<<<grid_nn(nn), 256, 0, s>>>(opt.guess_density_a, 1.0, opt.guess_density_b, -1.0, nn, Do);
+        GB_LAUNCH_CHECK();
+        if ((st = fock())) return st;
+        if ((st = coefficients(e, w.F, s, opt.eigensolver))) return st;
+    } else if (opt.initial_guess == HF_GUESS_GWH) {
+        gwh_kernel<<<grid_nn(nn), 256, 0, s>>>(w.H, w.S, n, w.E);
+        GB_LAUNCH_CHECK();
+        if ((st = coefficients(e, w.E, s, opt.eigensolver))) return st;
+    } else if ((st = coefficients(e, w.H, s, opt.eigensolver))) {
+        return st;
+    }
+    if ((st = density()) || (st = fock())) return st;
+
+    cudaEvent_t l0, l1;
+    cudaEventCreate(&l0);
+    cudaEventCreate(&l1);
+    cudaEventRecord(l0, s);
+    double prev = std::numeric_limits<double>::max(), energy = 0.0;
+    int iter = 0, diis_iter = 0;
+    bool converged = false;
+    while (iter < opt.max_iter) {
+        if ((st = coefficients(e, w.F, s, opt.eigensolver)) || (st = density()) || (st = fock())) break;
+        rohf_energy_kernel<<<1, 1024, 0, s>>>(Dc, Do, w.H, Fc, Fo, nn, e.d_scalar + 4);
+        if (cudaGetLastError() != cudaSuccess) { st = (set_error("rohf_energy_kernel launch failed"), HF_ERR_CUDA); break; }
+        if (cudaMemcpyAsync(h_energy, e.d_scalar + 4, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            st = (set_error("ROHF energy read failed"), HF_ERR_CUDA);
+            break;
+        }
+        energy = *h_energy;
+        if (opt.verbose)
+            std::printf("---- Iteration: %d ----  Energy: %.17g Total energy: %.17g\n", iter, energy,
+                        energy + res->nuclear_repulsion);
+        if (!std::isfinite(energy)) { st = (set_error("ROHF energy is not finite"), HF_ERR_NOT_CONVERGED); break; }
+        if (std::fabs(energy - prev) < opt.convergence_threshold) { converged = true; break; }
+        ++iter;
+        prev = energy;
+        // Convergence_ROHF_DIIS (include/rohf.hpp:307-360): unified F with D = D_c + D_o
+        const int slot = diis_iter % m;
+        if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, opt.diis_include_transform != 0, s))) break;
+        if (cudaMemcpyAsync(w.Fs + slot * nn, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+            st = (set_error("cudaMemcpyAsync failed"), HF_ERR_CUDA);
+            break;
+        }
+        const int nprev = std::min(diis_iter + 1, m);
+        if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, w.F, s))) break;
+        ++diis_iter;
+    }
+    cudaEventRecord(l1, s);
+    cudaEventSynchronize(l1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, l0, l1);
+    cudaEventDestroy(l0);
+    cudaEventDestroy(l1);
+    if (st) return st;
+    res->scf_ms_total = ms;
+    res->electronic_energy = energy;
+    res->total_energy = energy + res->nuclear_repulsion;
+    res->iterations = iter;
+    res->converged = converged ? 1 : 0;
+    int info[4] = {0, 0, 0, 0};
+    GB_CUDA_TRY(cudaMemcpy(info, w.info, sizeof(info), cudaMemcpyDeviceToHost));
+    if (info[0] != 0) return set_error("syevd reported info " + std::to_string(info[0])), HF_ERR_SOLVER;
+    // export_density_matrix (src/rohf.cu:288-315): alpha = D_c/2 + D_o, beta = D_c/2
+    if (d_density_a_out) {
+        combine_kernel<<<grid_nn(nn), 256, 0, s>>>(Dc, 0.5, Do, 1.0, nn, d_density_a_out);
+        GB_LAUNCH_CHECK();
+    }
+    if (d_density_b_out) {
+        combine_kernel<<<grid_nn(nn), 256, 0, s>>>(Dc, 0.5, nullptr, 0.0, nn, d_density_b_out);
+        GB_LAUNCH_CHECK();
+    }
+    if (d_orbital_energies_out)
+        GB_CUDA_TRY(cudaMemcpyAsync(d_orbital_energies_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (d_coefficients_out)
+        GB_CUDA_TRY(cudaMemcpyAsync(d_coefficients_out, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return converged ? HF_OK : (set_error("ROHF did not converge"), HF_ERR_NOT_CONVERGED);
 }
 
 }  // extern "C"

@@ -232,7 +232,11 @@ typedef struct {
     double anchor_threshold;        /* mixed tier: low-precision full builds (direct: all quartets FP32; RI:
                                        split-BF16 K) while max|dD| >= this, then one FP64 build, then
                                        incremental builds; 0 = the first build is the FP64 one */
-    int initial_guess;              /* HF_GUESS_CORE or HF_GUESS_GWH (initial_guess = core / gwh) */
+    int initial_guess;              /* HF_GUESS_CORE / _GWH / _DENSITY / _SAD (initial_guess = core / gwh /
+                                       density / sad) */
+    const double* guess_density_a;  /* HF_GUESS_DENSITY / HF_GUESS_SAD: device alpha-spin density (N x N;
+                                       a batch engine: the block layout); RHF takes D_a + D_b */
+    const double* guess_density_b;  /* beta-spin density, same layout; NULL for RHF means D_a is the total */
 } hf_scf_options;
 
 /* Density from the Fock matrix inside the SCF loop.  The reference diagonalises
@@ -247,10 +251,19 @@ enum {
     HF_EIGEN_PURIFICATION = 2
 };
 
-/* Initial guess (InitialGuess_RHF_Core / _GWH, include/rhf.hpp:378-588). */
+/* Initial guess (InitialGuess_RHF_Core / _GWH / _Density / _SAD, include/rhf.hpp:378-588;
+ * the UHF and ROHF classes of include/uhf.hpp and include/rohf.hpp).  DENSITY and SAD
+ * start from the caller's densities (options.guess_density_a/_b); the SAD density is
+ * the block-diagonal superposition of atomic densities that the host assembles
+ * (read_density_from_sad, src/utils.cpp:21-56, or atomic RHF/ROHF solves).
+ *   RHF   DENSITY: F = F(D_a + D_b);  SAD: F(D), C, D, F
+ *   UHF   DENSITY = SAD: F(D_a, D_b), C, beta symmetry break, D, F
+ *   ROHF  DENSITY = SAD: D_closed = 2 D_b, D_open = D_a - D_b, F, C, D, F */
 enum {
-    HF_GUESS_CORE = 0,  /* diagonalise H */
-    HF_GUESS_GWH = 1    /* diagonalise 1.75 S_pq (H_pp + H_qq) / 2 (src/gpu_kernels.cu:535-545) */
+    HF_GUESS_CORE = 0,     /* diagonalise H */
+    HF_GUESS_GWH = 1,      /* diagonalise 1.75 S_pq (H_pp + H_qq) / 2 (src/gpu_kernels.cu:535-545) */
+    HF_GUESS_DENSITY = 2,  /* the given density (initial_guess = density) */
+    HF_GUESS_SAD = 3       /* the given superposition of atomic densities (initial_guess = sad) */
 };
 
 /* Two-electron backend of the SCF. */
@@ -288,13 +301,32 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt, hf_
 /* Unrestricted HF on the device (UHF::solve, src/uhf.cu; Convergence_UHF_DIIS,
  * include/uhf.hpp:291-380): spin densities D_s = C_s,occ C_s,occ^T, Fock
  * F_a = H + J(D_a + D_b) - K(D_a) (and b), energy 1/2 sum[(D_a + D_b) H + D_a F_a
- * + D_b F_b], core guess for both spins, one DIIS ring per spin on the same
- * cyclic index, |dE| convergence.  Two direct J/K builds per iteration.
+ * + D_b F_b], guess orbitals for both spins with the beta symmetry break of
+ * InitialGuess_UHF::break_symmetry (include/uhf.hpp:429-436: the last basis
+ * function's row and the last orbital's column of C_b zeroed), one DIIS ring per
+ * spin on the same cyclic index, |dE| convergence.  Two direct J/K builds per
+ * iteration.
  * Outputs (may be NULL): spin densities and the orbital energies of the final
  * Fock matrices. */
 int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options* opt, hf_scf_result* result,
                double* d_density_a_out, double* d_density_b_out, double* d_orbital_energies_a_out,
                double* d_orbital_energies_b_out);
+
+/* Restricted open-shell HF on the device (ROHF::solve, src/rohf.cu; Fock build
+ * computeFockMatrix_ROHF, src/gpu_manager.cu:733-817).  num_beta closed and
+ * num_alpha - num_beta open orbitals; D_closed = 2 C_c C_c^T, D_open = C_o C_o^T;
+ * F_c = H + J(D) - K(D_c)/2 - K(D_o)/2, F_o = (H + J(D) - K(D_c)/2 - K(D_o))/2
+ * (D = D_c + D_o); the unified Fock matrix R in the MO basis from C^T F_c C and
+ * C^T F_o C with the coupling constants coupling[6] = {A_cc, B_cc, A_oo, B_oo,
+ * A_vv, B_vv} (NULL: Roothaan, src/rohf.cu:30-39), back to the AO basis as
+ * S C R C^T S; energy 1/2 [<D_c, H + F_c> + <D_o, H> + 2 <D_o, F_o>]; DIIS on the
+ * unified F with D.  Two direct J/K builds per iteration.  Outputs (device, may
+ * be NULL): alpha = D_c/2 + D_o and beta = D_c/2 densities (export_density_matrix,
+ * src/rohf.cu:288-315), orbital energies and coefficients of the last
+ * diagonalised unified Fock matrix. */
+int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupling, const hf_scf_options* opt,
+                hf_scf_result* result, double* d_density_a_out, double* d_density_b_out,
+                double* d_orbital_energies_out, double* d_coefficients_out);
 
 /* ---------------------------------------------------------------- batch */
 /* One engine over many independent molecules (no reference counterpart: the

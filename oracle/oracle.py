@@ -322,12 +322,21 @@ def gwh_guess(S, H):
     return 1.75 * S * (d[:, None] + d[None, :]) * 0.5
 
 
-def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False, guess="core"):
-    """The reference SCF loop (src/hf.cu:278-307) with the core (or GWH) guess and DIIS."""
+def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False, guess="core",
+        guess_density=None):
+    """The reference SCF loop (src/hf.cu:278-307) with DIIS and the core, GWH,
+    density (F = F(D)) or SAD (F(D), C, D, F) guess (include/rhf.hpp:378-588);
+    guess_density is the total density D_a + D_b."""
     X = transform_matrix(S)
-    _, Cm = coefficients(gwh_guess(S, H) if guess == "gwh" else H, X)
-    D = density(Cm, nocc)
-    F = fock(D)
+    if guess in ("density", "sad"):
+        F = fock(guess_density)
+        if guess == "sad":
+            _, Cm = coefficients(F, X)
+            F = fock(density(Cm, nocc))
+    else:
+        _, Cm = coefficients(gwh_guess(S, H) if guess == "gwh" else H, X)
+        D = density(Cm, nocc)
+        F = fock(D)
     prev, energy, it, diis_it = np.finfo(float).max, 0.0, 0, 0
     errs, focks = [None] * diis_size, [None] * diis_size
     eps = None
@@ -357,17 +366,38 @@ def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_tran
             "orbital_energies": eps, "density": D, "fock": F, "history": history}
 
 
-def uhf(S, H, jk, na, nb, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False):
+def break_symmetry(Cb):
+    """InitialGuess_UHF::break_symmetry (include/uhf.hpp:429-436): the last basis
+    function's row and the last orbital's column of the beta coefficients zeroed."""
+    Cb = Cb.copy()
+    Cb[-1, :] = 0.0
+    Cb[:, -1] = 0.0
+    return Cb
+
+
+def uhf(S, H, jk, na, nb, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False, guess="core",
+        guess_density=None):
     """The reference UHF loop (src/uhf.cu, Convergence_UHF_DIIS include/uhf.hpp:291-380):
-    core guess for both spins, F_s = H + J(Da + Db) - K(D_s), one DIIS ring per spin."""
+    F_s = H + J(Da + Db) - K(D_s), one DIIS ring per spin.  Guesses
+    (include/uhf.hpp:484-620): core / GWH orbitals for both spins with the beta
+    symmetry break; density / SAD: F(Da, Db), C, break, D, F."""
     X = transform_matrix(S)
-    _, Cm = coefficients(H, X)
-    Da, Db = Cm[:, :na] @ Cm[:, :na].T, Cm[:, :nb] @ Cm[:, :nb].T
 
     def fock(Da, Db):
         Ja, Ka = jk(Da)
         Jb, Kb = jk(Db)
         return H + Ja + Jb - Ka, H + Ja + Jb - Kb
+
+    if guess in ("density", "sad"):
+        Da, Db = guess_density
+        Fa, Fb = fock(Da, Db)
+        _, Ca = coefficients(Fa, X)
+        _, Cb = coefficients(Fb, X)
+    else:
+        _, Ca = coefficients(gwh_guess(S, H) if guess == "gwh" else H, X)
+        Cb = Ca
+    Cb = break_symmetry(Cb)
+    Da, Db = Ca[:, :na] @ Ca[:, :na].T, Cb[:, :nb] @ Cb[:, :nb].T
     Fa, Fb = fock(Da, Db)
     prev, energy, it, diis_it = np.finfo(float).max, 0.0, 0, 0
     ring = {"a": ([None] * diis_size, [None] * diis_size), "b": ([None] * diis_size, [None] * diis_size)}
@@ -397,6 +427,180 @@ def uhf(S, H, jk, na, nb, enuc, maxiter=100, thr=1e-6, diis_size=8, include_tran
         diis_it += 1
     return {"electronic_energy": energy, "total_energy": energy + enuc, "iterations": it, "converged": converged,
             "density_alpha": Da, "density_beta": Db}
+
+
+# ROHF coupling constants (A_cc, B_cc, A_oo, B_oo, A_vv, B_vv), src/rohf.cu:30-39
+ROHF_COUPLINGS = {
+    "roothaan": (-0.5, 1.5, 0.5, 0.5, 1.5, -0.5),
+    "mcweeny-diercksen": (1 / 3, 2 / 3, 1 / 3, 1 / 3, 2 / 3, 1 / 3),
+    "davidson": (0.5, 1.0, 0.0, 1.0, 1.0, 0.0),
+    "guest-saunders": (0.5, 0.5, 0.5, 0.5, 0.5, 0.5),
+    "binkley-pople-dobosh": (0.5, 0.5, 1.0, 0.0, 0.0, 1.0),
+    "faegri-manne": (0.5, 0.5, 1.0, 0.0, 0.5, 0.5),
+    "goddard": (0.5, 0.5, 0.5, 0.0, 1.0, 0.0),
+    "plakhutin-gorelik-breslavskaya": (0.0, 1.0, 1.0, 0.0, 1.0, 0.0),
+}
+
+
+def rohf_unified(Fc_mo, Fo_mo, nc, no, coupling):
+    """computeUnifiedFockMatrix_ROHF_kernel (src/gpu_kernels.cu:421-498): the MO-basis
+    unified Fock matrix by orbital classes, element (i, j) read at (min, max)."""
+    acc, bcc, aoo, boo, avv, bvv = coupling
+    n = Fc_mo.shape[0]
+    cls = np.where(np.arange(n) < nc, 0, np.where(np.arange(n) < nc + no, 1, 2))
+    R = np.zeros((n, n))
+    for i in range(n):
+        for j in range(i, n):
+            fc, fo = Fc_mo[i, j], Fo_mo[i, j]
+            a, b = cls[i], cls[j]
+            if a == 0 and b == 0:
+                d = 2.0 * (acc * fo + bcc * (fc - fo))
+            elif a == 0 and b == 1:
+                d = 2.0 * (fc - fo)
+            elif a == 0:
+                d = fc
+            elif a == 1 and b == 1:
+                d = 2.0 * (aoo * fo + boo * (fc - fo))
+            elif a == 1:
+                d = 2.0 * fo
+            else:
+                d = 2.0 * (avv * fo + bvv * (fc - fo))
+            R[i, j] = R[j, i] = d
+    return R
+
+
+def rohf(S, H, jk, na, nb, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False, guess="core",
+         guess_density=None, coupling="roothaan"):
+    """The reference ROHF (src/rohf.cu; computeFockMatrix_ROHF, src/gpu_manager.cu:733-817;
+    energy :871-884; Convergence_ROHF_DIIS include/rohf.hpp:307-360):
+    D_c = 2 C_c C_c^T, D_o = C_o C_o^T; F_c = H + J(D) - K(D_c)/2 - K(D_o)/2,
+    F_o = (H + J(D) - K(D_c)/2 - K(D_o))/2; unified R from C^T F_c C, C^T F_o C;
+    F = S C R C^T S; DIIS on F with D = D_c + D_o.  Density / SAD guess: D_c = 2 D_b,
+    D_o = D_a - D_b, first unified F with the core-guess orbitals, then C, D, F."""
+    cp = ROHF_COUPLINGS[coupling] if isinstance(coupling, str) else tuple(coupling)
+    nc, no = nb, na - nb
+    X = transform_matrix(S)
+
+    def dens(Cm):
+        Dc = 2.0 * Cm[:, :nc] @ Cm[:, :nc].T
+        Do = Cm[:, nc:nc + no] @ Cm[:, nc:nc + no].T
+        return Dc, Do
+
+    def fock(Dc, Do, Cm):
+        Jc, Kc = jk(Dc)
+        Jo, Ko = jk(Do) if no > 0 else (np.zeros_like(Dc), np.zeros_like(Dc))
+        h = H + Jc + Jo - 0.5 * Kc
+        Fc, Fo = h - 0.5 * Ko, 0.5 * (h - Ko)
+        R = rohf_unified(Cm.T @ Fc @ Cm, Cm.T @ Fo @ Cm, nc, no, cp)
+        SC = S @ Cm
+        return Fc, Fo, SC @ R @ SC.T
+
+    if guess in ("density", "sad"):
+        Da, Db = guess_density
+        _, Cm = coefficients(H, X)
+        _, _, F = fock(2.0 * Db, Da - Db, Cm)
+        _, Cm = coefficients(F, X)
+    else:
+        _, Cm = coefficients(gwh_guess(S, H) if guess == "gwh" else H, X)
+    Dc, Do = dens(Cm)
+    Fc, Fo, F = fock(Dc, Do, Cm)
+    prev, energy, it, diis_it = np.finfo(float).max, 0.0, 0, 0
+    errs, focks = [None] * diis_size, [None] * diis_size
+    converged = False
+    eps = None
+    while it < maxiter:
+        eps, Cm = coefficients(F, X)
+        Dc, Do = dens(Cm)
+        Fc, Fo, F = fock(Dc, Do, Cm)
+        energy = 0.5 * (np.vdot(Dc, H + Fc) + np.vdot(Do, H) + 2.0 * np.vdot(Do, Fo))
+        if abs(energy - prev) < thr:
+            converged = True
+            break
+        it += 1
+        prev = energy
+        D = Dc + Do
+        e = F @ D @ S - S @ D @ F
+        if include_transform:
+            e = X @ e @ X.T
+        slot = diis_it % diis_size
+        errs[slot], focks[slot] = e, F.copy()
+        nprev = min(diis_it + 1, diis_size)
+        if nprev > 1:
+            F = diis_extrapolate(errs[:nprev], focks[:nprev])
+        diis_it += 1
+    return {"electronic_energy": energy, "total_energy": energy + enuc, "iterations": it, "converged": converged,
+            "density_alpha": 0.5 * Dc + Do, "density_beta": 0.5 * Dc, "orbital_energies": eps}
+
+
+def rohf_from_basis(b: Basis, na: int, nb: int, thr_schwarz=1e-12, **kw):
+    S, T, V = one_electron(b)
+    eri = eri_tensor(b, thr_schwarz)
+    jk = lambda D: (np.einsum("ijkl,kl->ij", eri, D), np.einsum("ikjl,kl->ij", eri, D))
+    return rohf(S, T + V, jk, na, nb, nuclear_repulsion(b.atoms), **kw)
+
+
+# ------------------------------------------------------------ SAD
+def read_sad(path):
+    """Parse a .sad file (read_density_from_sad, src/utils.cpp:21-56): blocks of
+    "<element> <n>" followed by n rows of the alpha density and n rows of the beta
+    density (row-major).  Returns {element: (Da, Db)}."""
+    out = {}
+    toks = open(path).read().split()
+    i = 0
+    while i < len(toks):
+        el, n = toks[i], int(toks[i + 1])
+        i += 2
+        vals = np.array(toks[i:i + 2 * n * n], float)
+        i += 2 * n * n
+        out[el] = (vals[:n * n].reshape(n, n), vals[n * n:].reshape(n, n))
+    return out
+
+
+def atom_ranges(b: Basis):
+    """(start, count) of every atom's basis functions (get_atom_to_basis_range)."""
+    ranges = []
+    for ia in range(len(b.atoms)):
+        sh = np.nonzero(b.shell_atom == ia)[0]
+        start = int(b.bf_off[sh[0]])
+        count = int(sum((int(b.l[k]) + 1) * (int(b.l[k]) + 2) // 2 for k in sh))
+        ranges.append((start, count))
+    return ranges
+
+
+def sad_density(b: Basis, atom_densities):
+    """Block-diagonal alpha and beta densities (InitialGuess_RHF_SAD::guess,
+    include/rhf.hpp:551-584); atom_densities maps an atomic number to (Da, Db)."""
+    Da = np.zeros((b.nbf, b.nbf))
+    Db = np.zeros((b.nbf, b.nbf))
+    for (z, *_), (st, cnt) in zip(b.atoms, atom_ranges(b)):
+        a, bb = atom_densities[z]
+        assert a.shape == (cnt, cnt)
+        Da[st:st + cnt, st:st + cnt] = a
+        Db[st:st + cnt, st:st + cnt] = bb
+    return Da, Db
+
+
+def atom_sad_density(z, gbs_path, thr=1e-10, maxiter=200):
+    """The atomic density of a .sad file as the reference's generator makes it
+    (script/generate_sad_cache.py: even Z -> RHF, odd Z -> ROHF doublet; core
+    guess, stored ERIs): returns (Da, Db)."""
+    b = make_basis([(z, 0.0, 0.0, 0.0)], gbs_path)
+    ne = z
+    if ne % 2 == 0:
+        r = rhf_from_basis(b, thr=thr, maxiter=maxiter)
+        D = r["density"]
+        return 0.5 * D, 0.5 * D
+    r = rohf_from_basis(b, (ne + 1) // 2, (ne - 1) // 2, thr=thr, maxiter=maxiter)
+    return r["density_alpha"], r["density_beta"]
+
+
+def uhf_energy_of(S, H, jk, Da, Db):
+    """1/2 [<Da + Db, H> + <Da, Fa> + <Db, Fb>] of given spin densities (equals the
+    ROHF energy when Da = D_c/2 + D_o, Db = D_c/2, and the RHF one when Da = Db)."""
+    Ja, Ka = jk(Da)
+    Jb, Kb = jk(Db)
+    Fa, Fb = H + Ja + Jb - Ka, H + Ja + Jb - Kb
+    return 0.5 * (np.vdot(Da + Db, H) + np.vdot(Da, Fa) + np.vdot(Db, Fb))
 
 
 def uhf_from_basis(b: Basis, na: int, nb: int, thr_schwarz=1e-12, **kw):

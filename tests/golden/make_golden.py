@@ -6,6 +6,7 @@ committed so that the tests need neither the reference nor this script.
 
     python tests/golden/make_golden.py          # all fixtures
     python tests/golden/make_golden.py --ri     # the RI fixtures only
+    python tests/golden/make_golden.py --sad    # the SAD fixture only
 """
 import sys
 from pathlib import Path
@@ -91,7 +92,31 @@ def main_ri():
         print(f"{name}: N={b.nbf} naux={ax.nbf} E_RI={scf['total_energy']:.10f} iters={scf['iterations']}")
 
 
+SAD_BASES = ("sto-3g", "6-31g")
+SAD_ELEMENTS = ("H", "C", "N", "O")
+
+
+def main_sad():
+    """The reference's atomic SAD densities (basis/<name>.sad, the output of its
+    atomic RHF/ROHF solves) of H, C, N, O for the s/p basis sets, as data."""
+    import os
+
+    ref = Path(os.environ.get("GANSU_REFERENCE", "/root/reference"))
+    out = {}
+    for bas in SAD_BASES:
+        table = O.read_sad(ref / "basis" / f"{bas}.sad")
+        for el in SAD_ELEMENTS:
+            a, b = table[el]
+            out[f"{bas}_{el}_alpha"], out[f"{bas}_{el}_beta"] = a, b
+    np.savez_compressed(Path(__file__).parent / "sad_ref.npz", **out)
+    print(f"sad_ref: {len(out) // 2} atomic density pairs")
+
+
 if __name__ == "__main__":
-    if "--ri" not in sys.argv:
-        main()
-    main_ri()
+    if "--sad" in sys.argv:
+        main_sad()
+    else:
+        if "--ri" not in sys.argv:
+            main()
+            main_sad()
+        main_ri()

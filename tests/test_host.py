@@ -136,3 +136,26 @@ def test_geometries():
         if len(o) > 1:
             dd = np.linalg.norm(o[:, None] - o[None], axis=-1) + np.eye(len(o)) * 9
             assert dd.min() >= 2.7 - 1e-9
+
+
+def test_sad_format_roundtrip_and_atom_ranges(built_library, tmp_path):
+    """.sad write/read round trip (read_density_from_sad format) and the atoms'
+    basis ranges against the oracle's."""
+    from dft_gansu_gb300 import sad
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(0)
+    dens = {"H": (rng.normal(size=(2, 2)), rng.normal(size=(2, 2))),
+            "O": (rng.normal(size=(9, 9)), rng.normal(size=(9, 9)))}
+    sad.write_sad(tmp_path / "x.sad", dens)
+    back = sad.read_sad(tmp_path / "x.sad")
+    for el in dens:
+        for i in range(2):
+            np.testing.assert_allclose(back[el][i], dens[el][i], rtol=1e-10)
+    atoms = geometry.alkane(3, jitter=0.02, seed=1)
+    for gbs in ("6-31g", "cc-pvdz"):
+        mol = gg.Molecular(atoms, gg.basis_path(gbs))
+        assert sad.atom_basis_ranges(mol) == O.atom_ranges(O.make_basis(atoms, gg.basis_path(gbs)))
+    sad.export_sad_cache(tmp_path / "c.dat", dens["O"][0], dens["O"][1])
+    toks = (tmp_path / "c.dat").read_text().split()
+    assert toks[0] == "9" and len(toks) == 1 + 2 * 81
