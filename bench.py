@@ -630,7 +630,8 @@ def main():
     ap.add_argument("--ri-threshold", type=float, default=1e-2)
     ap.add_argument("--guess", default=None, choices=["core", "gwh", "sad"],
                     help="initial guess (default: core; water_batch: sad)")
-    ap.add_argument("--eigensolver", default="syevd", choices=["syevd", "purification"])
+    ap.add_argument("--eigensolver", default="purification", choices=["syevd", "purification"],
+                    help="density from F inside the SCF loop (both arms use the same)")
     args = ap.parse_args()
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":

@@ -283,7 +283,8 @@ class Engine:
         opt, _keep = _scf_options(self._with_guess(options))
         res = ScfResult()
         outs = [self._empty(self.N, self.N), self._empty(self.N, self.N), self._empty(self.N),
-                self._empty(self.N)] if want_matrices else [None] * 4
+                self._empty(self.N), self._empty(self.N, self.N),
+                self._empty(self.N, self.N)] if want_matrices else [None] * 6
         st = lib().hf_uhf_scf(self._h, int(num_alpha), int(num_beta), C.byref(opt), C.byref(res),
                               *[_ptr(t) for t in outs])
         out = {f: getattr(res, f) for f, _ in ScfResult._fields_}
@@ -291,7 +292,8 @@ class Engine:
         if st not in (0, 4):
             check(st, "hf_uhf_scf")
         if want_matrices:
-            out["density_alpha"], out["density_beta"], out["orbital_energies_alpha"], out["orbital_energies_beta"] = outs
+            (out["density_alpha"], out["density_beta"], out["orbital_energies_alpha"], out["orbital_energies_beta"],
+             out["coefficients_alpha"], out["coefficients_beta"]) = outs
         return out
 
     def sad_density(self, source: str = "auto"):
@@ -591,6 +593,24 @@ class _HFBase:
         Da, Db = self.export_density_matrix()
         sad.export_sad_cache(filename, Da, Db)
 
+    def export_molden_file(self, filename: str = "output.molden") -> None:
+        """export_molden_file (src/rhf.cu:363-425 and the UHF/ROHF variants)."""
+        from . import molden
+
+        molden.write_molden(filename, self.mol, self._orbital_sets())
+
+    def analyze_mulliken_population(self) -> np.ndarray:
+        """Mulliken atomic charges (analyze_mulliken_population, src/rhf.cu:427-460)."""
+        from . import molden
+
+        Da, Db = self.export_density_matrix()
+        S = self.engine.core_hamiltonian()[0].double().cpu().numpy()
+        return molden.mulliken_charges(self.mol, Da + Db, S)
+
+    @staticmethod
+    def _np(t):
+        return t.double().cpu().numpy()
+
 
 class RHF(_HFBase):
     """Mirror of gansu::RHF (include/rhf.hpp, src/rhf.cu): ``solve()`` runs the
@@ -614,6 +634,11 @@ class RHF(_HFBase):
         D = self.result["density"].double().cpu().numpy()
         return 0.5 * D, 0.5 * D
 
+    def _orbital_sets(self):
+        n, nocc = self.mol.num_basis, self.mol.num_electrons // 2
+        occ = np.where(np.arange(n) < nocc, 2.0, 0.0)
+        return [("Alpha", self._np(self.result["orbital_energies"]), self._np(self.result["coefficients"]), occ)]
+
 
 class UHF(_HFBase):
     """Mirror of gansu::UHF (include/uhf.hpp, src/uhf.cu): ``solve()`` runs
@@ -628,6 +653,14 @@ class UHF(_HFBase):
     def export_density_matrix(self):
         return (self.result["density_alpha"].double().cpu().numpy(),
                 self.result["density_beta"].double().cpu().numpy())
+
+    def _orbital_sets(self):
+        n, r = self.mol.num_basis, self.result
+        idx = np.arange(n)
+        return [("Alpha", self._np(r["orbital_energies_alpha"]), self._np(r["coefficients_alpha"]),
+                 np.where(idx < self.mol.num_alpha_spins, 1.0, 0.0)),
+                ("Beta", self._np(r["orbital_energies_beta"]), self._np(r["coefficients_beta"]),
+                 np.where(idx < self.mol.num_beta_spins, 1.0, 0.0))]
 
 
 class ROHF(_HFBase):
@@ -653,6 +686,12 @@ class ROHF(_HFBase):
     def export_density_matrix(self):
         return (self.result["density_alpha"].double().cpu().numpy(),
                 self.result["density_beta"].double().cpu().numpy())
+
+    def _orbital_sets(self):
+        n, r = self.mol.num_basis, self.result
+        idx = np.arange(n)
+        occ = np.where(idx < self.mol.num_beta_spins, 2.0, np.where(idx < self.mol.num_alpha_spins, 1.0, 0.0))
+        return [("Alpha", self._np(r["orbital_energies"]), self._np(r["coefficients"]), occ)]
 
     def get_total_spin(self) -> float:
         """S(S+1) with S = (open orbitals)/2 (ROHF::get_total_spin)."""

@@ -134,7 +134,7 @@ SIGNATURES = {
     "hf_compute_jk_ri": (_I, [_P, _P, _P, _P, _P]),
     "hf_split_bf16_matmul": (_I, [_P, _P, _P, _I, _I, _I, _I, _P]),
     "hf_engine_create_batch": (_I, [_I, _P, _P, _P, _P, _P, _P, _D, _P]),
-    "hf_uhf_scf": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "hf_uhf_scf": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "hf_rohf_scf": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "hf_batch_rhf_scf": (_I, [_P, _P, _P, _P, _P, _P]),
     "hf_scf_options_default": (None, [C.POINTER(ScfOptions)]),

@@ -970,7 +970,7 @@ extern "C" {
 
 int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options* opt_in, hf_scf_result* res,
                double* d_density_a_out, double* d_density_b_out, double* d_orbital_energies_a_out,
-               double* d_orbital_energies_b_out)
+               double* d_orbital_energies_b_out, double* d_coefficients_a_out, double* d_coefficients_b_out)
 {
     clear_error();
     if (!eng || !res) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
@@ -1121,14 +1121,20 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     res->converged = converged ? 1 : 0;
     if (d_density_a_out) GB_CUDA_TRY(cudaMemcpy(d_density_a_out, Da, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     if (d_density_b_out) GB_CUDA_TRY(cudaMemcpy(d_density_b_out, Db, nn * sizeof(double), cudaMemcpyDeviceToDevice));
-    // orbital energies of the final Fock matrices of both spins
-    if (d_orbital_energies_a_out) {
+    // orbital energies and coefficients of the final Fock matrices of both spins
+    if (d_orbital_energies_a_out || d_coefficients_a_out) {
         if ((st = coefficients(e, Fa, s, opt.eigensolver))) return st;
-        GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_a_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
+        if (d_orbital_energies_a_out)
+            GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_a_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
+        if (d_coefficients_a_out)
+            GB_CUDA_TRY(cudaMemcpy(d_coefficients_a_out, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     }
-    if (d_orbital_energies_b_out) {
+    if (d_orbital_energies_b_out || d_coefficients_b_out) {
         if ((st = coefficients(e, Fb, s, opt.eigensolver))) return st;
-        GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_b_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
+        if (d_orbital_energies_b_out)
+            GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_b_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
+        if (d_coefficients_b_out)
+            GB_CUDA_TRY(cudaMemcpy(d_coefficients_b_out, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     }
     return converged ? HF_OK : (set_error("UHF did not converge"), HF_ERR_NOT_CONVERGED);
 }

@@ -306,11 +306,11 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt, hf_
  * function's row and the last orbital's column of C_b zeroed), one DIIS ring per
  * spin on the same cyclic index, |dE| convergence.  Two direct J/K builds per
  * iteration.
- * Outputs (may be NULL): spin densities and the orbital energies of the final
- * Fock matrices. */
+ * Outputs (device, may be NULL): spin densities, and the orbital energies and
+ * coefficients (row-major, orbitals as columns) of the final Fock matrices. */
 int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options* opt, hf_scf_result* result,
                double* d_density_a_out, double* d_density_b_out, double* d_orbital_energies_a_out,
-               double* d_orbital_energies_b_out);
+               double* d_orbital_energies_b_out, double* d_coefficients_a_out, double* d_coefficients_b_out);
 
 /* Restricted open-shell HF on the device (ROHF::solve, src/rohf.cu; Fock build
  * computeFockMatrix_ROHF, src/gpu_manager.cu:733-817).  num_beta closed and

@@ -280,8 +280,9 @@ def test_purification_density_matches_diagonalisation(built_library, cuda):
     assert rp["converged"] == 1
     assert abs(rp["total_energy"] - rd["total_energy"]) < 1e-9
     assert abs(rp["iterations"] - rd["iterations"]) <= 1
-    np.testing.assert_allclose(_np(rp["density"]), _np(rd["density"]), atol=1e-6)
-    np.testing.assert_allclose(_np(rp["orbital_energies"]), _np(rd["orbital_energies"]), atol=1e-6)
+    # two runs stopped by |dE| < 1e-9 at different points: densities agree to ~sqrt(1e-9)
+    np.testing.assert_allclose(_np(rp["density"]), _np(rd["density"]), atol=1e-5)
+    np.testing.assert_allclose(_np(rp["orbital_energies"]), _np(rd["orbital_energies"]), atol=1e-5)
     rm = eng.rhf_scf(mol.num_electrons, dict(base, eigensolver=gg.HF_EIGEN_PURIFICATION, precision=gg.HF_PRECISION_MIXED,
                                              mixed_threshold=0.1, incremental=1, anchor_threshold=1e-2))
     assert rm["converged"] == 1 and abs(rm["total_energy"] - rd["total_energy"]) < 1e-6

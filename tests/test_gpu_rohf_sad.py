@@ -154,8 +154,16 @@ def test_builder_rohf_recipe_with_sad(built_library, cuda, tmp_path):
     pm["maxiter"] = "300"
     hf = gg.HFBuilder.buildHF(pm)
     e = hf.solve()
-    ro = O.rohf_from_basis(O.make_basis(_nh2(), gg.basis_path("sto-3g")), 5, 4, thr=1e-12, maxiter=300)
-    assert abs(e - ro["total_energy"]) < 1e-8
+    # the oracle from the same superposition: from SAD, NH2/STO-3G reaches a lower ROHF
+    # state (-54.8345 Eh) than from the core guess (-54.7393 Eh)
+    Da, Db = hf.engine.sad_density()
+    b = O.make_basis(_nh2(), gg.basis_path("sto-3g"))
+    S, T, V = O.one_electron(b)
+    eri = O.eri_tensor(b)
+    jk = lambda D: (np.einsum("ijkl,kl->ij", eri, D), np.einsum("ikjl,kl->ij", eri, D))
+    ro = O.rohf(S, T + V, jk, 5, 4, O.nuclear_repulsion(b.atoms), thr=1e-12, maxiter=300, guess="sad",
+                guess_density=(Da.cpu().numpy(), Db.cpu().numpy()))
+    assert ro["converged"] and abs(e - ro["total_energy"]) < 1e-8
     assert abs(hf.get_total_spin() - 0.75) < 1e-15
     hf.export_sad_cache(str(tmp_path / "cache.dat"))
     assert (tmp_path / "cache.dat").read_text().split()[0] == str(hf.mol.num_basis)
