@@ -506,6 +506,10 @@ def run_water_batch(args, rank, world):
     guess = args.guess or "sad"
     conv = {"convergence_threshold": CONV, "initial_guess": GUESSES[guess],
             "eigensolver": gg.HF_EIGEN_PURIFICATION if args.eigensolver == "purification" else gg.HF_EIGEN_SYEVD}
+    conv64 = dict(conv)
+    if args.batch_precision == "mixed":
+        conv.update({"precision": gg.HF_PRECISION_MIXED, "mixed_threshold": args.mixed_threshold,
+                     "incremental": 1, "anchor_threshold": args.anchor_threshold})
     t0 = time.perf_counter()
     mols = [gg.Molecular(c, gbs) for c in clusters]
     batch = gg.Batch(mols)
@@ -519,6 +523,10 @@ def run_water_batch(args, rank, world):
         runs = [batch.rhf_scf(batch_conv) for _ in range(args.steps)]
     res, ms, it = runs[-1]
     ms_iter = statistics.mean(r[1] / max(r[2], 1) for r in runs)
+    # the FP64 batch of the same molecules: the reference precision for |dE| and the speed-up
+    b64 = dict(batch_conv, **{k: conv64[k] for k in conv64})
+    b64.pop("precision", None)
+    res64, ms64, it64 = batch.rhf_scf(b64)
     # individual FP64 runs (engine + SCF per molecule), device time of their SCF loops
     ind_ms, ind_e, ind_it = 0.0, [], 0
     for c in clusters:
@@ -530,12 +538,14 @@ def run_water_batch(args, rank, world):
         ind_it = max(ind_it, r1["iterations"])
         e1.close()
     dE = max(abs(a["total_energy"] - b) for a, b in zip(res, ind_e))
+    dE64 = max(abs(a["total_energy"] - b["total_energy"]) for a, b in zip(res, res64))
     if rank == 0:
         sizes = [len(c) // 3 for c in clusters]
         line = {
             "metric": METRIC, "value": ms_iter, "unit": "ms/iter", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": statistics.mean(r[1] for r in runs), "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32" if args.batch_precision == "mixed" else "f64", "data": "synthetic",
             "config": {"workload": f"batched RHF/6-31G, {len(clusters)} water clusters (H2O)_n, n ~ U{{1..16}} "
                                    f"(sum N = {sum(m.num_basis for m in mols)}), O-H 0.96 A, HOH 104.5, O-O >= 2.7 A",
                        "seed": args.seed, "convergence": CONV, "waters": [min(sizes), max(sizes), sum(sizes)],
@@ -549,6 +559,11 @@ def run_water_batch(args, rank, world):
             "individual_iterations_max": ind_it,
             "individual_ms_total": ind_ms, "batch_speedup_vs_individual": ind_ms / ms,
             "max_delta_E_vs_individual": dE, "all_converged": all(r["converged"] == 1 for r in res),
+            "batch_precision": args.batch_precision,
+            "fp64_batch_ms_per_iter": ms64 / max(it64, 1), "fp64_batch_iterations": it64,
+            "mixed_speedup_vs_fp64_batch": (ms64 / max(it64, 1)) / ms_iter,
+            "max_delta_E_vs_fp64_batch": dE64,
+            "fp64_all_converged": all(r["converged"] == 1 for r in res64),
             "setup_s": setup_s, "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)
@@ -630,6 +645,7 @@ def main():
     ap.add_argument("--ri-threshold", type=float, default=1e-2)
     ap.add_argument("--guess", default=None, choices=["core", "gwh", "sad"],
                     help="initial guess (default: core; water_batch: sad)")
+    ap.add_argument("--batch-precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--eigensolver", default="purification", choices=["syevd", "purification"],
                     help="density from F inside the SCF loop (both arms use the same)")
     args = ap.parse_args()

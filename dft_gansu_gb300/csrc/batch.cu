@@ -127,6 +127,85 @@ __global__ void batch_fock_kernel(const double* __restrict__ Jp, const double* _
     }
 }
 
+// ---- mixed tier of the batch: the single-molecule anchored rule per molecule
+// out = D - Dprev over the block layout
+__global__ void batch_diff_kernel(const double* __restrict__ D, const double* __restrict__ Dp, long long ne,
+                                  double* __restrict__ out)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < ne;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        out[k] = D[k] - Dp[k];
+}
+
+// Per molecule, from max|D - Dprev|: FP32 full builds while unanchored and the change
+// is >= anchor (or on the first build), then one FP64 full build (the anchor), then
+// builds under the FP32 cut tau (incremental dD builds when incremental).  Molecules
+// no longer active are not built (tau = skip = inf).
+__global__ void batch_phase_kernel(const double* __restrict__ ddiff, const unsigned char* __restrict__ active,
+                                   int nmol, int first, double anchor, double tau, double full_tau, double schwarz,
+                                   int incremental,
+                                   unsigned char* __restrict__ anchored, unsigned char* __restrict__ incr,
+                                   double* __restrict__ mol_tau, double* __restrict__ mol_skip)
+{
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nmol; m += gridDim.x * blockDim.x) {
+        if (!active[m]) { mol_tau[m] = inf; mol_skip[m] = inf; incr[m] = 0; continue; }
+        if (!anchored[m]) {
+            incr[m] = 0;
+            mol_skip[m] = schwarz;
+            if (first || ddiff[m] >= anchor) {
+                mol_tau[m] = inf;  // every quartet FP32
+            } else {
+                mol_tau[m] = 0.0;  // every quartet FP64: the anchor
+                anchored[m] = 1;
+            }
+        } else {
+            // anchored: incremental builds under the cut, or full builds at full_tau
+            incr[m] = (incremental && !first) ? 1 : 0;
+            mol_tau[m] = incr[m] ? tau : full_tau;
+            mol_skip[m] = fmin(schwarz, mol_tau[m]);
+        }
+    }
+}
+
+// input density of the build: dD for incremental molecules, D otherwise
+__global__ void batch_input_kernel(const double* __restrict__ D, const double* __restrict__ diff,
+                                   const unsigned char* __restrict__ incr, const BlockMap M, double* __restrict__ out)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int m = block_of(M, k);
+        out[k] = incr[m] ? diff[k] : D[k];
+    }
+}
+
+// G (+)= both tiers' J', K' finished per block, F = H + G, Dprev = D (active molecules)
+__global__ void batch_fock_mixed_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
+                                        const float* __restrict__ Jp32, const float* __restrict__ Kp32,
+                                        const double* __restrict__ s, const double* __restrict__ H,
+                                        const double* __restrict__ D, const BlockMap M,
+                                        const unsigned char* __restrict__ active, const unsigned char* __restrict__ incr,
+                                        double* __restrict__ G, double* __restrict__ F, double* __restrict__ Dprev)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < M.nelem;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int m = block_of(M, k);
+        if (!active[m]) continue;
+        const int n = M.n[m], g0 = M.bf0[m];
+        const long long base = M.base[m], r = k - base;
+        const int i = static_cast<int>(r / n), j = static_cast<int>(r % n);
+        const long long kt = base + static_cast<long long>(j) * n + i;
+        const double ss = s[g0 + i] * s[g0 + j];
+        const double js = Jp[k] + Jp[kt] + static_cast<double>(Jp32[k]) + static_cast<double>(Jp32[kt]);
+        const double ks = Kp[k] + Kp[kt] + static_cast<double>(Kp32[k]) + static_cast<double>(Kp32[kt]);
+        const double g = (2.0 * js - 0.5 * ks) * ss;
+        const double gn = incr[m] ? G[k] + g : g;
+        G[k] = gn;
+        F[k] = H[k] + gn;
+        Dprev[k] = D[k];
+    }
+}
+
 // E_m = 1/2 sum D (H + F) over block m: one CTA per molecule
 __global__ void batch_energy_kernel(const double* __restrict__ D, const double* __restrict__ H,
                                     const double* __restrict__ F, const BlockMap M, double* __restrict__ out)
@@ -349,6 +428,14 @@ struct Batch {
     cudaEvent_t fork = nullptr, join[kSyevStreams] = {};
     std::vector<unsigned char> active;  // molecules still iterating (host copy)
     bool purify = false;                // eigensolver 2: SP2 + McWeeny instead of batched syev
+    // mixed tier (precision HF_PRECISION_MIXED): per-molecule anchored rule
+    bool mixed = false;
+    double anchor = 0.0, tau = 0.1, full_tau = 0.0;
+    int incremental = 1;
+    bool first_build = true;
+    double *G = nullptr, *Dprev = nullptr, *Din = nullptr, *mol_tau = nullptr, *mol_skip = nullptr,
+           *mol_dmax = nullptr, *mol_ddiff = nullptr;
+    unsigned char *d_anchored = nullptr, *d_incr = nullptr;
     float *P32a = nullptr, *P32b = nullptr, *P32c = nullptr;
     double* bounds = nullptr;
     unsigned char* square = nullptr;
@@ -358,7 +445,10 @@ struct Batch {
         if (d_ebase) cudaFree(d_ebase);
         if (params) cusolverDnDestroyParams(params);
         for (void* p : {static_cast<void*>(P32a), static_cast<void*>(P32b), static_cast<void*>(P32c),
-                        static_cast<void*>(bounds), static_cast<void*>(square), static_cast<void*>(d_nocc)})
+                        static_cast<void*>(bounds), static_cast<void*>(square), static_cast<void*>(d_nocc),
+                        static_cast<void*>(G), static_cast<void*>(Dprev), static_cast<void*>(Din),
+                        static_cast<void*>(mol_tau), static_cast<void*>(mol_skip), static_cast<void*>(mol_dmax),
+                        static_cast<void*>(mol_ddiff), static_cast<void*>(d_anchored), static_cast<void*>(d_incr)})
             if (p) cudaFree(p);
         for (int i = 0; i < kSyevStreams; ++i) {
             if (handles[i]) cusolverDnDestroy(handles[i]);
@@ -524,6 +614,27 @@ int batch_purify(Batch& b, cudaStream_t s)
 int batch_fock(Batch& b, cudaStream_t s)
 {
     Engine& e = *b.e;
+    if (b.mixed) {
+        const long long ne = e.nelem;
+        batch_diff_kernel<<<grid_of(ne), 256, 0, s>>>(b.w.D, b.Dprev, ne, b.Din);
+        GB_LAUNCH_CHECK();
+        int st = mol_absmax(e, b.Din, b.mol_ddiff, s);
+        if (st) return st;
+        batch_phase_kernel<<<(e.nmol + 255) / 256, 256, 0, s>>>(b.mol_ddiff, e.d_mol_active, e.nmol,
+                                                                b.first_build ? 1 : 0, b.anchor, b.tau, b.full_tau,
+                                                                e.schwarz_threshold, b.incremental, b.d_anchored,
+                                                                b.d_incr, b.mol_tau, b.mol_skip);
+        GB_LAUNCH_CHECK();
+        batch_input_kernel<<<grid_of(ne), 256, 0, s>>>(b.w.D, b.Din, b.d_incr, e.block_map(), b.Din);
+        GB_LAUNCH_CHECK();
+        if ((st = build_jk_batch(e, b.Din, b.mol_tau, b.mol_skip, b.mol_dmax, s))) return st;
+        batch_fock_mixed_kernel<<<grid_of(ne), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_Jp32, e.d_Kp32, e.d_scale, b.w.H,
+                                                            b.w.D, e.block_map(), e.d_mol_active, b.d_incr, b.G,
+                                                            b.w.F, b.Dprev);
+        GB_LAUNCH_CHECK();
+        b.first_build = false;
+        return HF_OK;
+    }
     int st = build_jk(e, b.w.D, nullptr, nullptr, HF_PRECISION_FP64, 0.0, s);
     if (st) return st;
     batch_fock_kernel<<<grid_of(e.nelem), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, b.w.H, e.block_map(),
@@ -613,6 +724,28 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
             return set_error("cudaMalloc (batch purification) failed"), HF_ERR_OUT_OF_MEMORY;
         GB_CUDA_TRY(cudaMemcpy(b.d_nocc, nocc.data(), sizeof(int) * nmol, cudaMemcpyHostToDevice));
     }
+    if (opt.precision != HF_PRECISION_FP64 && opt.precision != HF_PRECISION_MIXED)
+        return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.precision == HF_PRECISION_MIXED) {
+        // the anchored mixed tier of hf_rhf_scf, decided per molecule on the device
+        b.mixed = true;
+        b.anchor = opt.anchor_threshold;
+        b.tau = opt.mixed_threshold;
+        b.incremental = opt.incremental;
+        b.full_tau = (opt.full_build_precision == HF_PRECISION_MIXED) ? opt.mixed_threshold : 0.0;
+        const size_t nb = sizeof(double) * ne;
+        if (cudaMalloc(&b.G, nb) != cudaSuccess || cudaMalloc(&b.Dprev, nb) != cudaSuccess ||
+            cudaMalloc(&b.Din, nb) != cudaSuccess || cudaMalloc(&b.mol_tau, sizeof(double) * nmol) != cudaSuccess ||
+            cudaMalloc(&b.mol_skip, sizeof(double) * nmol) != cudaSuccess ||
+            cudaMalloc(&b.mol_dmax, sizeof(double) * nmol) != cudaSuccess ||
+            cudaMalloc(&b.mol_ddiff, sizeof(double) * nmol) != cudaSuccess ||
+            cudaMalloc(&b.d_anchored, nmol) != cudaSuccess || cudaMalloc(&b.d_incr, nmol) != cudaSuccess)
+            return set_error("cudaMalloc (batch mixed tier) failed"), HF_ERR_OUT_OF_MEMORY;
+        GB_CUDA_TRY(cudaMemsetAsync(b.Dprev, 0, nb, s));
+        GB_CUDA_TRY(cudaMemsetAsync(b.G, 0, nb, s));
+        // anchor_threshold <= 0: anchored from the start (the first build is a full one), as in hf_rhf_scf
+        GB_CUDA_TRY(cudaMemsetAsync(b.d_anchored, opt.anchor_threshold > 0.0 ? 0 : 1, nmol, s));
+    }
     GB_CUDA_TRY(cudaMemsetAsync(w.B, 0, sizeof(double) * nmol * kBatchDiis * kBatchDiis, s));
     // molecules still iterating: the Fock kernels, the F update, DIIS and the eigensolves skip the others
     unsigned char* d_active = nullptr;
@@ -661,6 +794,7 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     }
 
     std::vector<double> E(nmol), prev(nmol, std::numeric_limits<double>::max());
+    std::vector<unsigned char> anchored(nmol, 1);
     std::vector<int> done_iter(nmol, -1);
     std::vector<double> done_energy(nmol, 0.0);
     const int m = opt.diis_size;
@@ -680,6 +814,8 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
         batch_energy_kernel<<<nmol, 256, 0, s>>>(w.D, w.H, w.F, e.block_map(), w.energy);
         GB_LAUNCH_CHECK();
         GB_CUDA_TRY(cudaMemcpyAsync(E.data(), w.energy, sizeof(double) * nmol, cudaMemcpyDeviceToHost, s));
+        if (b.mixed)
+            GB_CUDA_TRY(cudaMemcpyAsync(anchored.data(), b.d_anchored, nmol, cudaMemcpyDeviceToHost, s));
         GB_CUDA_TRY(cudaStreamSynchronize(s));
         {
             float a = 0.f, c = 0.f;
@@ -690,7 +826,9 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
         }
         for (int k = 0; k < nmol; ++k) {
             if (!std::isfinite(E[k])) return set_error("batch SCF energy is not finite"), HF_ERR_NOT_CONVERGED;
-            if (done_iter[k] < 0 && std::fabs(E[k] - prev[k]) < opt.convergence_threshold) {
+            // the mixed tier may not converge before the molecule's FP64 anchor build
+            if (done_iter[k] < 0 && std::fabs(E[k] - prev[k]) < opt.convergence_threshold &&
+                (!b.mixed || anchored[k])) {
                 done_iter[k] = iter;
                 done_energy[k] = E[k];
                 ++ndone;

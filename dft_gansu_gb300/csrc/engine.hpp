@@ -181,6 +181,11 @@ int finish_fock(Engine& e, const double* d_H, const double* d_J, const double* d
 int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s);
 // device split of the static quartet lists into FP64 prefix / FP32 rest (e.plan)
 int mixed_plan(Engine& e, const double* d_D, double factor, bool square, double tau, double skip, cudaStream_t s);
+// max |A| of every molecule's block (fock.cu)
+int mol_absmax(Engine& e, const double* d_A, double* d_out, cudaStream_t s);
+// batch build with per-molecule FP32 cuts and drop thresholds (fock.cu)
+int build_jk_batch(Engine& e, const double* d_D, const double* d_mol_tau, const double* d_mol_skip,
+                   double* d_mol_dmax, cudaStream_t s);
 
 // one_electron.cu
 int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s);

@@ -100,6 +100,24 @@ __global__ void absmax_kernel(const double* __restrict__ A, long long n, double*
     }
 }
 
+// max |D| of every molecule's block: one CTA per molecule
+__global__ void mol_absmax_kernel(const double* __restrict__ A, const BlockMap M, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    const int m = blockIdx.x;
+    const long long b0 = M.base[m], b1 = M.base[m + 1];
+    double v = 0.0;
+    for (long long k = b0 + threadIdx.x; k < b1; k += blockDim.x) v = fmax(v, fabs(A[k]));
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) out[m] = v;
+    }
+}
+
 // Exclusive-scan helper over one block (values of this pass), returns the
 // pass total; the running base is kept by the caller.
 __device__ long long block_scan_exclusive(long long v, long long* smem, long long& total)
@@ -144,6 +162,13 @@ struct PlanArgs {
     long long* off64;
     long long* off32;
     int* lo32;
+    // batches: per-molecule max|D|, FP32 cut and drop threshold (the bra pair's
+    // molecule through pairs[bra].A -> shell_mol); null for one molecule
+    const ShellPairDev* pairs = nullptr;
+    const int* shell_mol = nullptr;
+    const double* mol_dmax = nullptr;
+    const double* mol_tau = nullptr;
+    const double* mol_skip = nullptr;
 };
 
 // One block per class pair.
@@ -163,11 +188,19 @@ __global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
             const int e = eb + i;
             const int cnt = a.entry_cnt[e];
             const int k0 = kb + a.entry_lo0[e];
-            const double qb = a.pair_qs[a.entry_bra[e]] * dm;
+            const int bra = a.entry_bra[e];
+            double qb = a.pair_qs[bra] * dm, tau = a.mixed_threshold, skip = a.skip_threshold;
+            if (a.mol_dmax) {
+                const int m = a.shell_mol[a.pairs[bra].A];
+                const double d = a.mol_dmax[m];
+                qb = a.pair_qs[bra] * (a.square ? d * d : d) * a.factor;
+                tau = a.mol_tau[m];
+                skip = a.mol_skip[m];
+            }
             int lo = 0, hi = cnt;  // first ket of the group with qb*Qs_ket < thr
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                if (qb * a.pair_qs[k0 + mid] >= a.mixed_threshold) lo = mid + 1; else hi = mid;
+                if (qb * a.pair_qs[k0 + mid] >= tau) lo = mid + 1; else hi = mid;
             }
             c64 = lo;
             // density-weighted screening: the tail whose bound times max|D| is below the
@@ -175,7 +208,7 @@ __global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
             int hi2 = cnt, lo2 = lo;
             while (lo2 < hi2) {
                 const int mid = (lo2 + hi2) >> 1;
-                if (qb * a.pair_qs[k0 + mid] >= a.skip_threshold) lo2 = mid + 1; else hi2 = mid;
+                if (qb * a.pair_qs[k0 + mid] >= skip) lo2 = mid + 1; else hi2 = mid;
             }
             c32 = lo2 - lo;
             a.lo32[e] = a.entry_lo0[e] + lo;
@@ -298,6 +331,73 @@ static int mixed_plan_args(Engine& e, const double* d_D, double factor, bool squ
 int mixed_plan(Engine& e, const double* d_D, double factor, bool square, double tau, double skip, cudaStream_t s)
 {
     return mixed_plan_args(e, d_D, factor, square, tau, skip, s, nullptr);
+}
+
+int mol_absmax(Engine& e, const double* d_A, double* d_out, cudaStream_t s)
+{
+    mol_absmax_kernel<<<e.nmol, 256, 0, s>>>(d_A, e.block_map(), d_out);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+// Batch build with a precision rule per molecule: quartets of molecule m go to
+// FP64 where Qs_ab Qs_cd c_max^4 max|D_m| >= mol_tau[m], to FP32 below that, and
+// are dropped below mol_skip[m] (tau = skip = inf: the molecule is not built).
+// d_D holds each molecule's density or density difference; mol_dmax receives
+// max|D_m|.  J', K' (FP64 and FP32 tiers) are left for the caller's finish.
+int build_jk_batch(Engine& e, const double* d_D, const double* d_mol_tau, const double* d_mol_skip,
+                   double* d_mol_dmax, cudaStream_t s)
+{
+    const size_t nn = static_cast<size_t>(e.nelem);
+    int st = scale_density(e, d_D, true, s);
+    if (st) return st;
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_Jp, 0, nn * sizeof(double), s));
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_Kp, 0, nn * sizeof(double), s));
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_Jp32, 0, nn * sizeof(float), s));
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_Kp32, 0, nn * sizeof(float), s));
+    e.last_mixed = true;
+    mol_absmax_kernel<<<e.nmol, 256, 0, s>>>(d_D, e.block_map(), d_mol_dmax);
+    GB_LAUNCH_CHECK();
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    const double c2 = e.cgto_max * e.cgto_max;
+    PlanArgs a;
+    a.entry_bra = e.d_entry_bra;
+    a.entry_cnt = e.d_entry_cnt;
+    a.entry_lo0 = e.d_entry_lo0;
+    a.pair_qs = e.d_pair_qs;
+    a.cp_entry_begin = e.d_cp_meta;
+    a.cp_nentry = e.d_cp_meta + ncp;
+    a.cp_ket_base = e.d_cp_meta + 2 * ncp;
+    a.cp_off_base = e.d_cp_meta + 3 * ncp;
+    a.dmax = d_mol_dmax;
+    a.factor = c2 * c2;
+    a.mixed_threshold = 0.0;
+    a.skip_threshold = 0.0;
+    a.square = 0;
+    a.off64 = e.plan.off64;
+    a.off32 = e.plan.off32;
+    a.lo32 = e.plan.lo32;
+    a.pairs = e.d_pairs;
+    a.shell_mol = e.d_shell_mol;
+    a.mol_dmax = d_mol_dmax;
+    a.mol_tau = d_mol_tau;
+    a.mol_skip = d_mol_skip;
+    mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
+    GB_LAUNCH_CHECK();
+    for (int c = 0; c < ncp; ++c) {
+        const ClassPair& cp = e.class_pairs[c];
+        if (cp.n_survivors == 0) continue;
+        const PairClass& X = e.pair_classes[cp.X];
+        const PairClass& Y = e.pair_classes[cp.Y];
+        FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
+        if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
+        const int grid = grid_for(cp.n_survivors, e.num_sms);
+        f(false, make_launch(e, c, false, e.plan.off64, e.d_entry_lo0), grid, s);
+        GB_LAUNCH_CHECK();
+        f(true, make_launch(e, c, true, e.plan.off32, e.plan.lo32), grid, s);
+        GB_LAUNCH_CHECK();
+    }
+    return HF_OK;
 }
 
 int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,

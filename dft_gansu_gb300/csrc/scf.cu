@@ -1014,13 +1014,14 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         return HF_OK;
     };
     double *Fb = nullptr, *Db = nullptr, *Ja = nullptr, *Ka = nullptr, *Jb = nullptr, *Kb = nullptr, *epsb = nullptr,
-           *Esb = nullptr, *Fsb = nullptr;
+           *Esb = nullptr, *Fsb = nullptr, *Ca = nullptr, *Cb = nullptr, *epsa = nullptr;
     struct Free {
         std::vector<void*>& v;
         ~Free() { for (void* p : v) cudaFree(p); }
     } guard{owned};
     if ((st = buf(Fb, nn)) || (st = buf(Db, nn)) || (st = buf(Ja, nn)) || (st = buf(Ka, nn)) || (st = buf(Jb, nn)) ||
-        (st = buf(Kb, nn)) || (st = buf(epsb, n)) || (st = buf(Esb, nn * m)) || (st = buf(Fsb, nn * m)))
+        (st = buf(Kb, nn)) || (st = buf(epsb, n)) || (st = buf(Esb, nn * m)) || (st = buf(Fsb, nn * m)) ||
+        (st = buf(Ca, nn)) || (st = buf(Cb, nn)) || (st = buf(epsa, n)))
         return st;
     double* Fa = w.F;
     double* Da = w.D;
@@ -1033,9 +1034,12 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     // spin densities from FA and FB; break = the guess's beta symmetry break
     auto densities = [&](const double* FA, const double* FB, bool brk) -> int {
         int r;
+        // the orbitals and orbital energies behind the densities are kept for the export
         if ((r = coefficients(e, FA, s, opt.eigensolver))) return r;
         density_factor_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, num_alpha, 1.0, Da);
         GB_LAUNCH_CHECK();
+        GB_CUDA_TRY(cudaMemcpyAsync(Ca, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        GB_CUDA_TRY(cudaMemcpyAsync(epsa, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         if ((r = coefficients(e, FB, s, opt.eigensolver))) return r;
         if (brk) {
             break_symmetry_kernel<<<(n + 255) / 256, 256, 0, s>>>(w.C, n);
@@ -1043,6 +1047,7 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         }
         density_factor_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, num_beta, 1.0, Db);
         GB_LAUNCH_CHECK();
+        GB_CUDA_TRY(cudaMemcpyAsync(Cb, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
         GB_CUDA_TRY(cudaMemcpyAsync(epsb, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         return HF_OK;
     };
@@ -1121,21 +1126,14 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     res->converged = converged ? 1 : 0;
     if (d_density_a_out) GB_CUDA_TRY(cudaMemcpy(d_density_a_out, Da, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     if (d_density_b_out) GB_CUDA_TRY(cudaMemcpy(d_density_b_out, Db, nn * sizeof(double), cudaMemcpyDeviceToDevice));
-    // orbital energies and coefficients of the final Fock matrices of both spins
-    if (d_orbital_energies_a_out || d_coefficients_a_out) {
-        if ((st = coefficients(e, Fa, s, opt.eigensolver))) return st;
-        if (d_orbital_energies_a_out)
-            GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_a_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
-        if (d_coefficients_a_out)
-            GB_CUDA_TRY(cudaMemcpy(d_coefficients_a_out, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice));
-    }
-    if (d_orbital_energies_b_out || d_coefficients_b_out) {
-        if ((st = coefficients(e, Fb, s, opt.eigensolver))) return st;
-        if (d_orbital_energies_b_out)
-            GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_b_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
-        if (d_coefficients_b_out)
-            GB_CUDA_TRY(cudaMemcpy(d_coefficients_b_out, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice));
-    }
+    // orbital energies and coefficients of the last diagonalisations (the ones behind the
+    // returned densities, as the reference's export reads them)
+    if (d_orbital_energies_a_out)
+        GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_a_out, epsa, n * sizeof(double), cudaMemcpyDeviceToDevice));
+    if (d_coefficients_a_out) GB_CUDA_TRY(cudaMemcpy(d_coefficients_a_out, Ca, nn * sizeof(double), cudaMemcpyDeviceToDevice));
+    if (d_orbital_energies_b_out)
+        GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_b_out, epsb, n * sizeof(double), cudaMemcpyDeviceToDevice));
+    if (d_coefficients_b_out) GB_CUDA_TRY(cudaMemcpy(d_coefficients_b_out, Cb, nn * sizeof(double), cudaMemcpyDeviceToDevice));
     return converged ? HF_OK : (set_error("UHF did not converge"), HF_ERR_NOT_CONVERGED);
 }
 

@@ -307,7 +307,8 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt, hf_
  * spin on the same cyclic index, |dE| convergence.  Two direct J/K builds per
  * iteration.
  * Outputs (device, may be NULL): spin densities, and the orbital energies and
- * coefficients (row-major, orbitals as columns) of the final Fock matrices. */
+ * coefficients (row-major, orbitals as columns) of the diagonalisations that
+ * produced them. */
 int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options* opt, hf_scf_result* result,
                double* d_density_a_out, double* d_density_b_out, double* d_orbital_energies_a_out,
                double* d_orbital_energies_b_out, double* d_coefficients_a_out, double* d_coefficients_b_out);

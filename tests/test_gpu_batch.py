@@ -62,3 +62,24 @@ def test_batch_purification_matches_diagonalisation(built_library, cuda):
     for a, b in zip(rd, rp):
         assert a["converged"] == 1 and b["converged"] == 1
         assert abs(a["total_energy"] - b["total_energy"]) < 1e-8
+
+
+def test_batch_mixed_tier_matches_single_molecule_rule(built_library, cuda):
+    """The batch's mixed tier (per molecule: FP32 full builds until max|dD| < anchor,
+    one FP64 anchor, then incremental builds with the FP32 cut) against the
+    single-molecule mixed SCF with the same options (1e-7 Eh) and FP64 (1e-6 Eh)."""
+    clusters = geometry.water_cluster_set(12, nmax=8, seed=3)
+    mols = [gg.Molecular(c, gg.basis_path("6-31g")) for c in clusters]
+    batch = gg.Batch(mols)
+    mixed = {"convergence_threshold": 1e-9, "max_iter": 200, "precision": gg.HF_PRECISION_MIXED,
+             "mixed_threshold": 0.1, "incremental": 1, "anchor_threshold": 1e-2,
+             "initial_guess": gg.HF_GUESS_SAD}
+    rm, _, _ = batch.rhf_scf(mixed)
+    r64, _, _ = batch.rhf_scf({k: v for k, v in mixed.items() if k not in ("precision",)})
+    for m, a, b in zip(mols, rm, r64):
+        assert a["converged"] == 1 and b["converged"] == 1
+        assert abs(a["total_energy"] - b["total_energy"]) < 1e-6
+        eng = gg.Engine(m, 1e-12)
+        single = eng.rhf_scf(m.num_electrons, mixed)
+        assert single["converged"] == 1 and abs(a["total_energy"] - single["total_energy"]) < 1e-7
+        eng.close()
