@@ -192,7 +192,7 @@ Engine::~Engine()
                     d_entry_bra, d_entry_cnt, d_entry_lo0, d_pair_qs, d_off_static, d_cp_meta, plan.off64, plan.off32,
                     plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_Jp32, d_Kp32, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
                     scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
-                    scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j, d_grad, d_shell_atom,
+                    scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j, d_grad, d_shell_atom, d_goff64, d_goff32,
                     d_shell_info, d_block_dmax, d_mol_base, d_mol_n, d_mol_bf0, d_mol_atoms, d_shell_mol,
                     scf.P32a, scf.P32b, scf.P32c};
     ri_destroy(ri);

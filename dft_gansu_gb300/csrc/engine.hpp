@@ -139,6 +139,8 @@ struct Engine {
     bool last_mixed = false;   // whether the last build used the FP32 accumulators
     double* d_grad = nullptr;     // 3 * natom gradient accumulators (allocated on first use)
     int* d_shell_atom = nullptr;  // contracted shell -> atom
+    long long* d_goff64 = nullptr;  // gradient work-item offsets (FP64 / FP32 lists)
+    long long* d_goff32 = nullptr;
     int2* d_shell_info = nullptr;   // per shell: first basis function, number of components
     float* d_block_dmax = nullptr;  // per shell block max |D| of the density being built (mixed plan)
     double* d_scalar = nullptr;  // small scratch scalars (8 doubles)

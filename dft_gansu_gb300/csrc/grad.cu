@@ -16,6 +16,7 @@
 // (dA + dB + dC + dD = 0).  One thread handles one ket component pair (c,d)
 // of one contracted quartet (the quartet lists of the Fock build), so the
 // density weights of a column fit in registers.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -152,16 +153,57 @@ __device__ __forceinline__ T ket_value(int t, int u, int v, const int c[3], cons
 }
 
 struct GradLaunch {
-    FockClassLaunch L;       // FP64 work list, pairs, primitive pairs, Boys table, D' (FP64)
+    FockClassLaunch L;       // work list, pairs, primitive pairs, Boys table, D' of the tier
+    const long long* goff;   // nentry+1 prefix offsets of items: (ket, bra primitive pair) per entry
     const int* shell_atom;   // contracted shell -> atom
     double* grad;            // 3 * natom accumulators
+    int natom;
+    int shared_grad;         // accumulate per block in shared memory (3 * natom doubles)
 };
+
+// Item offsets of a class pair's list: entry e owns cnt_e kets, each split into the
+// bra pair's pp_n primitive pairs, so one work item is one (ket, bra primitive pair).
+// One block per class pair (the layout of the quartet plan's offsets).
+__global__ void __launch_bounds__(256) grad_items_kernel(const long long* __restrict__ off,
+                                                         const int* __restrict__ entry_bra,
+                                                         const ShellPairDev* __restrict__ pairs,
+                                                         const int* __restrict__ cp_meta, int ncp,
+                                                         long long* __restrict__ goff)
+{
+    __shared__ long long part[256];
+    const int cp = blockIdx.x;
+    const int eb = cp_meta[cp], ne = cp_meta[ncp + cp], ob = cp_meta[3 * ncp + cp];
+    long long base = 0;
+    if (threadIdx.x == 0) goff[ob] = 0;
+    for (int start = 0; start < ne; start += blockDim.x) {
+        const int i = start + threadIdx.x;
+        long long v = 0;
+        if (i < ne) v = (off[ob + i + 1] - off[ob + i]) * static_cast<long long>(pairs[entry_bra[eb + i]].pp_n);
+        part[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < blockDim.x; o <<= 1) {  // inclusive Hillis-Steele scan
+            const long long add = (threadIdx.x >= o) ? part[threadIdx.x - o] : 0;
+            __syncthreads();
+            part[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (i < ne) goff[ob + i + 1] = base + part[threadIdx.x];
+        base += part[blockDim.x - 1];
+        __syncthreads();
+    }
+}
 
 template <class T>
 __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch G, int ncd)
 {
+    extern __shared__ double sgrad[];
     const FockClassLaunch& L = G.L;
-    const long long total = L.off[L.nentry];
+    if (G.shared_grad) {
+        for (int i = threadIdx.x; i < 3 * G.natom; i += blockDim.x) sgrad[i] = 0.0;
+        __syncthreads();
+    }
+    double* const gacc = G.shared_grad ? sgrad : G.grad;
+    const long long total = G.goff[L.nentry];
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((total + 31) >> 5) * ncd;
     const long long warp_stride = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
@@ -184,10 +226,12 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
         const int cdi = static_cast<int>(wid % ncd);
         const long long w = (wid / ncd) * 32 + lane;
         if (w >= total) continue;
-        const int e = find_entry(L.off, L.nentry, w);
+        const int e = find_entry(G.goff, L.nentry, w);
         const int bra = __ldg(L.entry_bra + e);
-        const int ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(w - __ldg(L.off + e));
         const ShellPairDev bp = L.pairs[bra];
+        const long long item = w - __ldg(G.goff + e);
+        const int ip = static_cast<int>(item % bp.pp_n);
+        const int ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(item / bp.pp_n);
         const ShellPairDev kp = L.pairs[ket];
         const int la = bp.la, lb = bp.lb, lc = kp.la, ld = kp.lb;
         const int na = ncart(la), nb = ncart(lb), nd = ncart(ld);
@@ -229,7 +273,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
         //   dC_k = sum H0 (2 gamma x[c + 1_k] - c_k x[c - 1_k]).
         T gA[3] = {0, 0, 0}, gP[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
         T H0[kGX], HA[3][kGX];
-        for (int ip = 0; ip < bp.pp_n; ++ip) {
+        {  // this item's bra primitive pair
             const PP pb = pp[bp.pp_off + ip];
             if (pb.Q * kQmax < thr) continue;
             const T alpha2 = T(2) * (pb.p - pb.b);
@@ -319,11 +363,16 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
         const int atA = G.shell_atom[bp.A], atB = G.shell_atom[bp.B], atC = G.shell_atom[kp.A],
                   atD = G.shell_atom[kp.B];
         for (int k = 0; k < 3; ++k) {
-            atomicAdd(&G.grad[3 * atA + k], static_cast<double>(gA[k]));
-            atomicAdd(&G.grad[3 * atB + k], static_cast<double>(gB[k]));
-            atomicAdd(&G.grad[3 * atC + k], static_cast<double>(gC[k]));
-            atomicAdd(&G.grad[3 * atD + k], -static_cast<double>(gA[k] + gB[k] + gC[k]));
+            atomicAdd(&gacc[3 * atA + k], static_cast<double>(gA[k]));
+            atomicAdd(&gacc[3 * atB + k], static_cast<double>(gB[k]));
+            atomicAdd(&gacc[3 * atC + k], static_cast<double>(gC[k]));
+            atomicAdd(&gacc[3 * atD + k], -static_cast<double>(gA[k] + gB[k] + gC[k]));
         }
+    }
+    if (G.shared_grad) {  // one flush per block
+        __syncthreads();
+        for (int i = threadIdx.x; i < 3 * G.natom; i += blockDim.x)
+            if (sgrad[i] != 0.0) atomicAdd(&G.grad[i], sgrad[i]);
     }
 }
 
@@ -499,11 +548,29 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
         const double c2 = e.cgto_max * e.cgto_max;
         if ((st = mixed_plan(e, d_D, c2 * c2, true, mixed_threshold, 0.0, s))) return st;
     }
+    // work items (ket, bra primitive pair) of every list in use
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    const size_t noff = e.off_static.size();
+    if (!e.d_goff64 && (cudaMalloc(&e.d_goff64, sizeof(long long) * noff) != cudaSuccess ||
+                        cudaMalloc(&e.d_goff32, sizeof(long long) * noff) != cudaSuccess))
+        return set_error("cudaMalloc of gradient item offsets failed"), HF_ERR_OUT_OF_MEMORY;
+    grad_items_kernel<<<ncp, 256, 0, s>>>(mixed ? e.plan.off64 : e.d_off_static, e.d_entry_bra, e.d_pairs, e.d_cp_meta,
+                                          ncp, e.d_goff64);
+    GB_LAUNCH_CHECK();
+    if (mixed) {
+        grad_items_kernel<<<ncp, 256, 0, s>>>(e.plan.off32, e.d_entry_bra, e.d_pairs, e.d_cp_meta, ncp, e.d_goff32);
+        GB_LAUNCH_CHECK();
+    }
+    const size_t sgrad_bytes = sizeof(double) * 3 * natom;
+    const bool shared_grad = sgrad_bytes <= 32 * 1024;
     // two-electron part over the quartet lists of every class
     for (int c = 0; c < static_cast<int>(e.class_pairs.size()); ++c) {
         const ClassPair& cp = e.class_pairs[c];
         if (cp.n_survivors == 0) continue;
         const PairClass& Y = e.pair_classes[cp.Y];
+        const PairClass& X = e.pair_classes[cp.X];
+        int max_pp = 1;
+        for (int i = X.begin; i < X.begin + X.count; ++i) max_pp = std::max(max_pp, e.pairs[i].pp_n);
         for (int tier = 0; tier < (mixed ? 2 : 1); ++tier) {
             const bool f32 = tier == 1;
             GradLaunch G;
@@ -530,17 +597,22 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
             G.L.skip_cut = 0.0;
             G.L.mol_active = nullptr;
             G.L.shell_mol = e.d_shell_mol;
+            G.goff = (f32 ? e.d_goff32 : e.d_goff64) + cp.entry_begin + c;
             G.shell_atom = e.d_shell_atom;
             G.grad = e.d_grad;
+            G.natom = natom;
+            G.shared_grad = shared_grad ? 1 : 0;
             const int ncd = ncart(Y.la) * ncart(Y.lb);
-            const long long warps = ((cp.n_survivors + 31) / 32) * ncd;
+            // items <= survivors x the class's largest bra primitive-pair count (grid-stride loop)
+            const long long warps = ((cp.n_survivors * max_pp + 31) / 32) * ncd;
             const int grid = static_cast<int>(std::max<long long>(
                 1, std::min<long long>((warps * 32 + kGradThreads - 1) / kGradThreads,
                                        static_cast<long long>(e.num_sms) * 32)));
+            const size_t smem = shared_grad ? sgrad_bytes : 0;
             if (f32)
-                grad_eri_kernel<float><<<grid, kGradThreads, 0, s>>>(G, ncd);
+                grad_eri_kernel<float><<<grid, kGradThreads, smem, s>>>(G, ncd);
             else
-                grad_eri_kernel<double><<<grid, kGradThreads, 0, s>>>(G, ncd);
+                grad_eri_kernel<double><<<grid, kGradThreads, smem, s>>>(G, ncd);
             GB_LAUNCH_CHECK();
         }
     }
