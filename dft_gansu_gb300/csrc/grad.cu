@@ -107,51 +107,6 @@ __device__ __forceinline__ void grad_r_table(int L, const T* Fs, T X, T Y, T Z, 
     }
 }
 
-// ket contraction of one ket component (c + sh along axis ax, d) into the bra
-// Hermite index up to order lmax: x[tuv] = sum (-1)^{tau+nu+phi} E^{cd} R
-template <class T>
-__device__ __forceinline__ void ket_contract(int lmax, const int c[3], const int d[3], const T* fx, const T* fy,
-                                             const T* fz, const T* r, T* x)
-{
-    const T* ex = fx + (c[0] * kGI + d[0]) * kGT;
-    const T* ey = fy + (c[1] * kGI + d[1]) * kGT;
-    const T* ez = fz + (c[2] * kGI + d[2]) * kGT;
-    for (int t = 0; t <= lmax; ++t)
-        for (int u = 0; u + t <= lmax; ++u)
-            for (int v = 0; v + u + t <= lmax; ++v) {
-                T s = T(0);
-                for (int tau = 0; tau <= c[0] + d[0]; ++tau)
-                    for (int nu = 0; nu <= c[1] + d[1]; ++nu) {
-                        const T exy = ex[tau] * ey[nu];
-                        for (int phi = 0; phi <= c[2] + d[2]; ++phi) {
-                            const T w = exy * ez[phi] * r[gidx(t + tau, u + nu, v + phi)];
-                            s += ((tau + nu + phi) & 1) ? -w : w;
-                        }
-                    }
-                x[gidx(t, u, v)] = s;
-            }
-}
-
-// one entry of the ket contraction: sum (-1)^{tau+nu+phi} E^{cd}_{tau nu phi} R_{t+tau, u+nu, v+phi}
-template <class T>
-__device__ __forceinline__ T ket_value(int t, int u, int v, const int c[3], const int d[3], const T* fx, const T* fy,
-                                       const T* fz, const T* r)
-{
-    const T* ex = fx + (c[0] * kGI + d[0]) * kGT;
-    const T* ey = fy + (c[1] * kGI + d[1]) * kGT;
-    const T* ez = fz + (c[2] * kGI + d[2]) * kGT;
-    T s = T(0);
-    for (int tau = 0; tau <= c[0] + d[0]; ++tau)
-        for (int nu = 0; nu <= c[1] + d[1]; ++nu) {
-            const T exy = ex[tau] * ey[nu];
-            for (int phi = 0; phi <= c[2] + d[2]; ++phi) {
-                const T w = exy * ez[phi] * r[gidx(t + tau, u + nu, v + phi)];
-                s += ((tau + nu + phi) & 1) ? -w : w;
-            }
-        }
-    return s;
-}
-
 struct GradLaunch {
     FockClassLaunch L;       // work list, pairs, primitive pairs, Boys table, D' of the tier
     const long long* goff;   // nentry+1 prefix offsets of items: (ket, bra primitive pair) per entry
@@ -219,6 +174,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
     T* const fy = ey;
     T* const fz = ez;
     T Fs[kGL + 1], r[kGR];
+    T z0[kGR], zD[kGR];  // separable ket-contraction intermediates (R's buffer holds the y stages)
     T wcol[kGNAB];
 
     for (long long wid = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; wid < nwarps;
@@ -329,13 +285,62 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
                 T scale = pb.KoP * pk.KoP * rr;
                 for (int n = 0; n <= lt; ++n) { Fs[n] *= scale; scale *= T(-2) * rho; }
                 grad_r_table<T>(lt, Fs, X, Y, Z, r);
-                // contractions evaluated where they are used (no x arrays):
-                //   gA += HA x0,  gP += H0[tuv - 1_k] x0[tuv],  gC += H0 (2 gamma x[c+1_k] - c_k x[c-1_k])
-                for (int t = 0; t <= lab + 1; ++t)
-                    for (int u = 0; u + t <= lab + 1; ++u)
-                        for (int v = 0; v + u + t <= lab + 1; ++v) {
+                // Separable ket contraction, one axis at a time, with (-1)^tau folded into
+                // the per-axis vectors:  e0_k = E^{c_k d_k},  eD_k = 2 gamma E^{c_k+1, d_k} - c_k E^{c_k-1, d_k}.
+                //   x0[tuv]  = sum e0_x e0_y e0_z R[t+tau, u+nu, v+phi]   (tuv <= lab + 1)
+                //   xD_k[tuv] = the same with eD along axis k              (tuv <= lab)
+                // built as z-, then y-, then x-contractions; the intermediates are only
+                // needed for v (and u + v) <= lab + 1.
+                T e0[3][kGT], eD[3][kGT];
+                int n0[3], nD[3];
+                for (int k = 0; k < 3; ++k) {
+                    const T* tab = k == 0 ? fx : (k == 1 ? fy : fz);
+                    const T* row0 = tab + (c[k] * kGI + d[k]) * kGT;
+                    const T* rowp = tab + ((c[k] + 1) * kGI + d[k]) * kGT;
+                    const T* rowm = tab + ((c[k] > 0 ? c[k] - 1 : 0) * kGI + d[k]) * kGT;
+                    n0[k] = c[k] + d[k];
+                    nD[k] = c[k] + d[k] + 1;
+                    for (int t = 0; t <= nD[k]; ++t) {
+                        const T sg = (t & 1) ? T(-1) : T(1);
+                        e0[k][t] = (t <= n0[k]) ? sg * row0[t] : T(0);
+                        T v = gamma2 * rowp[t];
+                        if (c[k] > 0 && t <= c[k] - 1 + d[k]) v -= T(c[k]) * rowm[t];
+                        eD[k][t] = sg * v;
+                    }
+                }
+                const int lv = lab + 1;
+                // z stage: out[t,u,v] = sum_phi ez[phi] R[t, u, v + phi]
+                auto zstage = [&](const T* ez, int nz, T* out) {
+                    for (int v = 0; v <= lv; ++v)
+                        for (int t = 0; t + v <= lt; ++t)
+                            for (int u = 0; t + u + v <= lt; ++u) {
+                                T acc = T(0);
+                                for (int f = 0; f <= nz && t + u + v + f <= lt; ++f) acc += ez[f] * r[gidx(t, u, v + f)];
+                                out[gidx(t, u, v)] = acc;
+                            }
+                };
+                // y stage: out[t,u,v] = sum_nu ey[nu] zin[t, u + nu, v]  (u + v <= lv)
+                auto ystage = [&](const T* ey, int ny, const T* zin, T* out) {
+                    for (int u = 0; u <= lv; ++u)
+                        for (int v = 0; u + v <= lv; ++v)
+                            for (int t = 0; t + u + v <= lt; ++t) {
+                                T acc = T(0);
+                                for (int g = 0; g <= ny && t + u + g + v <= lt; ++g) acc += ey[g] * zin[gidx(t, u + g, v)];
+                                out[gidx(t, u, v)] = acc;
+                            }
+                };
+                // both z stages first (R is then dead and its buffer holds each y stage)
+                zstage(e0[2], n0[2], z0);
+                zstage(eD[2], nD[2], zD);
+                // base: x stage fused with the bra contractions
+                //   gA += HA x0,  gP += H0[tuv - 1_k] x0[tuv],  gC_x += H0 xD_x
+                ystage(e0[1], n0[1], z0, r);
+                for (int t = 0; t <= lv; ++t)
+                    for (int u = 0; u + t <= lv; ++u)
+                        for (int v = 0; v + u + t <= lv; ++v) {
+                            T x = T(0);
+                            for (int a = 0; a <= n0[0] && t + a + u + v <= lt; ++a) x += e0[0][a] * r[gidx(t + a, u, v)];
                             const int h = gidx(t, u, v);
-                            const T x = ket_value<T>(t, u, v, c, d, fx, fy, fz, r);
                             gA[0] += HA[0][h] * x;
                             gA[1] += HA[1][h] * x;
                             gA[2] += HA[2][h] * x;
@@ -343,19 +348,25 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
                             if (u > 0) gP[1] += H0[gidx(t, u - 1, v)] * x;
                             if (v > 0) gP[2] += H0[gidx(t, u, v - 1)] * x;
                             if (t + u + v > lab) continue;
-                            const T h0 = H0[h];
-                            if (h0 == T(0)) continue;
-                            for (int k = 0; k < 3; ++k) {
-                                int cp[3] = {c[0], c[1], c[2]};
-                                cp[k] += 1;
-                                T dc = gamma2 * ket_value<T>(t, u, v, cp, d, fx, fy, fz, r);
-                                if (c[k] > 0) {
-                                    cp[k] -= 2;
-                                    dc -= T(c[k]) * ket_value<T>(t, u, v, cp, d, fx, fy, fz, r);
-                                }
-                                gC[k] += h0 * dc;
-                            }
+                            T xx = T(0);
+                            for (int a = 0; a <= nD[0] && t + a + u + v <= lt; ++a) xx += eD[0][a] * r[gidx(t + a, u, v)];
+                            gC[0] += H0[h] * xx;
                         }
+                // y and z derivatives of the ket centre: gC_k += H0 xD_k (tuv <= lab)
+                for (int k = 1; k < 3; ++k) {
+                    if (k == 1) ystage(eD[1], nD[1], z0, r); else ystage(e0[1], n0[1], zD, r);
+                    T acc = T(0);
+                    for (int t = 0; t <= lab; ++t)
+                        for (int u = 0; u + t <= lab; ++u)
+                            for (int v = 0; v + u + t <= lab; ++v) {
+                                const T h0 = H0[gidx(t, u, v)];
+                                if (h0 == T(0)) continue;
+                                T x = T(0);
+                                for (int a = 0; a <= n0[0] && t + a + u + v <= lt; ++a) x += e0[0][a] * r[gidx(t + a, u, v)];
+                                acc += h0 * x;
+                            }
+                    gC[k] += acc;
+                }
             }
         }
         T gB[3];
