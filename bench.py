@@ -640,7 +640,8 @@ def main():
     ap.add_argument("--skip-gradient", action="store_true")
     ap.add_argument("--workload", default="decane",
                     choices=["decane", "c60_ri", "decane_ri", "water_batch", "decane_grad_fd"])
-    ap.add_argument("--grad-threshold", type=float, default=1e-3)
+    ap.add_argument("--grad-threshold", type=float, default=MIXED_THRESHOLD,
+                    help="gradient FP32 cut on Qs_ab Qs_cd c_max^4 max|D|^2 (error ~1e-8 Eh/bohr at 0.1)")
     ap.add_argument("--batch-size", type=int, default=256)
     ap.add_argument("--ri-threshold", type=float, default=1e-2)
     ap.add_argument("--guess", default=None, choices=["core", "gwh", "sad"],
