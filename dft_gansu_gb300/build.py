@@ -30,7 +30,9 @@ FOCK_CLASSES = [
     (2, 2, 2, 0), (2, 2, 2, 1), (2, 2, 2, 2),
 ]
 
-CUDA_SOURCES = ["engine.cu", "fock.cu", "fock_generic.cu", "one_electron.cu", "scf.cu", "peaks.cu", "diis_noalloc.cu", "grad.cu", "ri.cu", "tc_gemm.cu", "batch.cu"]
+# longest translation units first (the pool starts them in this order)
+CUDA_SOURCES = ["grad_class_f32.cu", "grad_class_f64.cu", "grad.cu", "ri.cu", "batch.cu", "scf.cu", "engine.cu",
+                "fock.cu", "fock_generic.cu", "one_electron.cu", "peaks.cu", "diis_noalloc.cu", "tc_gemm.cu"]
 CXX_SOURCES = ["molecule.cpp", "errors.cpp"]
 
 
