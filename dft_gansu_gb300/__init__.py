@@ -132,7 +132,7 @@ def _scf_options(options: dict | None):
     lib().hf_scf_options_default(C.byref(opt))
     keep = []
     for k, v in (options or {}).items():
-        if k in ("guess_density_a", "guess_density_b"):
+        if k in ("guess_density_a", "guess_density_b", "orthogonalizer"):
             if v is not None and not isinstance(v, int):
                 v = v.contiguous().double()
                 keep.append(v)
@@ -304,9 +304,22 @@ class Engine:
         t = self.torch
         return t.from_numpy(a).to("cuda"), t.from_numpy(b).to("cuda")
 
+    def spherical_orthogonalizer(self):
+        """X over the pure (spherical-harmonic) functions (dft_gansu_gb300/spherical.py), CUDA N x N."""
+        if getattr(self, "_x_pure", None) is None:
+            from . import spherical
+
+            S = self.core_hamiltonian()[0].double().cpu().numpy()
+            X = spherical.orthogonalizer(S, spherical.transform(self.mol))
+            self._x_pure = self.torch.from_numpy(X).to("cuda")
+        return self._x_pure
+
     def _with_guess(self, options: dict | None) -> dict:
-        """initial_guess SAD without densities: assemble them from the atoms."""
+        """initial_guess SAD without densities: assemble them from the atoms;
+        spherical=True: the pure-function orthogonaliser."""
         options = dict(options or {})
+        if options.pop("spherical", False):
+            options["orthogonalizer"] = self.spherical_orthogonalizer()
         if options.get("initial_guess") == HF_GUESS_SAD and options.get("guess_density_a") is None:
             options["guess_density_a"], options["guess_density_b"] = self.sad_density()
         return options
@@ -396,7 +409,7 @@ _DEFAULTS = {
     "rohf_parameter_name": "roothaan", "geometry_optimization": "0", "geometry_optimization_method": "powell",
     "export_sad_cache": "0",
     # added by this engine, same parsing rules
-    "precision": "fp64", "mixed_threshold": "1e-7", "incremental_fock": "0",
+    "precision": "fp64", "mixed_threshold": "1e-7", "incremental_fock": "0", "spherical": "0",
 }
 _SHORT = {"-m": "method", "-v": "verbose", "-p": "parameter_file", "-x": "xyzfilename", "-g": "gbsfilename",
           "-ag": "auxiliary_gbsfilename", "-c": "charge"}
@@ -561,6 +574,7 @@ class _HFBase:
             "verbose": p.get("verbose", int),
             "eri_method": self.eri_method,
             "initial_guess": _GUESSES[guess],
+            "spherical": bool(p.get("spherical", bool)),
         }
         if guess == "density":
             if density_alpha is None or density_beta is None:

@@ -72,6 +72,7 @@ class ScfOptions(C.Structure):
         ("initial_guess", C.c_int),
         ("guess_density_a", C.c_void_p),
         ("guess_density_b", C.c_void_p),
+        ("orthogonalizer", C.c_void_p),
     ]
 
 

@@ -678,6 +678,9 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     const bool density_guess = opt.initial_guess == HF_GUESS_DENSITY || opt.initial_guess == HF_GUESS_SAD;
     if (density_guess && !opt.guess_density_a)
         return set_error("initial_guess density/SAD needs guess_density_a (block layout)"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.orthogonalizer)
+        return set_error("hf_batch_rhf_scf: the orthogonalizer option is single-molecule only"),
+               HF_ERR_INVALID_ARGUMENT;
     const int nmol = e.nmol;
     Batch b;
     b.e = &e;

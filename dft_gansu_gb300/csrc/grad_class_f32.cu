@@ -1,6 +1,5 @@
 // FP32 class kernels of the analytic gradient with compile-time loops:
-// la + lb + lc + ld <= 6 (FP32 tables take half the registers of FP64, so the
-// larger classes stay within a few hundred bytes of spills).
+// la + lb + lc + ld <= 4 (L = 5, 6 in grad_class_f32_l56.cu).
 #include "grad_kernel.cuh"
 
 namespace gb {
@@ -14,10 +13,9 @@ bool launch_grad_class_f32(int la, int lb, int lc, int ld, const GradLaunch& G, 
     }
     GB_GC(0, 0, 0, 0) GB_GC(1, 0, 0, 0) GB_GC(1, 0, 1, 0) GB_GC(1, 1, 0, 0) GB_GC(1, 1, 1, 0) GB_GC(1, 1, 1, 1)
     GB_GC(2, 0, 0, 0) GB_GC(2, 0, 1, 0) GB_GC(2, 0, 1, 1) GB_GC(2, 0, 2, 0) GB_GC(2, 1, 0, 0) GB_GC(2, 1, 1, 0)
-    GB_GC(2, 2, 0, 0) GB_GC(2, 1, 1, 1) GB_GC(2, 1, 2, 0) GB_GC(2, 2, 1, 0) GB_GC(2, 1, 2, 1) GB_GC(2, 2, 1, 1)
-    GB_GC(2, 2, 2, 0)
+    GB_GC(2, 2, 0, 0)
 #undef GB_GC
-    return false;
+    return launch_grad_class_f32_l56(la, lb, lc, ld, G, grid, smem, s);
 }
 
 }  // namespace gb

@@ -1,6 +1,6 @@
 // FP64 class kernels of the analytic gradient with compile-time loops:
-// la + lb + lc + ld <= 4 (the larger FP64 classes spill several KB and run the
-// generic kernel of grad.cu).
+// la + lb + lc + ld <= 4 (the L = 5 classes in grad_class_f64_l5.cu; the larger
+// FP64 classes run the generic kernel of grad.cu).
 #include "grad_kernel.cuh"
 
 namespace gb {
@@ -14,7 +14,7 @@ bool launch_grad_class_f64(int la, int lb, int lc, int ld, const GradLaunch& G, 
     }
     GB_GC(0, 0, 0, 0) GB_GC(1, 0, 0, 0) GB_GC(1, 0, 1, 0) GB_GC(1, 1, 0, 0) GB_GC(1, 1, 1, 0) GB_GC(1, 1, 1, 1)
     GB_GC(2, 0, 0, 0) GB_GC(2, 0, 1, 0) GB_GC(2, 0, 1, 1) GB_GC(2, 0, 2, 0) GB_GC(2, 1, 0, 0) GB_GC(2, 1, 1, 0)
-    GB_GC(2, 2, 0, 0)
+    GB_GC(2, 2, 0, 0) GB_GC(2, 1, 1, 1) GB_GC(2, 1, 2, 0) GB_GC(2, 2, 1, 0)
 #undef GB_GC
     return false;
 }

@@ -292,9 +292,13 @@ __global__ void __launch_bounds__(kGradThreads) grad_class_kernel(const GradLaun
 }
 
 
-// launchers of the class kernels (grad_class_f64.cu, grad_class_f32.cu): false
+// launchers of the class kernels (grad_class_f64*.cu, grad_class_f32*.cu): false
 // when the class has no compile-time kernel in that type
 bool launch_grad_class_f64(int la, int lb, int lc, int ld, const GradLaunch& G, int grid, size_t smem, cudaStream_t s);
 bool launch_grad_class_f32(int la, int lb, int lc, int ld, const GradLaunch& G, int grid, size_t smem, cudaStream_t s);
+bool launch_grad_class_f64_l5(int la, int lb, int lc, int ld, const GradLaunch& G, int grid, size_t smem,
+                              cudaStream_t s);
+bool launch_grad_class_f32_l56(int la, int lb, int lc, int ld, const GradLaunch& G, int grid, size_t smem,
+                               cudaStream_t s);
 
 }  // namespace gb

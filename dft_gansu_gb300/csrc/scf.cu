@@ -560,8 +560,12 @@ int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t
     return HF_OK;
 }
 
+// e = FDS - SDF; transform 1: X e X^T (diis_include_transform, computeDIISErrorMatrix,
+// src/gpu_manager.cu:1020-1068); transform 2: X^T e X, the error in the orthonormal
+// basis of a caller's orthogonaliser (its span is a subspace: the AO-basis error
+// has a component outside it that does not vanish at convergence)
 int diis_error(Engine& e, const double* S, const double* X, const double* F, const double* D, double* E,
-               bool include_transform, cudaStream_t s)
+               int transform, cudaStream_t s)
 {
     auto& w = e.scf;
     const long long nn = static_cast<long long>(w.n) * w.n;
@@ -572,9 +576,12 @@ int diis_error(Engine& e, const double* S, const double* X, const double* F, con
     if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, F, E))) return st;     // SDF
     sub_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T2, E, nn, E);
     GB_LAUNCH_CHECK();
-    if (include_transform) {
+    if (transform == 1) {
         if ((st = gemm_rm(e.cublas, false, false, w.n, X, E, w.T1))) return st;
         if ((st = gemm_rm(e.cublas, false, true, w.n, w.T1, X, E))) return st;
+    } else if (transform == 2) {
+        if ((st = gemm_rm(e.cublas, true, false, w.n, X, E, w.T1))) return st;
+        if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, X, E))) return st;
     }
     return HF_OK;
 }
@@ -619,6 +626,25 @@ int jk_of(Engine& e, bool use_ri, const double* D, double* J, double* K, int pre
 
 bool valid_guess(int g) { return g == HF_GUESS_CORE || g == HF_GUESS_GWH || g == HF_GUESS_DENSITY || g == HF_GUESS_SAD; }
 
+// X = U s^{-1/2} from the eigen-decomposition of S already in w.W / w.eps
+// (HF::compute_transform_matrix, src/hf.cu:171-243), or the caller's
+// orthogonaliser (options.orthogonalizer: a subspace of the AO space, e.g. the
+// spherical-harmonic functions; its DIIS error is taken in the orthogonal basis)
+int diis_x(const hf_scf_options& opt) { return opt.orthogonalizer ? 2 : (opt.diis_include_transform != 0 ? 1 : 0); }
+
+int orthogonalizer(Engine& e, const hf_scf_options& opt, cudaStream_t s)
+{
+    auto& w = e.scf;
+    const long long nn = static_cast<long long>(w.n) * w.n;
+    if (opt.orthogonalizer) {
+        GB_CUDA_TRY(cudaMemcpyAsync(w.X, opt.orthogonalizer, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        return HF_OK;
+    }
+    transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, w.n, w.X);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
 }  // namespace
 
 }  // namespace gb
@@ -642,6 +668,9 @@ void hf_scf_options_default(hf_scf_options* o)
     o->eri_method = HF_ERI_DIRECT;
     o->anchor_threshold = 0.0;
     o->initial_guess = HF_GUESS_CORE;
+    o->guess_density_a = nullptr;
+    o->guess_density_b = nullptr;
+    o->orthogonalizer = nullptr;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -657,7 +686,7 @@ int hf_compute_diis_error(hf_engine* eng, const double* d_overlap, const double*
     if (st) return st;
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     cublasSetStream(e.cublas, s);
-    return diis_error(e, d_overlap, d_transform, d_fock, d_density, d_error, include_transform != 0, s);
+    return diis_error(e, d_overlap, d_transform, d_fock, d_density, d_error, include_transform != 0 ? 1 : 0, s);
 }
 
 int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d_focks, double* d_new_fock,
@@ -832,7 +861,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     if (use_ri && (st = ri_require_b(e, s))) return st;
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
-    transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
+    if ((st = orthogonalizer(e, opt, s))) return st;
     GB_LAUNCH_CHECK();
     // purification needs no orbitals, but the RI K build uses the occupied ones
     const bool purify = opt.eigensolver == HF_EIGEN_PURIFICATION && !use_ri;
@@ -912,7 +941,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         cudaEventRecord(q0, s);
         diis_timed = true;
         const int slot = diis_iter % m;
-        if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, opt.diis_include_transform != 0, s))) return st;
+        if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, diis_x(opt), s))) return st;
         GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + slot * nn, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
         const int nprev = std::min(diis_iter + 1, m);
         if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, w.F, s))) return st;
@@ -1066,7 +1095,7 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     // include/uhf.hpp:484-620): orbitals for both spins with the beta symmetry break
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
-    transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
+    if ((st = orthogonalizer(e, opt, s))) return st;
     GB_LAUNCH_CHECK();
     if (density_guess) {
         // D_a, D_b given (D_b NULL: both halves of D_a); F, C, break, D, F
@@ -1104,10 +1133,10 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         // DIIS per spin on the same cyclic ring index (Convergence_UHF_DIIS, include/uhf.hpp:291-380)
         const int slot = diis_iter % m;
         const int nprev = std::min(diis_iter + 1, m);
-        if ((st = diis_error(e, w.S, w.X, Fa, Da, w.Es + slot * nn, opt.diis_include_transform != 0, s))) return st;
+        if ((st = diis_error(e, w.S, w.X, Fa, Da, w.Es + slot * nn, diis_x(opt), s))) return st;
         GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + slot * nn, Fa, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
         if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, Fa, s))) return st;
-        if ((st = diis_error(e, w.S, w.X, Fb, Db, Esb + slot * nn, opt.diis_include_transform != 0, s))) return st;
+        if ((st = diis_error(e, w.S, w.X, Fb, Db, Esb + slot * nn, diis_x(opt), s))) return st;
         GB_CUDA_TRY(cudaMemcpyAsync(Fsb + slot * nn, Fb, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
         if (nprev > 1 && (st = diis_extrapolate(e, Esb, Fsb, nprev, Fb, s))) return st;
         ++diis_iter;
@@ -1243,7 +1272,7 @@ int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupl
     // matrix is formed with the core-guess orbitals.
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
-    transform_kernel<<<grid_nn(nn), 256, 0, s>>>(w.W, w.eps, n, w.X);
+    if ((st = orthogonalizer(e, opt, s))) return st;
     GB_LAUNCH_CHECK();
     if (density_guess) {
         if ((st = coefficients(e, w.H, s, opt.eigensolver))) return st;
@@ -1287,7 +1316,7 @@ int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupl
         prev = energy;
         // Convergence_ROHF_DIIS (include/rohf.hpp:307-360): unified F with D = D_c + D_o
         const int slot = diis_iter % m;
-        if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, opt.diis_include_transform != 0, s))) break;
+        if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, diis_x(opt), s))) break;
         if (cudaMemcpyAsync(w.Fs + slot * nn, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
             st = (set_error("cudaMemcpyAsync failed"), HF_ERR_CUDA);
             break;

@@ -237,6 +237,11 @@ typedef struct {
     const double* guess_density_a;  /* HF_GUESS_DENSITY / HF_GUESS_SAD: device alpha-spin density (N x N;
                                        a batch engine: the block layout); RHF takes D_a + D_b */
     const double* guess_density_b;  /* beta-spin density, same layout; NULL for RHF means D_a is the total */
+    const double* orthogonalizer;   /* NULL: X = U s^{-1/2} of S (src/hf.cu:171-243).  Otherwise a device N x N
+                                       row-major X whose nonzero columns span the orbital space, e.g. the
+                                       spherical-harmonic subspace of the Cartesian basis (no reference
+                                       counterpart); the DIIS error is then X^T (FDS - SDF) X.
+                                       Single-molecule SCFs only. */
 } hf_scf_options;
 
 /* Density from the Fock matrix inside the SCF loop.  The reference diagonalises

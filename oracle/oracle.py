@@ -322,12 +322,44 @@ def gwh_guess(S, H):
     return 1.75 * S * (d[:, None] + d[None, :]) * 0.5
 
 
+def spherical_transform(b: Basis):
+    """Pure-function combinations over each shell's Cartesian functions: s, p kept;
+    d (xx, yy, zz, xy, xz, yz) -> xy, yz, 2zz - xx - yy, xz, xx - yy.  Restates the
+    real solid harmonics of degree 2 (no reference counterpart: GANSU is Cartesian)."""
+    cols = []
+    for L, off in zip(b.l, b.bf_off):
+        L, off = int(L), int(off)
+        if L <= 1:
+            for i in range((L + 1) * (L + 2) // 2):
+                v = np.zeros(b.nbf); v[off + i] = 1.0; cols.append(v)
+        else:
+            xx, yy, zz, xy, xz, yz = (off + i for i in range(6))
+            for comb in ({xy: 1.0}, {yz: 1.0}, {zz: 2.0, xx: -1.0, yy: -1.0}, {xz: 1.0}, {xx: 1.0, yy: -1.0}):
+                v = np.zeros(b.nbf)
+                for k, c in comb.items():
+                    v[k] = c
+                cols.append(v)
+    return np.array(cols).T
+
+
+def spherical_orthogonalizer(S, T, tol=1e-6):
+    """X = T U s^{-1/2} of T^T S T (eigenvalues below tol dropped), zero-padded to N x N."""
+    w, U = np.linalg.eigh(T.T @ S @ T)
+    keep = w >= tol
+    X = np.zeros((S.shape[0], S.shape[0]))
+    X[:, :keep.sum()] = T @ (U[:, keep] / np.sqrt(w[keep]))
+    return X
+
+
 def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False, guess="core",
-        guess_density=None):
+        guess_density=None, X=None):
     """The reference SCF loop (src/hf.cu:278-307) with DIIS and the core, GWH,
     density (F = F(D)) or SAD (F(D), C, D, F) guess (include/rhf.hpp:378-588);
-    guess_density is the total density D_a + D_b."""
-    X = transform_matrix(S)
+    guess_density is the total density D_a + D_b.  X: an orthogonaliser over a
+    subspace (the DIIS error is then taken in the orthogonal basis)."""
+    project = X is not None  # DIIS error X^T e X in the orthonormal basis of the subspace
+    if X is None:
+        X = transform_matrix(S)
     if guess in ("density", "sad"):
         F = fock(guess_density)
         if guess == "sad":
@@ -354,7 +386,9 @@ def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_tran
         it += 1
         prev = energy
         e = F @ D @ S - S @ D @ F
-        if include_transform:
+        if project:
+            e = X.T @ e @ X
+        elif include_transform:
             e = X @ e @ X.T
         slot = diis_it % diis_size
         errs[slot], focks[slot] = e, F.copy()

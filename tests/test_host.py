@@ -159,3 +159,19 @@ def test_sad_format_roundtrip_and_atom_ranges(built_library, tmp_path):
     sad.export_sad_cache(tmp_path / "c.dat", dens["O"][0], dens["O"][1])
     toks = (tmp_path / "c.dat").read_text().split()
     assert toks[0] == "9" and len(toks) == 1 + 2 * 81
+
+
+def test_pure_function_counts(built_library):
+    """Pure (spherical) function counts of the benchmark inputs: the spherical sizes
+    quoted for them (decane cc-pVDZ 250, C60 cc-pVDZ 840, cc-pVDZ-RIFIT 3360 needs f
+    shells and is not built); the transform's d block spans the pure functions."""
+    from dft_gansu_gb300 import spherical
+
+    dec = gg.Molecular(geometry.alkane(10, jitter=0.02, seed=0), gg.basis_path("cc-pvdz"))
+    assert dec.num_basis == 260 and spherical.num_pure(dec) == 250
+    c60 = gg.Molecular(geometry.c60(), gg.basis_path("cc-pvdz"))
+    assert c60.num_basis == 900 and spherical.num_pure(c60) == 840
+    T = spherical.transform(dec)
+    assert T.shape == (260, 250) and np.linalg.matrix_rank(T) == 250
+    # the pure d combinations carry no r^2 = xx + yy + zz component (coefficient space)
+    assert np.allclose(spherical.D_PURE.T @ np.array([1, 1, 1, 0, 0, 0.0]), 0.0)

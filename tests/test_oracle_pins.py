@@ -246,3 +246,27 @@ def test_oracle_sad_guess_reaches_the_core_guess_energy():
     r_den = O.rhf(S, H, fock, 5, enuc, thr=1e-10, guess="density", guess_density=Da + Db)
     for r in (r_sad, r_den):
         assert r["converged"] and abs(r["total_energy"] - r_core["total_energy"]) < 1e-9
+
+
+def test_oracle_spherical_scf_equals_pure_basis_scf():
+    """The SCF over the pure-function subspace through an orthogonaliser (DIIS error
+    X^T e X) equals an SCF run directly on the transformed S, H and ERI tensor; for
+    s/p-only bases it is the Cartesian SCF."""
+    for case, pure in (("water_sto-3g", False), ("water_6-31g_st", True)):
+        g, b = _basis(case)
+        S, T, V = O.one_electron(b)
+        H = T + V
+        eri = O.eri_tensor(b)
+        fock = lambda D: H + np.einsum("ijkl,kl->ij", eri, D) - 0.5 * np.einsum("ikjl,kl->ij", eri, D)
+        Tt = O.spherical_transform(b)
+        assert Tt.shape == (b.nbf, b.nbf - (1 if pure else 0))
+        enuc = O.nuclear_repulsion(b.atoms)
+        rs = O.rhf(S, H, fock, 5, enuc, thr=1e-11, X=O.spherical_orthogonalizer(S, Tt))
+        Sp, Hp = Tt.T @ S @ Tt, Tt.T @ H @ Tt
+        erip = np.einsum("pi,qj,rk,sl,pqrs->ijkl", Tt, Tt, Tt, Tt, eri, optimize=True)
+        fp = lambda D: Hp + np.einsum("ijkl,kl->ij", erip, D) - 0.5 * np.einsum("ikjl,kl->ij", erip, D)
+        rp = O.rhf(Sp, Hp, fp, 5, enuc, thr=1e-11)
+        assert rs["converged"] and rp["converged"]
+        assert abs(rs["total_energy"] - rp["total_energy"]) < 1e-10
+        if not pure:
+            assert abs(rs["total_energy"] - float(g["energy_total"])) < 1e-8
