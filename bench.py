@@ -462,6 +462,8 @@ def run_c60_ri(args, rank, world):
     opts_mx = {"convergence_threshold": CONV, "eri_method": gg.HF_ERI_RI, "precision": gg.HF_PRECISION_MIXED,
                "anchor_threshold": tau}
     opts_64 = {"convergence_threshold": CONV, "eri_method": gg.HF_ERI_RI}
+    for o in (opts_mx, opts_64):
+        o["eigensolver"] = gg.HF_EIGEN_PURIFICATION if args.eigensolver == "purification" else gg.HF_EIGEN_SYEVD
     for _ in range(args.warmup):
         eng.rhf_scf(nel, opts_mx)
     with ClockSampler(dev) as clocks:
@@ -479,7 +481,8 @@ def run_c60_ri(args, rank, world):
                        "seed": args.seed, "convergence": CONV,
                        "precision": f"mixed: split-BF16x3 tcgen05 K until max|dD| < {tau}, one FP64 anchor K, "
                                     "then K(dD) from aligned orbital differences; J FP64",
-                       "l2": "inputs (the B planes) larger than L2", "parallelism": "1 GPU"},
+                       "l2": "inputs (the B planes) larger than L2", "eigensolver": args.eigensolver,
+                       "parallelism": "1 GPU"},
             "fp64_ms_per_iter": ms_64, "mixed_speedup_vs_fp64": ms_64 / ms_mx,
             "delta_E_mixed_vs_fp64": max(abs(r["total_energy"] - r64["total_energy"]) for r in mx),
             "energy_fp64": r64["total_energy"], "iterations": {"mixed": mx[0]["iterations"], "fp64": r64["iterations"]},

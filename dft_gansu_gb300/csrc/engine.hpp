@@ -165,6 +165,9 @@ struct Engine {
         double* work_j = nullptr;
         syevjInfo_t syevj_params = nullptr;
         float *P32a = nullptr, *P32b = nullptr, *P32c = nullptr;  // purification (FP32 SP2) buffers
+        double *Qocc = nullptr, *Mocc = nullptr, *qwork = nullptr;  // occupied basis from the projector
+        int* qinfo = nullptr;
+        int qlwork = 0;
     } scf;
 
     ~Engine();

@@ -560,6 +560,68 @@ int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t
     return HF_OK;
 }
 
+// Occupied orbitals without an eigensolver, for the RI K build under purification:
+// after purify_density, w.W holds the projector P on the occupied space in the
+// orthonormal basis.  Q = orth(P Q_prev) by CholeskyQR2 (M = Y^T Y = U^T U, Y U^{-1},
+// twice) spans the same space as P whenever P Q_prev has full rank (the previous
+// iteration's occupied basis is close to the new one); C_occ = X Q.  K depends on
+// the occupied space only, so any orthonormal basis of it gives the same K.
+// first = true (or a failed Cholesky): the orbitals of one diagonalisation seed Q.
+int occupied_from_projector(Engine& e, const double* F, int nocc, bool first, cudaStream_t s)
+{
+    auto& w = e.scf;
+    const int n = w.n;
+    int st;
+    if (!w.Qocc) {
+        if ((st = alloc(w.Qocc, static_cast<size_t>(n) * n)) || (st = alloc(w.Mocc, static_cast<size_t>(n) * n)) ||
+            (st = alloc(w.qinfo, 1)))
+            return st;
+        if (cusolverDnDpotrf_bufferSize(e.cusolver, CUBLAS_FILL_MODE_UPPER, n, w.Mocc, n, &w.qlwork) !=
+            CUSOLVER_STATUS_SUCCESS)
+            return set_error("cusolverDnDpotrf_bufferSize failed"), HF_ERR_SOLVER;
+        if ((st = alloc(w.qwork, static_cast<size_t>(std::max(w.qlwork, 1))))) return st;
+    }
+    const double one = 1.0, zero = 0.0;
+    // seed: the eigenvectors of F' (C' = the column-major W^T), Q = first nocc columns
+    auto seed = [&]() -> int {
+        int r;
+        if ((r = coefficients(e, F, s, 0))) return r;
+        // row-major Q (n x nocc) = C'[:, :nocc]; column-major W holds eigenvector k in column k
+        if (cublasDgeam(e.cublas, CUBLAS_OP_T, CUBLAS_OP_N, nocc, n, &one, w.W, n, &zero, w.Qocc, nocc, w.Qocc,
+                        nocc) != CUBLAS_STATUS_SUCCESS)
+            return set_error("cublasDgeam (occupied seed) failed"), HF_ERR_SOLVER;
+        return HF_OK;
+    };
+    if (first) return seed();
+    // Y = P Q_prev (row-major n x nocc) into T2, then two Cholesky-QR passes in place
+    if (cublasDgemm(e.cublas, CUBLAS_OP_N, CUBLAS_OP_N, nocc, n, n, &one, w.Qocc, nocc, w.W, n, &zero, w.T2, nocc) !=
+        CUBLAS_STATUS_SUCCESS)
+        return set_error("cublasDgemm (P Q) failed"), HF_ERR_SOLVER;
+    for (int pass = 0; pass < 2; ++pass) {
+        // M = Y^T Y (nocc x nocc); column-major view of Y is Y^T (nocc x n, ld nocc)
+        if (cublasDgemm(e.cublas, CUBLAS_OP_N, CUBLAS_OP_T, nocc, nocc, n, &one, w.T2, nocc, w.T2, nocc, &zero, w.Mocc,
+                        nocc) != CUBLAS_STATUS_SUCCESS)
+            return set_error("cublasDgemm (Y^T Y) failed"), HF_ERR_SOLVER;
+        if (cusolverDnDpotrf(e.cusolver, CUBLAS_FILL_MODE_UPPER, nocc, w.Mocc, nocc, w.qwork, w.qlwork, w.qinfo) !=
+            CUSOLVER_STATUS_SUCCESS)
+            return set_error("cusolverDnDpotrf (occupied basis) failed"), HF_ERR_SOLVER;
+        // Y^T <- U^{-T} Y^T, i.e. Y <- Y U^{-1}
+        if (cublasDtrsm(e.cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, nocc, n,
+                        &one, w.Mocc, nocc, w.T2, nocc) != CUBLAS_STATUS_SUCCESS)
+            return set_error("cublasDtrsm (occupied basis) failed"), HF_ERR_SOLVER;
+    }
+    int info = 0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&info, w.qinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (info != 0) return seed();  // P Q_prev lost rank: reseed from a diagonalisation
+    GB_CUDA_TRY(cudaMemcpyAsync(w.Qocc, w.T2, sizeof(double) * n * nocc, cudaMemcpyDeviceToDevice, s));
+    // C[:, :nocc] = X Q (row-major, ld n)
+    if (cublasDgemm(e.cublas, CUBLAS_OP_N, CUBLAS_OP_N, nocc, n, n, &one, w.Qocc, nocc, w.X, n, &zero, w.C, n) !=
+        CUBLAS_STATUS_SUCCESS)
+        return set_error("cublasDgemm (X Q) failed"), HF_ERR_SOLVER;
+    return HF_OK;
+}
+
 // e = FDS - SDF; transform 1: X e X^T (diis_include_transform, computeDIISErrorMatrix,
 // src/gpu_manager.cu:1020-1068); transform 2: X^T e X, the error in the orthonormal
 // basis of a caller's orthogonaliser (its span is a subspace: the AO-basis error
@@ -863,11 +925,19 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
     if ((st = orthogonalizer(e, opt, s))) return st;
     GB_LAUNCH_CHECK();
-    // purification needs no orbitals, but the RI K build uses the occupied ones
-    const bool purify = opt.eigensolver == HF_EIGEN_PURIFICATION && !use_ri;
+    // purification needs no orbitals; the RI K build takes an orthonormal basis of the
+    // occupied space from the projector (occupied_from_projector)
+    const bool purify = opt.eigensolver == HF_EIGEN_PURIFICATION;
+    bool occ_seeded = false;
     auto density_from = [&](const double* Fm) -> int {
         int r;
-        if (purify) return purify_density(e, Fm, nocc, w.D, s);
+        if (purify) {
+            if ((r = purify_density(e, Fm, nocc, w.D, s))) return r;
+            if (!use_ri) return HF_OK;
+            r = occupied_from_projector(e, Fm, nocc, !occ_seeded, s);
+            occ_seeded = true;
+            return r;
+        }
         if ((r = coefficients(e, Fm, s, opt.eigensolver))) return r;
         density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nocc, w.D);
         GB_LAUNCH_CHECK();

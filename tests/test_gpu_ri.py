@@ -145,3 +145,22 @@ def test_mixed_ri_scf_propane(built_library, cuda):
         rmx = eng.rhf_scf(mol.num_electrons, dict(base, precision=gg.HF_PRECISION_MIXED, anchor_threshold=tau))
         assert rmx["converged"] == 1
         assert abs(rmx["total_energy"] - r64["total_energy"]) < 1e-6, tau
+
+
+def test_ri_scf_with_purification(built_library, cuda):
+    """RI with the purification eigensolver: the K build takes an orthonormal basis of
+    the occupied space from the projector (CholeskyQR2 of P Q_prev), FP64 and mixed."""
+    atoms = geometry.alkane(3, jitter=0.02, seed=11)
+    mol = gg.Molecular(atoms, gg.basis_path("cc-pvdz"))
+    eng = gg.Engine(mol, 1e-12)
+    eng.set_auxiliary_basis(gg.Molecular(atoms, gg.basis_path("cc-pvdz-rifit")))
+    base = {"convergence_threshold": 1e-10, "eri_method": gg.HF_ERI_RI}
+    r64 = eng.rhf_scf(mol.num_electrons, base, want_matrices=True)
+    rp = eng.rhf_scf(mol.num_electrons, dict(base, eigensolver=gg.HF_EIGEN_PURIFICATION), want_matrices=True)
+    assert rp["converged"] == 1 and abs(rp["total_energy"] - r64["total_energy"]) < 1e-9
+    assert abs(rp["iterations"] - r64["iterations"]) <= 1
+    np.testing.assert_allclose(rp["orbital_energies"].cpu().numpy(), r64["orbital_energies"].cpu().numpy(),
+                               atol=1e-5)
+    rm = eng.rhf_scf(mol.num_electrons, dict(base, eigensolver=gg.HF_EIGEN_PURIFICATION,
+                                             precision=gg.HF_PRECISION_MIXED, anchor_threshold=1e-2))
+    assert rm["converged"] == 1 and abs(rm["total_energy"] - r64["total_energy"]) < 1e-6
