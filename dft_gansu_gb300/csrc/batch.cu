@@ -152,11 +152,12 @@ __global__ void batch_phase_kernel(const double* __restrict__ ddiff, const unsig
         if (!active[m]) { mol_tau[m] = inf; mol_skip[m] = inf; incr[m] = 0; continue; }
         if (!anchored[m]) {
             incr[m] = 0;
-            mol_skip[m] = schwarz;
             if (first || ddiff[m] >= anchor) {
-                mol_tau[m] = inf;  // every quartet FP32
+                mol_tau[m] = inf;  // every quartet FP32, the small ones left out (kPreAnchorDrop)
+                mol_skip[m] = fmax(schwarz, kPreAnchorDrop);
             } else {
                 mol_tau[m] = 0.0;  // every quartet FP64: the anchor
+                mol_skip[m] = schwarz;
                 anchored[m] = 1;
             }
         } else {

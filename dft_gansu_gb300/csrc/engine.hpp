@@ -180,8 +180,14 @@ FockLauncher fock_launcher(int la, int lb, int lc, int ld);
 EriLauncher eri_launcher(int la, int lb, int lc, int ld);
 
 // fock.cu
+// mixed tier: drop threshold of the all-FP32 builds before the FP64 anchor (those
+// builds only steer the density towards the anchor, which keeps the Schwarz set)
+constexpr double kPreAnchorDrop = 1e-10;
+
+// drop > 0: under the mixed tier, quartets whose bound Qs_ab Qs_cd c_max^4 max|D| is
+// below drop are skipped (default: the Schwarz threshold, or the FP32 cut if lower)
 int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
-             cudaStream_t s, bool accumulate_counters = true);
+             cudaStream_t s, double drop = -1.0);
 int finish_fock(Engine& e, const double* d_H, const double* d_J, const double* d_K, double* d_F, cudaStream_t s);
 int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s);
 // device split of the static quartet lists into FP64 prefix / FP32 rest (e.plan)

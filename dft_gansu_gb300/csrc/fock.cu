@@ -401,7 +401,7 @@ int build_jk_batch(Engine& e, const double* d_D, const double* d_mol_tau, const 
 }
 
 int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
-             cudaStream_t s, bool /*accumulate_counters*/)
+             cudaStream_t s, double drop)
 {
     const size_t nn = static_cast<size_t>(e.nelem);
     const bool mixed = (precision == HF_PRECISION_MIXED);
@@ -429,7 +429,8 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
     } else {
         const double c2 = e.cgto_max * e.cgto_max;
         PlanArgs a;
-        int pst = mixed_plan_args(e, d_D, c2 * c2, false, mixed_thr, std::min(e.schwarz_threshold, mixed_thr), s, &a);
+        const double skip = drop > 0.0 ? drop : std::min(e.schwarz_threshold, mixed_thr);
+        int pst = mixed_plan_args(e, d_D, c2 * c2, false, mixed_thr, skip, s, &a);
         if (pst) return pst;
         // per-shell-block maxima of the (difference) density for the per-quartet screen
         // (single-molecule engines: the table is num_shells^2)

@@ -2,7 +2,7 @@
 // The build compiles this file once per class (GB_LA, GB_LB, GB_LC, GB_LD)
 // so that the classes compile in parallel; each object exports
 // launch_fock_<la>_<lb>_<lc>_<ld> and launch_eri_<la>_<lb>_<lc>_<ld>.
-#include "fock_kernel.cuh"
+#include "fock_column.cuh"
 
 #if !defined(GB_LA) || !defined(GB_LB) || !defined(GB_LC) || !defined(GB_LD)
 #error "fock_inst.cu needs GB_LA, GB_LB, GB_LC and GB_LD"
@@ -19,16 +19,21 @@ constexpr int kNCD = ncart(GB_LC) * ncart(GB_LD);
 // grid: blocks for one thread per quartet; the generic path needs kNCD times more
 void GB_CAT(launch_fock, GB_SUFFIX)(bool fp32, const FockClassLaunch& launch, int grid, cudaStream_t stream)
 {
+    // classes above the register budget: one thread per ket component pair, compile-time tables
+    using fock_column::ClassColumn;
+    using fock_column::column_kernel;
     if (fp32) {
         if constexpr (FockSplit<float, GB_LA, GB_LB, GB_LC, GB_LD>::value == 1)
             fock_direct_kernel<float, GB_LA, GB_LB, GB_LC, GB_LD><<<grid, kFockThreads, 0, stream>>>(launch);
         else
-            launch_fock_generic(true, launch, kNCD, grid * kNCD, stream);
+            column_kernel<float, ClassColumn<float, GB_LA, GB_LB, GB_LC, GB_LD>>
+                <<<grid * kNCD, kFockThreads, 0, stream>>>(launch, kNCD);
     } else {
         if constexpr (FockSplit<double, GB_LA, GB_LB, GB_LC, GB_LD>::value == 1)
             fock_direct_kernel<double, GB_LA, GB_LB, GB_LC, GB_LD><<<grid, kFockThreads, 0, stream>>>(launch);
         else
-            launch_fock_generic(false, launch, kNCD, grid * kNCD, stream);
+            column_kernel<double, ClassColumn<double, GB_LA, GB_LB, GB_LC, GB_LD>>
+                <<<grid * kNCD, kFockThreads, 0, stream>>>(launch, kNCD);
     }
 }
 

@@ -879,8 +879,11 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
             double dmax = 1.0;
             if (!first && (r = ri_absmax_diff(e, w.D, w.Dprev, &dmax, s))) return r;
             const bool low = first || dmax >= opt.anchor_threshold;
+            // the pre-anchor builds only steer the density towards the anchor: quartets whose
+            // bound is below kPreAnchorDrop are left out of them (the anchor builds every
+            // quartet the Schwarz screen keeps, in FP64)
             if ((r = build_jk(e, w.D, nullptr, nullptr, low ? HF_PRECISION_MIXED : HF_PRECISION_FP64,
-                              std::numeric_limits<double>::infinity(), s)))
+                              std::numeric_limits<double>::infinity(), s, low ? kPreAnchorDrop : -1.0)))
                 return r;
             if (!low) anchored = true;
             fock_from_jk_kernel<<<grid_nn(nn), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.last_mixed ? e.d_Jp32 : nullptr,
