@@ -31,8 +31,9 @@ FOCK_CLASSES = [
 ]
 
 # longest translation units first (the pool starts them in this order)
-CUDA_SOURCES = ["grad_class_f64_l5.cu", "grad_class_f32_l56.cu", "grad_class_f64.cu", "grad_class_f32.cu", "grad.cu",
-                "ri.cu", "batch.cu", "scf.cu", "engine.cu", "fock.cu", "fock_generic.cu", "one_electron.cu", "peaks.cu", "diis_noalloc.cu", "tc_gemm.cu"]
+CUDA_SOURCES = ["grad_class_f64_l5.cu", "grad_class_f64_l6.cu", "grad_class_f32_l56.cu", "grad_class_f64.cu",
+                "grad_class_f32.cu", "grad.cu", "ri.cu", "batch.cu", "scf.cu", "engine.cu", "fock.cu",
+                "fock_generic.cu", "one_electron.cu", "peaks.cu", "diis_noalloc.cu", "tc_gemm.cu"]
 CXX_SOURCES = ["molecule.cpp", "errors.cpp"]
 
 

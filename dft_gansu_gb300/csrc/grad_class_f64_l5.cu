@@ -16,7 +16,7 @@ bool launch_grad_class_f64_l5(int la, int lb, int lc, int ld, const GradLaunch& 
     }
     GB_GC(2, 1, 1, 1) GB_GC(2, 1, 2, 0) GB_GC(2, 2, 1, 0)
 #undef GB_GC
-    return false;
+    return launch_grad_class_f64_l6(la, lb, lc, ld, G, grid, smem, s);
 }
 
 }  // namespace gb

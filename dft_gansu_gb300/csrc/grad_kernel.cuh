@@ -298,6 +298,8 @@ bool launch_grad_class_f64(int la, int lb, int lc, int ld, const GradLaunch& G, 
 bool launch_grad_class_f32(int la, int lb, int lc, int ld, const GradLaunch& G, int grid, size_t smem, cudaStream_t s);
 bool launch_grad_class_f64_l5(int la, int lb, int lc, int ld, const GradLaunch& G, int grid, size_t smem,
                               cudaStream_t s);
+bool launch_grad_class_f64_l6(int la, int lb, int lc, int ld, const GradLaunch& G, int grid, size_t smem,
+                              cudaStream_t s);
 bool launch_grad_class_f32_l56(int la, int lb, int lc, int ld, const GradLaunch& G, int grid, size_t smem,
                                cudaStream_t s);
 
