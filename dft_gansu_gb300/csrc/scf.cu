@@ -77,6 +77,17 @@ __global__ void energy_kernel(const double* __restrict__ D, const double* __rest
     }
 }
 
+// E = T - T^T
+__global__ void antisym_kernel(const double* __restrict__ T, int n, double* __restrict__ E)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long i = k / n, j = k % n;
+        E[k] = T[k] - T[j * n + i];
+    }
+}
+
 __global__ void sub_kernel(const double* __restrict__ A, const double* __restrict__ B, long long nn,
                            double* __restrict__ C)
 {
@@ -627,17 +638,23 @@ int occupied_from_projector(Engine& e, const double* F, int nocc, bool first, cu
 // basis of a caller's orthogonaliser (its span is a subspace: the AO-basis error
 // has a component outside it that does not vanish at convergence)
 int diis_error(Engine& e, const double* S, const double* X, const double* F, const double* D, double* E,
-               int transform, cudaStream_t s)
+               int transform, cudaStream_t s, bool symmetric = true)
 {
     auto& w = e.scf;
     const long long nn = static_cast<long long>(w.n) * w.n;
     int st;
     if ((st = gemm_rm(e.cublas, false, false, w.n, F, D, w.T1))) return st;
     if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, S, w.T2))) return st;  // FDS
-    if ((st = gemm_rm(e.cublas, false, false, w.n, S, D, w.T1))) return st;
-    if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, F, E))) return st;     // SDF
-    sub_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T2, E, nn, E);
-    GB_LAUNCH_CHECK();
+    if (symmetric) {
+        // the SCF's F, D, S are symmetric: SDF = (FDS)^T, so e = FDS - (FDS)^T
+        antisym_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T2, w.n, E);
+        GB_LAUNCH_CHECK();
+    } else {
+        if ((st = gemm_rm(e.cublas, false, false, w.n, S, D, w.T1))) return st;
+        if ((st = gemm_rm(e.cublas, false, false, w.n, w.T1, F, E))) return st;  // SDF
+        sub_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T2, E, nn, E);
+        GB_LAUNCH_CHECK();
+    }
     if (transform == 1) {
         if ((st = gemm_rm(e.cublas, false, false, w.n, X, E, w.T1))) return st;
         if ((st = gemm_rm(e.cublas, false, true, w.n, w.T1, X, E))) return st;
@@ -748,7 +765,7 @@ int hf_compute_diis_error(hf_engine* eng, const double* d_overlap, const double*
     if (st) return st;
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     cublasSetStream(e.cublas, s);
-    return diis_error(e, d_overlap, d_transform, d_fock, d_density, d_error, include_transform != 0 ? 1 : 0, s);
+    return diis_error(e, d_overlap, d_transform, d_fock, d_density, d_error, include_transform != 0 ? 1 : 0, s, false);
 }
 
 int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d_focks, double* d_new_fock,
