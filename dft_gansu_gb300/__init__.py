@@ -12,7 +12,7 @@ from pathlib import Path
 
 import numpy as np
 
-from ._capi import (HF_EIGEN_PURIFICATION, HF_EIGEN_SYEVD, HF_GUESS_CORE, HF_GUESS_DENSITY, HF_GUESS_GWH,
+from ._capi import (HF_CONV_DAMPING, HF_CONV_DIIS, HF_CONV_OPTIMAL_DAMPING, HF_EIGEN_PURIFICATION, HF_EIGEN_SYEVD, HF_GUESS_CORE, HF_GUESS_DENSITY, HF_GUESS_GWH,
                     HF_GUESS_SAD, HF_ERR_NOT_CONVERGED,
                     HF_ERI_DIRECT, HF_ERI_RI, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
                     check, lib)
@@ -24,7 +24,8 @@ __all__ = [
     "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
     "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "basis_path",
     "optimize_geometry", "energy_and_gradient_at", "Batch", "UHF", "HF_EIGEN_PURIFICATION", "HF_EIGEN_SYEVD",
-    "HF_GUESS_CORE", "HF_GUESS_GWH", "HF_GUESS_DENSITY", "HF_GUESS_SAD", "ROHF", "ROHF_COUPLINGS",
+    "HF_GUESS_CORE", "HF_GUESS_GWH", "HF_GUESS_DENSITY", "HF_GUESS_SAD", "HF_CONV_DIIS", "HF_CONV_DAMPING",
+    "HF_CONV_OPTIMAL_DAMPING", "ROHF", "ROHF_COUPLINGS",
 ]
 
 
@@ -531,6 +532,7 @@ class ParameterManager:
 
 
 _GUESSES = {"core": HF_GUESS_CORE, "gwh": HF_GUESS_GWH, "density": HF_GUESS_DENSITY, "sad": HF_GUESS_SAD}
+_CONVERGENCE = {"diis": HF_CONV_DIIS, "damping": HF_CONV_DAMPING, "optimaldamping": HF_CONV_OPTIMAL_DAMPING}
 
 
 class _HFBase:
@@ -544,8 +546,8 @@ class _HFBase:
         method = parameters["eri_method"]
         if method not in ("stored", "direct", "ri"):
             raise ValueError(f"Invalid ERI method name: {method}")
-        if parameters["convergence_method"] != "diis":
-            raise ValueError("only the DIIS convergence method is provided by this engine")
+        if parameters["convergence_method"] not in _CONVERGENCE:
+            raise ValueError(f"Invalid convergence_method: {parameters['convergence_method']}")
         if parameters["initial_guess"] not in _GUESSES:
             raise ValueError(f"Invalid initial guess method: {parameters['initial_guess']}")
         if parameters["initial_guess"] == "sad" and not parameters["gbsfilename"] and \
@@ -575,6 +577,8 @@ class _HFBase:
             "eri_method": self.eri_method,
             "initial_guess": _GUESSES[guess],
             "spherical": bool(p.get("spherical", bool)),
+            "convergence_method": _CONVERGENCE[p["convergence_method"]],
+            "damping_factor": p.get("damping_factor", float),
         }
         if guess == "density":
             if density_alpha is None or density_beta is None:

@@ -28,6 +28,9 @@ HF_GUESS_CORE = 0
 HF_GUESS_GWH = 1
 HF_GUESS_DENSITY = 2
 HF_GUESS_SAD = 3
+HF_CONV_DIIS = 0
+HF_CONV_DAMPING = 1
+HF_CONV_OPTIMAL_DAMPING = 2
 HF_EIGEN_SYEVD = 0
 HF_EIGEN_SYEVJ = 1
 HF_EIGEN_PURIFICATION = 2
@@ -73,6 +76,8 @@ class ScfOptions(C.Structure):
         ("guess_density_a", C.c_void_p),
         ("guess_density_b", C.c_void_p),
         ("orthogonalizer", C.c_void_p),
+        ("convergence_method", C.c_int),
+        ("damping_factor", C.c_double),
     ]
 
 

@@ -77,6 +77,44 @@ __global__ void energy_kernel(const double* __restrict__ D, const double* __rest
     }
 }
 
+// s = sum Fp (D - Dp), c = sum (F - Fp)(D - Dp) (traces of products of symmetric
+// matrices), one block
+__global__ void damping_traces_kernel(const double* __restrict__ F, const double* __restrict__ Fp,
+                                      const double* __restrict__ D, const double* __restrict__ Dp, long long nn,
+                                      double* __restrict__ out)
+{
+    __shared__ double r1[32], r2[32];
+    double s1 = 0.0, s2 = 0.0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) {
+        const double dd = D[k] - Dp[k];
+        s1 += Fp[k] * dd;
+        s2 += (F[k] - Fp[k]) * dd;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if ((threadIdx.x & 31) == 0) { r1[threadIdx.x >> 5] = s1; r2[threadIdx.x >> 5] = s2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) { a += r1[w]; b += r2[w]; }
+        out[0] = a;
+        out[1] = b;
+    }
+}
+
+// damping (src/gpu_manager.cu:989-1007): M = (1 - a) M_prev + a M, stored in both
+__global__ void damp_kernel(double* __restrict__ Mp, double* __restrict__ M, double a, long long nn)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double v = (1.0 - a) * Mp[k] + a * M[k];
+        Mp[k] = v;
+        M[k] = v;
+    }
+}
+
 // E = T - T^T
 __global__ void antisym_kernel(const double* __restrict__ T, int n, double* __restrict__ E)
 {
@@ -709,6 +747,54 @@ bool valid_guess(int g) { return g == HF_GUESS_CORE || g == HF_GUESS_GWH || g ==
 // (HF::compute_transform_matrix, src/hf.cu:171-243), or the caller's
 // orthogonaliser (options.orthogonalizer: a subspace of the AO space, e.g. the
 // spherical-harmonic functions; its DIIS error is taken in the orthogonal basis)
+// Convergence_*_Damping (include/rhf.hpp:182-262): the first call keeps F and D, later
+// calls damp F (and D, with the optimal factor) against the kept ones
+struct Damper {
+    double* Fp = nullptr;
+    double* Dp = nullptr;
+    bool first = true;
+    ~Damper()
+    {
+        if (Fp) cudaFree(Fp);
+        if (Dp) cudaFree(Dp);
+    }
+    int step(Engine& e, const hf_scf_options& opt, double* F, double* D, long long nn, cudaStream_t s)
+    {
+        if (!Fp && (cudaMalloc(&Fp, nn * sizeof(double)) != cudaSuccess ||
+                    cudaMalloc(&Dp, nn * sizeof(double)) != cudaSuccess))
+            return set_error("cudaMalloc (damping) failed"), HF_ERR_OUT_OF_MEMORY;
+        if (first) {
+            first = false;
+            GB_CUDA_TRY(cudaMemcpyAsync(Fp, F, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            GB_CUDA_TRY(cudaMemcpyAsync(Dp, D, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            return HF_OK;
+        }
+        double a = opt.damping_factor;
+        const bool optimal = opt.convergence_method == HF_CONV_OPTIMAL_DAMPING;
+        if (optimal) {
+            damping_traces_kernel<<<1, 1024, 0, s>>>(F, Fp, D, Dp, nn, e.d_scalar + 10);
+            GB_LAUNCH_CHECK();
+            double sc[2];
+            GB_CUDA_TRY(cudaMemcpyAsync(sc, e.d_scalar + 10, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+            GB_CUDA_TRY(cudaStreamSynchronize(s));
+            a = (sc[1] <= -sc[0] / 2.0) ? 1.0 : -0.5 * sc[0] / sc[1];
+        }
+        damp_kernel<<<grid_nn(nn), 256, 0, s>>>(Fp, F, a, nn);
+        GB_LAUNCH_CHECK();
+        if (optimal) {
+            damp_kernel<<<grid_nn(nn), 256, 0, s>>>(Dp, D, a, nn);
+            GB_LAUNCH_CHECK();
+        }
+        return HF_OK;
+    }
+};
+
+bool valid_convergence(const hf_scf_options& opt)
+{
+    return opt.convergence_method == HF_CONV_DIIS || opt.convergence_method == HF_CONV_DAMPING ||
+           opt.convergence_method == HF_CONV_OPTIMAL_DAMPING;
+}
+
 int diis_x(const hf_scf_options& opt) { return opt.orthogonalizer ? 2 : (opt.diis_include_transform != 0 ? 1 : 0); }
 
 int orthogonalizer(Engine& e, const hf_scf_options& opt, cudaStream_t s)
@@ -750,6 +836,8 @@ void hf_scf_options_default(hf_scf_options* o)
     o->guess_density_a = nullptr;
     o->guess_density_b = nullptr;
     o->orthogonalizer = nullptr;
+    o->convergence_method = HF_CONV_DIIS;
+    o->damping_factor = 0.9;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -806,6 +894,9 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     const bool density_guess = opt.initial_guess == HF_GUESS_DENSITY || opt.initial_guess == HF_GUESS_SAD;
     if (density_guess && !opt.guess_density_a)
         return set_error("initial_guess density/SAD needs guess_density_a"), HF_ERR_INVALID_ARGUMENT;
+    if (!valid_convergence(opt)) return set_error("convergence_method: DIIS, damping or optimal damping"),
+                                 HF_ERR_INVALID_ARGUMENT;
+    Damper damper;
     const bool use_ri = opt.eri_method == HF_ERI_RI;
     if (use_ri && !e.ri)
         return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
@@ -1027,14 +1118,18 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         }
         ++iter;
         prev = energy;
-        // DIIS update (Convergence_RHF_DIIS::get_new_fock_matrix)
+        // Fock update: DIIS (Convergence_RHF_DIIS::get_new_fock_matrix) or damping
         cudaEventRecord(q0, s);
         diis_timed = true;
-        const int slot = diis_iter % m;
-        if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, diis_x(opt), s))) return st;
-        GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + slot * nn, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        const int nprev = std::min(diis_iter + 1, m);
-        if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, w.F, s))) return st;
+        if (opt.convergence_method != HF_CONV_DIIS) {
+            if ((st = damper.step(e, opt, w.F, w.D, nn, s))) return st;
+        } else {
+            const int slot = diis_iter % m;
+            if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, diis_x(opt), s))) return st;
+            GB_CUDA_TRY(cudaMemcpyAsync(w.Fs + slot * nn, w.F, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            const int nprev = std::min(diis_iter + 1, m);
+            if (nprev > 1 && (st = diis_extrapolate(e, w.Es, w.Fs, nprev, w.F, s))) return st;
+        }
         cudaEventRecord(q1, s);
         ++diis_iter;
     }
@@ -1111,6 +1206,11 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         return set_error("initial_guess density/SAD needs guess_density_a"), HF_ERR_INVALID_ARGUMENT;
     if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI)
         return set_error("unknown eri_method"), HF_ERR_INVALID_ARGUMENT;
+    if (!valid_convergence(opt)) return set_error("convergence_method: DIIS, damping or optimal damping"),
+                                 HF_ERR_INVALID_ARGUMENT;
+    hf_scf_options damp_opt = opt;
+    damp_opt.convergence_method = HF_CONV_DAMPING;
+    Damper damp_a, damp_b;
     const bool use_ri = opt.eri_method == HF_ERI_RI;
     if (use_ri && !e.ri)
         return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
@@ -1220,6 +1320,14 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         if (std::fabs(energy - prev) < opt.convergence_threshold) { converged = true; break; }
         ++iter;
         prev = energy;
+        if (opt.convergence_method != HF_CONV_DIIS) {
+            // Convergence_UHF_Damping (include/uhf.hpp:196-250): a constant factor for both spins
+            // (the reference has no optimal factor for UHF)
+            if ((st = damp_a.step(e, damp_opt, Fa, Da, nn, s)) || (st = damp_b.step(e, damp_opt, Fb, Db, nn, s)))
+                return cudaFreeHost(h_energy), st;
+            ++diis_iter;
+            continue;
+        }
         // DIIS per spin on the same cyclic ring index (Convergence_UHF_DIIS, include/uhf.hpp:291-380)
         const int slot = diis_iter % m;
         const int nprev = std::min(diis_iter + 1, m);
@@ -1280,6 +1388,9 @@ int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupl
     const bool density_guess = opt.initial_guess == HF_GUESS_DENSITY || opt.initial_guess == HF_GUESS_SAD;
     if (density_guess && (!opt.guess_density_a || !opt.guess_density_b))
         return set_error("ROHF initial_guess density/SAD needs guess_density_a and _b"), HF_ERR_INVALID_ARGUMENT;
+    if (!valid_convergence(opt)) return set_error("convergence_method: DIIS, damping or optimal damping"),
+                                 HF_ERR_INVALID_ARGUMENT;
+    Damper damper;
     if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI)
         return set_error("unknown eri_method"), HF_ERR_INVALID_ARGUMENT;
     const bool use_ri = opt.eri_method == HF_ERI_RI;
@@ -1404,6 +1515,12 @@ int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupl
         if (std::fabs(energy - prev) < opt.convergence_threshold) { converged = true; break; }
         ++iter;
         prev = energy;
+        if (opt.convergence_method != HF_CONV_DIIS) {
+            // Convergence_ROHF_Damping (include/rohf.hpp:216-290) on the unified F with D
+            if ((st = damper.step(e, opt, w.F, w.D, nn, s))) break;
+            ++diis_iter;
+            continue;
+        }
         // Convergence_ROHF_DIIS (include/rohf.hpp:307-360): unified F with D = D_c + D_o
         const int slot = diis_iter % m;
         if ((st = diis_error(e, w.S, w.X, w.F, w.D, w.Es + slot * nn, diis_x(opt), s))) break;

@@ -242,7 +242,22 @@ typedef struct {
                                        spherical-harmonic subspace of the Cartesian basis (no reference
                                        counterpart); the DIIS error is then X^T (FDS - SDF) X.
                                        Single-molecule SCFs only. */
+    int convergence_method;         /* HF_CONV_DIIS, HF_CONV_DAMPING or HF_CONV_OPTIMAL_DAMPING
+                                       (convergence_method = diis / damping / optimaldamping) */
+    double damping_factor;          /* HF_CONV_DAMPING: F <- (1 - a) F_prev + a F (reference default 0.9) */
 } hf_scf_options;
+
+/* Fock-matrix update between iterations (Convergence_RHF_DIIS / _Damping,
+ * include/rhf.hpp:182-353; UHF and ROHF alike).  Optimal damping
+ * (computeOptimalDampingFactor_RHF, src/gpu_manager.cu:898-963): with
+ * s = Tr[F_old (D - D_old)], c = Tr[(F - F_old)(D - D_old)], a = 1 if
+ * c <= -s/2, else -s/(2c); F and D are both damped.  Damping is RHF, UHF
+ * (constant factor, as the reference) and ROHF; the batch SCF is DIIS only. */
+enum {
+    HF_CONV_DIIS = 0,
+    HF_CONV_DAMPING = 1,
+    HF_CONV_OPTIMAL_DAMPING = 2
+};
 
 /* Density from the Fock matrix inside the SCF loop.  The reference diagonalises
  * (computeCoefficientMatrix, src/gpu_manager.cu:529-599); purification gives the

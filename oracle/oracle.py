@@ -351,8 +351,16 @@ def spherical_orthogonalizer(S, T, tol=1e-6):
     return X
 
 
+def damping_factor(F, Fp, D, Dp):
+    """computeOptimalDampingFactor_RHF (src/gpu_manager.cu:898-963): s = Tr[F_old dD],
+    c = Tr[(F - F_old) dD]; 1 if c <= -s/2, else -s/(2c)."""
+    dD = D - Dp
+    sv, cv = np.trace(Fp @ dD), np.trace((F - Fp) @ dD)
+    return 1.0 if cv <= -sv / 2.0 else -0.5 * sv / cv
+
+
 def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_transform=False, guess="core",
-        guess_density=None, X=None):
+        guess_density=None, X=None, convergence="diis", damping=0.9):
     """The reference SCF loop (src/hf.cu:278-307) with DIIS and the core, GWH,
     density (F = F(D)) or SAD (F(D), C, D, F) guess (include/rhf.hpp:378-588);
     guess_density is the total density D_a + D_b.  X: an orthogonaliser over a
@@ -374,6 +382,7 @@ def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_tran
     eps = None
     converged = False
     history = []
+    damp_prev = None
     while it < maxiter:
         eps, Cm = coefficients(F, X)
         D = density(Cm, nocc)
@@ -385,6 +394,20 @@ def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_tran
             break
         it += 1
         prev = energy
+        if convergence != "diis":  # Convergence_RHF_Damping (include/rhf.hpp:182-262)
+            if damp_prev is None:
+                damp_prev = (F.copy(), D.copy())
+            else:
+                Fp, Dp = damp_prev
+                a = damping_factor(F, Fp, D, Dp) if convergence == "optimaldamping" else damping
+                F = (1.0 - a) * Fp + a * F
+                if convergence == "optimaldamping":
+                    D = (1.0 - a) * Dp + a * D
+                    damp_prev = (F.copy(), D.copy())
+                else:
+                    damp_prev = (F.copy(), Dp)
+            diis_it += 1
+            continue
         e = F @ D @ S - S @ D @ F
         if project:
             e = X.T @ e @ X

@@ -270,3 +270,18 @@ def test_oracle_spherical_scf_equals_pure_basis_scf():
         assert abs(rs["total_energy"] - rp["total_energy"]) < 1e-10
         if not pure:
             assert abs(rs["total_energy"] - float(g["energy_total"])) < 1e-8
+
+
+def test_oracle_damping_reaches_the_diis_energy():
+    """Constant and optimal damping (Convergence_RHF_Damping, include/rhf.hpp:182-262)
+    converge to the DIIS energy (water STO-3G)."""
+    g, b = _basis("water_sto-3g")
+    S, T, V = O.one_electron(b)
+    H = T + V
+    eri = O.eri_tensor(b)
+    fock = lambda D: H + np.einsum("ijkl,kl->ij", eri, D) - 0.5 * np.einsum("ikjl,kl->ij", eri, D)
+    enuc = O.nuclear_repulsion(b.atoms)
+    ref = O.rhf(S, H, fock, 5, enuc, thr=1e-11)
+    for conv, a in (("damping", 0.5), ("optimaldamping", 0.0)):
+        r = O.rhf(S, H, fock, 5, enuc, thr=1e-11, maxiter=300, convergence=conv, damping=a)
+        assert r["converged"] and abs(r["total_energy"] - ref["total_energy"]) < 1e-9, conv
