@@ -31,12 +31,12 @@ void host_boys_table(std::vector<double>& table)
 {
     table.assign(static_cast<size_t>(kBoysRows) * kBoysPoints, 0.0);
     for (int k = 0; k < kBoysPoints; ++k)
-        table[static_cast<size_t>(kBoysExpRow) * kBoysPoints + k] = static_cast<double>(expl(-k * (long double)kBoysStep));
+        table[boys_exp_at(k)] = static_cast<double>(expl(-k * (long double)kBoysStep));
     const int nmax = kBoysOrders - 1;
     for (int k = 0; k < kBoysPoints; ++k) {
         const long double x = k * static_cast<long double>(kBoysStep);
         if (k == 0) {
-            for (int n = 0; n <= nmax; ++n) table[static_cast<size_t>(n) * kBoysPoints] = 1.0 / (2 * n + 1);
+            for (int n = 0; n <= nmax; ++n) table[boys_at(n, 0)] = 1.0 / (2 * n + 1);
             continue;
         }
         const long double ex = expl(-x);
@@ -47,10 +47,10 @@ void host_boys_table(std::vector<double>& table)
             if (term < 1e-24L * sum) break;
         }
         long double f = ex * sum;
-        table[static_cast<size_t>(nmax) * kBoysPoints + k] = static_cast<double>(f);
+        table[boys_at(nmax, k)] = static_cast<double>(f);
         for (int n = nmax; n > 0; --n) {
             f = (2.0L * x * f + ex) / (2 * n - 1);
-            table[static_cast<size_t>(n - 1) * kBoysPoints + k] = static_cast<double>(f);
+            table[boys_at(n - 1, k)] = static_cast<double>(f);
         }
     }
 }

@@ -23,8 +23,7 @@ namespace gb {
 constexpr int kMaxL = 2;            // AO shells up to d (every configured basis)
 constexpr int kMaxLTotal = 4 * kMaxL + 1;  // +1 order for derivative integrals
 constexpr int kBoysOrders = 32;     // tabulated orders 0..31
-constexpr int kBoysExpRow = kBoysOrders;  // extra table row: exp(-x_k)
-constexpr int kBoysRows = kBoysOrders + 1;
+constexpr int kBoysRows = kBoysOrders + 1;  // values per grid-point record: exp(-x_k), F_0 .. F_31
 constexpr int kBoysTaylor = 6;      // Taylor terms around a grid point (FP64)
 constexpr int kBoysTaylorF = 4;     // Taylor terms (FP32)
 constexpr double kBoysStep = 1.0 / 32.0;
@@ -76,8 +75,9 @@ __host__ __device__ inline double component_factor(int l, int i)
 }
 
 // ------------------------------------------------------------------ Boys
-// Tabulated F_n(x_k), x_k = k/32, n < kBoysOrders: table[n * kBoysPoints + k],
-// plus exp(-x_k) in row kBoysExpRow.  F_{nmax}(x) from a Taylor expansion
+// Tabulated F_n(x_k), x_k = k/32, n < kBoysOrders, and exp(-x_k), one record of
+// kBoysRows values per grid point (boys_at): the Taylor terms of one evaluation
+// are consecutive in memory (one or two cache lines instead of one per term).  F_{nmax}(x) from a Taylor expansion
 // about the nearest grid point (dF_n/dx = -F_{n+1}), then the stable downward
 // recursion F_{n-1} = (2x F_n + e^{-x}) / (2n - 1), with
 // e^{-x} = e^{-x_k} e^{x_k - x} and the second factor from its degree-6
@@ -85,16 +85,20 @@ __host__ __device__ inline double component_factor(int l, int i)
 // F_0 = sqrt(pi/x)/2 (erf(sqrt x) = 1 to the precision of the type) and the
 // upward recursion F_{n+1} = ((2n+1) F_n - e^{-x}) / (2x), stable for large
 // x; for x >= 64, e^{-x} is below 1e-27 and is dropped.
+// record of grid point k: [0] = exp(-x_k), [n + 1] = F_n(x_k)
+__host__ __device__ constexpr long long boys_at(int n, int k) { return static_cast<long long>(k) * kBoysRows + n + 1; }
+__host__ __device__ constexpr long long boys_exp_at(int k) { return static_cast<long long>(k) * kBoysRows; }
+
 template <int NMAX>
 __host__ __device__ __forceinline__ void boys_fp64(double x, const double* __restrict__ table, double (&F)[NMAX + 1])
 {
     if (x < kBoysXMax) {
         const int k = static_cast<int>(x * 32.0 + 0.5);
         const double dx = k * kBoysStep - x;  // expand at x_k: F(x) = sum F_{n+j}(x_k) dx^j / j!
-        const double* t = table + NMAX * kBoysPoints + k;
-        double f = t[(kBoysTaylor - 1) * kBoysPoints];
+        const double* t = table + boys_at(NMAX, k);
+        double f = t[kBoysTaylor - 1];
 #pragma unroll
-        for (int j = kBoysTaylor - 1; j >= 1; --j) f = t[(j - 1) * kBoysPoints] + f * dx * (1.0 / j);
+        for (int j = kBoysTaylor - 1; j >= 1; --j) f = t[j - 1] + f * dx * (1.0 / j);
         F[NMAX] = f;
         if (NMAX > 0) {
             double e = 1.0 / 720.0;
@@ -104,7 +108,7 @@ __host__ __device__ __forceinline__ void boys_fp64(double x, const double* __res
             e = e * dx + 0.5;
             e = e * dx + 1.0;
             e = e * dx + 1.0;
-            const double ex = table[kBoysExpRow * kBoysPoints + k] * e;
+            const double ex = table[boys_exp_at(k)] * e;
 #pragma unroll
             for (int n = NMAX; n >= 1; --n) F[n - 1] = (2.0 * x * F[n] + ex) * (1.0 / (2 * n - 1));
         }
@@ -127,10 +131,10 @@ __host__ __device__ __forceinline__ void boys_fp32(float x, const float* __restr
     if (x < kBoysXMaxF) {
         const int k = static_cast<int>(x * 32.0f + 0.5f);
         const float dx = k * static_cast<float>(kBoysStep) - x;
-        const float* t = table + NMAX * kBoysPoints + k;
-        float f = t[(kBoysTaylorF - 1) * kBoysPoints];
+        const float* t = table + boys_at(NMAX, k);
+        float f = t[kBoysTaylorF - 1];
 #pragma unroll
-        for (int j = kBoysTaylorF - 1; j >= 1; --j) f = t[(j - 1) * kBoysPoints] + f * dx * (1.0f / j);
+        for (int j = kBoysTaylorF - 1; j >= 1; --j) f = t[j - 1] + f * dx * (1.0f / j);
         F[NMAX] = f;
         if (NMAX > 0) {
 #ifdef __CUDA_ARCH__
