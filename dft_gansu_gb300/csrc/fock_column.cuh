@@ -356,8 +356,8 @@ __global__ void __launch_bounds__(kFockThreads) column_kernel(const FockClassLau
         int bra = -1, ket = -1;
         ShellPairDev bp{}, kp{};
         T fsym = T(0);
+        const int e = find_entry_warp(L.off, L.nentry, (wid / ncd) * 32, w, total);
         if (active) {
-            const int e = find_entry(L.off, L.nentry, w);
             bra = __ldg(L.entry_bra + e);
             ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(w - __ldg(L.off + e));
             if (negligible_quartet(L, bra, ket)) {

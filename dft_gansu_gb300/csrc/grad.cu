@@ -158,8 +158,8 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
          wid += warp_stride) {
         const int cdi = static_cast<int>(wid % ncd);
         const long long w = (wid / ncd) * 32 + lane;
+        const int e = find_entry_warp(G.goff, L.nentry, (wid / ncd) * 32, w, total);
         if (w >= total) continue;
-        const int e = find_entry(G.goff, L.nentry, w);
         const int bra = __ldg(L.entry_bra + e);
         const ShellPairDev bp = L.pairs[bra];
         const long long item = w - __ldg(G.goff + e);

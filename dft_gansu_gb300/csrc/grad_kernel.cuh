@@ -66,8 +66,8 @@ __global__ void __launch_bounds__(kGradThreads) grad_class_kernel(const GradLaun
          wid += warp_stride) {
         const int cdi = static_cast<int>(wid % NCD);
         const long long w = (wid / NCD) * 32 + lane;
+        const int e = find_entry_warp(G.goff, L.nentry, (wid / NCD) * 32, w, total);
         if (w >= total) continue;
-        const int e = find_entry(G.goff, L.nentry, w);
         const int bra = __ldg(L.entry_bra + e);
         const ShellPairDev bp = L.pairs[bra];
         const long long item = w - __ldg(G.goff + e);
