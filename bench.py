@@ -226,6 +226,13 @@ def run_reference(args, rank, world):
 FULL_PRIM_QUARTETS = {0: 62489524}
 
 
+def _lib_jk(eng, D, J, K):
+    """One FP64 direct J/K build into fixed buffers (a repeated build replays its graph under a graph schedule)."""
+    from dft_gansu_gb300._capi import check, lib
+    check(lib().hf_compute_jk_direct(eng._h, D.data_ptr(), J.data_ptr(), K.data_ptr(), 0, 0.0, None),
+          "hf_compute_jk_direct")
+
+
 def run_ours(args, rank, world):
     import torch
     import dft_gansu_gb300 as gg
@@ -247,14 +254,27 @@ def run_ours(args, rank, world):
         o["initial_guess"] = GUESSES[args.guess or "core"]
         o["eigensolver"] = gg.HF_EIGEN_PURIFICATION if args.eigensolver == "purification" else gg.HF_EIGEN_SYEVD
 
-    def solve(opts):
+    def solve(opts, e=eng):
         flush.zero_()
         torch.cuda.synchronize()
-        return eng.rhf_scf(nel, opts)
+        return e.rhf_scf(nel, opts)
+
+    # Fock launch schedules: the default (class launches in turn on one stream, 16
+    # blocks/SM) on `eng`; on `eng_t` the autotuned grid caps and branch count with
+    # every repeated build replayed from a CUDA graph.  --schedule picks the headline.
+    eng_t = gg.Engine(mol, 1e-12)
+    r_d = eng_t.rhf_scf(nel, opts_fp64, want_matrices=True)
+    tune = eng_t.autotune(r_d["density"])
+    eng_t.set_fock_schedule(tune["num_branches"], use_graph=True)
+    head, alt = (eng_t, eng) if args.schedule == "tuned" else (eng, eng_t)
 
     for _ in range(args.warmup):
-        solve(opts_mixed)
-        solve(opts_fp64)
+        for e_ in (head, alt):
+            solve(opts_mixed, e_)
+            solve(opts_fp64, e_)
+
+    def per_iter(rs):
+        return sum(r["scf_ms_total"] for r in rs) / max(sum(r["iterations"] for r in rs), 1)
 
     # ---- timed: mixed (the headline), then FP64 for the comparison
     dist_barrier(world)
@@ -263,12 +283,22 @@ def run_ours(args, rank, world):
     mixed, fp64 = [], []
     with ClockSampler(dev) as clocks:
         for _ in range(args.steps):
-            mixed.append(solve(opts_mixed))
+            mixed.append(solve(opts_mixed, head))
         l1 = gg.kernel_launch_count()
         for _ in range(args.steps):
-            fp64.append(solve(opts_fp64))
+            fp64.append(solve(opts_fp64, head))
     torch.cuda.synchronize()
     dist_barrier(world)
+    # the other schedule, same solves (not part of the headline)
+    alt_mixed = [solve(opts_mixed, alt) for _ in range(args.steps)]
+    alt_fp64 = [solve(opts_fp64, alt) for _ in range(args.steps)]
+    sched_ms = {args.schedule: {"mixed_ms_per_iter": per_iter(mixed), "fp64_ms_per_iter": per_iter(fp64)},
+                ("default" if args.schedule == "tuned" else "tuned"):
+                    {"mixed_ms_per_iter": per_iter(alt_mixed), "fp64_ms_per_iter": per_iter(alt_fp64)}}
+    schedule = {"headline": args.schedule, **sched_ms,
+                "delta_E_tuned_vs_default": max(abs(a["total_energy"] - b["total_energy"])
+                                                for a, b in zip(mixed + fp64, alt_mixed + alt_fp64)),
+                "autotune": tune}
     it_mx = sum(r["iterations"] for r in mixed)
     it_64 = sum(r["iterations"] for r in fp64)
     ms_mx = sum(r["scf_ms_total"] for r in mixed) / max(it_mx, 1)
@@ -286,6 +316,8 @@ def run_ours(args, rank, world):
         t0 = time.perf_counter()
         m2 = gg.Molecular(atoms, gbs)
         e2 = gg.Engine(m2, 1e-12)
+        if args.schedule == "tuned":  # branches and graph replay; the autotuner is not re-run per engine
+            e2.set_fock_schedule(tune["num_branches"], use_graph=True)
         r2 = e2.rhf_scf(nel, opts_mixed)
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) * 1e3
@@ -296,21 +328,21 @@ def run_ours(args, rank, world):
 
     # ---- roofline of the dominant kernel family: one FP64 direct Fock build
     import numpy as np
-    D = torch.tensor(np.eye(mol.num_basis) * 0.5, dtype=torch.float64, device="cuda")
-    r_ref = eng.rhf_scf(nel, opts_fp64, want_matrices=True)
+    r_ref = head.rhf_scf(nel, opts_fp64, want_matrices=True)
     D = r_ref["density"]
-    for _ in range(2):
-        eng.jk(D)
-    eng.reset_stats()
+    Jr, Kr = torch.empty_like(D), torch.empty_like(D)
+    for _ in range(3):
+        _lib_jk(head, D, Jr, Kr)
+    head.reset_stats()
     flush.zero_()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
-    eng.jk(D)
+    _lib_jk(head, D, Jr, Kr)
     ev1.record()
     ev1.synchronize()
     build_ms = ev0.elapsed_time(ev1)
-    st = eng.class_stats()
+    st = head.class_stats()
     flops = model_flops(st, "fp64")
     peak64 = gg.measure_fma_peak(0)
     achieved = flops / (build_ms * 1e-3) / 1e12
@@ -325,11 +357,11 @@ def run_ours(args, rank, world):
         Fs = torch.randn(m8, N, N, dtype=torch.float64, device="cuda", generator=gen)
         Fout = torch.empty(N, N, dtype=torch.float64, device="cuda")
         for _ in range(3):
-            eng.fock_diis(Es, Fs)
+            head.fock_diis(Es, Fs)
         q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         q0.record()
         for _ in range(20):
-            eng.fock_diis(Es, Fs)
+            head.fock_diis(Es, Fs)
         q1.record()
         q1.synchronize()
         per_call = q0.elapsed_time(q1) / 20
@@ -401,6 +433,7 @@ def run_ours(args, rank, world):
                        f"with FP32 quartets where Q_ab*Q_cd*max|dD| < {args.mixed_threshold})",
                        "convergence": CONV, "l2": "flushed (512 MB write) before every step",
                        "initial_guess": args.guess or "core", "eigensolver": args.eigensolver,
+                       "fock_schedule": args.schedule,
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "fp64_ms_per_iter": ms_64, "mixed_speedup_vs_fp64": ms_64 / ms_mx,
             "delta_E_mixed_vs_fp64": dE, "energy_fp64": fp64[0]["total_energy"],
@@ -415,9 +448,11 @@ def run_ours(args, rank, world):
             "e2e": {"value": statistics.mean(e2e_vals), "unit": "ms/iter", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": l1 - l0,
+            "schedule": schedule,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                          "frac": achieved / peak64, "traffic": None,
-                         "kernel": "direct Fock build, FP64 tier (21 quartet-class launches), one launch set",
+                         "kernel": "direct Fock build, FP64 tier (21 quartet-class launches), one launch set under the "
+                                   "headline schedule",
                          "build_ms": build_ms, "model_flops": flops,
                          "peak_source": "hf_measure_fma_peak FP64 FMA chains (MEASURED_PEAKS.json has no FP64)"},
             "clocks": clocks.summary(),
@@ -656,6 +691,9 @@ def main():
     ap.add_argument("--batch-precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--skip-fd", action="store_true",
                     help="decane_grad_fd: the FP64 and mixed gradients only, no finite differences")
+    ap.add_argument("--schedule", default="default", choices=["default", "tuned"],
+                    help="Fock launch schedule of the headline: default, or autotuned grid caps and branches "
+                         "with CUDA-graph replay (the other one is timed beside it)")
     ap.add_argument("--eigensolver", default="purification", choices=["syevd", "purification"],
                     help="density from F inside the SCF loop (both arms use the same)")
     args = ap.parse_args()

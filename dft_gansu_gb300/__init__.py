@@ -245,6 +245,29 @@ class Engine:
                                          _stream(stream)), "hf_compute_jk_direct")
         return J, K
 
+    def set_fock_schedule(self, num_branches: int = 1, use_graph: bool = False):
+        """Launch schedule of the direct Fock build: class launches on num_branches
+        concurrent streams, each distinct build replayed from a CUDA graph."""
+        check(lib().hf_engine_set_fock_schedule(self._h, int(num_branches), 1 if use_graph else 0),
+              "hf_engine_set_fock_schedule")
+
+    def autotune(self, D, stream=None) -> dict:
+        """Chooses the Fock build's grid caps and branch count by timing on density D."""
+        from ._capi import AutotuneReport
+        rep = AutotuneReport()
+        check(lib().hf_engine_autotune(self._h, _ptr(D), C.byref(rep), _stream(stream)), "hf_engine_autotune")
+        out = {f: getattr(rep, f) for f, _ in AutotuneReport._fields_}
+        out.update(self.fock_schedule())
+        return out
+
+    def fock_schedule(self) -> dict:
+        n = C.c_int()
+        check(lib().hf_engine_fock_schedule(self._h, 0, C.byref(n), None, None, None), "hf_engine_fock_schedule")
+        k = n.value
+        c64, c32, br = (C.c_int * max(k, 1))(), (C.c_int * max(k, 1))(), (C.c_int * max(k, 1))()
+        check(lib().hf_engine_fock_schedule(self._h, k, C.byref(n), c64, c32, br), "hf_engine_fock_schedule")
+        return {"cap_fp64": list(c64)[:k], "cap_fp32": list(c32)[:k], "branch": list(br)[:k]}
+
     def diis_error(self, S, X, F, D, include_transform=False, stream=None):
         E = self._empty(self.N, self.N)
         check(lib().hf_compute_diis_error(self._h, _ptr(S), _ptr(X), _ptr(F), _ptr(D), _ptr(E),

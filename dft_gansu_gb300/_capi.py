@@ -98,6 +98,16 @@ class ScfResult(C.Structure):
     ]
 
 
+class AutotuneReport(C.Structure):
+    _fields_ = [
+        ("build_ms_default", C.c_double),
+        ("build_ms_tuned", C.c_double),
+        ("num_branches", C.c_int),
+        ("num_class_pairs", C.c_int),
+        ("num_caps_changed", C.c_int),
+    ]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _D = C.c_double
@@ -126,6 +136,9 @@ SIGNATURES = {
     "hf_compute_fock_stored_rhf": (_I, [_P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_direct_rhf": (_I, [_P, _P, _P, _P, _I, _D, _P]),
     "hf_compute_jk_direct": (_I, [_P, _P, _P, _P, _I, _D, _P]),
+    "hf_engine_set_fock_schedule": (_I, [_P, _I, _I]),
+    "hf_engine_autotune": (_I, [_P, _P, C.POINTER(AutotuneReport), _P]),
+    "hf_engine_fock_schedule": (_I, [_P, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "hf_compute_diis_error": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_diis": (_I, [_P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_diis_noalloc": (_I, [_P, _P, _P, _I, _I, _P]),

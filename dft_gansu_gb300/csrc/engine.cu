@@ -196,6 +196,7 @@ Engine::~Engine()
                     d_shell_info, d_block_dmax, d_mol_base, d_mol_n, d_mol_bf0, d_mol_atoms, d_shell_mol,
                     scf.P32a, scf.P32b, scf.P32c, scf.Qocc, scf.Mocc, scf.qwork, scf.qinfo};
     ri_destroy(ri);
+    schedule_release(sched);
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (scf.syevj_params) cusolverDnDestroySyevjInfo(scf.syevj_params);

@@ -83,6 +83,38 @@ struct MixedPlan {
 
 struct RiState;  // ri.hpp
 
+// Launch schedule of the direct Fock build (fock.cu).  The class-pair launches
+// run on nbranch streams forked from and joined back to the caller's stream
+// (1: all on the caller's stream); with use_graph every distinct build (same
+// density and output pointers, precision and cuts) is captured into a CUDA
+// graph on its second occurrence and replayed from then on.  cap64/cap32 are
+// the grid caps (blocks per SM) of each class pair's FP64 and FP32 launches,
+// chosen by hf_engine_autotune (0: kFockBlocksPerSm).
+constexpr int kMaxBranches = 8;
+constexpr int kFockBlocksPerSm = 16;
+constexpr int kMaxFockGraphs = 16;
+struct FockSchedule {
+    int nbranch = 1;
+    bool use_graph = false;
+    std::vector<int> branch_of;     // per class pair (empty: round robin)
+    std::vector<int> cap64, cap32;  // per class pair (empty: default)
+    cudaStream_t branch[kMaxBranches] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kMaxBranches] = {};
+    cudaStream_t capture = nullptr;  // graphs are captured on this stream (the caller's may be the legacy stream)
+    struct Graph {
+        const double* D;
+        double *J, *K;
+        int precision;
+        double mixed_thr, drop;
+        int uses;
+        cudaGraphExec_t exec;  // null until the second use
+        bool mixed;            // Engine::last_mixed after this build
+        long long launches;    // kernels in the graph
+    };
+    std::vector<Graph> graphs;
+};
+
 struct Engine {
     int num_basis = 0, num_shells = 0, num_atoms = 0, num_prims = 0;
     // molecules (a batch engine holds several; a plain engine one)
@@ -148,6 +180,7 @@ struct Engine {
     long long bytes_h2d = 0;                   // bytes uploaded by engine creation
 
     RiState* ri = nullptr;  // auxiliary basis and B tensor (RI), attached on request
+    FockSchedule sched;     // launch schedule of the direct Fock build (fock.cu)
 
     cublasHandle_t cublas = nullptr;
     cusolverDnHandle_t cusolver = nullptr;
@@ -197,6 +230,8 @@ int mol_absmax(Engine& e, const double* d_A, double* d_out, cudaStream_t s);
 // batch build with per-molecule FP32 cuts and drop thresholds (fock.cu)
 int build_jk_batch(Engine& e, const double* d_D, const double* d_mol_tau, const double* d_mol_skip,
                    double* d_mol_dmax, cudaStream_t s);
+// releases the schedule's streams, events and graphs (fock.cu)
+void schedule_release(FockSchedule& S);
 
 // one_electron.cu
 int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s);

@@ -14,6 +14,8 @@
 // finds that prefix by bisection and prefix-sums both queues on the device,
 // so no host round trip is needed between the density and the launches.
 #include <algorithm>
+#include <limits>
+#include <string>
 
 #include "engine.hpp"
 #include "fock_kernel.cuh"
@@ -251,10 +253,65 @@ __global__ void finish_kernel(const double* __restrict__ Jp, const double* __res
     }
 }
 
-int grid_for(long long work, int num_sms)
+// blocks for one thread per work item, at most num_sms * blocks_per_sm (the kernels loop over the rest)
+int grid_for_cap(long long work, int num_sms, int blocks_per_sm)
 {
     const long long blocks = (work + kFockThreads - 1) / kFockThreads;
-    return static_cast<int>(std::max<long long>(1, std::min<long long>(blocks, static_cast<long long>(num_sms) * 16)));
+    return static_cast<int>(
+        std::max<long long>(1, std::min<long long>(blocks, static_cast<long long>(num_sms) * blocks_per_sm)));
+}
+
+int grid_for(long long work, int num_sms) { return grid_for_cap(work, num_sms, kFockBlocksPerSm); }
+
+// grid of class pair c's FP64 or FP32 launch under the engine's schedule
+int class_grid(const Engine& e, int c, bool fp32)
+{
+    const std::vector<int>& v = fp32 ? e.sched.cap32 : e.sched.cap64;
+    const int cap = (c < static_cast<int>(v.size()) && v[c] > 0) ? v[c] : kFockBlocksPerSm;
+    return grid_for_cap(e.class_pairs[c].n_survivors, e.num_sms, cap);
+}
+
+// branch streams and events of the schedule, created on first use
+int schedule_streams(Engine& e)
+{
+    FockSchedule& S = e.sched;
+    if (!S.fork) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming));
+    for (int b = 0; b < S.nbranch && b < kMaxBranches; ++b) {
+        if (!S.branch[b]) GB_CUDA_TRY(cudaStreamCreateWithFlags(&S.branch[b], cudaStreamNonBlocking));
+        if (!S.join[b]) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.join[b], cudaEventDisableTiming));
+    }
+    if (S.use_graph && !S.capture) GB_CUDA_TRY(cudaStreamCreateWithFlags(&S.capture, cudaStreamNonBlocking));
+    return HF_OK;
+}
+
+// Issues launch(c, stream) for every class pair with work: on s itself when the
+// schedule has one branch, else on the branch streams, forked from s (an event
+// recorded on s) and joined back into s, so s sees one ordered build either way.
+template <class Launch>
+int launch_class_pairs(Engine& e, cudaStream_t s, Launch&& launch)
+{
+    FockSchedule& S = e.sched;
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    const int nb = std::max(1, std::min(S.nbranch, kMaxBranches));
+    int st;
+    if (nb == 1) {
+        for (int c = 0; c < ncp; ++c)
+            if (e.class_pairs[c].n_survivors > 0 && (st = launch(c, s))) return st;
+        return HF_OK;
+    }
+    if ((st = schedule_streams(e))) return st;
+    GB_CUDA_TRY(cudaEventRecord(S.fork, s));
+    for (int b = 0; b < nb; ++b) GB_CUDA_TRY(cudaStreamWaitEvent(S.branch[b], S.fork, 0));
+    for (int c = 0; c < ncp; ++c) {
+        if (e.class_pairs[c].n_survivors == 0) continue;
+        const int b = (c < static_cast<int>(S.branch_of.size()) ? S.branch_of[c] : c) % nb;
+        if ((st = launch(c, S.branch[b]))) return st;
+    }
+    for (int b = 0; b < nb; ++b) {
+        GB_CUDA_TRY(cudaEventRecord(S.join[b], S.branch[b]));
+        GB_CUDA_TRY(cudaStreamWaitEvent(s, S.join[b], 0));
+    }
+    return HF_OK;
 }
 
 FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off, const int* lo)
@@ -384,24 +441,25 @@ int build_jk_batch(Engine& e, const double* d_D, const double* d_mol_tau, const 
     a.mol_skip = d_mol_skip;
     mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
     GB_LAUNCH_CHECK();
-    for (int c = 0; c < ncp; ++c) {
+    return launch_class_pairs(e, s, [&](int c, cudaStream_t cs) -> int {
         const ClassPair& cp = e.class_pairs[c];
-        if (cp.n_survivors == 0) continue;
         const PairClass& X = e.pair_classes[cp.X];
         const PairClass& Y = e.pair_classes[cp.Y];
         FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
         if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
-        const int grid = grid_for(cp.n_survivors, e.num_sms);
-        f(false, make_launch(e, c, false, e.plan.off64, e.d_entry_lo0), grid, s);
+        f(false, make_launch(e, c, false, e.plan.off64, e.d_entry_lo0), class_grid(e, c, false), cs);
         GB_LAUNCH_CHECK();
-        f(true, make_launch(e, c, true, e.plan.off32, e.plan.lo32), grid, s);
+        f(true, make_launch(e, c, true, e.plan.off32, e.plan.lo32), class_grid(e, c, true), cs);
         GB_LAUNCH_CHECK();
-    }
-    return HF_OK;
+        return HF_OK;
+    });
 }
 
-int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
-             cudaStream_t s, double drop)
+namespace {
+
+// One direct J/K build as ordinary launches (build_jk below adds the graph replay).
+int build_jk_body(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
+                  cudaStream_t s, double drop)
 {
     const size_t nn = static_cast<size_t>(e.nelem);
     const bool mixed = (precision == HF_PRECISION_MIXED);
@@ -414,18 +472,18 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
         GB_CUDA_TRY(cudaMemsetAsync(e.d_Jp32, 0, nn * sizeof(float), s));
         GB_CUDA_TRY(cudaMemsetAsync(e.d_Kp32, 0, nn * sizeof(float), s));
     }
-    const int ncp = static_cast<int>(e.class_pairs.size());
     if (!mixed) {
-        for (int c = 0; c < ncp; ++c) {
+        st = launch_class_pairs(e, s, [&](int c, cudaStream_t cs) -> int {
             const ClassPair& cp = e.class_pairs[c];
-            if (cp.n_survivors == 0) continue;
             const PairClass& X = e.pair_classes[cp.X];
             const PairClass& Y = e.pair_classes[cp.Y];
             FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
             if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
-            f(false, make_launch(e, c, false, e.d_off_static, e.d_entry_lo0), grid_for(cp.n_survivors, e.num_sms), s);
+            f(false, make_launch(e, c, false, e.d_off_static, e.d_entry_lo0), class_grid(e, c, false), cs);
             GB_LAUNCH_CHECK();
-        }
+            return HF_OK;
+        });
+        if (st) return st;
     } else {
         const double c2 = e.cgto_max * e.cgto_max;
         PlanArgs a;
@@ -447,29 +505,252 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
             block_absmax_kernel<<<g, 256, 0, s>>>(d_D, e.d_shell_info, e.num_shells, e.num_basis, e.d_block_dmax);
             GB_LAUNCH_CHECK();
         }
-        for (int c = 0; c < ncp; ++c) {
+        st = launch_class_pairs(e, s, [&](int c, cudaStream_t cs) -> int {
             const ClassPair& cp = e.class_pairs[c];
-            if (cp.n_survivors == 0) continue;
             const PairClass& X = e.pair_classes[cp.X];
             const PairClass& Y = e.pair_classes[cp.Y];
             FockLauncher f = fock_launcher(X.la, X.lb, Y.la, Y.lb);
             if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
-            const int grid = grid_for(cp.n_survivors, e.num_sms);
             FockClassLaunch l64 = make_launch(e, c, false, e.plan.off64, e.d_entry_lo0);
             FockClassLaunch l32 = make_launch(e, c, true, e.plan.off32, e.plan.lo32);
             l64.block_dmax = l32.block_dmax = e.d_block_dmax;
             l64.skip_cut = l32.skip_cut = a.skip_threshold / a.factor;  // Qs Qs c_max^4 max|dD| < thr
-            f(false, l64, grid, s);
+            f(false, l64, class_grid(e, c, false), cs);
             GB_LAUNCH_CHECK();
-            f(true, l32, grid, s);
+            f(true, l32, class_grid(e, c, true), cs);
             GB_LAUNCH_CHECK();
-        }
+            return HF_OK;
+        });
+        if (st) return st;
     }
     if (d_J || d_K) {
         const int grid = static_cast<int>(std::min<long long>((static_cast<long long>(nn) + 255) / 256, 4096));
         finish_kernel<<<grid, 256, 0, s>>>(e.d_Jp, e.d_Kp, mixed ? e.d_Jp32 : nullptr, mixed ? e.d_Kp32 : nullptr,
                                            e.d_scale, nullptr, e.block_map(), d_J, d_K, nullptr);
         GB_LAUNCH_CHECK();
+    }
+    return HF_OK;
+}
+
+void destroy_graph(FockSchedule::Graph& g)
+{
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+}
+
+// graphs hold the grid caps and branch assignment of the schedule they were captured under
+void clear_graphs(FockSchedule& S)
+{
+    for (auto& g : S.graphs) destroy_graph(g);
+    S.graphs.clear();
+}
+
+}  // namespace
+
+void schedule_release(FockSchedule& S)
+{
+    clear_graphs(S);
+    for (int b = 0; b < kMaxBranches; ++b) {
+        if (S.branch[b]) cudaStreamDestroy(S.branch[b]);
+        if (S.join[b]) cudaEventDestroy(S.join[b]);
+        S.branch[b] = nullptr;
+        S.join[b] = nullptr;
+    }
+    if (S.fork) cudaEventDestroy(S.fork);
+    if (S.capture) cudaStreamDestroy(S.capture);
+    S.fork = nullptr;
+    S.capture = nullptr;
+}
+
+// One direct J/K build.  With the schedule's use_graph (single-molecule engines),
+// the first build with a given (density, J, K, precision, cuts) runs as ordinary
+// launches (it also makes the lazy allocations), the second is captured into a
+// CUDA graph on the schedule's capture stream, and that and every later one
+// replay the graph on s.  The graph reads the density and writes J'/K' (and J, K)
+// at replay, so the buffers' contents may change between builds, not their addresses.
+int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precision, double mixed_thr,
+             cudaStream_t s, double drop)
+{
+    FockSchedule& S = e.sched;
+    if (!S.use_graph || e.nmol != 1) return build_jk_body(e, d_D, d_J, d_K, precision, mixed_thr, s, drop);
+    FockSchedule::Graph* g = nullptr;
+    for (auto& x : S.graphs)
+        if (x.D == d_D && x.J == d_J && x.K == d_K && x.precision == precision && x.mixed_thr == mixed_thr &&
+            x.drop == drop) {
+            g = &x;
+            break;
+        }
+    if (!g) {
+        if (static_cast<int>(S.graphs.size()) >= kMaxFockGraphs) {
+            destroy_graph(S.graphs.front());
+            S.graphs.erase(S.graphs.begin());
+        }
+        S.graphs.push_back(FockSchedule::Graph{d_D, d_J, d_K, precision, mixed_thr, drop, 0, nullptr, false, 0});
+        g = &S.graphs.back();
+    }
+    if (!g->exec && g->uses++ == 0) return build_jk_body(e, d_D, d_J, d_K, precision, mixed_thr, s, drop);
+    if (!g->exec) {
+        int st = schedule_streams(e);
+        if (st) return st;
+        const long long l0 = launch_count();
+        GB_CUDA_TRY(cudaStreamBeginCapture(S.capture, cudaStreamCaptureModeThreadLocal));
+        st = build_jk_body(e, d_D, d_J, d_K, precision, mixed_thr, S.capture, drop);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(S.capture, &graph);
+        const long long recorded = launch_count() - l0;
+        count_launches(-recorded);  // recorded, not launched
+        if (st || ce != cudaSuccess || !graph) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            if (!st) set_error(std::string("Fock build capture: ") + cudaGetErrorString(ce));
+            return st ? st : HF_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&g->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            g->exec = nullptr;
+            return set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie)), HF_ERR_CUDA;
+        }
+        g->mixed = e.last_mixed;
+        g->launches = recorded;
+    }
+    GB_CUDA_TRY(cudaGraphLaunch(g->exec, s));
+    count_launches(g->launches);
+    e.last_mixed = g->mixed;
+    return HF_OK;
+}
+
+// Autotuner of the direct Fock build's launch schedule (hf_engine_autotune).
+// Times, on the caller's density, every class pair's FP64 and FP32 launch over
+// its whole quartet list at grid caps of 2, 4, 8, 16 and 32 blocks per SM and
+// keeps the fastest (the default unless another is 3% faster), then assigns
+// the class pairs to 1, 2 or 4 branches (longest measured time first, to the
+// least loaded branch) and keeps the branch count whose FP64 build is fastest.
+int autotune_schedule(Engine& e, const double* d_D, hf_autotune_report* rep, cudaStream_t s)
+{
+    if (e.nmol != 1) return set_error("hf_engine_autotune: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
+    FockSchedule& S = e.sched;
+    clear_graphs(S);
+    const bool use_graph = S.use_graph;
+    S.use_graph = false;
+    S.nbranch = 1;
+    S.branch_of.clear();
+    S.cap64.clear();
+    S.cap32.clear();
+    struct Events {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Events()
+        {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev;
+    GB_CUDA_TRY(cudaEventCreate(&ev.a));
+    GB_CUDA_TRY(cudaEventCreate(&ev.b));
+    // best of `reps` timings of issue() on s, in ms
+    auto timed = [&](int reps, auto&& issue, double* ms) -> int {
+        double best = std::numeric_limits<double>::infinity();
+        for (int r = 0; r < reps; ++r) {
+            GB_CUDA_TRY(cudaEventRecord(ev.a, s));
+            int st = issue();
+            if (st) return st;
+            GB_CUDA_TRY(cudaEventRecord(ev.b, s));
+            GB_CUDA_TRY(cudaEventSynchronize(ev.b));
+            float f = 0.f;
+            GB_CUDA_TRY(cudaEventElapsedTime(&f, ev.a, ev.b));
+            best = std::min(best, static_cast<double>(f));
+        }
+        *ms = best;
+        return HF_OK;
+    };
+    auto fp64_build = [&]() { return build_jk_body(e, d_D, nullptr, nullptr, HF_PRECISION_FP64, 0.0, s, -1.0); };
+    int st;
+    double ms_default = 0.0;
+    if ((st = fp64_build())) return st;  // warm-up
+    if ((st = timed(2, fp64_build, &ms_default))) return st;
+
+    // per class pair and precision tier: grid cap
+    if ((st = scale_density(e, d_D, true, s))) return st;  // the FP32 tier reads D' in FP32
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    const int caps[] = {kFockBlocksPerSm, 2, 4, 8, 32};
+    S.cap64.assign(ncp, 0);
+    S.cap32.assign(ncp, 0);
+    std::vector<double> cost(ncp, 0.0);
+    int active = 0, changed = 0;
+    for (int c = 0; c < ncp; ++c) {
+        const ClassPair& cp = e.class_pairs[c];
+        if (cp.n_survivors == 0) continue;
+        ++active;
+        FockLauncher f = fock_launcher(e.pair_classes[cp.X].la, e.pair_classes[cp.X].lb, e.pair_classes[cp.Y].la,
+                                       e.pair_classes[cp.Y].lb);
+        if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
+        for (int tier = 0; tier < 2; ++tier) {
+            const bool fp32 = tier == 1;
+            const FockClassLaunch L = make_launch(e, c, fp32, e.d_off_static, e.d_entry_lo0);
+            f(fp32, L, grid_for_cap(cp.n_survivors, e.num_sms, kFockBlocksPerSm), s);  // warm-up
+            GB_LAUNCH_CHECK();
+            int best = kFockBlocksPerSm;
+            double best_ms = std::numeric_limits<double>::infinity();
+            for (int cap : caps) {
+                const int grid = grid_for_cap(cp.n_survivors, e.num_sms, cap);
+                double ms = 0.0;
+                if ((st = timed(2, [&]() -> int {
+                         f(fp32, L, grid, s);
+                         GB_LAUNCH_CHECK();
+                         return HF_OK;
+                     }, &ms)))
+                    return st;
+                if (cap == kFockBlocksPerSm || ms < 0.97 * best_ms) {
+                    best_ms = ms;
+                    best = cap;
+                }
+            }
+            (fp32 ? S.cap32 : S.cap64)[c] = best;
+            if (best != kFockBlocksPerSm) ++changed;
+            cost[c] += best_ms;
+        }
+    }
+
+    // branches: longest processing time first onto the least loaded branch
+    std::vector<int> order(ncp);
+    for (int c = 0; c < ncp; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    int best_nb = 1;
+    std::vector<int> best_map(ncp, 0);
+    double best_ms = std::numeric_limits<double>::infinity();
+    for (int nb : {1, 2, 4}) {
+        std::vector<int> map(ncp, 0);
+        std::vector<double> load(nb, 0.0);
+        for (int c : order) {
+            const int b = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+            map[c] = b;
+            load[b] += cost[c];
+        }
+        S.nbranch = nb;
+        S.branch_of = map;
+        double ms = 0.0;
+        if ((st = fp64_build())) return st;  // warm-up (creates the branch streams)
+        if ((st = timed(2, fp64_build, &ms))) return st;
+        if (nb == 1 || ms < 0.97 * best_ms) {
+            best_ms = ms;
+            best_nb = nb;
+            best_map = map;
+        }
+    }
+    S.nbranch = best_nb;
+    S.branch_of = best_map;
+    S.use_graph = use_graph;
+    // the timings ran the class kernels outside any build: J'/K' and the class counters start afresh
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_counters, 0, kCounterSlots * sizeof(unsigned long long), s));
+    if ((st = fp64_build())) return st;
+    GB_CUDA_TRY(cudaMemsetAsync(e.d_counters, 0, kCounterSlots * sizeof(unsigned long long), s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (rep) {
+        rep->build_ms_default = ms_default;
+        rep->build_ms_tuned = best_ms;
+        rep->num_branches = best_nb;
+        rep->num_class_pairs = active;
+        rep->num_caps_changed = changed;
     }
     return HF_OK;
 }
@@ -542,6 +823,43 @@ int hf_compute_fock_direct_rhf(hf_engine* eng, const double* d_density, const do
     int st = build_jk(e, d_density, nullptr, nullptr, precision, mixed_threshold, s);
     if (st) return st;
     return finish_fock(e, d_core_hamiltonian, nullptr, nullptr, d_fock, s);
+}
+
+int hf_engine_set_fock_schedule(hf_engine* eng, int num_branches, int use_graph)
+{
+    clear_error();
+    if (!eng || num_branches < 1 || num_branches > kMaxBranches)
+        return set_error("hf_engine_set_fock_schedule: num_branches must be 1..8"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    clear_graphs(e.sched);
+    e.sched.nbranch = num_branches;
+    e.sched.use_graph = use_graph != 0;
+    return HF_OK;
+}
+
+int hf_engine_autotune(hf_engine* eng, const double* d_density, hf_autotune_report* report, void* stream)
+{
+    clear_error();
+    if (!eng || !d_density) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    return autotune_schedule(*reinterpret_cast<Engine*>(eng), d_density, report, static_cast<cudaStream_t>(stream));
+}
+
+int hf_engine_fock_schedule(const hf_engine* eng, int max_class_pairs, int* num_class_pairs, int* cap_fp64,
+                            int* cap_fp32, int* branch)
+{
+    clear_error();
+    if (!eng || !num_class_pairs) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    const Engine& e = *reinterpret_cast<const Engine*>(eng);
+    const FockSchedule& S = e.sched;
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    *num_class_pairs = ncp;
+    const int nb = std::max(1, std::min(S.nbranch, kMaxBranches));
+    for (int c = 0; c < ncp && c < max_class_pairs; ++c) {
+        if (cap_fp64) cap_fp64[c] = (c < static_cast<int>(S.cap64.size()) && S.cap64[c] > 0) ? S.cap64[c] : kFockBlocksPerSm;
+        if (cap_fp32) cap_fp32[c] = (c < static_cast<int>(S.cap32.size()) && S.cap32[c] > 0) ? S.cap32[c] : kFockBlocksPerSm;
+        if (branch) branch[c] = nb == 1 ? 0 : (c < static_cast<int>(S.branch_of.size()) ? S.branch_of[c] : c) % nb;
+    }
+    return HF_OK;
 }
 
 int hf_compute_eri_matrix(hf_engine* eng, double* d_eri, void* stream)

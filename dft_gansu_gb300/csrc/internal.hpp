@@ -12,6 +12,10 @@ void set_error(const std::string& msg);
 void clear_error();
 // process-wide count of kernel launches issued by this library
 void count_launch();
+// adds n (may be negative) to the count: launches replayed from a CUDA graph,
+// or recorded into one during a capture (which run later, not then)
+void count_launches(long long n);
+long long launch_count();
 
 struct Molecule {
     std::vector<hf_atom> atoms;

@@ -146,6 +146,39 @@ int hf_compute_fock_direct_rhf(hf_engine* eng, const double* d_density, const do
 int hf_compute_jk_direct(hf_engine* eng, const double* d_density, double* d_J, double* d_K, int precision,
                          double mixed_threshold, void* stream);
 
+/* Launch schedule of the direct Fock build of a single-molecule engine (no
+ * reference counterpart: the reference launches one kernel per class in turn,
+ * src/gpu_manager.cu:2327-2540).  num_branches in 1..8: the quartet-class
+ * launches run on that many streams forked from and joined back into the
+ * caller's stream (1, the default: all on the caller's stream).  use_graph != 0:
+ * each distinct build (same density and output pointers, precision and cuts) is
+ * captured into a CUDA graph on its second call and replayed from then on; the
+ * graph reads the buffers at replay, so their contents may change between calls,
+ * not their addresses.  Batch engines use the branches, not the graphs. */
+int hf_engine_set_fock_schedule(hf_engine* eng, int num_branches, int use_graph);
+
+typedef struct {
+    double build_ms_default;  /* one FP64 build under the default schedule */
+    double build_ms_tuned;    /* the same build under the chosen schedule */
+    int num_branches;         /* chosen branch count (1, 2 or 4) */
+    int num_class_pairs;      /* quartet class pairs with work */
+    int num_caps_changed;     /* class-pair launches (FP64 and FP32 counted apart) whose grid cap differs from 16 blocks/SM */
+} hf_autotune_report;
+
+/* Autotuner of that schedule (no reference counterpart): on the caller's density
+ * (device N x N), times every quartet class pair's FP64 and FP32 launch at grid
+ * caps of 2..32 blocks per SM and keeps the fastest, then the branch count (1, 2
+ * or 4, class pairs placed longest first on the least loaded branch) with the
+ * fastest FP64 build.  The choice stays with the engine; the class statistics
+ * are reset.  Synchronises the stream.  report may be NULL. */
+int hf_engine_autotune(hf_engine* eng, const double* d_density, hf_autotune_report* report, void* stream);
+
+/* The schedule in force: per class pair (engine order, *num_class_pairs of them,
+ * arrays filled up to max_class_pairs, each may be NULL) the grid caps in blocks
+ * per SM of its FP64 and FP32 launches and its branch. */
+int hf_engine_fock_schedule(const hf_engine* eng, int max_class_pairs, int* num_class_pairs, int* cap_fp64,
+                            int* cap_fp32, int* branch);
+
 /* Replaces gansu::gpu::computeDIISErrorMatrix (src/gpu_manager.cu:1020-1067):
  * E = FDS - SDF, and X E X^T when include_transform != 0. */
 int hf_compute_diis_error(hf_engine* eng, const double* d_overlap, const double* d_transform, const double* d_fock,

@@ -175,3 +175,13 @@ def test_pure_function_counts(built_library):
     assert T.shape == (260, 250) and np.linalg.matrix_rank(T) == 250
     # the pure d combinations carry no r^2 = xx + yy + zz component (coefficient space)
     assert np.allclose(spherical.D_PURE.T @ np.array([1, 1, 1, 0, 0, 0.0]), 0.0)
+
+
+def test_command_line_rejects_bad_arguments(capsys):
+    """The HF_main front end stops on its arguments before any device work."""
+    from dft_gansu_gb300.__main__ import main
+    assert main(["--no_such_key", "1"]) == 2
+    assert "no_such_key" in capsys.readouterr().err
+    assert main(["-m", "rhf"]) == 2  # no xyz file, no basis
+    assert "required" in capsys.readouterr().err
+    assert main(["-x"]) == 2  # option without a value
