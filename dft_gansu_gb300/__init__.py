@@ -157,7 +157,54 @@ ROHF_COUPLINGS = {
 }
 
 
-class Engine:
+class _FockScheduleMixin:
+    """Launch schedule of the direct Fock build (hf_engine_set_fock_schedule,
+    hf_engine_set_fock_grid_caps, hf_engine_autotune, hf_engine_fock_schedule);
+    the analytic gradient's class launches use the same branches."""
+
+    def set_fock_schedule(self, num_branches: int = 1, use_graph: bool = False, grid_caps=None):
+        """Class launches on num_branches concurrent streams; use_graph replays each
+        distinct build from a CUDA graph (single-molecule engines).  grid_caps: a
+        schedule from autotune() or fock_schedule() of an engine over the same
+        molecules (cap_fp64, cap_fp32, branch lists), applied without timing, or
+        "default" for 16 blocks per SM everywhere; None keeps the caps in force."""
+        check(lib().hf_engine_set_fock_schedule(self._h, int(num_branches), 1 if use_graph else 0),
+              "hf_engine_set_fock_schedule")
+        if isinstance(grid_caps, str):
+            if grid_caps != "default":
+                raise ValueError(f"unknown grid_caps {grid_caps!r}")
+            n = len(self.fock_schedule()["cap_fp64"])
+            check(lib().hf_engine_set_fock_grid_caps(self._h, n, None, None, None), "hf_engine_set_fock_grid_caps")
+        elif grid_caps is not None:
+            k = len(grid_caps["cap_fp64"])
+            arr = [(C.c_int * max(k, 1))(*grid_caps[key]) for key in ("cap_fp64", "cap_fp32", "branch")]
+            check(lib().hf_engine_set_fock_grid_caps(self._h, k, *arr), "hf_engine_set_fock_grid_caps")
+
+    def _schedule_density(self):
+        raise NotImplementedError
+
+    def autotune(self, D=None, stream=None) -> dict:
+        """Chooses grid caps and the branch count by timing Fock builds on density D
+        (the timed class lists do not depend on its values; default: zeros)."""
+        from ._capi import AutotuneReport
+        if D is None:
+            D = self._schedule_density()
+        rep = AutotuneReport()
+        check(lib().hf_engine_autotune(self._h, _ptr(D), C.byref(rep), _stream(stream)), "hf_engine_autotune")
+        out = {f: getattr(rep, f) for f, _ in AutotuneReport._fields_}
+        out.update(self.fock_schedule())
+        return out
+
+    def fock_schedule(self) -> dict:
+        n = C.c_int()
+        check(lib().hf_engine_fock_schedule(self._h, 0, C.byref(n), None, None, None), "hf_engine_fock_schedule")
+        k = n.value
+        c64, c32, br = (C.c_int * max(k, 1))(), (C.c_int * max(k, 1))(), (C.c_int * max(k, 1))()
+        check(lib().hf_engine_fock_schedule(self._h, k, C.byref(n), c64, c32, br), "hf_engine_fock_schedule")
+        return {"cap_fp64": list(c64)[:k], "cap_fp32": list(c32)[:k], "branch": list(br)[:k]}
+
+
+class Engine(_FockScheduleMixin):
     """Device-resident integral engine (the ERI plugin's precomputation)."""
 
     def __init__(self, mol: Molecular, schwarz_screening_threshold: float = 1e-12):
@@ -245,28 +292,8 @@ class Engine:
                                          _stream(stream)), "hf_compute_jk_direct")
         return J, K
 
-    def set_fock_schedule(self, num_branches: int = 1, use_graph: bool = False):
-        """Launch schedule of the direct Fock build: class launches on num_branches
-        concurrent streams, each distinct build replayed from a CUDA graph."""
-        check(lib().hf_engine_set_fock_schedule(self._h, int(num_branches), 1 if use_graph else 0),
-              "hf_engine_set_fock_schedule")
-
-    def autotune(self, D, stream=None) -> dict:
-        """Chooses the Fock build's grid caps and branch count by timing on density D."""
-        from ._capi import AutotuneReport
-        rep = AutotuneReport()
-        check(lib().hf_engine_autotune(self._h, _ptr(D), C.byref(rep), _stream(stream)), "hf_engine_autotune")
-        out = {f: getattr(rep, f) for f, _ in AutotuneReport._fields_}
-        out.update(self.fock_schedule())
-        return out
-
-    def fock_schedule(self) -> dict:
-        n = C.c_int()
-        check(lib().hf_engine_fock_schedule(self._h, 0, C.byref(n), None, None, None), "hf_engine_fock_schedule")
-        k = n.value
-        c64, c32, br = (C.c_int * max(k, 1))(), (C.c_int * max(k, 1))(), (C.c_int * max(k, 1))()
-        check(lib().hf_engine_fock_schedule(self._h, k, C.byref(n), c64, c32, br), "hf_engine_fock_schedule")
-        return {"cap_fp64": list(c64)[:k], "cap_fp32": list(c32)[:k], "branch": list(br)[:k]}
+    def _schedule_density(self):
+        return self._empty(self.N, self.N).zero_()
 
     def diis_error(self, S, X, F, D, include_transform=False, stream=None):
         E = self._empty(self.N, self.N)
@@ -440,7 +467,7 @@ _SHORT = {"-m": "method", "-v": "verbose", "-p": "parameter_file", "-x": "xyzfil
 _KEEP_CASE = {"xyzfilename", "gbsfilename", "parameter_file", "auxiliary_gbsfilename"}
 
 
-class Batch:
+class Batch(_FockScheduleMixin):
     """Many independent molecules in one engine (hf_engine_create_batch) and
     their RHF in lockstep (hf_batch_rhf_scf).  Molecules are ordered by
     (N, electrons) inside, so that equal sizes form batched linear-algebra
@@ -472,6 +499,10 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+    def _schedule_density(self):
+        import torch
+        return torch.zeros(sum(m.num_basis ** 2 for m in self._sorted), dtype=torch.float64, device="cuda")
 
     def sad_density(self, source: str = "auto"):
         """SAD alpha and beta densities of every molecule in the block layout (CUDA tensors)."""

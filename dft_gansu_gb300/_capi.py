@@ -137,6 +137,7 @@ SIGNATURES = {
     "hf_compute_fock_direct_rhf": (_I, [_P, _P, _P, _P, _I, _D, _P]),
     "hf_compute_jk_direct": (_I, [_P, _P, _P, _P, _I, _D, _P]),
     "hf_engine_set_fock_schedule": (_I, [_P, _I, _I]),
+    "hf_engine_set_fock_grid_caps": (_I, [_P, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "hf_engine_autotune": (_I, [_P, _P, C.POINTER(AutotuneReport), _P]),
     "hf_engine_fock_schedule": (_I, [_P, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "hf_compute_diis_error": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),

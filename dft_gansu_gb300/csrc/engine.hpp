@@ -4,6 +4,7 @@
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
+#include <algorithm>
 #include <array>
 #include <utility>
 #include <vector>
@@ -232,6 +233,40 @@ int build_jk_batch(Engine& e, const double* d_D, const double* d_mol_tau, const 
                    double* d_mol_dmax, cudaStream_t s);
 // releases the schedule's streams, events and graphs (fock.cu)
 void schedule_release(FockSchedule& S);
+// creates the schedule's branch streams and events on first use (fock.cu)
+int schedule_streams(Engine& e);
+
+#ifdef __CUDACC__
+// Issues launch(c, stream) for every class pair with work: on s itself when the
+// schedule has one branch, else on the branch streams, forked from s (an event
+// recorded on s) and joined back into s, so s sees one ordered build either way.
+template <class Launch>
+int launch_class_pairs(Engine& e, cudaStream_t s, Launch&& launch)
+{
+    FockSchedule& S = e.sched;
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    const int nb = std::max(1, std::min(S.nbranch, kMaxBranches));
+    int st;
+    if (nb == 1) {
+        for (int c = 0; c < ncp; ++c)
+            if (e.class_pairs[c].n_survivors > 0 && (st = launch(c, s))) return st;
+        return HF_OK;
+    }
+    if ((st = schedule_streams(e))) return st;
+    GB_CUDA_TRY(cudaEventRecord(S.fork, s));
+    for (int b = 0; b < nb; ++b) GB_CUDA_TRY(cudaStreamWaitEvent(S.branch[b], S.fork, 0));
+    for (int c = 0; c < ncp; ++c) {
+        if (e.class_pairs[c].n_survivors == 0) continue;
+        const int b = (c < static_cast<int>(S.branch_of.size()) ? S.branch_of[c] : c) % nb;
+        if ((st = launch(c, S.branch[b]))) return st;
+    }
+    for (int b = 0; b < nb; ++b) {
+        GB_CUDA_TRY(cudaEventRecord(S.join[b], S.branch[b]));
+        GB_CUDA_TRY(cudaStreamWaitEvent(s, S.join[b], 0));
+    }
+    return HF_OK;
+}
+#endif
 
 // one_electron.cu
 int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s);

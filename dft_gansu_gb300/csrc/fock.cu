@@ -271,49 +271,6 @@ int class_grid(const Engine& e, int c, bool fp32)
     return grid_for_cap(e.class_pairs[c].n_survivors, e.num_sms, cap);
 }
 
-// branch streams and events of the schedule, created on first use
-int schedule_streams(Engine& e)
-{
-    FockSchedule& S = e.sched;
-    if (!S.fork) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming));
-    for (int b = 0; b < S.nbranch && b < kMaxBranches; ++b) {
-        if (!S.branch[b]) GB_CUDA_TRY(cudaStreamCreateWithFlags(&S.branch[b], cudaStreamNonBlocking));
-        if (!S.join[b]) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.join[b], cudaEventDisableTiming));
-    }
-    if (S.use_graph && !S.capture) GB_CUDA_TRY(cudaStreamCreateWithFlags(&S.capture, cudaStreamNonBlocking));
-    return HF_OK;
-}
-
-// Issues launch(c, stream) for every class pair with work: on s itself when the
-// schedule has one branch, else on the branch streams, forked from s (an event
-// recorded on s) and joined back into s, so s sees one ordered build either way.
-template <class Launch>
-int launch_class_pairs(Engine& e, cudaStream_t s, Launch&& launch)
-{
-    FockSchedule& S = e.sched;
-    const int ncp = static_cast<int>(e.class_pairs.size());
-    const int nb = std::max(1, std::min(S.nbranch, kMaxBranches));
-    int st;
-    if (nb == 1) {
-        for (int c = 0; c < ncp; ++c)
-            if (e.class_pairs[c].n_survivors > 0 && (st = launch(c, s))) return st;
-        return HF_OK;
-    }
-    if ((st = schedule_streams(e))) return st;
-    GB_CUDA_TRY(cudaEventRecord(S.fork, s));
-    for (int b = 0; b < nb; ++b) GB_CUDA_TRY(cudaStreamWaitEvent(S.branch[b], S.fork, 0));
-    for (int c = 0; c < ncp; ++c) {
-        if (e.class_pairs[c].n_survivors == 0) continue;
-        const int b = (c < static_cast<int>(S.branch_of.size()) ? S.branch_of[c] : c) % nb;
-        if ((st = launch(c, S.branch[b]))) return st;
-    }
-    for (int b = 0; b < nb; ++b) {
-        GB_CUDA_TRY(cudaEventRecord(S.join[b], S.branch[b]));
-        GB_CUDA_TRY(cudaStreamWaitEvent(s, S.join[b], 0));
-    }
-    return HF_OK;
-}
-
 FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off, const int* lo)
 {
     const ClassPair& cp = e.class_pairs[cpi];
@@ -343,6 +300,19 @@ FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off,
 }
 
 }  // namespace
+
+// branch streams and events of the schedule, created on first use
+int schedule_streams(Engine& e)
+{
+    FockSchedule& S = e.sched;
+    if (!S.fork) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming));
+    for (int b = 0; b < S.nbranch && b < kMaxBranches; ++b) {
+        if (!S.branch[b]) GB_CUDA_TRY(cudaStreamCreateWithFlags(&S.branch[b], cudaStreamNonBlocking));
+        if (!S.join[b]) GB_CUDA_TRY(cudaEventCreateWithFlags(&S.join[b], cudaEventDisableTiming));
+    }
+    if (S.use_graph && !S.capture) GB_CUDA_TRY(cudaStreamCreateWithFlags(&S.capture, cudaStreamNonBlocking));
+    return HF_OK;
+}
 
 int scale_density(Engine& e, const double* d_D, bool want_fp32, cudaStream_t s)
 {
@@ -624,11 +594,10 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
 // Times, on the caller's density, every class pair's FP64 and FP32 launch over
 // its whole quartet list at grid caps of 2, 4, 8, 16 and 32 blocks per SM and
 // keeps the fastest (the default unless another is 3% faster), then assigns
-// the class pairs to 1, 2 or 4 branches (longest measured time first, to the
+// the class pairs to 1, 2, 4 or 8 branches (longest measured time first, to the
 // least loaded branch) and keeps the branch count whose FP64 build is fastest.
 int autotune_schedule(Engine& e, const double* d_D, hf_autotune_report* rep, cudaStream_t s)
 {
-    if (e.nmol != 1) return set_error("hf_engine_autotune: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
     FockSchedule& S = e.sched;
     clear_graphs(S);
     const bool use_graph = S.use_graph;
@@ -718,7 +687,7 @@ int autotune_schedule(Engine& e, const double* d_D, hf_autotune_report* rep, cud
     int best_nb = 1;
     std::vector<int> best_map(ncp, 0);
     double best_ms = std::numeric_limits<double>::infinity();
-    for (int nb : {1, 2, 4}) {
+    for (int nb : {1, 2, 4, 8}) {
         std::vector<int> map(ncp, 0);
         std::vector<double> load(nb, 0.0);
         for (int c : order) {
@@ -834,6 +803,30 @@ int hf_engine_set_fock_schedule(hf_engine* eng, int num_branches, int use_graph)
     clear_graphs(e.sched);
     e.sched.nbranch = num_branches;
     e.sched.use_graph = use_graph != 0;
+    return HF_OK;
+}
+
+int hf_engine_set_fock_grid_caps(hf_engine* eng, int num_class_pairs, const int* cap_fp64, const int* cap_fp32,
+                                 const int* branch)
+{
+    clear_error();
+    if (!eng) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    FockSchedule& S = e.sched;
+    const int ncp = static_cast<int>(e.class_pairs.size());
+    if (num_class_pairs != ncp)
+        return set_error("hf_engine_set_fock_grid_caps: the engine has " + std::to_string(ncp) + " class pairs, not " +
+                         std::to_string(num_class_pairs)),
+               HF_ERR_INVALID_ARGUMENT;
+    for (int c = 0; c < ncp; ++c)
+        if ((cap_fp64 && (cap_fp64[c] < 1 || cap_fp64[c] > 64)) || (cap_fp32 && (cap_fp32[c] < 1 || cap_fp32[c] > 64)) ||
+            (branch && (branch[c] < 0 || branch[c] >= kMaxBranches)))
+            return set_error("hf_engine_set_fock_grid_caps: caps must be 1..64 blocks per SM, branches 0..7"),
+                   HF_ERR_INVALID_ARGUMENT;
+    clear_graphs(S);
+    S.cap64.assign(cap_fp64 ? cap_fp64 : nullptr, cap_fp64 ? cap_fp64 + ncp : nullptr);
+    S.cap32.assign(cap_fp32 ? cap_fp32 : nullptr, cap_fp32 ? cap_fp32 + ncp : nullptr);
+    S.branch_of.assign(branch ? branch : nullptr, branch ? branch + ncp : nullptr);
     return HF_OK;
 }
 

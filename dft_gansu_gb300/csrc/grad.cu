@@ -553,10 +553,10 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
     }
     const size_t sgrad_bytes = sizeof(double) * 3 * natom;
     const bool shared_grad = sgrad_bytes <= 32 * 1024;
-    // two-electron part over the quartet lists of every class
-    for (int c = 0; c < static_cast<int>(e.class_pairs.size()); ++c) {
+    // two-electron part over the quartet lists of every class, on the branches of
+    // the engine's Fock schedule (class pairs accumulate into d_grad with atomics)
+    st = launch_class_pairs(e, s, [&](int c, cudaStream_t cs) -> int {
         const ClassPair& cp = e.class_pairs[c];
-        if (cp.n_survivors == 0) continue;
         const PairClass& Y = e.pair_classes[cp.Y];
         const PairClass& X = e.pair_classes[cp.X];
         int max_pp = 1;
@@ -599,17 +599,19 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
                 1, std::min<long long>((warps * 32 + kGradThreads - 1) / kGradThreads,
                                        static_cast<long long>(e.num_sms) * 32)));
             const size_t smem = shared_grad ? sgrad_bytes : 0;
-            const bool done = f32 ? launch_grad_class_f32(X.la, X.lb, Y.la, Y.lb, G, grid, smem, s)
-                                  : launch_grad_class_f64(X.la, X.lb, Y.la, Y.lb, G, grid, smem, s);
+            const bool done = f32 ? launch_grad_class_f32(X.la, X.lb, Y.la, Y.lb, G, grid, smem, cs)
+                                  : launch_grad_class_f64(X.la, X.lb, Y.la, Y.lb, G, grid, smem, cs);
             if (!done) {
                 if (f32)
-                    grad_eri_kernel<float><<<grid, kGradThreads, smem, s>>>(G, ncd);
+                    grad_eri_kernel<float><<<grid, kGradThreads, smem, cs>>>(G, ncd);
                 else
-                    grad_eri_kernel<double><<<grid, kGradThreads, smem, s>>>(G, ncd);
+                    grad_eri_kernel<double><<<grid, kGradThreads, smem, cs>>>(G, ncd);
             }
             GB_LAUNCH_CHECK();
         }
-    }
+        return HF_OK;
+    });
+    if (st) return st;
     // one-electron part
     const double kfold = std::sqrt(2.0 * std::pow(kPi, 2.5));
     for (const PairClass& pc : e.pair_classes) {

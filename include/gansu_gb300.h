@@ -146,7 +146,7 @@ int hf_compute_fock_direct_rhf(hf_engine* eng, const double* d_density, const do
 int hf_compute_jk_direct(hf_engine* eng, const double* d_density, double* d_J, double* d_K, int precision,
                          double mixed_threshold, void* stream);
 
-/* Launch schedule of the direct Fock build of a single-molecule engine (no
+/* Launch schedule of the direct Fock build (no
  * reference counterpart: the reference launches one kernel per class in turn,
  * src/gpu_manager.cu:2327-2540).  num_branches in 1..8: the quartet-class
  * launches run on that many streams forked from and joined back into the
@@ -160,18 +160,27 @@ int hf_engine_set_fock_schedule(hf_engine* eng, int num_branches, int use_graph)
 typedef struct {
     double build_ms_default;  /* one FP64 build under the default schedule */
     double build_ms_tuned;    /* the same build under the chosen schedule */
-    int num_branches;         /* chosen branch count (1, 2 or 4) */
+    int num_branches;         /* chosen branch count (1, 2, 4 or 8) */
     int num_class_pairs;      /* quartet class pairs with work */
     int num_caps_changed;     /* class-pair launches (FP64 and FP32 counted apart) whose grid cap differs from 16 blocks/SM */
 } hf_autotune_report;
 
 /* Autotuner of that schedule (no reference counterpart): on the caller's density
- * (device N x N), times every quartet class pair's FP64 and FP32 launch at grid
- * caps of 2..32 blocks per SM and keeps the fastest, then the branch count (1, 2
- * or 4, class pairs placed longest first on the least loaded branch) with the
- * fastest FP64 build.  The choice stays with the engine; the class statistics
+ * (device N x N; a batch engine's in its block layout), times every quartet class pair's FP64 and FP32 launch at grid
+ * caps of 2..32 blocks per SM and keeps the fastest, then the branch count (1, 2,
+ * 4 or 8, class pairs placed longest first on the least loaded branch) with the
+ * fastest FP64 build.  The analytic gradient's class launches use the same
+ * branches.  The choice stays with the engine; the class statistics
  * are reset.  Synchronises the stream.  report may be NULL. */
 int hf_engine_autotune(hf_engine* eng, const double* d_density, hf_autotune_report* report, void* stream);
+
+/* Applies a schedule chosen earlier (hf_engine_fock_schedule of a tuned engine
+ * over the same molecule, e.g. kept in a file) without timing anything: per class
+ * pair the grid caps (1..64 blocks per SM) of the FP64 and FP32 launches and the
+ * branch (0..7, taken modulo the branch count); a NULL array restores that
+ * default.  num_class_pairs must equal the engine's. */
+int hf_engine_set_fock_grid_caps(hf_engine* eng, int num_class_pairs, const int* cap_fp64, const int* cap_fp32,
+                                 const int* branch);
 
 /* The schedule in force: per class pair (engine order, *num_class_pairs of them,
  * arrays filled up to max_class_pairs, each may be NULL) the grid caps in blocks

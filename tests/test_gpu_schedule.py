@@ -96,7 +96,7 @@ def test_autotune_then_scf(built_library, cuda):
 
     rep = eng.autotune(D)
     assert rep["build_ms_default"] > 0 and rep["build_ms_tuned"] > 0
-    assert rep["num_branches"] in (1, 2, 4)
+    assert rep["num_branches"] in (1, 2, 4, 8)
     k = len(rep["cap_fp64"])
     assert 0 < rep["num_class_pairs"] <= k
     assert all(c in (2, 4, 8, 16, 32) for c in rep["cap_fp64"] + rep["cap_fp32"])
@@ -115,3 +115,54 @@ def test_autotune_then_scf(built_library, cuda):
         assert abs(r_mixed["total_energy"] - e_mixed) < 1e-8
         assert abs(r_fp64["total_energy"] - e_fp64) < 1e-8
     eng.close()
+
+
+def test_grid_caps_transfer_and_gradient_branches(built_library, cuda):
+    torch = cuda
+    mol, eng, D, H = _setup(torch, seed=7)
+    nel = mol.num_electrons
+    r = eng.rhf_scf(nel, {"convergence_threshold": 1e-10}, want_matrices=True)
+    W = eng.energy_weighted_density(r["coefficients"], r["orbital_energies"], nel // 2)
+    g_ref, _ = eng.gradient(r["density"], W)
+    F_ref = eng.fock_direct(D, H).clone()
+    tune = eng.autotune(r["density"])
+
+    # another engine over the same molecule takes the tuned schedule without timing
+    eng2 = gg.Engine(mol, 1e-12)
+    eng2.set_fock_schedule(tune["num_branches"], use_graph=True, grid_caps=tune)
+    assert eng2.fock_schedule() == {k: tune[k] for k in ("cap_fp64", "cap_fp32", "branch")}
+    for _ in range(3):
+        F2 = eng2.fock_direct(D, H)
+        torch.cuda.synchronize()
+        assert _maxdiff(F2, F_ref) < 1e-11
+    eng2.close()
+
+    # the gradient's class launches on the branches of the schedule
+    for nb in (tune["num_branches"], 4):
+        eng.set_fock_schedule(nb)
+        g, _ = eng.gradient(r["density"], W)
+        assert np.abs(g - g_ref).max() < 1e-10
+
+    eng.set_fock_schedule(1, grid_caps="default")
+    assert set(eng.fock_schedule()["cap_fp64"]) == {16} and set(eng.fock_schedule()["cap_fp32"]) == {16}
+    with pytest.raises(gg.HFError):  # a schedule of another class-pair count
+        eng.set_fock_schedule(1, grid_caps={"cap_fp64": [16], "cap_fp32": [16], "branch": [0]})
+    with pytest.raises(gg.HFError):  # caps outside 1..64
+        k = len(tune["cap_fp64"])
+        eng.set_fock_schedule(1, grid_caps={"cap_fp64": [0] * k, "cap_fp32": [16] * k, "branch": [0] * k})
+    eng.close()
+
+
+def test_batch_schedule_matches_default(built_library, cuda):
+    clusters = geometry.water_cluster_set(6, nmax=3, seed=2)
+    b = gg.Batch([gg.Molecular(c, gg.basis_path("6-31g")) for c in clusters])
+    opts = {"convergence_threshold": 1e-10}
+    ref, _, _ = b.rhf_scf(opts)
+    tune = b.autotune()
+    assert tune["num_branches"] in (1, 2, 4, 8)
+    b.set_fock_schedule(max(2, tune["num_branches"]), grid_caps=tune)
+    res, _, _ = b.rhf_scf(opts)
+    assert all(r["converged"] for r in res)
+    for a, c in zip(ref, res):
+        assert abs(a["total_energy"] - c["total_energy"]) < 1e-8
+    b.close()
