@@ -298,7 +298,7 @@ def run_ours(args, rank, world):
     schedule = {"headline": args.schedule, **sched_ms,
                 "delta_E_tuned_vs_default": max(abs(a["total_energy"] - b["total_energy"])
                                                 for a, b in zip(mixed + fp64, alt_mixed + alt_fp64)),
-                "autotune": tune}
+                "autotune": tune, "graphs": eng_t.graph_stats()}
     it_mx = sum(r["iterations"] for r in mixed)
     it_64 = sum(r["iterations"] for r in fp64)
     ms_mx = sum(r["scf_ms_total"] for r in mixed) / max(it_mx, 1)

@@ -195,6 +195,13 @@ class _FockScheduleMixin:
         out.update(self.fock_schedule())
         return out
 
+    def graph_stats(self) -> dict:
+        """Graphs captured under use_graph (Fock builds, RHF purifications) and replays so far."""
+        nf, npur, rep = C.c_int(), C.c_int(), C.c_longlong()
+        check(lib().hf_engine_graph_stats(self._h, C.byref(nf), C.byref(npur), C.byref(rep)),
+              "hf_engine_graph_stats")
+        return {"fock_graphs": nf.value, "purification_graphs": npur.value, "replays": rep.value}
+
     def fock_schedule(self) -> dict:
         n = C.c_int()
         check(lib().hf_engine_fock_schedule(self._h, 0, C.byref(n), None, None, None), "hf_engine_fock_schedule")

@@ -139,6 +139,7 @@ SIGNATURES = {
     "hf_engine_set_fock_schedule": (_I, [_P, _I, _I]),
     "hf_engine_set_fock_grid_caps": (_I, [_P, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "hf_engine_autotune": (_I, [_P, _P, C.POINTER(AutotuneReport), _P]),
+    "hf_engine_graph_stats": (_I, [_P, C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_longlong)]),
     "hf_engine_fock_schedule": (_I, [_P, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "hf_compute_diis_error": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_diis": (_I, [_P, _P, _P, _P, _I, _P]),

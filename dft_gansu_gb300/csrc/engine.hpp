@@ -114,7 +114,21 @@ struct FockSchedule {
         long long launches;    // kernels in the graph
     };
     std::vector<Graph> graphs;
+    // the RHF loop's purification (scf.cu), captured and replayed the same way
+    struct PurifyGraph {
+        const double* F;
+        double* D;
+        int nocc;
+        int uses;
+        bool failed;           // the capture failed: this purification runs as ordinary launches
+        cudaGraphExec_t exec;
+        long long launches;
+    };
+    std::vector<PurifyGraph> purify;
+    void* cublas_ws = nullptr;     // cuBLAS workspace while capturing (cuBLAS's own pool may allocate)
+    long long graph_replays = 0;   // builds and purifications replayed from graphs
 };
+constexpr size_t kCublasCaptureWorkspace = size_t(16) << 20;
 
 struct Engine {
     int num_basis = 0, num_shells = 0, num_atoms = 0, num_prims = 0;

@@ -513,6 +513,9 @@ void clear_graphs(FockSchedule& S)
 {
     for (auto& g : S.graphs) destroy_graph(g);
     S.graphs.clear();
+    for (auto& g : S.purify)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    S.purify.clear();
 }
 
 }  // namespace
@@ -528,8 +531,10 @@ void schedule_release(FockSchedule& S)
     }
     if (S.fork) cudaEventDestroy(S.fork);
     if (S.capture) cudaStreamDestroy(S.capture);
+    if (S.cublas_ws) cudaFree(S.cublas_ws);
     S.fork = nullptr;
     S.capture = nullptr;
+    S.cublas_ws = nullptr;
 }
 
 // One direct J/K build.  With the schedule's use_graph (single-molecule engines),
@@ -586,6 +591,7 @@ int build_jk(Engine& e, const double* d_D, double* d_J, double* d_K, int precisi
     }
     GB_CUDA_TRY(cudaGraphLaunch(g->exec, s));
     count_launches(g->launches);
+    ++S.graph_replays;
     e.last_mixed = g->mixed;
     return HF_OK;
 }
@@ -835,6 +841,20 @@ int hf_engine_autotune(hf_engine* eng, const double* d_density, hf_autotune_repo
     clear_error();
     if (!eng || !d_density) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
     return autotune_schedule(*reinterpret_cast<Engine*>(eng), d_density, report, static_cast<cudaStream_t>(stream));
+}
+
+int hf_engine_graph_stats(const hf_engine* eng, int* fock_graphs, int* purification_graphs, long long* replays)
+{
+    clear_error();
+    if (!eng) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    const FockSchedule& S = reinterpret_cast<const Engine*>(eng)->sched;
+    int nf = 0, np = 0;
+    for (const auto& g : S.graphs) nf += g.exec ? 1 : 0;
+    for (const auto& g : S.purify) np += g.exec ? 1 : 0;
+    if (fock_graphs) *fock_graphs = nf;
+    if (purification_graphs) *purification_graphs = np;
+    if (replays) *replays = S.graph_replays;
+    return HF_OK;
 }
 
 int hf_engine_fock_schedule(const hf_engine* eng, int max_class_pairs, int* num_class_pairs, int* cap_fp64,

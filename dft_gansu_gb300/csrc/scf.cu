@@ -609,6 +609,71 @@ int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t
     return HF_OK;
 }
 
+// purify_density under the engine's graph schedule (single-molecule engines): the
+// first call with a given (F, D, nocc) runs as ordinary launches (it also makes the
+// lazy allocations), the second is captured on the schedule's capture stream and
+// every call from then on replays the graph on s.  cuBLAS runs on the capture
+// stream with an engine-owned workspace during the capture (cublasSetStream resets
+// cuBLAS to its own workspace pool, which may allocate, and a capture must not).
+// If the capture fails, that purification keeps running as ordinary launches.
+int purify_density_scheduled(Engine& e, const double* F, int nocc, double* D, cudaStream_t s)
+{
+    FockSchedule& S = e.sched;
+    if (!S.use_graph || e.nmol != 1) return purify_density(e, F, nocc, D, s);
+    FockSchedule::PurifyGraph* g = nullptr;
+    for (auto& x : S.purify)
+        if (x.F == F && x.D == D && x.nocc == nocc) {
+            g = &x;
+            break;
+        }
+    if (!g) {
+        if (static_cast<int>(S.purify.size()) >= kMaxFockGraphs) {
+            if (S.purify.front().exec) cudaGraphExecDestroy(S.purify.front().exec);
+            S.purify.erase(S.purify.begin());
+        }
+        S.purify.push_back(FockSchedule::PurifyGraph{F, D, nocc, 0, false, nullptr, 0});
+        g = &S.purify.back();
+    }
+    if (g->failed || (!g->exec && g->uses++ == 0)) return purify_density(e, F, nocc, D, s);
+    if (!g->exec) {
+        int st = schedule_streams(e);
+        if (st) return st;
+        if (!S.cublas_ws) GB_CUDA_TRY(cudaMalloc(&S.cublas_ws, kCublasCaptureWorkspace));
+        if (cublasSetStream(e.cublas, S.capture) != CUBLAS_STATUS_SUCCESS ||
+            cublasSetWorkspace(e.cublas, S.cublas_ws, kCublasCaptureWorkspace) != CUBLAS_STATUS_SUCCESS) {
+            cublasSetStream(e.cublas, s);
+            g->failed = true;
+            return purify_density(e, F, nocc, D, s);
+        }
+        const long long l0 = launch_count();
+        cudaGraph_t graph = nullptr;
+        cudaError_t ce = cudaStreamBeginCapture(S.capture, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+            st = purify_density(e, F, nocc, D, S.capture);
+            ce = cudaStreamEndCapture(S.capture, &graph);
+        }
+        cublasSetStream(e.cublas, s);
+        const long long recorded = launch_count() - l0;
+        count_launches(-recorded);  // recorded, not launched
+        cudaGraphExec_t exec = nullptr;
+        if (!st && ce == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+            g->exec = exec;
+            g->launches = recorded;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        if (!g->exec) {
+            cudaGetLastError();  // capture errors are not sticky; clear the last-error slot
+            g->failed = true;
+            clear_error();
+            return purify_density(e, F, nocc, D, s);
+        }
+    }
+    GB_CUDA_TRY(cudaGraphLaunch(g->exec, s));
+    count_launches(g->launches);
+    ++S.graph_replays;
+    return HF_OK;
+}
+
 // Occupied orbitals without an eigensolver, for the RI K build under purification:
 // after purify_density, w.W holds the projector P on the occupied space in the
 // orthonormal basis.  Q = orth(P Q_prev) by CholeskyQR2 (M = Y^T Y = U^T U, Y U^{-1},
@@ -1043,7 +1108,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     auto density_from = [&](const double* Fm) -> int {
         int r;
         if (purify) {
-            if ((r = purify_density(e, Fm, nocc, w.D, s))) return r;
+            if ((r = purify_density_scheduled(e, Fm, nocc, w.D, s))) return r;
             if (!use_ri) return HF_OK;
             r = occupied_from_projector(e, Fm, nocc, !occ_seeded, s);
             occ_seeded = true;

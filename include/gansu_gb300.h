@@ -152,7 +152,8 @@ int hf_compute_jk_direct(hf_engine* eng, const double* d_density, double* d_J, d
  * launches run on that many streams forked from and joined back into the
  * caller's stream (1, the default: all on the caller's stream).  use_graph != 0:
  * each distinct build (same density and output pointers, precision and cuts) is
- * captured into a CUDA graph on its second call and replayed from then on; the
+ * captured into a CUDA graph on its second call and replayed from then on (so is
+ * the RHF loop's purification density, HF_EIGEN_PURIFICATION); the
  * graph reads the buffers at replay, so their contents may change between calls,
  * not their addresses.  Batch engines use the branches, not the graphs. */
 int hf_engine_set_fock_schedule(hf_engine* eng, int num_branches, int use_graph);
@@ -181,6 +182,10 @@ int hf_engine_autotune(hf_engine* eng, const double* d_density, hf_autotune_repo
  * default.  num_class_pairs must equal the engine's. */
 int hf_engine_set_fock_grid_caps(hf_engine* eng, int num_class_pairs, const int* cap_fp64, const int* cap_fp32,
                                  const int* branch);
+
+/* Graphs of the schedule (use_graph): Fock builds and RHF purifications captured
+ * so far, and how many builds and purifications were replayed from them. */
+int hf_engine_graph_stats(const hf_engine* eng, int* fock_graphs, int* purification_graphs, long long* replays);
 
 /* The schedule in force: per class pair (engine order, *num_class_pairs of them,
  * arrays filled up to max_class_pairs, each may be NULL) the grid caps in blocks

@@ -166,3 +166,25 @@ def test_batch_schedule_matches_default(built_library, cuda):
     for a, c in zip(ref, res):
         assert abs(a["total_energy"] - c["total_energy"]) < 1e-8
     b.close()
+
+
+def test_purification_replayed_from_graph(built_library, cuda):
+    """The RHF loop's purification density (HF_EIGEN_PURIFICATION) under the graph
+    schedule: captured once, replayed every later iteration, same energies."""
+    torch = cuda
+    mol, eng, D, H = _setup(torch, seed=11)
+    nel = mol.num_electrons
+    opts = {"convergence_threshold": 1e-10, "eigensolver": gg.HF_EIGEN_PURIFICATION}
+    mixed = dict(opts, precision=gg.HF_PRECISION_MIXED, mixed_threshold=0.1, incremental=1, rebuild_every=0,
+                 full_build_precision=gg.HF_PRECISION_FP64, anchor_threshold=1e-2)
+    ref = [eng.rhf_scf(nel, o) for o in (opts, mixed)]
+    assert eng.graph_stats() == {"fock_graphs": 0, "purification_graphs": 0, "replays": 0}
+    eng.set_fock_schedule(2, use_graph=True)
+    for _ in range(2):
+        got = [eng.rhf_scf(nel, o) for o in (opts, mixed)]
+        for a, b in zip(ref, got):
+            assert b["converged"] and abs(a["total_energy"] - b["total_energy"]) < 1e-8
+    st = eng.graph_stats()
+    assert st["purification_graphs"] >= 1 and st["fock_graphs"] >= 1
+    assert st["replays"] > 2 * ref[0]["iterations"]
+    eng.close()
