@@ -14,7 +14,7 @@ import numpy as np
 
 from ._capi import (HF_CONV_DAMPING, HF_CONV_DIIS, HF_CONV_OPTIMAL_DAMPING, HF_EIGEN_PURIFICATION, HF_EIGEN_SYEVD, HF_GUESS_CORE, HF_GUESS_DENSITY, HF_GUESS_GWH,
                     HF_GUESS_SAD, HF_ERR_NOT_CONVERGED,
-                    HF_ERI_DIRECT, HF_ERI_RI, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
+                    HF_ERI_DIRECT, HF_ERI_RI, HF_ERI_STORED, HF_PRECISION_FP64, HF_PRECISION_MIXED, Atom, HFError, PrimitiveShell, ScfOptions, ScfResult,
                     check, lib)
 
 BASIS_DIR = Path(__file__).resolve().parent / "basis"
@@ -22,7 +22,7 @@ ANGSTROM_TO_BOHR = 1.8897259886
 
 __all__ = [
     "Molecular", "Engine", "ParameterManager", "HFBuilder", "RHF", "HFError", "BASIS_DIR",
-    "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "basis_path",
+    "HF_PRECISION_FP64", "HF_PRECISION_MIXED", "HF_ERI_DIRECT", "HF_ERI_RI", "HF_ERI_STORED", "basis_path",
     "optimize_geometry", "energy_and_gradient_at", "Batch", "UHF", "HF_EIGEN_PURIFICATION", "HF_EIGEN_SYEVD",
     "HF_GUESS_CORE", "HF_GUESS_GWH", "HF_GUESS_DENSITY", "HF_GUESS_SAD", "HF_CONV_DIIS", "HF_CONV_DAMPING",
     "HF_CONV_OPTIMAL_DAMPING", "ROHF", "ROHF_COUPLINGS",
@@ -601,6 +601,8 @@ class _HFBase:
     and ROHF mirrors: parameter checks, the engine (and the auxiliary basis for
     eri_method ri, src/rhf.cu:76-79), the SCF options and the guess densities."""
 
+    _stored_tensor = False  # eri_method stored keeps an N^4 tensor (RHF)
+
     def __init__(self, molecular: Molecular, parameters: ParameterManager):
         self.mol = molecular
         self.params = parameters
@@ -615,7 +617,11 @@ class _HFBase:
                 not getattr(molecular, "gbs_filename", ""):
             raise ValueError("The basis set file is not specified for SAD initial guess method.")
         self.engine = Engine(molecular, parameters.get("schwarz_screening_threshold", float))
-        self.eri_method = HF_ERI_RI if method == "ri" else HF_ERI_DIRECT
+        # stored: the conventional RHF build from the N^4 tensor (ERI_Stored_RHF), FP64; the
+        # UHF and ROHF mirrors and the mixed tier build the same Fock matrices directly
+        stored = self._stored_tensor and parameters["precision"] != "mixed"
+        self.eri_method = {"ri": HF_ERI_RI, "direct": HF_ERI_DIRECT}.get(
+            method, HF_ERI_STORED if stored else HF_ERI_DIRECT)
         if method == "ri":
             atoms = [(a.atomic_number, a.x, a.y, a.z) for a in molecular._atoms]
             self.auxiliary = Molecular(atoms, parameters["auxiliary_gbsfilename"])
@@ -693,9 +699,13 @@ class _HFBase:
 
 class RHF(_HFBase):
     """Mirror of gansu::RHF (include/rhf.hpp, src/rhf.cu): ``solve()`` runs the
-    SCF on the GPU.  ``stored`` and ``direct`` both run the fused direct build
-    (no N^4 tensor); ``ri`` uses Molecular(atoms, auxiliary_gbsfilename).
+    SCF on the GPU.  ``stored`` (the default) computes the N^4 ERI tensor once
+    and builds F from it every iteration (ERI_Stored_RHF; FP64), ``direct`` runs
+    the fused direct build (no tensor), ``ri`` uses Molecular(atoms,
+    auxiliary_gbsfilename).
     Guesses core / gwh / density / sad (include/rhf.hpp:378-588)."""
+
+    _stored_tensor = True
 
     def __init__(self, molecular: Molecular, parameters: ParameterManager):
         if molecular.num_alpha_spins != molecular.num_beta_spins:

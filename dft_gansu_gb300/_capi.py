@@ -24,6 +24,7 @@ HF_PRECISION_FP64 = 0
 HF_PRECISION_MIXED = 1
 HF_ERI_DIRECT = 0
 HF_ERI_RI = 1
+HF_ERI_STORED = 2
 HF_GUESS_CORE = 0
 HF_GUESS_GWH = 1
 HF_GUESS_DENSITY = 2

@@ -190,6 +190,7 @@ struct Engine {
     long long* d_goff32 = nullptr;
     int2* d_shell_info = nullptr;   // per shell: first basis function, number of components
     float* d_block_dmax = nullptr;  // per shell block max |D| of the density being built (mixed plan)
+    double* d_eri = nullptr;     // stored N^4 ERI tensor of eri_method = stored (allocated on first use)
     double* d_scalar = nullptr;  // small scratch scalars (8 doubles)
     unsigned long long* d_counters = nullptr;  // [class pair][precision][prim, contracted]
     long long bytes_h2d = 0;                   // bytes uploaded by engine creation
@@ -245,6 +246,10 @@ int mol_absmax(Engine& e, const double* d_A, double* d_out, cudaStream_t s);
 // batch build with per-molecule FP32 cuts and drop thresholds (fock.cu)
 int build_jk_batch(Engine& e, const double* d_D, const double* d_mol_tau, const double* d_mol_skip,
                    double* d_mol_dmax, cudaStream_t s);
+// the full ERI tensor ((i*N+j)*N+k)*N+l of a single-molecule engine (fock.cu)
+int compute_eri_tensor(Engine& e, double* d_eri, cudaStream_t s);
+// F = H + sum_kl D_kl [(ij|kl) - 1/2 (ik|jl)] from a stored tensor (fock.cu)
+int stored_fock(const double* d_D, const double* d_H, const double* d_eri, double* d_F, int n, cudaStream_t s);
 // releases the schedule's streams, events and graphs (fock.cu)
 void schedule_release(FockSchedule& S);
 // creates the schedule's branch streams and events on first use (fock.cu)

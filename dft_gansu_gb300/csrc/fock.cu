@@ -769,6 +769,35 @@ __global__ void stored_fock_kernel(const double* __restrict__ D, const double* _
 }
 
 }  // namespace
+
+int compute_eri_tensor(Engine& e, double* d_eri, cudaStream_t s)
+{
+    if (e.nmol != 1) return set_error("the stored ERI tensor is for single-molecule engines"), HF_ERR_INVALID_ARGUMENT;
+    const size_t n = e.num_basis;
+    GB_CUDA_TRY(cudaMemsetAsync(d_eri, 0, n * n * n * n * sizeof(double), s));
+    for (int c = 0; c < static_cast<int>(e.class_pairs.size()); ++c) {
+        const ClassPair& cp = e.class_pairs[c];
+        if (cp.n_survivors == 0) continue;
+        const PairClass& X = e.pair_classes[cp.X];
+        const PairClass& Y = e.pair_classes[cp.Y];
+        EriLauncher f = eri_launcher(X.la, X.lb, Y.la, Y.lb);
+        if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
+        f(make_launch(e, c, false, e.d_off_static, e.d_entry_lo0), e.d_scale, d_eri, grid_for(cp.n_survivors, e.num_sms),
+          s);
+        GB_LAUNCH_CHECK();
+    }
+    return HF_OK;
+}
+
+int stored_fock(const double* d_D, const double* d_H, const double* d_eri, double* d_F, int n, cudaStream_t s)
+{
+    const long long warps = static_cast<long long>(n) * n;
+    const long long blocks = (warps * 32 + 255) / 256;
+    stored_fock_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(d_D, d_H, d_eri, d_F, n);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -879,23 +908,7 @@ int hf_compute_eri_matrix(hf_engine* eng, double* d_eri, void* stream)
 {
     clear_error();
     if (!eng || !d_eri) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
-    Engine& e = *reinterpret_cast<Engine*>(eng);
-    if (e.nmol != 1) return set_error("hf_compute_eri_matrix: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
-    const cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const size_t n = e.num_basis;
-    GB_CUDA_TRY(cudaMemsetAsync(d_eri, 0, n * n * n * n * sizeof(double), s));
-    for (int c = 0; c < static_cast<int>(e.class_pairs.size()); ++c) {
-        const ClassPair& cp = e.class_pairs[c];
-        if (cp.n_survivors == 0) continue;
-        const PairClass& X = e.pair_classes[cp.X];
-        const PairClass& Y = e.pair_classes[cp.Y];
-        EriLauncher f = eri_launcher(X.la, X.lb, Y.la, Y.lb);
-        if (!f) return set_error("no kernel for quartet class"), HF_ERR_INVALID_ARGUMENT;
-        f(make_launch(e, c, false, e.d_off_static, e.d_entry_lo0), e.d_scale, d_eri, grid_for(cp.n_survivors, e.num_sms),
-          s);
-        GB_LAUNCH_CHECK();
-    }
-    return HF_OK;
+    return compute_eri_tensor(*reinterpret_cast<Engine*>(eng), d_eri, static_cast<cudaStream_t>(stream));
 }
 
 int hf_compute_fock_stored_rhf(const double* d_density, const double* d_core_hamiltonian, const double* d_eri,
@@ -904,12 +917,7 @@ int hf_compute_fock_stored_rhf(const double* d_density, const double* d_core_ham
     clear_error();
     if (!d_density || !d_core_hamiltonian || !d_eri || !d_fock || num_basis <= 0)
         return set_error("null argument or bad size"), HF_ERR_INVALID_ARGUMENT;
-    const long long warps = static_cast<long long>(num_basis) * num_basis;
-    const long long blocks = (warps * 32 + 255) / 256;
-    stored_fock_kernel<<<static_cast<unsigned>(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        d_density, d_core_hamiltonian, d_eri, d_fock, num_basis);
-    GB_LAUNCH_CHECK();
-    return HF_OK;
+    return stored_fock(d_density, d_core_hamiltonian, d_eri, d_fock, num_basis, static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

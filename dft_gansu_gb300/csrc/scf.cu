@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <limits>
+#include <string>
 #include <vector>
 
 #include "engine.hpp"
@@ -952,8 +953,11 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         return set_error("diis_size must be in [1, 16]"), HF_ERR_INVALID_ARGUMENT;
     if (opt.precision != HF_PRECISION_FP64 && opt.precision != HF_PRECISION_MIXED)
         return set_error("unknown precision"), HF_ERR_INVALID_ARGUMENT;
-    if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI)
+    if (opt.eri_method != HF_ERI_DIRECT && opt.eri_method != HF_ERI_RI && opt.eri_method != HF_ERI_STORED)
         return set_error("unknown eri_method"), HF_ERR_INVALID_ARGUMENT;
+    if (opt.eri_method == HF_ERI_STORED && opt.precision != HF_PRECISION_FP64)
+        return set_error("eri_method stored is FP64 (the mixed tier belongs to the direct and RI builds)"),
+               HF_ERR_INVALID_ARGUMENT;
     if (!valid_guess(opt.initial_guess))
         return set_error("initial_guess: core, GWH, density or SAD"), HF_ERR_INVALID_ARGUMENT;
     const bool density_guess = opt.initial_guess == HF_GUESS_DENSITY || opt.initial_guess == HF_GUESS_SAD;
@@ -963,6 +967,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
                                  HF_ERR_INVALID_ARGUMENT;
     Damper damper;
     const bool use_ri = opt.eri_method == HF_ERI_RI;
+    const bool use_stored = opt.eri_method == HF_ERI_STORED;
     if (use_ri && !e.ri)
         return set_error("eri_method RI needs an auxiliary basis (hf_engine_set_auxiliary_basis)"),
                HF_ERR_INVALID_ARGUMENT;
@@ -1002,6 +1007,14 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     // one Fock build: F = H + G(D), full or incremental
     auto fock_build = [&](bool first) -> int {
         cudaEventRecord(f0, s);
+        if (use_stored) {
+            // ERI_Stored_RHF::compute_fock_matrix (src/eri.cu): F from the stored tensor
+            int r = stored_fock(w.D, w.H, e.d_eri, w.F, n, s);
+            if (r) return r;
+            cudaEventRecord(f1, s);
+            ++fock_builds;
+            return HF_OK;
+        }
         if (use_ri) {
             // J (FP64) from the packed B and D.  K: FP64 from the occupied orbitals
             // (D = 2 C_occ C_occ^T); under the mixed tier, split-BF16 tensor-core builds
@@ -1097,6 +1110,18 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     const auto t_setup = std::chrono::steady_clock::now();
     // core Hamiltonian, X, core guess (and the RI B tensor)
     if (use_ri && (st = ri_require_b(e, s))) return st;
+    if (use_stored && !e.d_eri) {
+        // the tensor stays with the engine (ERI_Stored_RHF::precomputation, src/eri.cu)
+        const size_t bytes = static_cast<size_t>(nn) * static_cast<size_t>(nn) * sizeof(double);
+        if (cudaMalloc(&e.d_eri, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            e.d_eri = nullptr;
+            return set_error("eri_method stored: the N^4 ERI tensor (" + std::to_string(bytes >> 20) +
+                             " MiB) does not fit in device memory; use eri_method direct"),
+                   HF_ERR_OUT_OF_MEMORY;
+        }
+        if ((st = compute_eri_tensor(e, e.d_eri, s))) return st;
+    }
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
     if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
     if ((st = orthogonalizer(e, opt, s))) return st;

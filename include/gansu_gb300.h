@@ -275,7 +275,8 @@ typedef struct {
     int full_build_precision;       /* precision of full (non-incremental) builds under the mixed tier */
     int eigensolver;                /* HF_EIGEN_SYEVD, HF_EIGEN_SYEVJ or HF_EIGEN_PURIFICATION */
     int verbose;                    /* print per-iteration lines like the reference */
-    int eri_method;                 /* HF_ERI_DIRECT or HF_ERI_RI (eri_method = direct / ri, src/rhf.cu:72-88) */
+    int eri_method;                 /* HF_ERI_DIRECT, HF_ERI_RI or HF_ERI_STORED (eri_method = direct / ri / stored,
+                                       src/rhf.cu:72-88) */
     double anchor_threshold;        /* mixed tier: low-precision full builds (direct: all quartets FP32; RI:
                                        split-BF16 K) while max|dD| >= this, then one FP64 build, then
                                        incremental builds; 0 = the first build is the FP64 one */
@@ -336,7 +337,9 @@ enum {
 /* Two-electron backend of the SCF. */
 enum {
     HF_ERI_DIRECT = 0,  /* fused direct J/K build every iteration */
-    HF_ERI_RI = 1       /* density fitting; needs hf_engine_set_auxiliary_basis */
+    HF_ERI_RI = 1,      /* density fitting; needs hf_engine_set_auxiliary_basis */
+    HF_ERI_STORED = 2   /* RHF only: the N^4 tensor computed once and kept with the engine, F from it
+                           every iteration (ERI_Stored_RHF, the reference's default eri_method); FP64 */
 };
 
 typedef struct {
