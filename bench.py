@@ -137,7 +137,8 @@ def dist_init(n_gpus):
     if world > 1:
         import torch.distributed as dist
         import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, world
 
@@ -147,7 +148,7 @@ def dist_max(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
