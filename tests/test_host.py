@@ -116,6 +116,27 @@ def test_parameter_manager_rules(tmp_path):
     assert pm.get("diis_size", int) == 6 and pm["convergence_method"] == "diis"
 
 
+def test_reference_recipes_parse():
+    """Every recipe of the reference's parameter_recipe/ (RHF, UHF, ROHF with DIIS,
+    damping and optimal damping, the evaluation recipe) loads into the mirror with
+    the reference's values, so HF_main recipes run unchanged."""
+    from oracle import oracle as O
+    recipes = sorted((O.REFERENCE_ROOT / "parameter_recipe").glob("*.txt"))
+    if not recipes:
+        pytest.skip("reference tree not mounted")
+    for f in recipes:
+        pm = gg.ParameterManager()
+        pm.load_from_file(f)
+        assert pm["method"] == f.name.split("_")[0].lower()
+        assert pm["convergence_method"] in ("diis", "damping", "optimaldamping")
+        assert pm.get("diis_include_transform", bool) is False
+        assert 0.0 < pm.get("damping_factor", float) <= 1.0
+        assert 0.0 < pm.get("convergence_energy_threshold", float) <= 1e-6
+    ev = gg.ParameterManager()
+    ev.load_from_file(O.REFERENCE_ROOT / "parameter_recipe" / "RHF_eval.txt")
+    assert ev["initial_guess"] == "sad" and ev.get("schwarz_screening_threshold", float) == 1e-13
+
+
 def test_geometries():
     dec = geometry.alkane(10, jitter=0.0)
     x = np.array([a[1:] for a in dec]) / geometry.ANGSTROM_TO_BOHR
