@@ -351,6 +351,12 @@ def spherical_orthogonalizer(S, T, tol=1e-6):
     return X
 
 
+def damp(old, new, a):
+    """damping (src/gpu_manager.cu:989, the update behind Convergence_RHF_Damping):
+    (1 - a) old + a new."""
+    return (1.0 - a) * old + a * new
+
+
 def damping_factor(F, Fp, D, Dp):
     """computeOptimalDampingFactor_RHF (src/gpu_manager.cu:898-963): s = Tr[F_old dD],
     c = Tr[(F - F_old) dD]; 1 if c <= -s/2, else -s/(2c)."""
@@ -400,9 +406,9 @@ def rhf(S, H, fock, nocc, enuc, maxiter=100, thr=1e-6, diis_size=8, include_tran
             else:
                 Fp, Dp = damp_prev
                 a = damping_factor(F, Fp, D, Dp) if convergence == "optimaldamping" else damping
-                F = (1.0 - a) * Fp + a * F
+                F = damp(Fp, F, a)
                 if convergence == "optimaldamping":
-                    D = (1.0 - a) * Dp + a * D
+                    D = damp(Dp, D, a)
                     damp_prev = (F.copy(), D.copy())
                 else:
                     damp_prev = (F.copy(), Dp)

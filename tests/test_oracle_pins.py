@@ -110,6 +110,20 @@ def test_reference_linear_algebra_known_answers():
     np.testing.assert_allclose(np.abs(X), [[0.0, 0.5], [0.0, 0.0]], atol=1e-15)
 
 
+def test_reference_damping_known_answers():
+    # test/test_gpu_manager.cu:405-455: damping with alpha = 0.1, tol 1e-6
+    old = np.arange(1.0, 10.0).reshape(3, 3)
+    new = np.arange(9.0, 0.0, -1.0).reshape(3, 3)
+    np.testing.assert_allclose(O.damp(old, new, 0.1), [[1.8, 2.6, 3.4], [4.2, 5.0, 5.8], [6.6, 7.4, 8.2]],
+                               atol=1e-6)
+    # test/test_gpu_manager.cu:464-511: computeOptimalDampingFactor_RHF = 0.613207547, tol 1e-6
+    F = np.array([[2.0, 2.0, 1.0], [2.0, 3.0, 1.0], [1.0, 1.0, 2.0]])
+    Fp = np.array([[1.0, 2.0, 3.0], [4.0, 6.0, 6.0], [7.0, 8.0, 10.0]])
+    D = np.full((3, 3), 3.0)
+    Dp = np.array([[2.0, 4.0, 6.0], [4.0, 1.0, 1.0], [6.0, 1.0, 10.0]])
+    assert abs(O.damping_factor(F, Fp, D, Dp) - 0.613207547) < 1e-6
+
+
 def test_diis_bordered_solve_is_affine():
     rng = np.random.default_rng(0)
     errs = [rng.normal(size=(5, 5)) for _ in range(4)]
