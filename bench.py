@@ -463,7 +463,10 @@ def run_ours(args, rank, world):
             "gradient": grad,
             "diis": diis,
             "e2e": {"value": statistics.mean(e2e_vals), "unit": "ms/iter", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h,
+                    "path": "host atoms -> Molecular -> Engine (H2D copies) -> rhf_scf -> host energy, per iteration"
+                            + ("; the tuned schedule applied from the tuned engine's caps, the autotuner not re-run"
+                               if args.schedule == "tuned" else "")},
             "gpu_launches": l1 - l0,
             "schedule": schedule,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
