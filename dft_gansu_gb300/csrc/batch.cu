@@ -26,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "diis_solve.cuh"
 #include "engine.hpp"
 
 namespace gb {
@@ -268,38 +269,8 @@ __global__ void batch_diis_kernel(const double* __restrict__ Es, const double* _
         __syncthreads();
     }
     if (nprev < 2) return;
-    if (threadIdx.x == 0) {
-        // bordered system [B -1; -1 0] c = [0 .. 0 -1], partial pivoting
-        const int n = nprev + 1;
-        double A[kBatchDiis + 1][kBatchDiis + 2];
-        for (int i = 0; i < n; ++i) {
-            for (int j = 0; j < n; ++j) {
-                if (i < nprev && j < nprev) A[i][j] = B[i * kBatchDiis + j];
-                else if (i == nprev && j == nprev) A[i][j] = 0.0;
-                else A[i][j] = -1.0;
-            }
-            A[i][n] = (i == nprev) ? -1.0 : 0.0;
-        }
-        for (int c = 0; c < n; ++c) {
-            int piv = c;
-            for (int r = c + 1; r < n; ++r)
-                if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
-            if (A[piv][c] == 0.0) continue;
-            if (piv != c)
-                for (int k = 0; k <= n; ++k) { const double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
-            for (int r = c + 1; r < n; ++r) {
-                const double f = A[r][c] / A[c][c];
-                for (int k = c; k <= n; ++k) A[r][k] -= f * A[c][k];
-            }
-        }
-        double x[kBatchDiis + 1];
-        for (int r = n - 1; r >= 0; --r) {
-            double s = A[r][n];
-            for (int k = r + 1; k < n; ++k) s -= A[r][k] * x[k];
-            x[r] = (A[r][r] != 0.0) ? s / A[r][r] : 0.0;
-        }
-        for (int i = 0; i < nprev; ++i) coef[i] = x[i];
-    }
+    // weights of the independent error vectors (diis_solve.cuh)
+    if (threadIdx.x == 0) diis_coefficients<kBatchDiis>(B, kBatchDiis, nprev, coef);
     __syncthreads();
     for (long long k = threadIdx.x; k < nn; k += blockDim.x) {
         double s = 0.0;
@@ -771,9 +742,8 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
                 enuc[m] += static_cast<double>(A.atomic_number) * B.atomic_number / std::sqrt(dx * dx + dy * dy + dz * dz);
             }
 
-    cudaEvent_t l0, l1;
-    cudaEventCreate(&l0);
-    cudaEventCreate(&l1);
+    ScopedEvents<5> evs;
+    cudaEvent_t l0 = evs.ev[0], l1 = evs.ev[1];
     // setup: S, H, X = U s^-1/2, guess (core, GWH, density, SAD as in hf_rhf_scf)
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
     GB_CUDA_TRY(cudaMemcpyAsync(w.Fp, w.S, sizeof(double) * ne, cudaMemcpyDeviceToDevice, s));
@@ -804,10 +774,7 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     const int m = opt.diis_size;
     int iter = 0, diis_iter = 0, ndone = 0;
     cudaEventRecord(l0, s);
-    cudaEvent_t p0, p1, p2;
-    cudaEventCreate(&p0);
-    cudaEventCreate(&p1);
-    cudaEventCreate(&p2);
+    cudaEvent_t p0 = evs.ev[2], p1 = evs.ev[3], p2 = evs.ev[4];
     double diag_ms = 0.0, fock_ms = 0.0;
     while (iter < opt.max_iter) {
         cudaEventRecord(p0, s);
@@ -874,8 +841,6 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     GB_CUDA_TRY(cudaEventSynchronize(l1));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, l0, l1);
-    cudaEventDestroy(l0);
-    cudaEventDestroy(l1);
     if (batch_scf_ms) *batch_scf_ms = ms;
     if (batch_iterations) *batch_iterations = iter;
     for (int k = 0; k < nmol; ++k) {
@@ -890,9 +855,6 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
         r.diag_ms_total = diag_ms;
         r.fock_ms_total = fock_ms;
     }
-    cudaEventDestroy(p0);
-    cudaEventDestroy(p1);
-    cudaEventDestroy(p2);
     return ndone == nmol ? HF_OK : (set_error("batch SCF: not every molecule converged"), HF_ERR_NOT_CONVERGED);
 }
 

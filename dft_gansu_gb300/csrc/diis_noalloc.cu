@@ -13,18 +13,30 @@
 // use the array's name as a device address, so the first call on each device
 // looks the address up once with cudaGetSymbolAddress while that device is
 // current (make that first call before any stream capture), and later calls
-// reuse the cached pointer.
+// reuse the cached pointer.  The cache is keyed on the device's current CUDA
+// context as well: after cudaDeviceReset (a new primary context) the next
+// call looks the address up again, and that call too belongs before any
+// stream capture.
+//
+// Dependent error vectors: the weights come from diis_coefficients
+// (diis_solve.cuh), which leaves out error vectors that are linear
+// combinations of others (two equal vectors count once) and returns the
+// constrained minimiser over the rest; the number left out is written to the
+// status word of the scratch.  The output is therefore always a finite
+// extrapolation, never the zero matrix.
 //
 // Limits and sharing: at most kNoAllocMaxPrev (16) stored error/Fock pairs.
 // All calls share the one scratch array and every call rewrites the parts it
 // reads, so nothing carries over between calls; calls that overlap on the GPU
 // (different streams or threads without ordering) race on the scratch and
 // must be serialised by the caller.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <mutex>
 
+#include "diis_solve.cuh"
 #include "internal.hpp"
 
 namespace gb {
@@ -39,6 +51,7 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 
 std::mutex g_noalloc_mutex;
 double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+CUcontext g_noalloc_ctx[kNoAllocMaxDevices] = {};
 
 // B_ij = <e_i, e_j> for i <= j < m, one block per pair; writes every B entry
 // the solve reads, so the scratch needs no clearing between calls.
@@ -65,42 +78,13 @@ __global__ void noalloc_dots_kernel(const double* __restrict__ Es, int m, long l
     }
 }
 
-// bordered system [B -1; -1 0] c = [0 .. 0 -1] by Gaussian elimination with
-// partial pivoting in FP64 (one thread); coefficients to scratch[kNoAllocB ..]
+// weights of the independent error vectors (diis_solve.cuh) to scratch[kNoAllocB ..];
+// the count of vectors left out as dependent goes to the status word
 __global__ void noalloc_solve_kernel(int m, double* __restrict__ scratch)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int n = m + 1;
-    double A[kNoAllocMaxPrev + 1][kNoAllocMaxPrev + 2];
-    for (int i = 0; i < n; ++i) {
-        for (int j = 0; j < n; ++j) {
-            if (i < m && j < m) A[i][j] = scratch[i * kNoAllocMaxPrev + j];
-            else if (i == m && j == m) A[i][j] = 0.0;
-            else A[i][j] = -1.0;
-        }
-        A[i][n] = (i == m) ? -1.0 : 0.0;
-    }
-    int singular = 0;
-    for (int c = 0; c < n; ++c) {
-        int piv = c;
-        for (int r = c + 1; r < n; ++r)
-            if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
-        if (A[piv][c] == 0.0) { singular = 1; continue; }
-        if (piv != c)
-            for (int k = 0; k <= n; ++k) { const double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
-        for (int r = c + 1; r < n; ++r) {
-            const double f = A[r][c] / A[c][c];
-            for (int k = c; k <= n; ++k) A[r][k] -= f * A[c][k];
-        }
-    }
-    double x[kNoAllocMaxPrev + 1];
-    for (int r = n - 1; r >= 0; --r) {
-        double s = A[r][n];
-        for (int k = r + 1; k < n; ++k) s -= A[r][k] * x[k];
-        x[r] = (A[r][r] != 0.0) ? s / A[r][r] : 0.0;
-    }
-    for (int i = 0; i < m; ++i) scratch[kNoAllocB + i] = x[i];
-    scratch[kNoAllocB + kNoAllocMaxPrev] = singular;
+    const int dropped = diis_coefficients<kNoAllocMaxPrev>(scratch, kNoAllocMaxPrev, m, scratch + kNoAllocB);
+    scratch[kNoAllocB + kNoAllocMaxPrev] = static_cast<double>(dropped);
 }
 
 __global__ void noalloc_combine_kernel(const double* __restrict__ Fs, int m, long long nn,
@@ -114,14 +98,35 @@ __global__ void noalloc_combine_kernel(const double* __restrict__ Fs, int m, lon
     }
 }
 
-// device address of the scratch array for the current device (looked up once)
+// the current CUDA context (cuCtxGetCurrent through the runtime's driver entry point)
+CUcontext current_context()
+{
+    using Fn = CUresult (*)(CUcontext*);
+    static Fn fn = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<Fn>(p);
+        looked = true;
+    }
+    CUcontext c = nullptr;
+    if (fn) fn(&c);
+    return c;
+}
+
+// device address of the scratch array for the current device and context
+// (looked up once per device, again after the device's context changed)
 int noalloc_scratch(double** out)
 {
     int dev = 0;
     GB_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error("device ordinal out of range"), HF_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    const CUcontext ctx = current_context();  // null before the runtime made a context current
+    if (!ctx || !g_noalloc_ptr[dev] || g_noalloc_ctx[dev] != ctx) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) {
@@ -129,6 +134,7 @@ int noalloc_scratch(double** out)
             return HF_ERR_CUDA;
         }
         g_noalloc_ptr[dev] = static_cast<double*>(p);
+        g_noalloc_ctx[dev] = current_context();
     }
     *out = g_noalloc_ptr[dev];
     return HF_OK;

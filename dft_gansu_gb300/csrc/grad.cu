@@ -526,9 +526,8 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
         GB_CUDA_TRY(cudaMemcpy(e.d_shell_atom, sa.data(), sizeof(int) * e.num_shells, cudaMemcpyHostToDevice));
     }
     const bool mixed = precision == HF_PRECISION_MIXED;
-    cudaEvent_t t0, t1;
-    cudaEventCreate(&t0);
-    cudaEventCreate(&t1);
+    ScopedEvents<2> evs;
+    cudaEvent_t t0 = evs.ev[0], t1 = evs.ev[1];
     cudaEventRecord(t0, s);
     GB_CUDA_TRY(cudaMemsetAsync(e.d_grad, 0, sizeof(double) * 3 * natom, s));
     int st = scale_density(e, d_D, mixed, s);
@@ -631,8 +630,6 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, t0, t1);
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
     if (ms_out) *ms_out = ms;
     // nuclear repulsion: d/dR_A sum_{A<B} Z_A Z_B / |R_A - R_B|
     for (int A = 0; A < natom; ++A)

@@ -41,6 +41,24 @@ double cgto_factor(int L, const std::vector<double>& a, const std::vector<double
             return (_e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;                \
         }                                                                                                 \
     } while (0)
+namespace gb {
+// CUDA events released when the scope ends (early error returns included)
+template <int N>
+struct ScopedEvents {
+    cudaEvent_t ev[N] = {};
+    ScopedEvents()
+    {
+        for (auto& x : ev) cudaEventCreate(&x);
+    }
+    ~ScopedEvents()
+    {
+        for (auto x : ev)
+            if (x) cudaEventDestroy(x);
+    }
+    ScopedEvents(const ScopedEvents&) = delete;
+    ScopedEvents& operator=(const ScopedEvents&) = delete;
+};
+}  // namespace gb
 #define GB_LAUNCH_CHECK()                                                                                 \
     do {                                                                                                  \
         gb::count_launch();                                                                               \

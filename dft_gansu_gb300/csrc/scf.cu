@@ -18,6 +18,7 @@
 #include <string>
 #include <vector>
 
+#include "diis_solve.cuh"
 #include "engine.hpp"
 #include "ri.hpp"
 
@@ -26,6 +27,26 @@ namespace gb {
 namespace {
 
 constexpr int kMaxDiis = 16;
+
+// CUDA events and the pinned read-back slot of one SCF call, released on every
+// return path (early error returns included)
+struct LoopResources {
+    cudaEvent_t ev[8] = {};
+    double* h_energy = nullptr;
+    LoopResources()
+    {
+        for (auto& x : ev) cudaEventCreate(&x);
+        cudaMallocHost(&h_energy, 4 * sizeof(double));
+    }
+    ~LoopResources()
+    {
+        for (auto x : ev)
+            if (x) cudaEventDestroy(x);
+        if (h_energy) cudaFreeHost(h_energy);
+    }
+    LoopResources(const LoopResources&) = delete;
+    LoopResources& operator=(const LoopResources&) = delete;
+};
 
 int gemm_rm(cublasHandle_t h, bool ta, bool tb, int n, const double* A, const double* B, double* C,
             double alpha = 1.0, double beta = 0.0)
@@ -179,42 +200,13 @@ __global__ void diis_dots_kernel(const double* __restrict__ Es, int m, long long
     }
 }
 
-// Bordered system [B -1; -1 0] c = [0 .. 0 -1], Gaussian elimination with
-// partial pivoting in FP64 (one thread; m+1 <= 17).  Coefficients to coef[].
+// DIIS weights (diis_solve.cuh: the constrained minimiser on the independent error
+// vectors); *status = how many vectors were left out as dependent on others.
 __global__ void diis_solve_kernel(const double* __restrict__ B, int m, double* __restrict__ coef, int* status)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int n = m + 1;
-    double A[kMaxDiis + 1][kMaxDiis + 2];
-    for (int i = 0; i < n; ++i) {
-        for (int j = 0; j < n; ++j) {
-            if (i < m && j < m) A[i][j] = B[i * kMaxDiis + j];
-            else if (i == m && j == m) A[i][j] = 0.0;
-            else A[i][j] = -1.0;
-        }
-        A[i][n] = (i == m) ? -1.0 : 0.0;
-    }
-    int bad = 0;
-    for (int c = 0; c < n; ++c) {
-        int piv = c;
-        for (int r = c + 1; r < n; ++r)
-            if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
-        if (A[piv][c] == 0.0) { bad = 1; continue; }
-        if (piv != c)
-            for (int k = 0; k <= n; ++k) { const double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
-        for (int r = c + 1; r < n; ++r) {
-            const double f = A[r][c] / A[c][c];
-            for (int k = c; k <= n; ++k) A[r][k] -= f * A[c][k];
-        }
-    }
-    double x[kMaxDiis + 1];
-    for (int r = n - 1; r >= 0; --r) {
-        double s = A[r][n];
-        for (int k = r + 1; k < n; ++k) s -= A[r][k] * x[k];
-        x[r] = (A[r][r] != 0.0) ? s / A[r][r] : 0.0;
-    }
-    for (int i = 0; i < m; ++i) coef[i] = x[i];
-    *status = bad;
+    const int dropped = diis_coefficients<kMaxDiis>(B, kMaxDiis, m, coef);
+    if (dropped) atomicAdd(status, dropped);
 }
 
 __global__ void diis_combine_kernel(const double* __restrict__ Fs, const double* __restrict__ coef, int m, long long nn,
@@ -984,18 +976,12 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     GB_CUDA_TRY(cudaMemsetAsync(e.d_counters, 0, kCounterSlots * sizeof(unsigned long long), s));
     GB_CUDA_TRY(cudaMemsetAsync(w.info, 0, 4 * sizeof(int), s));
 
-    cudaEvent_t f0, f1, c0, c1, q0, q1;
-    cudaEventCreate(&f0);
-    cudaEventCreate(&f1);
-    cudaEventCreate(&c0);
-    cudaEventCreate(&c1);
-    cudaEventCreate(&q0);
-    cudaEventCreate(&q1);
+    LoopResources lr;
+    cudaEvent_t f0 = lr.ev[0], f1 = lr.ev[1], c0 = lr.ev[2], c1 = lr.ev[3], q0 = lr.ev[4], q1 = lr.ev[5];
     double fock_ms = 0.0, diag_ms = 0.0, diis_ms = 0.0;
     bool diis_timed = false;
     int fock_builds = 0;
-    double* h_energy = nullptr;
-    cudaMallocHost(&h_energy, sizeof(double));
+    double* h_energy = lr.h_energy;
 
     // Mixed tier with anchor_threshold > 0: full low-precision builds (direct: every
     // quartet FP32; RI: split-BF16 K) while max|dD| >= anchor_threshold, then one FP64
@@ -1177,9 +1163,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     if (!(density_guess && use_ri && opt.initial_guess == HF_GUESS_DENSITY)) fock_ms += elapsed(f0, f1);
     res->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_setup).count();
 
-    cudaEvent_t l0, l1;
-    cudaEventCreate(&l0);
-    cudaEventCreate(&l1);
+    cudaEvent_t l0 = lr.ev[6], l1 = lr.ev[7];
     cudaEventRecord(l0, s);
     double prev = std::numeric_limits<double>::max(), energy = 0.0;
     int iter = 0, diis_iter = 0;
@@ -1231,8 +1215,6 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         cudaEventElapsedTime(&ms, l0, l1);
         res->scf_ms_total = ms;  // device timeline of the SCF loop (CUDA events on the launching stream)
     }
-    cudaEventDestroy(l0);
-    cudaEventDestroy(l1);
     int info[4] = {0, 0, 0, 0};
     GB_CUDA_TRY(cudaMemcpy(info, w.info, sizeof(info), cudaMemcpyDeviceToHost));
     std::vector<unsigned long long> cnt(kCounterSlots, 0);
@@ -1242,8 +1224,8 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         prim64 += cnt[4 * c + 0];
         prim32 += cnt[4 * c + 2];
     }
-    cudaFreeHost(h_energy);
-    for (cudaEvent_t ev : {f0, f1, c0, c1, q0, q1}) cudaEventDestroy(ev);
+    if (opt.verbose && info[1])
+        std::printf("DIIS: %d error vectors left out of extrapolations as dependent on others\n", info[1]);
     res->diag_ms_total = diag_ms;
     res->diis_ms_total = diis_ms;
     res->electronic_energy = energy;
@@ -1337,8 +1319,8 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     *res = hf_scf_result{};
     res->nuclear_repulsion = nuclear_repulsion(e);
     GB_CUDA_TRY(cudaMemsetAsync(w.info, 0, 4 * sizeof(int), s));
-    double* h_energy = nullptr;
-    cudaMallocHost(&h_energy, sizeof(double));
+    LoopResources lr;
+    double* h_energy = lr.h_energy;
 
     // spin densities from FA and FB; break = the guess's beta symmetry break
     auto densities = [&](const double* FA, const double* FB, bool brk) -> int {
@@ -1368,9 +1350,7 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         GB_LAUNCH_CHECK();
         return HF_OK;
     };
-    cudaEvent_t l0, l1;
-    cudaEventCreate(&l0);
-    cudaEventCreate(&l1);
+    cudaEvent_t l0 = lr.ev[0], l1 = lr.ev[1];
     // core Hamiltonian, X, guess (InitialGuess_UHF_Core / _GWH / _Density / _SAD,
     // include/uhf.hpp:484-620): orbitals for both spins with the beta symmetry break
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
@@ -1406,7 +1386,7 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
         GB_CUDA_TRY(cudaMemcpyAsync(h_energy, e.d_scalar + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
         GB_CUDA_TRY(cudaStreamSynchronize(s));
         energy = *h_energy;
-        if (!std::isfinite(energy)) return cudaFreeHost(h_energy), set_error("UHF energy is not finite"), HF_ERR_NOT_CONVERGED;
+        if (!std::isfinite(energy)) return set_error("UHF energy is not finite"), HF_ERR_NOT_CONVERGED;
         if (std::fabs(energy - prev) < opt.convergence_threshold) { converged = true; break; }
         ++iter;
         prev = energy;
@@ -1414,7 +1394,7 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
             // Convergence_UHF_Damping (include/uhf.hpp:196-250): a constant factor for both spins
             // (the reference has no optimal factor for UHF)
             if ((st = damp_a.step(e, damp_opt, Fa, Da, nn, s)) || (st = damp_b.step(e, damp_opt, Fb, Db, nn, s)))
-                return cudaFreeHost(h_energy), st;
+                return st;
             ++diis_iter;
             continue;
         }
@@ -1433,9 +1413,6 @@ int hf_uhf_scf(hf_engine* eng, int num_alpha, int num_beta, const hf_scf_options
     GB_CUDA_TRY(cudaEventSynchronize(l1));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, l0, l1);
-    cudaEventDestroy(l0);
-    cudaEventDestroy(l1);
-    cudaFreeHost(h_energy);
     res->scf_ms_total = ms;
     res->electronic_energy = energy;
     res->total_energy = energy + res->nuclear_repulsion;
@@ -1519,12 +1496,8 @@ int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupl
     *res = hf_scf_result{};
     res->nuclear_repulsion = nuclear_repulsion(e);
     GB_CUDA_TRY(cudaMemsetAsync(w.info, 0, 4 * sizeof(int), s));
-    double* h_energy = nullptr;
-    cudaMallocHost(&h_energy, sizeof(double));
-    struct FreeHost {
-        double* p;
-        ~FreeHost() { cudaFreeHost(p); }
-    } host_guard{h_energy};
+    LoopResources lr;
+    double* h_energy = lr.h_energy;
 
     auto density = [&]() -> int {
         rohf_density_kernel<<<grid_nn(nn), 256, 0, s>>>(w.C, n, nc, no, Dc, Do, w.D);
@@ -1581,9 +1554,7 @@ int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupl
     }
     if ((st = density()) || (st = fock())) return st;
 
-    cudaEvent_t l0, l1;
-    cudaEventCreate(&l0);
-    cudaEventCreate(&l1);
+    cudaEvent_t l0 = lr.ev[0], l1 = lr.ev[1];
     cudaEventRecord(l0, s);
     double prev = std::numeric_limits<double>::max(), energy = 0.0;
     int iter = 0, diis_iter = 0;
@@ -1626,8 +1597,6 @@ int hf_rohf_scf(hf_engine* eng, int num_alpha, int num_beta, const double* coupl
     cudaEventSynchronize(l1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, l0, l1);
-    cudaEventDestroy(l0);
-    cudaEventDestroy(l1);
     if (st) return st;
     res->scf_ms_total = ms;
     res->electronic_energy = energy;

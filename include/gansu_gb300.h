@@ -199,8 +199,13 @@ int hf_compute_diis_error(hf_engine* eng, const double* d_overlap, const double*
                           const double* d_density, double* d_error, int include_transform, void* stream);
 
 /* Replaces gansu::gpu::computeFockMatrixDIIS (src/gpu_manager.cu:1078-1194):
- * B_ij = <e_i, e_j>, bordered system solved in FP64, F = sum_i c_i F_i.
- * num_prev in [2, 16]; d_errors/d_focks hold num_prev N x N matrices. */
+ * B_ij = <e_i, e_j>, F = sum_i c_i F_i with the weights that minimise
+ * |sum_i c_i e_i| subject to sum_i c_i = 1 (FP64, on the device).
+ * num_prev in [2, 16]; d_errors/d_focks hold num_prev N x N matrices.
+ * Error vectors that are linear combinations of others (two equal vectors,
+ * to within ~1e-6 rad) get weight 0 and the minimiser over the rest is used,
+ * where the reference's LU would return non-finite weights; an exactly zero
+ * error vector gets weight 1. */
 int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d_focks, double* d_new_fock,
                          int num_prev, void* stream);
 
@@ -213,8 +218,9 @@ int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d
  * (2..16) stored error/Fock pairs, N = num_basis.  Its scratch is a static
  * device array of 280 doubles held by every GPU that loads the library; the
  * first call on a device looks its address up (make that call before any
- * stream capture).  Calls that overlap on the GPU share the scratch and race:
- * serialise them. */
+ * stream capture; after cudaDeviceReset the next call looks it up again).
+ * Dependent error vectors are handled as in hf_compute_fock_diis.  Calls that
+ * overlap on the GPU share the scratch and race: serialise them. */
 int hf_compute_fock_diis_noalloc(const double* d_errors, const double* d_focks, double* d_new_fock, int num_prev,
                                  int num_basis, void* stream);
 

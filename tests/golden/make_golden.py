@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference's own
 integral kernels (oracle/refcpu: src/int2e.cu, src/int1e.cu, src/int2c2e.cu
 and src/int3c2e.cu of the reference compiled for the CPU) on the inputs below.  Needs the reference
-tree (GANSU_REFERENCE, default /root/reference); the fixtures themselves are
+tree (environment variable GANSU_REFERENCE); the fixtures themselves are
 committed so that the tests need neither the reference nor this script.
 
     python tests/golden/make_golden.py          # all fixtures
@@ -101,7 +101,9 @@ def main_sad():
     atomic RHF/ROHF solves) of H, C, N, O for the s/p basis sets, as data."""
     import os
 
-    ref = Path(os.environ.get("GANSU_REFERENCE", "/root/reference"))
+    if not os.environ.get("GANSU_REFERENCE"):
+        raise SystemExit("set GANSU_REFERENCE to the reference source tree")
+    ref = Path(os.environ["GANSU_REFERENCE"])
     out = {}
     for bas in SAD_BASES:
         table = O.read_sad(ref / "basis" / f"{bas}.sad")

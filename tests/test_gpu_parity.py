@@ -204,6 +204,30 @@ def test_diis_entry_points_match_numpy(built_library, cuda):
     np.testing.assert_allclose(Fn, O.diis_extrapolate(list(errs), list(focks)), atol=1e-9)
 
 
+def test_diis_dependent_error_vectors(built_library, cuda):
+    """Error vectors that repeat others: the reference's LU (src/gpu_manager.cu:1078-1194)
+    has no answer for a singular B; here the repeated vector gets weight 0 and the
+    extrapolation is the one over the distinct vectors (never the zero matrix)."""
+    g, atoms, gbs = _case("water_6-31g_st")
+    _, eng = _engine(atoms, gbs)
+    n = g["S"].shape[0]
+    rng = np.random.default_rng(9)
+    sym = lambda: (lambda a: a + a.T)(rng.normal(size=(n, n)))
+    t = lambda a: cuda.tensor(np.ascontiguousarray(a), device="cuda")
+    e = [rng.normal(size=(n, n)) for _ in range(3)]
+    f = [sym() for _ in range(4)]
+    # e0 twice (slots 0 and 2): the later copy is left out
+    errs = np.stack([e[0], e[1], e[0], e[2]])
+    Fn = _np(eng.fock_diis(t(errs), t(np.stack(f))))
+    np.testing.assert_allclose(Fn, O.diis_extrapolate([e[0], e[1], e[2]], [f[0], f[1], f[3]]), atol=1e-9)
+    # two equal vectors only: the first one's Fock matrix
+    Fn = _np(eng.fock_diis(t(np.stack([e[1], e[1]])), t(np.stack(f[:2]))))
+    np.testing.assert_allclose(Fn, f[0], atol=1e-12)
+    # a zero error vector: that Fock matrix is self-consistent and is returned
+    Fn = _np(eng.fock_diis(t(np.stack([e[1], 0.0 * e[1], e[2]])), t(np.stack(f[:3]))))
+    np.testing.assert_allclose(Fn, f[1], atol=1e-12)
+
+
 def test_builder_recipe_end_to_end(built_library, cuda, tmp_path):
     xyz = tmp_path / "h2o.xyz"
     geometry.write_xyz(xyz, geometry.water())

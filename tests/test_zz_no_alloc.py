@@ -51,3 +51,26 @@ def test_noalloc_diis_rejects_more_pairs_than_its_scratch(built_library, cuda):
     out = torch.zeros((n, n), dtype=torch.float64, device="cuda")
     assert _call_noalloc(errs, errs, out) == HF_ERR_INVALID_ARGUMENT
     assert b"between 2 and 16" in lib().hf_last_error()
+
+
+def test_noalloc_diis_dependent_error_vectors(built_library, cuda):
+    """A repeated error vector gets weight 0 in both DIIS entry points, so the
+    extrapolation is the one over the distinct vectors and never zero."""
+    torch = cuda
+    mol = gg.Molecular(geometry.water(), gg.basis_path("6-31g_st"))
+    eng = gg.Engine(mol)
+    n = mol.num_basis
+    rng = np.random.default_rng(12)
+    e = [rng.normal(size=(n, n)) for _ in range(2)]
+    f = rng.normal(size=(3, n, n))
+    f = f + f.transpose(0, 2, 1)
+    errs = torch.tensor(np.stack([e[0], e[1], e[1]]), device="cuda")
+    focks = torch.tensor(f, device="cuda")
+    for _ in range(2):  # twice in a row: the shared scratch keeps nothing between calls
+        out = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        assert _call_noalloc(errs, focks, out) == 0, lib().hf_last_error()
+        ref = eng.fock_diis(errs, focks)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        np.testing.assert_allclose(got, ref.cpu().numpy(), atol=1e-11, rtol=0)
+        assert np.abs(got).max() > 0.1
