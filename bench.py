@@ -290,6 +290,7 @@ def run_ours(args, rank, world):
             fp64.append(solve(opts_fp64, head))
     torch.cuda.synchronize()
     dist_barrier(world)
+    purification = head.purification_status() if args.eigensolver == "purification" else None
     # the other schedule, same solves (not part of the headline)
     alt_mixed = [solve(opts_mixed, alt) for _ in range(args.steps)]
     alt_fp64 = [solve(opts_fp64, alt) for _ in range(args.steps)]
@@ -459,6 +460,7 @@ def run_ours(args, rank, world):
                 "fock": statistics.mean(r["fock_ms_total"] / (r["iterations"] + 1) for r in mixed),
                 "diag": statistics.mean(r["diag_ms_total"] / max(r["iterations"], 1) for r in mixed),
                 "diis": statistics.mean(r["diis_ms_total"] / max(r["iterations"], 1) for r in mixed)},
+            "purification_last_call": purification,
             "gradient_ms": grad["value"] if grad else None,
             "gradient": grad,
             "diis": diis,

@@ -195,6 +195,16 @@ class _FockScheduleMixin:
         out.update(self.fock_schedule())
         return out
 
+    def purification_status(self) -> dict:
+        """Diagnostics of the last RHF purification (hf_engine_purification_status)."""
+        out = (C.c_double * 16)()
+        check(lib().hf_engine_purification_status(self._h, out, 16), "hf_engine_purification_status")
+        v = list(out)
+        return {"sp2_steps": int(v[0]), "trace_error": v[1], "idempotency_error": v[2], "sp2_error": v[3],
+                "sp2_converged": bool(v[4]), "mcweeny_steps": int(v[5]), "barrier_timeout": bool(v[6]),
+                "barriers": int(v[7]),
+                "phase_end_us": dict(zip(("fprime", "p0", "sp2", "mcweeny", "xp", "density"), v[8:14]))}
+
     def graph_stats(self) -> dict:
         """Graphs captured under use_graph (Fock builds, RHF purifications) and replays so far."""
         nf, npur, rep = C.c_int(), C.c_int(), C.c_longlong()
@@ -468,7 +478,9 @@ _DEFAULTS = {
     "export_sad_cache": "0",
     # added by this engine, same parsing rules
     "precision": "fp64", "mixed_threshold": "1e-7", "incremental_fock": "0", "spherical": "0",
+    "eigensolver": "syevd",
 }
+_EIGENSOLVERS = {"syevd": HF_EIGEN_SYEVD, "syevj": 1, "purification": HF_EIGEN_PURIFICATION}
 _SHORT = {"-m": "method", "-v": "verbose", "-p": "parameter_file", "-x": "xyzfilename", "-g": "gbsfilename",
           "-ag": "auxiliary_gbsfilename", "-c": "charge"}
 _KEEP_CASE = {"xyzfilename", "gbsfilename", "parameter_file", "auxiliary_gbsfilename"}
@@ -646,6 +658,7 @@ class _HFBase:
             "spherical": bool(p.get("spherical", bool)),
             "convergence_method": _CONVERGENCE[p["convergence_method"]],
             "damping_factor": p.get("damping_factor", float),
+            "eigensolver": _EIGENSOLVERS[p["eigensolver"]],
         }
         if guess == "density":
             if density_alpha is None or density_beta is None:

@@ -79,6 +79,7 @@ class ScfOptions(C.Structure):
         ("orthogonalizer", C.c_void_p),
         ("convergence_method", C.c_int),
         ("damping_factor", C.c_double),
+        ("purification_max_steps", C.c_int),
     ]
 
 
@@ -96,6 +97,7 @@ class ScfResult(C.Structure):
         ("diis_ms_total", C.c_double),
         ("fp64_quartets", C.c_longlong),
         ("fp32_quartets", C.c_longlong),
+        ("eigensolver_used", C.c_int),
     ]
 
 
@@ -145,6 +147,8 @@ SIGNATURES = {
     "hf_compute_diis_error": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_diis": (_I, [_P, _P, _P, _P, _I, _P]),
     "hf_compute_fock_diis_noalloc": (_I, [_P, _P, _P, _I, _I, _P]),
+    "hf_combine_uhf_fock": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P]),
+    "hf_engine_purification_status": (_I, [_P, _P, _I]),
     "hf_energy_weighted_density": (_I, [_P, _P, _P, _I, _P, _P]),
     "hf_rhf_gradient": (_I, [_P, _P, _P, C.POINTER(_D), C.POINTER(_D), _P]),
     "hf_rhf_gradient_mixed": (_I, [_P, _P, _P, _D, C.POINTER(_D), C.POINTER(_D), _P]),

@@ -20,6 +20,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libgansu_gb300.so"
+HF_MAIN = PKG / "HF_main"  # the C++ program (git-ignored build output)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # quartet classes (la, lb, lc, ld) with la>=lb, lc>=ld, (la,lb) >= (lc,ld)
@@ -33,7 +34,7 @@ FOCK_CLASSES = [
 # longest translation units first (the pool starts them in this order)
 CUDA_SOURCES = ["grad_class_f64_l5.cu", "grad_class_f64_l6.cu", "grad_class_f32_l56.cu", "grad_class_f64.cu",
                 "grad_class_f32.cu", "grad.cu", "ri.cu", "batch.cu", "scf.cu", "engine.cu", "fock.cu",
-                "fock_generic.cu", "one_electron.cu", "peaks.cu", "diis_noalloc.cu", "tc_gemm.cu"]
+                "fock_generic.cu", "one_electron.cu", "peaks.cu", "diis_noalloc.cu", "tc_gemm.cu", "purify.cu"]
 CXX_SOURCES = ["molecule.cpp", "errors.cpp"]
 
 
@@ -104,7 +105,28 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         if rc != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{out}")
         os.replace(tmp, LIB)
+    build_programs()
     return LIB
+
+
+def _cuda_home() -> Path:
+    return Path(_nvcc()).resolve().parent.parent
+
+
+def build_programs() -> Path:
+    """The C++ HF_main (programs/hf_main.cpp) over the C ABI, linked to the library."""
+    src = PKG / "programs" / "hf_main.cpp"
+    if _stale(HF_MAIN, [src, LIB, ROOT / "include" / "gansu_gb300.h"]):
+        cuda = _cuda_home()
+        tmp = HF_MAIN.with_suffix(".tmp")
+        cmd = ["g++", "-std=c++17", "-O2", f"-I{ROOT / 'include'}", f"-I{cuda / 'include'}", str(src), "-o", str(tmp),
+               f"-L{PKG}", "-lgansu_gb300", f"-L{cuda / 'lib64'}", "-lcudart", "-Wl,-rpath,$ORIGIN",
+               f"-Wl,-rpath,{cuda / 'lib64'}"]
+        rc, out = _run(cmd)
+        if rc != 0:
+            raise RuntimeError(f"HF_main build failed:\n{' '.join(cmd)}\n{out}")
+        os.replace(tmp, HF_MAIN)
+    return HF_MAIN
 
 
 if __name__ == "__main__":

@@ -18,12 +18,12 @@
 // call looks the address up again, and that call too belongs before any
 // stream capture.
 //
-// Dependent error vectors: the weights come from diis_coefficients
-// (diis_solve.cuh), which leaves out error vectors that are linear
-// combinations of others (two equal vectors count once) and returns the
-// constrained minimiser over the rest; the number left out is written to the
-// status word of the scratch.  The output is therefore always a finite
-// extrapolation, never the zero matrix.
+// Repeated error vectors: the weights come from diis_coefficients
+// (diis_solve.cuh), which gives weight 0 to an error vector that repeats
+// others (two equal vectors count once: the case in which the bordered
+// system is singular) and returns the constrained minimiser over the rest;
+// the number left out is written to the status word of the scratch.  The
+// output is therefore always a finite extrapolation, never the zero matrix.
 //
 // Limits and sharing: at most kNoAllocMaxPrev (16) stored error/Fock pairs.
 // All calls share the one scratch array and every call rewrites the parts it

@@ -194,7 +194,7 @@ Engine::~Engine()
                     scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
                     scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j, d_grad, d_shell_atom, d_goff64, d_goff32,
                     d_shell_info, d_block_dmax, d_mol_base, d_mol_n, d_mol_bf0, d_mol_atoms, d_shell_mol,
-                    scf.P32a, scf.P32b, scf.P32c, scf.Qocc, scf.Mocc, scf.qwork, scf.qinfo, d_eri};
+                    scf.P32a, scf.P32b, scf.P32c, scf.Qocc, scf.Mocc, scf.qwork, scf.qinfo, d_eri, scf.pur};
     ri_destroy(ri);
     schedule_release(sched);
     for (void* p : ptrs)

@@ -119,6 +119,7 @@ struct FockSchedule {
         const double* F;
         double* D;
         int nocc;
+        int max_steps;         // SP2 step limit of the options (part of the key)
         int uses;
         bool failed;           // the capture failed: this purification runs as ordinary launches
         cudaGraphExec_t exec;
@@ -217,6 +218,8 @@ struct Engine {
         double *Qocc = nullptr, *Mocc = nullptr, *qwork = nullptr;  // occupied basis from the projector
         int* qinfo = nullptr;
         int qlwork = 0;
+        double* pur = nullptr;  // purification status words, grid barrier and partial sums (purify.cu)
+        size_t pur_doubles = 0;
     } scf;
 
     ~Engine();

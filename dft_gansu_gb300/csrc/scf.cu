@@ -20,6 +20,7 @@
 
 #include "diis_solve.cuh"
 #include "engine.hpp"
+#include "purify.hpp"
 #include "ri.hpp"
 
 namespace gb {
@@ -28,15 +29,16 @@ namespace {
 
 constexpr int kMaxDiis = 16;
 
-// CUDA events and the pinned read-back slot of one SCF call, released on every
-// return path (early error returns included)
+// CUDA events and the pinned read-back slots of one SCF call (energy at 0, the
+// purification status words at 8), released on every return path (early error
+// returns included)
 struct LoopResources {
     cudaEvent_t ev[8] = {};
     double* h_energy = nullptr;
     LoopResources()
     {
         for (auto& x : ev) cudaEventCreate(&x);
-        cudaMallocHost(&h_energy, 4 * sizeof(double));
+        cudaMallocHost(&h_energy, 16 * sizeof(double));
     }
     ~LoopResources()
     {
@@ -286,6 +288,20 @@ __global__ void combine_kernel(const double* __restrict__ a, double fa, const do
     for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
          k += static_cast<long long>(gridDim.x) * blockDim.x)
         out[k] = fa * a[k] + (b ? fb * b[k] : 0.0);
+}
+
+// F_a = H + Ja + Jb - Ka, F_b = H + Ja + Jb - Kb
+__global__ void uhf_combine_kernel(const double* __restrict__ H, const double* __restrict__ Ja,
+                                   const double* __restrict__ Jb, const double* __restrict__ Ka,
+                                   const double* __restrict__ Kb, long long nn, double* __restrict__ Fa,
+                                   double* __restrict__ Fb)
+{
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double c = H[k] + Ja[k] + Jb[k];
+        Fa[k] = c - Ka[k];
+        Fb[k] = c - Kb[k];
+    }
 }
 
 // InitialGuess_UHF::break_symmetry (include/uhf.hpp:429-436): the last basis function's
@@ -559,12 +575,51 @@ int coefficients(Engine& e, const double* F, cudaStream_t s, int solver = 0)
 constexpr int kSp2Steps = 50;
 constexpr int kMcWeenySteps = 3;
 
-int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t s)
+// status words of the library-call purification: tr(P) - nocc and |tr(P) - |P|_F^2|
+// of the FP64 projector (one block)
+__global__ void purify_check_kernel(const double* __restrict__ P, int n, int nocc, int sp2_steps,
+                                    double* __restrict__ status)
 {
+    __shared__ double rt[32], rf[32];
+    double t = 0.0, f = 0.0;
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) {
+        const double v = P[k];
+        f += v * v;
+        if (k / n == k % n) t += v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+        f += __shfl_xor_sync(0xffffffffu, f, o);
+    }
+    if ((threadIdx.x & 31) == 0) { rt[threadIdx.x >> 5] = t; rf[threadIdx.x >> 5] = f; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        t = 0.0;
+        f = 0.0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) { t += rt[w]; f += rf[w]; }
+        status[kPurifyStatusSteps] = sp2_steps;
+        status[kPurifyStatusTraceError] = t - nocc;
+        status[kPurifyStatusIdempotency] = fabs(t - f);
+        status[kPurifyStatusSp2Error] = 0.0;
+        status[kPurifyStatusSp2Converged] = 1.0;
+        status[kPurifyStatusMcWeeny] = kMcWeenySteps;
+        status[kPurifyStatusFlags] = 0.0;
+    }
+}
+
+// N <= 512: the fused single-launch purification (purify.cu); larger N: SP2 steps
+// as cuBLAS SGEMMs, then McWeeny as DGEMMs.  Both leave their status words.
+int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t s, int max_steps)
+{
+    if (purify_fused_supported(e)) return purify_fused(e, F, nocc, D, s, max_steps);
+    const int sp2_steps = max_steps > 0 ? max_steps : kSp2Steps;
     auto& w = e.scf;
     const int n = w.n;
     const long long nn = static_cast<long long>(n) * n;
     int st;
+    double* status = nullptr;
+    if ((st = purify_status(e, &status))) return st;
     if (!w.P32a) {
         if ((st = alloc(w.P32a, nn)) || (st = alloc(w.P32b, nn)) || (st = alloc(w.P32c, nn))) return st;
     }
@@ -578,7 +633,7 @@ int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t
     float* Pn = w.P32b;
     float* P2 = w.P32c;
     const float one = 1.f, zero = 0.f;
-    for (int k = 0; k < kSp2Steps; ++k) {
+    for (int k = 0; k < sp2_steps; ++k) {
         // P symmetric: the column-major product is P^2 as well
         if (cublasSgemm(e.cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, P, n, P, n, &zero, P2, n) !=
             CUBLAS_STATUS_SUCCESS)
@@ -595,6 +650,8 @@ int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t
         mcweeny_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T1, w.T2, nn, w.W);
         GB_LAUNCH_CHECK();
     }
+    purify_check_kernel<<<1, 1024, 0, s>>>(w.W, n, nocc, sp2_steps, status);
+    GB_LAUNCH_CHECK();
     if ((st = gemm_rm(e.cublas, false, false, n, w.X, w.W, w.T1))) return st;  // X P
     if ((st = gemm_rm(e.cublas, false, true, n, w.T1, w.X, w.T2))) return st;  // X P X^T
     scale_copy_kernel<<<grid_nn(nn), 256, 0, s>>>(w.T2, 2.0, nn, D);
@@ -609,13 +666,14 @@ int purify_density(Engine& e, const double* F, int nocc, double* D, cudaStream_t
 // stream with an engine-owned workspace during the capture (cublasSetStream resets
 // cuBLAS to its own workspace pool, which may allocate, and a capture must not).
 // If the capture fails, that purification keeps running as ordinary launches.
-int purify_density_scheduled(Engine& e, const double* F, int nocc, double* D, cudaStream_t s)
+int purify_density_scheduled(Engine& e, const double* F, int nocc, double* D, cudaStream_t s, int max_steps)
 {
     FockSchedule& S = e.sched;
-    if (!S.use_graph || e.nmol != 1) return purify_density(e, F, nocc, D, s);
+    // the fused path is one launch already: nothing to replay
+    if (!S.use_graph || e.nmol != 1 || purify_fused_supported(e)) return purify_density(e, F, nocc, D, s, max_steps);
     FockSchedule::PurifyGraph* g = nullptr;
     for (auto& x : S.purify)
-        if (x.F == F && x.D == D && x.nocc == nocc) {
+        if (x.F == F && x.D == D && x.nocc == nocc && x.max_steps == max_steps) {
             g = &x;
             break;
         }
@@ -624,10 +682,10 @@ int purify_density_scheduled(Engine& e, const double* F, int nocc, double* D, cu
             if (S.purify.front().exec) cudaGraphExecDestroy(S.purify.front().exec);
             S.purify.erase(S.purify.begin());
         }
-        S.purify.push_back(FockSchedule::PurifyGraph{F, D, nocc, 0, false, nullptr, 0});
+        S.purify.push_back(FockSchedule::PurifyGraph{F, D, nocc, max_steps, 0, false, nullptr, 0});
         g = &S.purify.back();
     }
-    if (g->failed || (!g->exec && g->uses++ == 0)) return purify_density(e, F, nocc, D, s);
+    if (g->failed || (!g->exec && g->uses++ == 0)) return purify_density(e, F, nocc, D, s, max_steps);
     if (!g->exec) {
         int st = schedule_streams(e);
         if (st) return st;
@@ -636,13 +694,13 @@ int purify_density_scheduled(Engine& e, const double* F, int nocc, double* D, cu
             cublasSetWorkspace(e.cublas, S.cublas_ws, kCublasCaptureWorkspace) != CUBLAS_STATUS_SUCCESS) {
             cublasSetStream(e.cublas, s);
             g->failed = true;
-            return purify_density(e, F, nocc, D, s);
+            return purify_density(e, F, nocc, D, s, max_steps);
         }
         const long long l0 = launch_count();
         cudaGraph_t graph = nullptr;
         cudaError_t ce = cudaStreamBeginCapture(S.capture, cudaStreamCaptureModeThreadLocal);
         if (ce == cudaSuccess) {
-            st = purify_density(e, F, nocc, D, S.capture);
+            st = purify_density(e, F, nocc, D, S.capture, max_steps);
             ce = cudaStreamEndCapture(S.capture, &graph);
         }
         cublasSetStream(e.cublas, s);
@@ -658,7 +716,7 @@ int purify_density_scheduled(Engine& e, const double* F, int nocc, double* D, cu
             cudaGetLastError();  // capture errors are not sticky; clear the last-error slot
             g->failed = true;
             clear_error();
-            return purify_density(e, F, nocc, D, s);
+            return purify_density(e, F, nocc, D, s, max_steps);
         }
     }
     GB_CUDA_TRY(cudaGraphLaunch(g->exec, s));
@@ -896,6 +954,7 @@ void hf_scf_options_default(hf_scf_options* o)
     o->orthogonalizer = nullptr;
     o->convergence_method = HF_CONV_DIIS;
     o->damping_factor = 0.9;
+    o->purification_max_steps = 0;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -927,8 +986,39 @@ int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d
     return diis_extrapolate(e, d_errors, d_focks, num_prev, d_new_fock, static_cast<cudaStream_t>(stream));
 }
 
-int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, hf_scf_result* res,
-               double* d_density_out, double* d_fock_out, double* d_orbital_energies_out, double* d_coefficients_out)
+int hf_engine_purification_status(hf_engine* eng, double* h_out, int max_words)
+{
+    clear_error();
+    if (!eng || !h_out || max_words <= 0) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    for (int i = 0; i < max_words; ++i) h_out[i] = 0.0;
+    if (!e.scf.pur) return HF_OK;
+    GB_CUDA_TRY(cudaMemcpy(h_out, e.scf.pur, sizeof(double) * std::min(max_words, kPurifyStatusWords),
+                           cudaMemcpyDeviceToHost));
+    return HF_OK;
+}
+
+int hf_combine_uhf_fock(const double* d_core_hamiltonian, const double* d_j_a, const double* d_j_b,
+                        const double* d_k_a, const double* d_k_b, double* d_fock_a, double* d_fock_b, int num_basis,
+                        void* stream)
+{
+    clear_error();
+    if (!d_core_hamiltonian || !d_j_a || !d_j_b || !d_k_a || !d_k_b || !d_fock_a || !d_fock_b || num_basis <= 0)
+        return set_error("hf_combine_uhf_fock: null pointer or non-positive num_basis"), HF_ERR_INVALID_ARGUMENT;
+    const long long nn = static_cast<long long>(num_basis) * num_basis;
+    uhf_combine_kernel<<<grid_nn(nn), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        d_core_hamiltonian, d_j_a, d_j_b, d_k_a, d_k_b, nn, d_fock_a, d_fock_b);
+    GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+// internal status of rhf_scf_run: a purified density failed its checks (the SCF
+// is rerun with a diagonalisation)
+constexpr int kPurificationRejected = -100;
+
+static int rhf_scf_run(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, hf_scf_result* res,
+                       double* d_density_out, double* d_fock_out, double* d_orbital_energies_out,
+                       double* d_coefficients_out)
 {
     clear_error();
     if (!eng || !res) return set_error("null argument"), HF_ERR_INVALID_ARGUMENT;
@@ -1119,7 +1209,7 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     auto density_from = [&](const double* Fm) -> int {
         int r;
         if (purify) {
-            if ((r = purify_density_scheduled(e, Fm, nocc, w.D, s))) return r;
+            if ((r = purify_density_scheduled(e, Fm, nocc, w.D, s, opt.purification_max_steps))) return r;
             if (!use_ri) return HF_OK;
             r = occupied_from_projector(e, Fm, nocc, !occ_seeded, s);
             occ_seeded = true;
@@ -1168,6 +1258,8 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
     double prev = std::numeric_limits<double>::max(), energy = 0.0;
     int iter = 0, diis_iter = 0;
     bool converged = false;
+    double* d_purify_status = nullptr;
+    if (purify && (st = purify_status(e, &d_purify_status))) return st;
     while (iter < opt.max_iter) {
         cudaEventRecord(c0, s);
         if ((st = density_from(w.F))) return st;
@@ -1176,11 +1268,30 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         energy_kernel<<<1, 1024, 0, s>>>(w.D, w.H, w.F, nn, e.d_scalar + 4);
         GB_LAUNCH_CHECK();
         GB_CUDA_TRY(cudaMemcpyAsync(h_energy, e.d_scalar + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (purify)
+            GB_CUDA_TRY(cudaMemcpyAsync(h_energy + 8, d_purify_status, kPurifyStatusWords * sizeof(double),
+                                        cudaMemcpyDeviceToHost, s));
         fock_ms += elapsed(f0, f1);
         diag_ms += elapsed(c0, c1);
         if (diis_timed) diis_ms += elapsed(q0, q1);
         GB_CUDA_TRY(cudaStreamSynchronize(s));
         energy = *h_energy;
+        if (purify) {
+            // the purified projector must hold nocc states and be idempotent (a small or
+            // closed HOMO-LUMO gap leaves eigenvalues between 0 and 1)
+            const double* ps = h_energy + 8;
+            if (ps[kPurifyStatusFlags] != 0.0)
+                return set_error("purification: a grid-barrier wait ran out"), HF_ERR_CUDA;
+            if (!(std::fabs(ps[kPurifyStatusTraceError]) <= kPurifyTraceTol) ||
+                !(ps[kPurifyStatusIdempotency] <= kPurifyIdempotencyTol)) {
+                if (opt.verbose)
+                    std::printf("purification rejected at iteration %d (trace error %.3g, idempotency error %.3g, "
+                                "%d SP2 steps): rerunning the SCF with syevd\n",
+                                iter, ps[kPurifyStatusTraceError], ps[kPurifyStatusIdempotency],
+                                static_cast<int>(ps[kPurifyStatusSteps]));
+                return kPurificationRejected;
+            }
+        }
         const double diff = std::fabs(energy - prev);
         if (opt.verbose)
             std::printf("---- Iteration: %d ----  Energy: %.17g Total energy: %.17g Difference: %.17g\n", iter, energy,
@@ -1247,7 +1358,22 @@ int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, 
         GB_CUDA_TRY(cudaMemcpy(d_orbital_energies_out, w.eps, n * sizeof(double), cudaMemcpyDeviceToDevice));
     }
     if (d_coefficients_out) GB_CUDA_TRY(cudaMemcpy(d_coefficients_out, w.C, nn * sizeof(double), cudaMemcpyDeviceToDevice));
+    res->eigensolver_used = opt.eigensolver;
     return converged ? HF_OK : (set_error("SCF did not converge"), HF_ERR_NOT_CONVERGED);
+}
+
+int hf_rhf_scf(hf_engine* eng, int num_electrons, const hf_scf_options* opt_in, hf_scf_result* res,
+               double* d_density_out, double* d_fock_out, double* d_orbital_energies_out, double* d_coefficients_out)
+{
+    int st = rhf_scf_run(eng, num_electrons, opt_in, res, d_density_out, d_fock_out, d_orbital_energies_out,
+                         d_coefficients_out);
+    if (st != kPurificationRejected) return st;
+    // a purified density failed its checks: the same SCF with a diagonalisation
+    hf_scf_options opt;
+    if (opt_in) opt = *opt_in; else hf_scf_options_default(&opt);
+    opt.eigensolver = HF_EIGEN_SYEVD;
+    return rhf_scf_run(eng, num_electrons, &opt, res, d_density_out, d_fock_out, d_orbital_energies_out,
+                       d_coefficients_out);
 }
 
 }  // extern "C"

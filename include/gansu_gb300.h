@@ -202,12 +202,28 @@ int hf_compute_diis_error(hf_engine* eng, const double* d_overlap, const double*
  * B_ij = <e_i, e_j>, F = sum_i c_i F_i with the weights that minimise
  * |sum_i c_i e_i| subject to sum_i c_i = 1 (FP64, on the device).
  * num_prev in [2, 16]; d_errors/d_focks hold num_prev N x N matrices.
- * Error vectors that are linear combinations of others (two equal vectors,
- * to within ~1e-6 rad) get weight 0 and the minimiser over the rest is used,
- * where the reference's LU would return non-finite weights; an exactly zero
- * error vector gets weight 1. */
+ * Where the reference's LU has no answer (an error vector that repeats
+ * another, or a combination of others, to ~1e-7 relative: the bordered
+ * matrix is singular), the repeated vector gets weight 0 and the minimiser
+ * over the rest is used; an exactly zero error vector gets weight 1. */
 int hf_compute_fock_diis(hf_engine* eng, const double* d_errors, const double* d_focks, double* d_new_fock,
                          int num_prev, void* stream);
+
+/* Diagnostics of the last RHF purification (HF_EIGEN_PURIFICATION; no
+ * reference counterpart): up to 16 words -- SP2 steps, tr(P) - nocc and
+ * |tr(P) - |P|_F^2| after McWeeny, the SP2 stopping error, 1 if SP2 met its
+ * stopping rule, McWeeny steps, a barrier-timeout flag, the grid barriers
+ * passed, then (N <= 512, one launch) the microseconds from the launch's start
+ * to the end of F' = X^T F X, P0, the SP2 steps, McWeeny, X P and D.  Zeros
+ * before the first purification.  Synchronises. */
+int hf_engine_purification_status(hf_engine* eng, double* h_out, int max_words);
+
+/* The UHF Fock matrices of computeFockMatrix_UHF (src/gpu_manager.cu:707-731)
+ * from separately built J and K of the two spin densities
+ * (hf_compute_jk_direct): F_a = H + J_a + J_b - K_a, F_b = H + J_a + J_b - K_b. */
+int hf_combine_uhf_fock(const double* d_core_hamiltonian, const double* d_j_a, const double* d_j_b,
+                        const double* d_k_a, const double* d_k_b, double* d_fock_a, double* d_fock_b, int num_basis,
+                        void* stream);
 
 /* DIIS extrapolation that allocates nothing (no reference counterpart: the
  * reference's computeFockMatrixDIIS allocates on every call).  For callers
@@ -299,6 +315,9 @@ typedef struct {
     int convergence_method;         /* HF_CONV_DIIS, HF_CONV_DAMPING or HF_CONV_OPTIMAL_DAMPING
                                        (convergence_method = diis / damping / optimaldamping) */
     double damping_factor;          /* HF_CONV_DAMPING: F <- (1 - a) F_prev + a F (reference default 0.9) */
+    int purification_max_steps;     /* HF_EIGEN_PURIFICATION: SP2 steps at most (0: 100 when N <= 512, else a
+                                       fixed 50); a projector that has not converged within them fails the
+                                       trace/idempotency check and the SCF reruns with syevd */
 } hf_scf_options;
 
 /* Fock-matrix update between iterations (Convergence_RHF_DIIS / _Damping,
@@ -316,9 +335,12 @@ enum {
 /* Density from the Fock matrix inside the SCF loop.  The reference diagonalises
  * (computeCoefficientMatrix, src/gpu_manager.cu:529-599); purification gives the
  * same aufbau density when the HOMO-LUMO gap is open, without eigenvectors:
- * FP32 SP2 steps then FP64 McWeeny steps; orbitals and orbital energies come
- * from one diagonalisation of the final Fock matrix.  RI keeps syevd (its K
- * build uses the occupied orbitals). */
+ * FP32 SP2 steps until their idempotency error stops shrinking, then FP64
+ * McWeeny steps (N <= 512: the whole step is one launch); orbitals and orbital
+ * energies come from one diagonalisation of the final Fock matrix.  Every
+ * purified projector is checked (trace = number of occupied orbitals to 1e-6,
+ * idempotency to 1e-8); if one fails (small or closed gap) the RHF SCF is
+ * rerun with HF_EIGEN_SYEVD and hf_scf_result.eigensolver_used says so. */
 enum {
     HF_EIGEN_SYEVD = 0,
     HF_EIGEN_SYEVJ = 1,
@@ -361,6 +383,8 @@ typedef struct {
     double diis_ms_total;           /* DIIS error, B matrix, solve and extrapolation (loop) */
     long long fp64_quartets;        /* summed over all Fock builds */
     long long fp32_quartets;
+    int eigensolver_used;           /* RHF: the eigensolver the SCF finished with (a purified density that
+                                       fails its trace/idempotency checks reruns the SCF with HF_EIGEN_SYEVD) */
 } hf_scf_result;
 
 void hf_scf_options_default(hf_scf_options* opt);

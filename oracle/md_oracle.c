@@ -690,3 +690,59 @@ int oracle_ri_integrals(int nshell, const int* l, const int* nprim, const int* p
     free(QP); free(Q); free(off);
     return 0;
 }
+
+/* Three-centre integrals (mu nu|P) of selected AO shell pairs only (checks of the
+ * B tensor at sizes where the full naux x N^2 tensor is too large for the CPU):
+ * T[((k * ncart_max^2) + ia * nb + ib) * naux + r] for the k-th pair (pairA[k],
+ * pairB[k]), ncart_max = 15; same screening and factors as oracle_ri_integrals. */
+int oracle_ri_three_center_pairs(int nshell, const int* l, const int* nprim, const int* prim_off, const int* bf_off,
+                                 const double* xyz, const double* alpha, const double* coef, const double* cgto,
+                                 int nbf, int ashell, const int* al, const int* anprim, const int* aprim_off,
+                                 const int* abf_off, const double* axyz, const double* aalpha, const double* acoef,
+                                 const double* acgto, int naux, double thr, int npairs, const int* pairA,
+                                 const int* pairB, double* T)
+{
+    or_basis bs, ax;
+    or_make_basis(&bs, nshell, l, nprim, prim_off, bf_off, xyz, alpha, coef, cgto, nbf);
+    or_make_basis(&ax, ashell, al, anprim, aprim_off, abf_off, axyz, aalpha, acoef, acgto, naux);
+    int naprim = 0;
+    for (int P = 0; P < ashell; ++P) naprim += anprim[P];
+    double* QP = (double*)malloc(sizeof(double) * (naprim > 0 ? naprim : 1));
+    or_aux_bounds(&ax, QP);
+    int* off;
+    double* Q = or_all_bounds(&bs, &off);
+    const size_t M = (size_t)naux;
+    memset(T, 0, sizeof(double) * (size_t)npairs * 225 * M);
+#pragma omp parallel for collapse(2) schedule(dynamic)
+    for (int k = 0; k < npairs; ++k)
+        for (int P = 0; P < ashell; ++P) {
+            const int A = pairA[k], B = pairB[k];
+            const int la = l[A], lb = l[B], na = or_ncart(la), nb = or_ncart(lb);
+            const int lp = al[P], np = or_ncart(lp);
+            double blk[15 * 15 * 15], tmp[15 * 15 * 15];
+            memset(blk, 0, sizeof(double) * na * nb * np);
+            for (int i = 0; i < nprim[A]; ++i)
+                for (int j = 0; j < nprim[B]; ++j) {
+                    const int pa = prim_off[A] + i, pb = prim_off[B] + j;
+                    const double qab = Q[off[A * nshell + B] + i * nprim[B] + j];
+                    for (int q = 0; q < anprim[P]; ++q) {
+                        const int pk = aprim_off[P] + q;
+                        if (qab * QP[pk] < thr) continue;
+                        or_prim_quartet_o(la, lb, lp, 0, alpha[pa], alpha[pb], aalpha[pk], 0.0, &xyz[3 * A],
+                                          &xyz[3 * B], &axyz[3 * P], &axyz[3 * P], or_cart, or_cart, or_cart_ri,
+                                          or_cart, tmp);
+                        const double cf = coef[pa] * coef[pb] * acoef[pk];
+                        for (int e = 0; e < na * nb * np; ++e) blk[e] += cf * tmp[e];
+                    }
+                }
+            for (int ia = 0; ia < na; ++ia)
+                for (int ib = 0; ib < nb; ++ib)
+                    for (int ip = 0; ip < np; ++ip) {
+                        const size_t mu = bf_off[A] + ia, nu = bf_off[B] + ib, r = abf_off[P] + ip;
+                        T[((size_t)k * 225 + ia * nb + ib) * M + r] =
+                            blk[(ia * nb + ib) * np + ip] * cgto[mu] * cgto[nu] * acgto[r];
+                    }
+        }
+    free(QP); free(Q); free(off);
+    return 0;
+}

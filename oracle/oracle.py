@@ -90,6 +90,7 @@ def _lib():
         L.oracle_direct_jk_sample.restype = C.c_long
         L.oracle_one_electron.argtypes = basis + [C.c_int, dp, dp, dp, dp, dp]
         L.oracle_prim_pair_bounds.argtypes = basis + [C.c_int, dp]
+        L.oracle_ri_three_center_pairs.argtypes = basis + basis + [C.c_double, C.c_int, ip, ip, dp]
         _oracle = L
     return _oracle
 
@@ -698,6 +699,31 @@ def ri_integrals(b: Basis, aux: Basis, thr=1e-12):
     qp = np.zeros(len(aux.alpha))
     _lib().oracle_ri_integrals(*b.cargs(), *aux.cargs(), C.c_double(thr), _dp(V), _dp(T), _dp(qp))
     return V, T, qp
+
+
+def ri_metric(b: Basis, aux: Basis, thr=1e-12):
+    """The metric V = (P|Q) alone (oracle_ri_integrals without the three-centre tensor)."""
+    M = aux.nbf
+    V = np.zeros((M, M))
+    _lib().oracle_ri_integrals(*b.cargs(), *aux.cargs(), C.c_double(thr), _dp(V), None, None)
+    return V
+
+
+def ri_three_center_pairs(b: Basis, aux: Basis, shell_pairs, thr=1e-12):
+    """(mu nu|P) for the AO shell pairs listed (A, B): {(mu, nu): vector over P}."""
+    pa = np.array([p[0] for p in shell_pairs], np.int32)
+    pb = np.array([p[1] for p in shell_pairs], np.int32)
+    M = aux.nbf
+    T = np.zeros((len(shell_pairs), 225, M))
+    _lib().oracle_ri_three_center_pairs(*b.cargs(), *aux.cargs(), C.c_double(thr), len(shell_pairs), _ip(pa),
+                                        _ip(pb), _dp(T))
+    out = {}
+    for k, (A, B) in enumerate(shell_pairs):
+        na, nb = (b.l[A] + 1) * (b.l[A] + 2) // 2, (b.l[B] + 1) * (b.l[B] + 2) // 2
+        for ia in range(na):
+            for ib in range(nb):
+                out[(int(b.bf_off[A]) + ia, int(b.bf_off[B]) + ib)] = T[k, ia * nb + ib].copy()
+    return out
 
 
 def ri_factor(V, T):

@@ -168,9 +168,11 @@ def test_batch_schedule_matches_default(built_library, cuda):
     b.close()
 
 
-def test_purification_replayed_from_graph(built_library, cuda):
+def test_purification_under_graph_schedule(built_library, cuda):
     """The RHF loop's purification density (HF_EIGEN_PURIFICATION) under the graph
-    schedule: captured once, replayed every later iteration, same energies."""
+    schedule: at this size (N <= 512) the purification is one cooperative launch and
+    needs no graph; the Fock builds are captured once and replayed; same energies.
+    (The library-call purification above N = 512 and its graph: test_gpu_purify.py.)"""
     torch = cuda
     mol, eng, D, H = _setup(torch, seed=11)
     nel = mol.num_electrons
@@ -185,6 +187,6 @@ def test_purification_replayed_from_graph(built_library, cuda):
         for a, b in zip(ref, got):
             assert b["converged"] and abs(a["total_energy"] - b["total_energy"]) < 1e-8
     st = eng.graph_stats()
-    assert st["purification_graphs"] >= 1 and st["fock_graphs"] >= 1
+    assert st["purification_graphs"] == 0 and st["fock_graphs"] >= 1
     assert st["replays"] > 2 * ref[0]["iterations"]
     eng.close()

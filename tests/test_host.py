@@ -208,3 +208,31 @@ def test_command_line_rejects_bad_arguments(capsys):
     assert main(["-m", "rhf"]) == 2  # no xyz file, no basis
     assert "required" in capsys.readouterr().err
     assert main(["-x"]) == 2  # option without a value
+
+
+def test_public_header_compiles_as_c():
+    """include/gansu_gb300.h is a C header: tests/cabi/header_c_check.c takes the
+    address of entry points with their declared types (gcc, -Werror)."""
+    import shutil
+    import subprocess
+    root = Path(__file__).resolve().parents[1]
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", f"-I{root / 'include'}", "-fsyntax-only",
+                    str(root / "tests" / "cabi" / "header_c_check.c")], check=True)
+
+
+def test_reference_side_plugin_compiles_against_reference_headers(tmp_path):
+    """The gansu::ERI plugins and gansu::gpu shims (dft_gansu_gb300/plugin/) compile
+    against the reference's own include/eri.hpp, rhf.hpp, uhf.hpp and gpu_manager.hpp."""
+    import subprocess
+    from oracle import oracle as O
+    from dft_gansu_gb300 import build as b
+    if O.REFERENCE_ROOT is None:
+        pytest.skip("GANSU_REFERENCE not set")
+    root = Path(__file__).resolve().parents[1]
+    ref = O.REFERENCE_ROOT
+    subprocess.run([b._nvcc(), "-std=c++17", f"-I{root / 'include'}", f"-I{ref / 'include'}", f"-I{ref / 'src'}",
+                    f"-I{root / 'dft_gansu_gb300' / 'plugin'}", "-c",
+                    str(root / "dft_gansu_gb300" / "plugin" / "plugin_check.cu"), "-o", str(tmp_path / "p.o")],
+                   check=True)

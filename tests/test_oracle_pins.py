@@ -299,3 +299,19 @@ def test_oracle_damping_reaches_the_diis_energy():
     for conv, a in (("damping", 0.5), ("optimaldamping", 0.0)):
         r = O.rhf(S, H, fock, 5, enuc, thr=1e-11, maxiter=300, convergence=conv, damping=a)
         assert r["converged"] and abs(r["total_energy"] - ref["total_energy"]) < 1e-9, conv
+
+
+def test_oracle_three_center_pairs_match_full_tensor():
+    """The selected-pair three-centre routine (used to check B columns at C60 size)
+    equals the full tensor's columns, and ri_metric its metric."""
+    from dft_gansu_gb300 import geometry
+    atoms = geometry.alkane(1, jitter=0.03, seed=4)
+    b = O.make_basis(atoms, BASIS / "cc-pvdz.gbs")
+    ax = O.make_basis(atoms, BASIS / "cc-pvdz-rifit.gbs")
+    V, T, _ = O.ri_integrals(b, ax)
+    np.testing.assert_array_equal(O.ri_metric(b, ax), V)
+    pairs = [(0, 0), (2, 1), (b.nshell - 1, 3), (4, b.nshell - 2)]
+    cols = O.ri_three_center_pairs(b, ax, pairs)
+    assert len(cols) == sum(((b.l[A] + 1) * (b.l[A] + 2) // 2) * ((b.l[B] + 1) * (b.l[B] + 2) // 2) for A, B in pairs)
+    for (mu, nu), t in cols.items():
+        np.testing.assert_array_equal(t, T[:, mu, nu])
