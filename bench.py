@@ -31,6 +31,7 @@ METRIC = "SCF ms/iter & gradient ms, mixed vs FP64 on 1 GB300 at |ΔE|≤1e-6 Eh
 WORKLOAD = "RHF/6-31G* n-decane C10H22 (N=194 Cartesian, 238 primitive shells), zig-zag + N(0,0.02 A) jitter"
 MIXED_THRESHOLD = 0.1
 ANCHOR_THRESHOLD = 1e-2
+ANCHOR_MIXED_THRESHOLD = 0.0
 CONV = 1e-8
 GUESSES = {"core": 0, "gwh": 1, "sad": 3}  # HF_GUESS_CORE / _GWH / _SAD
 # gradient FP32 cut: on decane cc-pVDZ max|g_mixed - g_FP64| = 1.6e-7 Eh/bohr at 1.0
@@ -249,7 +250,8 @@ def run_ours(args, rank, world):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     opts_mixed = {"convergence_threshold": CONV, "precision": gg.HF_PRECISION_MIXED,
                   "mixed_threshold": args.mixed_threshold, "incremental": 1, "rebuild_every": 0,
-                  "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": args.anchor_threshold}
+                  "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": args.anchor_threshold,
+                  "anchor_mixed_threshold": args.anchor_mixed_threshold}
     opts_fp64 = {"convergence_threshold": CONV}
     for o in (opts_mixed, opts_fp64):
         o["initial_guess"] = GUESSES[args.guess or "core"]
@@ -717,6 +719,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--mixed-threshold", type=float, default=MIXED_THRESHOLD)
     ap.add_argument("--anchor-threshold", type=float, default=ANCHOR_THRESHOLD)
+    ap.add_argument("--anchor-mixed-threshold", type=float, default=ANCHOR_MIXED_THRESHOLD,
+                    help="FP32 cut of the anchor build on Q_ab*Q_cd*max|D| (0: an all-FP64 anchor)")
     ap.add_argument("--sample-stride", type=int, default=4)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-gradient", action="store_true")

@@ -346,6 +346,15 @@ class Engine(_FockScheduleMixin):
                   "hf_rhf_gradient_mixed")
         return g.reshape(-1, 3), ms.value
 
+    def gradient_ri(self, density, energy_weighted_density, coefficients, num_occupied: int, stream=None):
+        """Analytic gradient of the RI energy (eri_method ri; hf_rhf_gradient_ri): (natom, 3) Eh/bohr, ms."""
+        g = np.zeros(3 * self.mol.num_atoms)
+        ms = C.c_double()
+        check(lib().hf_rhf_gradient_ri(self._h, _ptr(density), _ptr(energy_weighted_density), _ptr(coefficients),
+                                       int(num_occupied), g.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ms),
+                                       _stream(stream)), "hf_rhf_gradient_ri")
+        return g.reshape(-1, 3), ms.value
+
     def uhf_scf(self, num_alpha: int, num_beta: int, options: dict | None = None, want_matrices: bool = False):
         """Unrestricted HF (hf_uhf_scf)."""
         opt, _keep = _scf_options(self._with_guess(options))
@@ -449,7 +458,11 @@ class Engine(_FockScheduleMixin):
         """Forward (SCF energy) and backward (analytic gradient) pair."""
         r = self.rhf_scf(num_electrons, options, want_matrices=True)
         W = self.energy_weighted_density(r["coefficients"], r["orbital_energies"], num_electrons // 2)
-        g, ms = self.gradient(r["density"], W)
+        if (options or {}).get("eri_method") == HF_ERI_RI:
+            # the gradient of the RI energy (derivative three-centre and metric integrals)
+            g, ms = self.gradient_ri(r["density"], W, r["coefficients"], num_electrons // 2)
+        else:
+            g, ms = self.gradient(r["density"], W)
         r["gradient"], r["gradient_ms"] = g, ms
         return r
 

@@ -80,6 +80,7 @@ class ScfOptions(C.Structure):
         ("convergence_method", C.c_int),
         ("damping_factor", C.c_double),
         ("purification_max_steps", C.c_int),
+        ("anchor_mixed_threshold", C.c_double),
     ]
 
 
@@ -149,6 +150,7 @@ SIGNATURES = {
     "hf_compute_fock_diis_noalloc": (_I, [_P, _P, _P, _I, _I, _P]),
     "hf_combine_uhf_fock": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _P]),
     "hf_engine_purification_status": (_I, [_P, _P, _I]),
+    "hf_rhf_gradient_ri": (_I, [_P, _P, _P, _P, _I, _P, _P, _P]),
     "hf_energy_weighted_density": (_I, [_P, _P, _P, _I, _P, _P]),
     "hf_rhf_gradient": (_I, [_P, _P, _P, C.POINTER(_D), C.POINTER(_D), _P]),
     "hf_rhf_gradient_mixed": (_I, [_P, _P, _P, _D, C.POINTER(_D), C.POINTER(_D), _P]),

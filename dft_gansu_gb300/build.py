@@ -33,7 +33,7 @@ FOCK_CLASSES = [
 
 # longest translation units first (the pool starts them in this order)
 CUDA_SOURCES = ["grad_class_f64_l5.cu", "grad_class_f64_l6.cu", "grad_class_f32_l56.cu", "grad_class_f64.cu",
-                "grad_class_f32.cu", "grad.cu", "ri.cu", "batch.cu", "scf.cu", "engine.cu", "fock.cu",
+                "grad_class_f32.cu", "grad.cu", "ri_grad.cu", "ri.cu", "batch.cu", "scf.cu", "engine.cu", "fock.cu",
                 "fock_generic.cu", "one_electron.cu", "peaks.cu", "diis_noalloc.cu", "tc_gemm.cu", "purify.cu"]
 CXX_SOURCES = ["molecule.cpp", "errors.cpp"]
 
@@ -62,6 +62,11 @@ def _jobs() -> list[tuple[list[str], Path, list[Path]]]:
     common = [nvcc, "-std=c++17", "-O3", "-lineinfo", ARCH, "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", *inc]
     hdr = _headers()
     jobs = []
+    # the RI derivative kernels, one unit per auxiliary angular momentum (long units first)
+    for lp in (3, 2, 1, 0):
+        obj = BUILD / f"ri_grad_l{lp}.o"
+        jobs.append(([*common, f"-DGB_RI_LP={lp}", "-c", str(CSRC / "ri_grad_inst.cu"), "-o", str(obj)], obj,
+                     [CSRC / "ri_grad_inst.cu", *hdr]))
     for src in CUDA_SOURCES:
         obj = BUILD / (Path(src).stem + ".o")
         jobs.append(([*common, "-c", str(CSRC / src), "-o", str(obj)], obj, [CSRC / src, *hdr]))

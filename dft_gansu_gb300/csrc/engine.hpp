@@ -295,8 +295,11 @@ int core_hamiltonian(Engine& e, double* d_S, double* d_H, cudaStream_t s);
 
 // grad.cu
 int energy_weighted_density(Engine& e, const double* d_C, const double* d_eps, int nocc, double* d_W, cudaStream_t s);
+// d_C != nullptr: the two-electron part is the RI one (ri_grad.cu) from the occupied
+// orbitals C[:, :nocc] (row-major, row stride ldc) instead of the four-centre one
 int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad, cudaStream_t s, float* ms_out,
-                 int precision = 0, double mixed_threshold = 0.0);
+                 int precision = 0, double mixed_threshold = 0.0, const double* d_C = nullptr, int ldc = 0,
+                 int nocc = 0);
 
 // host MD helpers (engine.cu)
 void host_boys_table(std::vector<double>& table);

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "grad_kernel.cuh"
+#include "ri.hpp"
 
 namespace gb {
 namespace {
@@ -514,7 +515,7 @@ int energy_weighted_density(Engine& e, const double* d_C, const double* d_eps, i
 }
 
 int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad, cudaStream_t s, float* ms_out,
-                 int precision, double mixed_threshold)
+                 int precision, double mixed_threshold, const double* d_C, int ldc, int nocc)
 {
     const int natom = e.num_atoms;
     if (!e.d_grad) {
@@ -530,7 +531,12 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
     cudaEvent_t t0 = evs.ev[0], t1 = evs.ev[1];
     cudaEventRecord(t0, s);
     GB_CUDA_TRY(cudaMemsetAsync(e.d_grad, 0, sizeof(double) * 3 * natom, s));
-    int st = scale_density(e, d_D, mixed, s);
+    int st = HF_OK;
+    if (d_C) {
+        // density fitting: derivative three-centre and metric integrals (ri_grad.cu)
+        if ((st = ri_gradient_two_electron(e, d_D, d_C, ldc, nocc, s))) return st;
+    } else {
+    st = scale_density(e, d_D, mixed, s);
     if (st) return st;
     if (mixed) {
         // FP64 for the quartets with Qs_ab Qs_cd c_max^4 max|D|^2 >= mixed_threshold, FP32 for the rest
@@ -611,6 +617,7 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
         return HF_OK;
     });
     if (st) return st;
+    }  // four-centre part
     // one-electron part
     const double kfold = std::sqrt(2.0 * std::pow(kPi, 2.5));
     for (const PairClass& pc : e.pair_classes) {
@@ -673,6 +680,25 @@ int hf_rhf_gradient(hf_engine* eng, const double* d_density, const double* d_ene
     float ms = 0.f;
     const int st = rhf_gradient(*reinterpret_cast<Engine*>(eng), d_density, d_energy_weighted_density, h_gradient,
                                 static_cast<cudaStream_t>(stream), &ms);
+    if (gradient_ms) *gradient_ms = ms;
+    return st;
+}
+
+int hf_rhf_gradient_ri(hf_engine* eng, const double* d_density, const double* d_energy_weighted_density,
+                       const double* d_coefficients, int num_occupied, double* h_gradient, double* gradient_ms,
+                       void* stream)
+{
+    clear_error();
+    if (!eng || !d_density || !d_energy_weighted_density || !d_coefficients || !h_gradient || num_occupied <= 0)
+        return set_error("null argument or non-positive num_occupied"), HF_ERR_INVALID_ARGUMENT;
+    Engine& e = *reinterpret_cast<Engine*>(eng);
+    if (e.nmol != 1) return set_error("hf_rhf_gradient_ri: single-molecule engines only"), HF_ERR_INVALID_ARGUMENT;
+    if (!e.ri) return set_error("hf_rhf_gradient_ri needs an auxiliary basis"), HF_ERR_INVALID_ARGUMENT;
+    if (num_occupied > e.num_basis)
+        return set_error("more occupied orbitals than basis functions"), HF_ERR_INVALID_ARGUMENT;
+    float ms = 0.f;
+    const int st = rhf_gradient(e, d_density, d_energy_weighted_density, h_gradient, static_cast<cudaStream_t>(stream),
+                                &ms, HF_PRECISION_FP64, 0.0, d_coefficients, e.num_basis, num_occupied);
     if (gradient_ms) *gradient_ms = ms;
     return st;
 }

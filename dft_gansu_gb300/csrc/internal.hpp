@@ -38,6 +38,7 @@ double cgto_factor(int L, const std::vector<double>& a, const std::vector<double
         cudaError_t _e = (expr);                                                                          \
         if (_e != cudaSuccess) {                                                                          \
             gb::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));                            \
+            cudaGetLastError(); /* a non-sticky error must not surface again at the next launch check */  \
             return (_e == cudaErrorMemoryAllocation) ? HF_ERR_OUT_OF_MEMORY : HF_ERR_CUDA;                \
         }                                                                                                 \
     } while (0)

@@ -387,6 +387,7 @@ int ri_set_auxiliary(Engine& e, const hf_primitive_shell* prims, int nprim, cons
             s.bf = static_cast<int>(kv.first.second);
             s.p_off = static_cast<int>(pp.size());
             s.np = static_cast<int>(kv.second.size());
+            s.atom = p0.atom_index;
             if (s.bf < 0 || s.bf + ncart(l) > naux)
                 return set_error("auxiliary basis index out of range"), HF_ERR_INVALID_ARGUMENT;
             const double C[3] = {s.x, s.y, s.z};
@@ -552,6 +553,20 @@ static int ensure_full_b(Engine& e, cudaStream_t s)
     if ((st = ri_alloc(r.d_B, nn * r.naux))) return st;
     if ((st = ri_expand(e, r.d_Bp, r.naux, r.d_B, s))) return st;
     r.have_full = true;
+    return HF_OK;
+}
+
+int ri_full_b(Engine& e, cudaStream_t s) { return ensure_full_b(e, s); }
+
+int ri_w_of(Engine& e, const double* d_D, double* d_Dt, double* d_w, cudaStream_t s)
+{
+    RiState& r = *e.ri;
+    const int n = e.num_basis;
+    const long long npk = static_cast<long long>(n) * (n + 1) / 2;
+    pack_density_kernel<<<grid_for(npk, 256, e.num_sms), 256, 0, s>>>(d_D, n, d_Dt);
+    GB_LAUNCH_CHECK();
+    ri_w_kernel<<<r.naux, 256, 0, s>>>(r.d_Bp, d_Dt, npk, d_w);
+    GB_LAUNCH_CHECK();
     return HF_OK;
 }
 

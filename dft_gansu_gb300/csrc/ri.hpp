@@ -14,6 +14,7 @@ constexpr int kMaxAuxL = 3;  // auxiliary shells up to f (cc-pVDZ-RIFIT for H..A
 struct AuxShellDev {
     double x, y, z;
     int l, bf, p_off, np;
+    int atom;  // atom of the shell (the RI gradient's third centre)
 };
 
 struct RiState {
@@ -68,6 +69,12 @@ int ri_k_density(Engine& e, const double* d_D, double* d_K, cudaStream_t s);
 int ri_fock_from_jk(Engine& e, const double* d_H, const double* d_J, const double* d_K, double* d_G, bool accumulate,
                     double* d_F, cudaStream_t s);
 int ri_work_buffers(Engine& e, double** J, double** K);
+// B in the full [P][mu][nu] layout (expanded once from the packed B)
+int ri_full_b(Engine& e, cudaStream_t s);
+// w_P = sum_mu nu B_P,mu nu D_mu nu (packed density into d_Dt, N(N+1)/2 doubles)
+int ri_w_of(Engine& e, const double* d_D, double* d_Dt, double* d_w, cudaStream_t s);
+// RI two-electron part of the RHF gradient, accumulated into e.d_grad (ri_grad.cu)
+int ri_gradient_two_electron(Engine& e, const double* d_D, const double* d_C, int ldc, int nocc, cudaStream_t s);
 
 // mixed tier (tensor cores)
 int ri_prepare_planes(Engine& e, int nocc, cudaStream_t s);

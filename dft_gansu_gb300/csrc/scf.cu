@@ -38,7 +38,7 @@ struct LoopResources {
     LoopResources()
     {
         for (auto& x : ev) cudaEventCreate(&x);
-        cudaMallocHost(&h_energy, 16 * sizeof(double));
+        cudaMallocHost(&h_energy, (8 + kPurifyStatusWords) * sizeof(double));
     }
     ~LoopResources()
     {
@@ -955,6 +955,7 @@ void hf_scf_options_default(hf_scf_options* o)
     o->convergence_method = HF_CONV_DIIS;
     o->damping_factor = 0.9;
     o->purification_max_steps = 0;
+    o->anchor_mixed_threshold = 0.0;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -1143,9 +1144,13 @@ static int rhf_scf_run(hf_engine* eng, int num_electrons, const hf_scf_options* 
             const bool low = first || dmax >= opt.anchor_threshold;
             // the pre-anchor builds only steer the density towards the anchor: quartets whose
             // bound is below kPreAnchorDrop are left out of them (the anchor builds every
-            // quartet the Schwarz screen keeps, in FP64)
-            if ((r = build_jk(e, w.D, nullptr, nullptr, low ? HF_PRECISION_MIXED : HF_PRECISION_FP64,
-                              std::numeric_limits<double>::infinity(), s, low ? kPreAnchorDrop : -1.0)))
+            // quartet the Schwarz screen keeps: in FP64, or with anchor_mixed_threshold > 0
+            // the quartets with Q_ab Q_cd max|D| below it in FP32)
+            const bool mixed_anchor = opt.anchor_mixed_threshold > 0.0;
+            if ((r = build_jk(e, w.D, nullptr, nullptr,
+                              (low || mixed_anchor) ? HF_PRECISION_MIXED : HF_PRECISION_FP64,
+                              low ? std::numeric_limits<double>::infinity() : opt.anchor_mixed_threshold, s,
+                              low ? kPreAnchorDrop : -1.0)))
                 return r;
             if (!low) anchored = true;
             fock_from_jk_kernel<<<grid_nn(nn), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.last_mixed ? e.d_Jp32 : nullptr,

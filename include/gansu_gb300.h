@@ -318,6 +318,8 @@ typedef struct {
     int purification_max_steps;     /* HF_EIGEN_PURIFICATION: SP2 steps at most (0: 100 when N <= 512, else a
                                        fixed 50); a projector that has not converged within them fails the
                                        trace/idempotency check and the SCF reruns with syevd */
+    double anchor_mixed_threshold;  /* mixed tier, direct builds: 0 = the anchor build is all FP64; > 0 = the
+                                       anchor takes quartets with Q_ab*Q_cd*max|D| below this in FP32 */
 } hf_scf_options;
 
 /* Fock-matrix update between iterations (Convergence_RHF_DIIS / _Damping,
@@ -467,6 +469,19 @@ int hf_energy_weighted_density(hf_engine* eng, const double* d_coefficients, con
  * device time. */
 int hf_rhf_gradient(hf_engine* eng, const double* d_density, const double* d_energy_weighted_density,
                     double* h_gradient, double* gradient_ms, void* stream);
+
+/* Analytic RHF gradient of the RI (density-fitted) energy of eri_method = ri
+ * (the energy of the reference's RI Fock build, src/gpu_manager.cu:1448-1632):
+ * the one-electron and nuclear terms of hf_rhf_gradient plus derivative
+ * three-centre integrals contracted with Gamma_P = c_P D - 1/2 D C_P D and
+ * derivative metric integrals with gamma_PQ = c_P c_Q - 1/2 tr(C_P D C_Q D)
+ * (c = V^-1 (T . D), C_P = sum_Q (V^-1)_PQ T_Q), formed from the occupied
+ * orbitals d_coefficients[:, :num_occupied] (row-major N x N, the SCF's
+ * coefficient output).  Needs hf_engine_set_auxiliary_basis.  FP64.  No
+ * reference counterpart. */
+int hf_rhf_gradient_ri(hf_engine* eng, const double* d_density, const double* d_energy_weighted_density,
+                       const double* d_coefficients, int num_occupied, double* h_gradient, double* gradient_ms,
+                       void* stream);
 
 /* hf_rhf_gradient with the two-electron part split by bound: derivative
  * integrals of quartets with Qs_ab Qs_cd c_max^4 max|D|^2 >= mixed_threshold in

@@ -13,8 +13,8 @@
   config 4  RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT C60 (N = 900, naux = 3960): mixed
             RI SCF within 1e-6 Eh of the FP64 RI SCF; B = L^-1 (mu nu|P) on
             sampled columns against the oracle (metric and three-centre
-            integrals restated in oracle/md_oracle.c): residual L B - T to 1e-12
-            of |T|, forward error to 1e-7 of |B| (the metric's conditioning).
+            integrals restated in oracle/md_oracle.c): backward error of L B = T
+            to 1e-13, forward error to 1e-7 of |B| (the metric's conditioning).
   config 5  batched RHF/6-31G on water clusters (H2O)n: a stratified 32 of the
             seeded 256 (two clusters for each n = 1..16), every mixed-batch
             energy within 1e-6 Eh of its own FP64 single-molecule SCF.
@@ -133,10 +133,14 @@ def test_config4_c60_ri_mixed_vs_fp64_and_b_columns(built_library, cuda):
     for (mu, nu), t in cols.items():
         ref = scipy.linalg.solve_triangular(L, t, lower=True)
         got = _np(B[:, mu, nu])
-        # residual L B - T (well conditioned): FP64 round-off of the two factorisations
-        assert np.abs(L @ got - t).max() <= 1e-12 * max(np.abs(t).max(), 1e-300), (mu, nu)
+        if not np.any(t):  # a pair the Schwarz screen removes entirely: B column zero too
+            assert not np.any(got), (mu, nu)
+            continue
+        # normwise backward error of the triangular solve: |L B - T| against |L| |B|
+        backward = np.abs(L @ got - t).max() / (np.abs(L).sum(axis=1).max() * np.abs(got).max())
+        assert backward <= 1e-13, (mu, nu, backward)
         # forward error, amplified by the metric's condition number (cc-pVDZ-RIFIT on C60)
-        assert np.abs(got - ref).max() <= 1e-7 * max(np.abs(ref).max(), 1e-300), (mu, nu)
+        assert np.abs(got - ref).max() <= 1e-7 * np.abs(ref).max(), (mu, nu)
     del B
     torch.cuda.empty_cache()
     base = {"convergence_threshold": 1e-8, "eri_method": gg.HF_ERI_RI}

@@ -164,3 +164,63 @@ def test_ri_scf_with_purification(built_library, cuda):
     rm = eng.rhf_scf(mol.num_electrons, dict(base, eigensolver=gg.HF_EIGEN_PURIFICATION,
                                              precision=gg.HF_PRECISION_MIXED, anchor_threshold=1e-2))
     assert rm["converged"] == 1 and abs(rm["total_energy"] - r64["total_energy"]) < 1e-6
+
+
+RI_CONV = {"convergence_threshold": 1e-11, "max_iter": 200, "eri_method": gg.HF_ERI_RI}
+FD_STEP = 1e-4  # bohr
+
+
+def _ri_energy(atoms, gbs):
+    mol = gg.Molecular(atoms, gg.basis_path(gbs))
+    eng = gg.Engine(mol, 1e-14)
+    eng.set_auxiliary_basis(gg.Molecular(atoms, gg.basis_path("cc-pvdz-rifit")))
+    r = eng.rhf_scf(mol.num_electrons, RI_CONV)
+    eng.close()
+    assert r["converged"] == 1
+    return r["total_energy"]
+
+
+@pytest.mark.parametrize("name,atoms,atom_subset", [
+    ("water", [(z, x + 0.01 * i, y - 0.02 * i, w + 0.015) for i, (z, x, y, w) in enumerate(geometry.water())],
+     None),
+    ("methane", geometry.alkane(1, jitter=0.03, seed=4), [0, 1]),
+])
+def test_ri_gradient_matches_finite_differences(built_library, cuda, name, atoms, atom_subset):
+    """Analytic gradient of the RI energy (derivative three-centre and metric
+    integrals, hf_rhf_gradient_ri) against central finite differences (h = 1e-4
+    bohr) of RI-SCF energies converged to 1e-11 Eh: 1e-6 Eh/bohr; cc-pVDZ with
+    cc-pVDZ-RIFIT (p shells on H, d on C/O in the AO basis, up to f in the
+    auxiliary basis)."""
+    gbs = "cc-pvdz"
+    mol = gg.Molecular(atoms, gg.basis_path(gbs))
+    eng = gg.Engine(mol, 1e-14)
+    eng.set_auxiliary_basis(gg.Molecular(atoms, gg.basis_path("cc-pvdz-rifit")))
+    r = eng.energy_and_gradient(mol.num_electrons, RI_CONV)
+    assert r["converged"] == 1
+    g = r["gradient"]
+    eng.close()
+    # no net force on an isolated molecule
+    assert np.abs(g.sum(axis=0)).max() < 1e-8
+    for a in (atom_subset if atom_subset is not None else range(len(atoms))):
+        for k in range(3):
+            plus = [list(x) for x in atoms]
+            minus = [list(x) for x in atoms]
+            plus[a][1 + k] += FD_STEP
+            minus[a][1 + k] -= FD_STEP
+            fd = (_ri_energy([tuple(x) for x in plus], gbs) - _ri_energy([tuple(x) for x in minus], gbs)) / (2 * FD_STEP)
+            assert abs(g[a, k] - fd) < 1e-6, (name, a, k, g[a, k], fd)
+
+
+def test_ri_gradient_differs_from_four_centre_gradient_by_the_fitting_error(built_library, cuda):
+    """The RI and the four-centre gradients of the same molecule agree to the
+    density-fitting error (~1e-4 Eh/bohr), not exactly: the RI one is the gradient
+    of the RI energy."""
+    atoms = geometry.water()
+    mol = gg.Molecular(atoms, gg.basis_path("cc-pvdz"))
+    eng = gg.Engine(mol, 1e-14)
+    eng.set_auxiliary_basis(gg.Molecular(atoms, gg.basis_path("cc-pvdz-rifit")))
+    g_ri = eng.energy_and_gradient(mol.num_electrons, RI_CONV)["gradient"]
+    g_4c = eng.energy_and_gradient(mol.num_electrons, {"convergence_threshold": 1e-11})["gradient"]
+    eng.close()
+    d = np.abs(g_ri - g_4c).max()
+    assert 1e-9 < d < 1e-3
