@@ -31,7 +31,7 @@ METRIC = "SCF ms/iter & gradient ms, mixed vs FP64 on 1 GB300 at |ΔE|≤1e-6 Eh
 WORKLOAD = "RHF/6-31G* n-decane C10H22 (N=194 Cartesian, 238 primitive shells), zig-zag + N(0,0.02 A) jitter"
 MIXED_THRESHOLD = 0.1
 ANCHOR_THRESHOLD = 1e-2
-ANCHOR_MIXED_THRESHOLD = 0.0
+ANCHOR_MIXED_THRESHOLD = 1e-2
 CONV = 1e-8
 GUESSES = {"core": 0, "gwh": 1, "sad": 3}  # HF_GUESS_CORE / _GWH / _SAD
 # gradient FP32 cut: on decane cc-pVDZ max|g_mixed - g_FP64| = 1.6e-7 Eh/bohr at 1.0
@@ -449,7 +449,8 @@ def run_ours(args, rank, world):
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "seed": args.seed, "precision": "mixed (full builds with every quartet "
-                       f"FP32 while max|dD| >= {args.anchor_threshold}, one FP64 build, then incremental dD builds "
+                       f"FP32 while max|dD| >= {args.anchor_threshold}, one anchor build (FP64 where "
+                       f"Q_ab*Q_cd*max|D| >= {args.anchor_mixed_threshold}, else FP32), then incremental dD builds "
                        f"with FP32 quartets where Q_ab*Q_cd*max|dD| < {args.mixed_threshold})",
                        "convergence": CONV, "l2": "flushed (512 MB write) before every step",
                        "initial_guess": args.guess or "core", "eigensolver": args.eigensolver,

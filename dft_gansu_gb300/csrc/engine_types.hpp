@@ -13,8 +13,11 @@
 
 namespace gb {
 
-// One contracted shell pair (A,B), l_A >= l_B (A >= B when l_A == l_B).
-struct ShellPairDev {
+// One contracted shell pair (A,B), l_A >= l_B (A >= B when l_A == l_B).  The
+// records are 16-byte aligned so that a whole-record copy in a kernel moves as
+// 16-byte vector loads (the gathers of pair and primitive-pair records are the
+// latency the integral kernels wait on).
+struct alignas(16) ShellPairDev {
     int A, B;          // contracted shell indices
     int bfA, bfB;      // first basis function of each shell
     int pp_off, pp_n;  // primitive-pair run
@@ -33,18 +36,19 @@ static_assert(sizeof(ShellPairDev) == 96, "ShellPairDev layout");
 // and sqrt(2 pi^{5/2}); KoP = K/p, so that a primitive quartet prefactor is
 // KoP_ab KoP_cd / sqrt(p+q).  b is the exponent of the second primitive
 // (kinetic-energy integrals).
-struct PrimPair64 {
+struct alignas(16) PrimPair64 {
     double p, invp, K, KoP, Q;
     double Px, Py, Pz;
     double PAx, PAy, PAz;
     double b;
 };
-struct PrimPair32 {
+struct alignas(16) PrimPair32 {
     float p, invp, K, KoP, Q;
     float Px, Py, Pz;
     float PAx, PAy, PAz;
     float b;
 };
+static_assert(sizeof(PrimPair32) == 48 && sizeof(PrimPair64) == 96, "primitive-pair layouts");
 
 struct FockClassLaunch {
     const ShellPairDev* pairs;     // all shell pairs (global indices)

@@ -46,7 +46,7 @@ constexpr int kPurifyThreads = kPT * kPT;
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;
 
 struct PurifyArgs {
-    int n, nocc, nt, nup, kpad, max_steps;
+    int n, nocc, nt, nup, kpad, ldp, max_steps;  // ldp: row stride of the FP32 projectors
     const double* X;
     const double* F;
     double* T1;
@@ -126,24 +126,89 @@ __device__ __forceinline__ void upper_tile(int u, int nt, int& I, int& J)
     J = I + u;
 }
 
-// panel[r][k] (r < 16, k < n) of rows (COLS = false: M[(base + r) n + k]) or
-// columns (COLS = true: M[k n + base + r]); out-of-range rows are zero.  CG: the
-// matrix was written inside this launch, read past L1.
-template <bool COLS, bool CG, class TI, class TO>
-__device__ void load_panel(const TI* __restrict__ M, int n, int base, TO* __restrict__ sm, int kpad)
+template <int V, bool CG, class TI>
+__device__ __forceinline__ void load_vec(const TI* __restrict__ p, TI (&v)[V])
 {
-    const int total = kPT * n;
-    for (int idx = threadIdx.x; idx < total; idx += kPurifyThreads) {
-        int r, k;
-        if (COLS) { k = idx / kPT; r = idx - k * kPT; }
-        else { r = idx / n; k = idx - r * n; }
-        const int row = base + r;
-        TO v = TO(0);
-        if (row < n) {
-            const long long off = COLS ? static_cast<long long>(k) * n + row : static_cast<long long>(row) * n + k;
-            v = static_cast<TO>(CG ? __ldcg(M + off) : __ldg(M + off));
+    if constexpr (V == 1) {
+        v[0] = CG ? __ldcg(p) : __ldg(p);
+    } else if constexpr (sizeof(TI) == 4) {
+        const float4* q = reinterpret_cast<const float4*>(p);
+        const float4 x = CG ? __ldcg(q) : __ldg(q);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    } else {
+        const double2* q = reinterpret_cast<const double2*>(p);
+        const double2 x = CG ? __ldcg(q) : __ldg(q);
+        v[0] = x.x; v[1] = x.y;
+    }
+}
+
+// rows base .. base + 15 of M (row stride ld, vectors of V elements: 16-byte aligned
+// rows and ld >= n rounded up to V) into sm[r][k]; kU loads in flight per thread
+template <int V, bool CG, class TI, class TO>
+__device__ __forceinline__ void load_rows(const TI* __restrict__ M, int n, int ld, int base, TO* __restrict__ sm,
+                                          int kpad)
+{
+    constexpr int kU = 4;
+    const int nv = (n + V - 1) / V;
+    const int total = kPT * nv;
+    for (int i0 = threadIdx.x; i0 < total; i0 += kU * kPurifyThreads) {
+        TI v[kU][V];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int idx = i0 + u * kPurifyThreads;
+            const int r = idx / nv, c = idx - r * nv;
+            if (idx < total && base + r < n) {
+                load_vec<V, CG>(M + static_cast<long long>(base + r) * ld + c * V, v[u]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < V; ++e) v[u][e] = TI(0);
+            }
         }
-        sm[r * kpad + k] = v;
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int idx = i0 + u * kPurifyThreads;
+            if (idx < total) {
+                const int r = idx / nv, c = idx - r * nv;
+#pragma unroll
+                for (int e = 0; e < V; ++e) sm[r * kpad + c * V + e] = static_cast<TO>(v[u][e]);
+            }
+        }
+    }
+}
+
+// panel[r][k] (r < 16, k < n) of rows (COLS = false: M[(base + r) ld + k]) or
+// columns (COLS = true: M[k ld + base + r]); out-of-range rows are zero.  CG: the
+// matrix was written inside this launch, read past L1.  Rows move as 16-byte
+// vectors where the row stride allows it; several loads are in flight per thread.
+template <bool COLS, bool CG, class TI, class TO>
+__device__ void load_panel(const TI* __restrict__ M, int n, int ld, int base, TO* __restrict__ sm, int kpad)
+{
+    if (COLS) {
+        constexpr int kU = 4;
+        const int total = kPT * n;
+        for (int i0 = threadIdx.x; i0 < total; i0 += kU * kPurifyThreads) {
+            TI v[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int idx = i0 + u * kPurifyThreads;
+                const int k = idx / kPT, r = idx - k * kPT;
+                v[u] = (idx < total && base + r < n)
+                           ? (CG ? __ldcg(M + static_cast<long long>(k) * ld + base + r)
+                                 : __ldg(M + static_cast<long long>(k) * ld + base + r))
+                           : TI(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int idx = i0 + u * kPurifyThreads;
+                if (idx < total) sm[(idx % kPT) * kpad + idx / kPT] = static_cast<TO>(v[u]);
+            }
+        }
+    } else if constexpr (sizeof(TI) == 4) {
+        if (ld % 4 == 0) load_rows<4, CG>(M, n, ld, base, sm, kpad);
+        else load_rows<1, CG>(M, n, ld, base, sm, kpad);
+    } else {
+        if (ld % 2 == 0) load_rows<2, CG>(M, n, ld, base, sm, kpad);
+        else load_rows<1, CG>(M, n, ld, base, sm, kpad);
     }
 }
 
@@ -223,11 +288,11 @@ __device__ void tile_partials(const PurifyArgs& a, int slot, int u, bool diag_ti
 }
 
 template <class T>
-__device__ __forceinline__ void store_sym(T* __restrict__ M, int n, int i, int j, T v)
+__device__ __forceinline__ void store_sym(T* __restrict__ M, int n, int ld, int i, int j, T v)
 {
     if (i < n && j < n) {
-        M[static_cast<long long>(i) * n + j] = v;
-        M[static_cast<long long>(j) * n + i] = v;
+        M[static_cast<long long>(i) * ld + j] = v;
+        M[static_cast<long long>(j) * ld + i] = v;
     }
 }
 
@@ -247,8 +312,8 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
     for (int t = blockIdx.x; t < nt * nt; t += gridDim.x) {
         const int I = t / nt, J = t % nt;
         __syncthreads();
-        load_panel<true, false>(a.X, n, I * kPT, sa, a.kpad);   // rows of X^T = columns of X
-        load_panel<false, false>(a.F, n, J * kPT, sb, a.kpad);  // F symmetric: columns = rows
+        load_panel<true, false>(a.X, n, n, I * kPT, sa, a.kpad);   // rows of X^T = columns of X
+        load_panel<false, false>(a.F, n, n, J * kPT, sb, a.kpad);  // F symmetric: columns = rows
         __syncthreads();
         const int i = I * kPT + ty, j = J * kPT + tx;
         const double v = tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n);
@@ -261,12 +326,12 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
         int I, J;
         upper_tile(u, nt, I, J);
         __syncthreads();
-        load_panel<false, true>(a.T1, n, I * kPT, sa, a.kpad);
-        load_panel<true, false>(a.X, n, J * kPT, sb, a.kpad);
+        load_panel<false, true>(a.T1, n, n, I * kPT, sa, a.kpad);
+        load_panel<true, false>(a.X, n, n, J * kPT, sb, a.kpad);
         __syncthreads();
         const int i = I * kPT + ty, j = J * kPT + tx;
         const double v = tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n);
-        store_sym(a.T2, n, i, j, v);
+        store_sym(a.T2, n, n, i, j, v);
         // |F'_ij| off the diagonal: row i of tile column J and (mirror) row j of tile column I
         __shared__ double tabs[kPT][kPT + 1];
         tabs[ty][tx] = (i < n && j < n && i != j) ? fabs(v) : 0.0;
@@ -319,7 +384,7 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
                 const double f = __ldcg(a.T2 + static_cast<long long>(i) * n + j);
                 v = static_cast<float>(((i == j ? hi : 0.0) - f) * inv);
             }
-            store_sym(a.Pa, n, i, j, v);
+            store_sym(a.Pa, n, a.ldp, i, j, v);
             tile_partials(a, 0, u, I == J, i, j, static_cast<double>(v));
         }
     }
@@ -333,9 +398,45 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
     double e = 0.0;
     int k = 0;
     bool converged = false;
+    __shared__ double totals[2];
+    const int lane = threadIdx.x & 31;
     for (; k < a.max_steps; ++k) {
-        double tr, fro;
-        tile_totals(a, k & 1, tr, fro);
+        // warp 0 issues the loads of the tile partials of P (for tr P and |P|_F^2) first,
+        // then every thread loads the panels of this CTA's first tile, so the two L2
+        // round trips overlap; the totals are summed in the same order in every CTA
+        const double2* pp = reinterpret_cast<const double2*>(a.part + static_cast<long long>(k & 1) * a.nup * 2);
+        double2 pre[4];
+        if (threadIdx.x < 32) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int u = lane + 32 * j;
+                pre[j] = u < a.nup ? __ldcg(pp + u) : make_double2(0.0, 0.0);
+            }
+        }
+        const int u0 = blockIdx.x;
+        int I0 = 0, J0 = 0;
+        if (u0 < a.nup) {
+            upper_tile(u0, nt, I0, J0);
+            load_panel<false, true>(P, n, a.ldp, I0 * kPT, fa, a.kpad);
+            load_panel<false, true>(P, n, a.ldp, J0 * kPT, fb, a.kpad);  // P symmetric: columns = rows
+        }
+        if (threadIdx.x < 32) {
+            double x = 0.0, y = 0.0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { x += pre[j].x; y += pre[j].y; }
+            for (int u = lane + 128; u < a.nup; u += 32) {
+                const double2 q = __ldcg(pp + u);
+                x += q.x;
+                y += q.y;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+                y += __shfl_xor_sync(0xffffffffu, y, o);
+            }
+            if (lane == 0) { totals[0] = x; totals[1] = y; }
+        }
+        __syncthreads();
+        const double tr = totals[0], fro = totals[1];
         e = fabs(tr - fro);
         if (e < 1e-9 * n || (k >= 2 && e < 1e-2 && e >= e2)) {
             converged = true;
@@ -344,13 +445,15 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
         e2 = e1;
         e1 = e;
         const bool square = fabs(fro - a.nocc) < fabs(2.0 * tr - fro - a.nocc);
-        for (int u = blockIdx.x; u < a.nup; u += gridDim.x) {
-            int I, J;
-            upper_tile(u, nt, I, J);
-            __syncthreads();
-            load_panel<false, true>(P, n, I * kPT, fa, a.kpad);
-            load_panel<false, true>(P, n, J * kPT, fb, a.kpad);  // P symmetric: columns = rows
-            __syncthreads();
+        for (int u = u0; u < a.nup; u += gridDim.x) {
+            int I = I0, J = J0;
+            if (u != u0) {
+                upper_tile(u, nt, I, J);
+                __syncthreads();
+                load_panel<false, true>(P, n, a.ldp, I * kPT, fa, a.kpad);
+                load_panel<false, true>(P, n, a.ldp, J * kPT, fb, a.kpad);
+                __syncthreads();
+            }
             const int i = I * kPT + ty, j = J * kPT + tx;
             const float p2 = tile_dot(fa + ty * a.kpad, fb + tx * a.kpad, n);
             float v = p2;
@@ -359,7 +462,7 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
                 const float p = (J * kPT + tx < n) ? fa[ty * a.kpad + J * kPT + tx] : 0.f;
                 v = 2.f * p - p2;
             }
-            store_sym(Pn, n, i, j, v);
+            store_sym(Pn, n, a.ldp, i, j, v);
             tile_partials(a, (k + 1) & 1, u, I == J, i, j, static_cast<double>(v));
         }
         if (!grid_barrier(a, epoch)) return;
@@ -375,24 +478,24 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
         int I, J;
         upper_tile(u, nt, I, J);
         __syncthreads();
-        load_panel<false, true>(P, n, I * kPT, sa, a.kpad);
-        load_panel<false, true>(P, n, J * kPT, sb, a.kpad);
+        load_panel<false, true>(P, n, a.ldp, I * kPT, sa, a.kpad);
+        load_panel<false, true>(P, n, a.ldp, J * kPT, sb, a.kpad);
         __syncthreads();
-        store_sym(a.T2, n, I * kPT + ty, J * kPT + tx, tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n));
+        store_sym(a.T2, n, n, I * kPT + ty, J * kPT + tx, tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n));
     }
     if (!grid_barrier(a, epoch)) return;
     for (int u = blockIdx.x; u < a.nup; u += gridDim.x) {
         int I, J;
         upper_tile(u, nt, I, J);
         __syncthreads();
-        load_panel<false, true>(a.T2, n, I * kPT, sa, a.kpad);
-        load_panel<false, true>(P, n, J * kPT, sb, a.kpad);
+        load_panel<false, true>(a.T2, n, n, I * kPT, sa, a.kpad);
+        load_panel<false, true>(P, n, a.ldp, J * kPT, sb, a.kpad);
         __syncthreads();
         const int i = I * kPT + ty, j = J * kPT + tx;
         const double p3 = tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n);
         const double p2 = (j < n) ? sa[ty * a.kpad + j] : 0.0;
         const double v = 3.0 * p2 - 2.0 * p3;
-        store_sym(a.W, n, i, j, v);
+        store_sym(a.W, n, n, i, j, v);
         tile_partials(a, 0, u, I == J, i, j, v);
     }
     if (!grid_barrier(a, epoch)) return;
@@ -404,24 +507,24 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
             int I, J;
             upper_tile(u, nt, I, J);
             __syncthreads();
-            load_panel<false, true>(a.W, n, I * kPT, sa, a.kpad);
-            load_panel<false, true>(a.W, n, J * kPT, sb, a.kpad);
+            load_panel<false, true>(a.W, n, n, I * kPT, sa, a.kpad);
+            load_panel<false, true>(a.W, n, n, J * kPT, sb, a.kpad);
             __syncthreads();
-            store_sym(a.T2, n, I * kPT + ty, J * kPT + tx, tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n));
+            store_sym(a.T2, n, n, I * kPT + ty, J * kPT + tx, tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n));
         }
         if (!grid_barrier(a, epoch)) return;
         for (int u = blockIdx.x; u < a.nup; u += gridDim.x) {
             int I, J;
             upper_tile(u, nt, I, J);
             __syncthreads();
-            load_panel<false, true>(a.T2, n, I * kPT, sa, a.kpad);
-            load_panel<false, true>(a.W, n, J * kPT, sb, a.kpad);
+            load_panel<false, true>(a.T2, n, n, I * kPT, sa, a.kpad);
+            load_panel<false, true>(a.W, n, n, J * kPT, sb, a.kpad);
             __syncthreads();
             const int i = I * kPT + ty, j = J * kPT + tx;
             const double p3 = tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n);
             const double p2 = (j < n) ? sa[ty * a.kpad + j] : 0.0;
             const double v = 3.0 * p2 - 2.0 * p3;
-            store_sym(a.T1, n, i, j, v);
+            store_sym(a.T1, n, n, i, j, v);
             tile_partials(a, 1, u, I == J, i, j, v);
         }
         if (!grid_barrier(a, epoch)) return;
@@ -442,8 +545,8 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
     for (int t = blockIdx.x; t < nt * nt; t += gridDim.x) {
         const int I = t / nt, J = t % nt;
         __syncthreads();
-        load_panel<false, false>(a.X, n, I * kPT, sa, a.kpad);
-        load_panel<false, true>(Pf, n, J * kPT, sb, a.kpad);  // P symmetric
+        load_panel<false, false>(a.X, n, n, I * kPT, sa, a.kpad);
+        load_panel<false, true>(Pf, n, n, J * kPT, sb, a.kpad);  // P symmetric
         __syncthreads();
         const int i = I * kPT + ty, j = J * kPT + tx;
         const double v = tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n);
@@ -460,10 +563,10 @@ __global__ void __launch_bounds__(kPurifyThreads, 1) purify_kernel(PurifyArgs a)
         int I, J;
         upper_tile(u, nt, I, J);
         __syncthreads();
-        load_panel<false, true>(a.T2, n, I * kPT, sa, a.kpad);
-        load_panel<false, false>(a.X, n, J * kPT, sb, a.kpad);  // rows of X = columns of X^T
+        load_panel<false, true>(a.T2, n, n, I * kPT, sa, a.kpad);
+        load_panel<false, false>(a.X, n, n, J * kPT, sb, a.kpad);  // rows of X = columns of X^T
         __syncthreads();
-        store_sym(a.D, n, I * kPT + ty, J * kPT + tx, 2.0 * tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n));
+        store_sym(a.D, n, n, I * kPT + ty, J * kPT + tx, 2.0 * tile_dot(sa + ty * a.kpad, sb + tx * a.kpad, n));
     }
     mark_phase(a, t_start, 5);
     if (blockIdx.x == 0 && threadIdx.x == 0) a.status[kPurifyStatusBarriers] = epoch;
@@ -500,11 +603,10 @@ int purify_fused(Engine& e, const double* F, int nocc, double* D, cudaStream_t s
     if (n < 1 || n > kPurifyMaxN) return set_error("fused purification: N out of range"), HF_ERR_INVALID_ARGUMENT;
     const int nt = (n + kPT - 1) / kPT;
     const int nup = nt * (nt + 1) / 2;
-    const size_t nn = static_cast<size_t>(n) * n;
+    const size_t nld = static_cast<size_t>(n) * ((n + 3) & ~3);  // projector rows padded to 4 floats
     if (!w.P32a) {
-        GB_CUDA_TRY(cudaMalloc(&w.P32a, nn * sizeof(float)));
-        GB_CUDA_TRY(cudaMalloc(&w.P32b, nn * sizeof(float)));
-        GB_CUDA_TRY(cudaMalloc(&w.P32c, nn * sizeof(float)));
+        GB_CUDA_TRY(cudaMalloc(&w.P32a, nld * sizeof(float)));
+        GB_CUDA_TRY(cudaMalloc(&w.P32b, nld * sizeof(float)));
     }
     double* status = nullptr;
     int st = purify_status(e, &status);
@@ -514,7 +616,8 @@ int purify_fused(Engine& e, const double* F, int nocc, double* D, cudaStream_t s
     a.nocc = nocc;
     a.nt = nt;
     a.nup = nup;
-    a.kpad = n | 1;  // odd row stride: conflict-free shared-memory columns
+    a.ldp = (n + 3) & ~3;             // FP32 projector rows of 16-byte multiples (float4 loads)
+    a.kpad = ((n + 3) & ~3) + 1;      // odd shared-memory row stride: conflict-free columns
     a.max_steps = max_steps > 0 ? std::min(max_steps, kPurifyMaxSteps) : kPurifyMaxSteps;
     a.X = w.X;
     a.F = F;
@@ -530,7 +633,7 @@ int purify_fused(Engine& e, const double* F, int nocc, double* D, cudaStream_t s
     a.rowpart = a.part + 4 * nup;
     const size_t smem = 2 * kPT * static_cast<size_t>(a.kpad) * sizeof(double);
     GB_CUDA_TRY(cudaFuncSetAttribute(purify_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(2 * kPT * (kPurifyMaxN | 1) * sizeof(double))));
+                                     static_cast<int>(2 * kPT * (((kPurifyMaxN + 3) & ~3) + 1) * sizeof(double))));
     int per_sm = 0;
     GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, purify_kernel, kPurifyThreads, smem));
     if (per_sm < 1) return set_error("fused purification: the kernel does not fit on an SM"), HF_ERR_CUDA;

@@ -13,8 +13,9 @@
   config 4  RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT C60 (N = 900, naux = 3960): mixed
             RI SCF within 1e-6 Eh of the FP64 RI SCF; B = L^-1 (mu nu|P) on
             sampled columns against the oracle (metric and three-centre
-            integrals restated in oracle/md_oracle.c): backward error of L B = T
-            to 1e-13, forward error to 1e-7 of |B| (the metric's conditioning).
+            integrals restated in oracle/md_oracle.c): the fitted integrals
+            B_mu nu . B_la si = T V^-1 T to 1e-10 of |B_mu nu| |B_la si|, B
+            itself to 1e-6 of its largest element (the metric's conditioning).
   config 5  batched RHF/6-31G on water clusters (H2O)n: a stratified 32 of the
             seeded 256 (two clusters for each n = 1..16), every mixed-batch
             energy within 1e-6 Eh of its own FP64 single-molecule SCF.
@@ -31,9 +32,9 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 GOLDEN = Path(__file__).parent / "golden"
 
-# the bench's mixed-tier options (bench.py: MIXED_THRESHOLD, ANCHOR_THRESHOLD)
+# the bench's mixed-tier options (bench.py: MIXED_THRESHOLD, ANCHOR_THRESHOLD, ANCHOR_MIXED_THRESHOLD)
 MIXED = {"precision": gg.HF_PRECISION_MIXED, "mixed_threshold": 0.1, "incremental": 1, "rebuild_every": 0,
-         "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": 1e-2}
+         "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": 1e-2, "anchor_mixed_threshold": 1e-2}
 
 
 def _np(t):
@@ -130,17 +131,23 @@ def test_config4_c60_ri_mixed_vs_fp64_and_b_columns(built_library, cuda):
     pairs = [tuple(int(s) for s in rng.integers(0, b.nshell, 2)) for _ in range(6)] + [(0, 0), (3, 1)]
     cols = O.ri_three_center_pairs(b, ax, pairs)
     import scipy.linalg
+    got, ref = {}, {}
     for (mu, nu), t in cols.items():
-        ref = scipy.linalg.solve_triangular(L, t, lower=True)
-        got = _np(B[:, mu, nu])
+        ref[mu, nu] = scipy.linalg.solve_triangular(L, t, lower=True)
+        got[mu, nu] = _np(B[:, mu, nu])
         if not np.any(t):  # a pair the Schwarz screen removes entirely: B column zero too
-            assert not np.any(got), (mu, nu)
+            assert not np.any(got[mu, nu]), (mu, nu)
             continue
-        # normwise backward error of the triangular solve: |L B - T| against |L| |B|
-        backward = np.abs(L @ got - t).max() / (np.abs(L).sum(axis=1).max() * np.abs(got).max())
-        assert backward <= 1e-13, (mu, nu, backward)
-        # forward error, amplified by the metric's condition number (cc-pVDZ-RIFIT on C60)
-        assert np.abs(got - ref).max() <= 1e-7 * np.abs(ref).max(), (mu, nu)
+        # forward error of B itself: two Cholesky factors of the same ill-conditioned metric
+        # (cc-pVDZ-RIFIT on C60) differ along its small-eigenvalue directions
+        assert np.abs(got[mu, nu] - ref[mu, nu]).max() <= 1e-6 * np.abs(ref[mu, nu]).max(), (mu, nu)
+    # what J and K use: the fitted integrals (mu nu|la si)_RI = B_mu nu . B_la si = T V^-1 T
+    keys = [k for k in cols if np.any(cols[k])]
+    for k1 in keys:
+        for k2 in keys:
+            g_ = got[k1] @ got[k2]
+            r_ = ref[k1] @ ref[k2]
+            assert abs(g_ - r_) <= 1e-10 * np.linalg.norm(ref[k1]) * np.linalg.norm(ref[k2]), (k1, k2, g_, r_)
     del B
     torch.cuda.empty_cache()
     base = {"convergence_threshold": 1e-8, "eri_method": gg.HF_ERI_RI}
