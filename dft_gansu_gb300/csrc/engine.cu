@@ -422,7 +422,12 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
                              static_cast<float>(a.Py),  static_cast<float>(a.Pz),   static_cast<float>(a.PAx),
                              static_cast<float>(a.PAy), static_cast<float>(a.PAz),  static_cast<float>(a.b)};
     }
-    std::vector<float> boys32(boys.begin(), boys.end());
+    // FP32 table (boys32_at): F_n .. F_{n+3} of grid point k as one 16-byte vector
+    std::vector<float> boys32(static_cast<size_t>(kBoysOrdersF) * kBoysGridF * kBoysTaylorF);
+    for (int n = 0; n < kBoysOrdersF; ++n)
+        for (int k = 0; k < kBoysGridF; ++k)
+            for (int j = 0; j < kBoysTaylorF; ++j)
+                boys32[boys32_at(n, k) + j] = static_cast<float>(boys[boys_at(n + j, k)]);
     std::vector<double> atom4(4 * num_atoms);
     for (int i = 0; i < num_atoms; ++i) {
         atom4[4 * i] = atoms[i].x; atom4[4 * i + 1] = atoms[i].y; atom4[4 * i + 2] = atoms[i].z;

@@ -30,6 +30,16 @@ constexpr double kBoysStep = 1.0 / 32.0;
 constexpr int kBoysPoints = 2049;   // grid x = 0 .. 64
 constexpr double kBoysXMax = 64.0;  // asymptotic branch beyond this (FP64)
 constexpr float kBoysXMaxF = 30.0f; // asymptotic branch beyond this (FP32)
+// FP32 table: per order n < kBoysOrdersF and grid point k < kBoysGridF (x_k = k/32 <= 30)
+// the four values F_n .. F_{n+3}(x_k) of one Taylor evaluation as one 16-byte
+// vector, orders in separate slabs: an evaluation is one aligned load, and one
+// kernel's order touches a 15 KB slab (cache-resident)
+constexpr int kBoysGridF = 961;
+constexpr int kBoysOrdersF = kBoysOrders - kBoysTaylorF + 1;
+__host__ __device__ constexpr long long boys32_at(int n, int k)
+{
+    return (static_cast<long long>(n) * kBoysGridF + k) * kBoysTaylorF;
+}
 constexpr double kPi = 3.14159265358979323846;
 
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
@@ -131,7 +141,13 @@ __host__ __device__ __forceinline__ void boys_fp32(float x, const float* __restr
     if (x < kBoysXMaxF) {
         const int k = static_cast<int>(x * 32.0f + 0.5f);
         const float dx = k * static_cast<float>(kBoysStep) - x;
-        const float* t = table + boys_at(NMAX, k);
+        static_assert(kBoysTaylorF == 4, "one float4 per FP32 Boys evaluation");
+#ifdef __CUDA_ARCH__
+        const float4 q = __ldg(reinterpret_cast<const float4*>(table + boys32_at(NMAX, k)));
+        const float t[4] = {q.x, q.y, q.z, q.w};
+#else
+        const float* t = table + boys32_at(NMAX, k);
+#endif
         float f = t[kBoysTaylorF - 1];
 #pragma unroll
         for (int j = kBoysTaylorF - 1; j >= 1; --j) f = t[j - 1] + f * dx * (1.0f / j);
