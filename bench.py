@@ -294,6 +294,7 @@ def run_ours(args, rank, world):
             if step == args.steps - 1:
                 torch.cuda.nvtx.range_pop()
         l1 = gg.kernel_launch_count()
+        mixed_stats = head.class_stats()  # per-class quartet counts of the last mixed solve
         for _ in range(args.steps):
             fp64.append(solve(opts_fp64, head))
     torch.cuda.synchronize()
@@ -347,14 +348,29 @@ def run_ours(args, rank, world):
     flush.zero_()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("fp64_build")  # the roofline's build, selectable by a profiler
     ev0.record()
     _lib_jk(head, D, Jr, Kr)
     ev1.record()
     ev1.synchronize()
+    torch.cuda.nvtx.range_pop()
     build_ms = ev0.elapsed_time(ev1)
     st = head.class_stats()
     flops = model_flops(st, "fp64")
     peak64 = gg.measure_fma_peak(0)
+    peak32 = gg.measure_fma_peak(1)
+    # the headline path: FP64 and FP32 model work of one mixed solve against the time
+    # the Fock builds took; frac = (W64 / P64 + W32 / P32) / t_fock (1 = both tiers at peak)
+    f64_mx, f32_mx = model_flops(mixed_stats, "fp64"), model_flops(mixed_stats, "fp32")
+    fock_mx_ms = mixed[-1]["fock_ms_total"]
+    t_peak_ms = (f64_mx / (peak64 * 1e12) + f32_mx / (peak32 * 1e12)) * 1e3
+    roofline_mixed = {"bound": "fp64+fp32", "fp64_model_gflop": f64_mx * 1e-9, "fp32_model_gflop": f32_mx * 1e-9,
+                      "fock_ms_per_solve": fock_mx_ms, "time_at_peak_ms": t_peak_ms,
+                      "frac": t_peak_ms / fock_mx_ms if fock_mx_ms > 0 else None,
+                      "peak_fp64_tflops": peak64, "peak_fp32_tflops": peak32,
+                      "kernel": "every direct Fock build of one mixed solve (pre-anchor FP32 builds, the anchor, "
+                                "incremental dD builds), all quartet classes and both tiers",
+                      "peak_source": "hf_measure_fma_peak FMA chains (MEASURED_PEAKS.json has neither FP64 nor FP32)"}
     achieved = flops / (build_ms * 1e-3) / 1e12
 
     # ---- DIIS extrapolation (m = 8, N x N): per call, and the allocation-free entry replayed from a CUDA graph
@@ -394,6 +410,41 @@ def run_ours(args, rank, world):
         diis = {"m": m8, "n": N, "per_call_ms": per_call, "graph_replay_ms": q0.elapsed_time(q1) / 20}
     except Exception as exc:  # the DIIS timing is informational; the SCF numbers stand without it
         diis = {"error": str(exc)[:200]}
+
+    # ---- RI-JK on C60 (N=900, naux=3960): the B build, a mixed RI SCF, and an FP64 RI SCF
+    # started from the mixed density (the same fixed point; FP64 ms/iter of its iterations)
+    c60 = None
+    if not args.skip_c60:
+        atoms_c = geometry.c60(jitter=0.01, seed=args.seed)
+        mol_c = gg.Molecular(atoms_c, gg.basis_path("cc-pvdz"))
+        eng_c = gg.Engine(mol_c, 1e-12)
+        eng_c.set_auxiliary_basis(gg.Molecular(atoms_c, gg.basis_path("cc-pvdz-rifit")))
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        c0.record()
+        eng_c.ri_intermediate_b(want=False)
+        c1.record()
+        c1.synchronize()
+        eig = gg.HF_EIGEN_PURIFICATION if args.eigensolver == "purification" else gg.HF_EIGEN_SYEVD
+        o_mx = {"convergence_threshold": CONV, "eri_method": gg.HF_ERI_RI, "precision": gg.HF_PRECISION_MIXED,
+                "anchor_threshold": args.ri_threshold, "eigensolver": eig}
+        eng_c.rhf_scf(mol_c.num_electrons, o_mx)  # warm-up
+        r_mx = eng_c.rhf_scf(mol_c.num_electrons, o_mx, want_matrices=True)
+        r_64 = eng_c.rhf_scf(mol_c.num_electrons, {"convergence_threshold": CONV, "eri_method": gg.HF_ERI_RI,
+                                                   "eigensolver": eig, "initial_guess": gg.HF_GUESS_DENSITY,
+                                                   "guess_density_a": r_mx["density"]})
+        c60 = {"workload": "RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT C60 (N=900, naux=3960 Cartesian)",
+               "b_tensor_build_ms": c0.elapsed_time(c1),
+               "mixed_ms_per_iter": r_mx["scf_ms_total"] / max(r_mx["iterations"], 1),
+               "mixed_iterations": r_mx["iterations"],
+               "fp64_ms_per_iter": r_64["scf_ms_total"] / max(r_64["iterations"], 1),
+               "fp64_iterations_from_mixed_density": r_64["iterations"],
+               "delta_E_mixed_vs_fp64": abs(r_mx["total_energy"] - r_64["total_energy"]),
+               "converged": bool(r_mx["converged"] and r_64["converged"])}
+        c60["mixed_speedup_vs_fp64"] = c60["fp64_ms_per_iter"] / c60["mixed_ms_per_iter"]
+        eng_c.close()
+        del r_mx
+        torch.cuda.empty_cache()
 
     # ---- analytic gradient on n-decane cc-pVDZ (N=260): SCF (FP64), then the gradient, timed alone
     grad = None
@@ -472,6 +523,7 @@ def run_ours(args, rank, world):
             "purification_last_call": purification,
             "gradient_ms": grad["value"] if grad else None,
             "gradient": grad,
+            "c60_ri": c60,
             "diis": diis,
             "e2e": {"value": statistics.mean(e2e_vals), "unit": "ms/iter", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
@@ -485,7 +537,13 @@ def run_ours(args, rank, world):
                          "kernel": "direct Fock build, FP64 tier (21 quartet-class launches), one launch set under the "
                                    "headline schedule",
                          "build_ms": build_ms, "model_flops": flops,
-                         "peak_source": "hf_measure_fma_peak FP64 FMA chains (MEASURED_PEAKS.json has no FP64)"},
+                         # per quartet class of this build: "la lb lc ld": [primitive quartets, contracted
+                         # quartets, model flops] (the flop model's input, for counter cross-checks)
+                         "classes": {"".join(map(str, c["class"])): [c["prim_fp64"], c["contracted_fp64"],
+                                                                      model_flops([c], "fp64")]
+                                     for c in st if c["prim_fp64"]},
+                         "peak_source": "hf_measure_fma_peak FP64 FMA chains (MEASURED_PEAKS.json has no FP64)",
+                         "mixed": roofline_mixed},
             "clocks": clocks.summary(),
         }
         if cpu:
@@ -731,6 +789,7 @@ def main():
     ap.add_argument("--sample-stride", type=int, default=4)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-gradient", action="store_true")
+    ap.add_argument("--skip-c60", action="store_true", help="leave out the C60 RI sub-object of the decane line")
     ap.add_argument("--workload", default="decane",
                     choices=["decane", "c60_ri", "decane_ri", "water_batch", "decane_grad_fd"])
     ap.add_argument("--grad-threshold", type=float, default=GRAD_THRESHOLD,

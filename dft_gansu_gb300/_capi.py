@@ -81,6 +81,7 @@ class ScfOptions(C.Structure):
         ("damping_factor", C.c_double),
         ("purification_max_steps", C.c_int),
         ("anchor_mixed_threshold", C.c_double),
+        ("incremental_drop", C.c_double),
     ]
 
 

@@ -956,6 +956,7 @@ void hf_scf_options_default(hf_scf_options* o)
     o->damping_factor = 0.9;
     o->purification_max_steps = 0;
     o->anchor_mixed_threshold = 0.0;
+    o->incremental_drop = 0.0;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -1167,7 +1168,9 @@ static int rhf_scf_run(hf_engine* eng, int num_electrons, const hf_scf_options* 
         if (incremental) {
             sub_kernel<<<grid_nn(nn), 256, 0, s>>>(w.D, w.Dprev, nn, w.dD);
             GB_LAUNCH_CHECK();
-            if ((r = build_jk(e, w.dD, nullptr, nullptr, opt.precision, opt.mixed_threshold, s))) return r;
+            if ((r = build_jk(e, w.dD, nullptr, nullptr, opt.precision, opt.mixed_threshold, s,
+                              opt.incremental_drop > 0.0 ? opt.incremental_drop : -1.0)))
+                return r;
         } else {
             const int prec = (opt.precision == HF_PRECISION_MIXED) ? opt.full_build_precision : opt.precision;
             if ((r = build_jk(e, w.D, nullptr, nullptr, prec, opt.mixed_threshold, s))) return r;

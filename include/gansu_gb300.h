@@ -320,6 +320,9 @@ typedef struct {
                                        trace/idempotency check and the SCF reruns with syevd */
     double anchor_mixed_threshold;  /* mixed tier, direct builds: 0 = the anchor build is all FP64; > 0 = the
                                        anchor takes quartets with Q_ab*Q_cd*max|D| below this in FP32 */
+    double incremental_drop;        /* incremental dD builds (direct): quartets whose Qs_ab*Qs_cd times the
+                                       largest |dD| of the shell blocks they read is below this are left out
+                                       (0: the Schwarz threshold) */
 } hf_scf_options;
 
 /* Fock-matrix update between iterations (Convergence_RHF_DIIS / _Damping,
