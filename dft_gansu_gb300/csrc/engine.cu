@@ -90,7 +90,7 @@ double prim_pair_bound_t(const PrimPair64& pp, double abx, double aby, double ab
                                 for (int phi = 0; phi <= az + bz; ++phi) {
                                     const double e2 = Ex.e[ax][bx][tau] * Ey.e[ay][by][nu] * Ez.e[az][bz][phi];
                                     const double sg = ((tau + nu + phi) & 1) ? -1.0 : 1.0;
-                                    s += e1 * sg * e2 * R.r[t + tau][u + nu][v + phi];
+                                    s += e1 * sg * e2 * R(t + tau, u + nu, v + phi);
                                 }
                     }
             (void)LAB;

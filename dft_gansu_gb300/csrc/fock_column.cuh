@@ -218,6 +218,10 @@ __device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const S
     int count = 0;
     const typename TierTypes<T>::Geom gb_(bp), gk_(kp);
     const T qket_max = gk_.qmax;
+    constexpr bool kPrefetch = sizeof(T) == 4;  // next ket record one iteration ahead (FP32 tier)
+    const PP* __restrict__ kpp = pp + kp.pp_off;
+    PP pk_next;
+    if constexpr (kPrefetch) pk_next = kpp[0];
     for (int ip = 0; ip < bp.pp_n; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
         if (pb.Q * qket_max < thr) continue;
@@ -227,7 +231,13 @@ __device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const S
         Ey.build(pb.PAy, pb.PAy + gb_.y, oo2p);
         Ez.build(pb.PAz, pb.PAz + gb_.z, oo2p);
         for (int jq = 0; jq < kp.pp_n; ++jq) {
-            const PP pk = pp[kp.pp_off + jq];
+            PP pk;
+            if constexpr (kPrefetch) {
+                pk = pk_next;
+                pk_next = kpp[jq + 1 < kp.pp_n ? jq + 1 : 0];
+            } else {
+                pk = kpp[jq];
+            }
             if (pb.Q * pk.Q < thr) continue;
             ++count;
             T e[3][PC];
@@ -275,7 +285,7 @@ __device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const S
                             T acc = T(0);
 #pragma unroll
                             for (int f = 0; f < PC; ++f)
-                                if (t + u + v + f <= LT) acc += e[2][f] * R.r[t][u][v + f];
+                                if (t + u + v + f <= LT) acc += e[2][f] * R(t, u, v + f);
                             zb[hx(t, u, v)] = acc;
                         }
             }

@@ -143,6 +143,12 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
     const T qket_max = gk_.qmax;
     const T abx = gb_.x, aby = gb_.y, abz = gb_.z;
     const T cdx = gk_.x, cdy = gk_.y, cdz = gk_.z;
+    // FP32 tier (latency-bound): the next ket primitive-pair record is loaded one
+    // iteration ahead (wrapping to the first for the next bra primitive)
+    constexpr bool kPrefetch = sizeof(T) == 4;
+    const PP* __restrict__ kpp = pp + kp.pp_off;
+    PP pk_next;
+    if constexpr (kPrefetch) pk_next = kpp[0];
     for (int ip = 0; ip < bp.pp_n; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
         if (pb.Q * qket_max < thr) continue;
@@ -153,7 +159,13 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
         Ey.build(pb.PAy, pb.PAy + aby, oo2p);
         Ez.build(pb.PAz, pb.PAz + abz, oo2p);
         for (int jq = 0; jq < kp.pp_n; ++jq) {
-            const PP pk = pp[kp.pp_off + jq];
+            PP pk;
+            if constexpr (kPrefetch) {
+                pk = pk_next;
+                pk_next = kpp[jq + 1 < kp.pp_n ? jq + 1 : 0];
+            } else {
+                pk = kpp[jq];
+            }
             if (pb.Q * pk.Q < thr) continue;
             ++count;
             const T q = pk.p;
@@ -180,7 +192,7 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
                 const int cx = cart_exp(LC, ic, 0), cy = cart_exp(LC, ic, 1), cz = cart_exp(LC, ic, 2);
                 const int dx = cart_exp(LD, id, 0), dy = cart_exp(LD, id, 1), dz = cart_exp(LD, id, 2);
                 // ket contraction into the bra Hermite index
-                T Xh[LAB + 1][LAB + 1][LAB + 1];
+                T Xh[nherm(LAB)];
 #pragma unroll
                 for (int t = 0; t <= LAB; ++t)
 #pragma unroll
@@ -199,12 +211,12 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
                                     for (int phi = 0; phi <= LCD; ++phi) {
                                         if (phi > cz + dz) continue;
                                         const T c = exy * Fz.e[cz][dz][phi];
-                                        const T rv = R.r[t + tau][u + nu][v + phi];
+                                        const T rv = R(t + tau, u + nu, v + phi);
                                         if ((tau + nu + phi) & 1) s -= c * rv; else s += c * rv;
                                     }
                                 }
                             }
-                            Xh[t][u][v] = s;
+                            Xh[hermite_index(t, u, v)] = s;
                         }
                 // bra contraction
 #pragma unroll
@@ -224,7 +236,7 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
 #pragma unroll
                                 for (int v = 0; v <= LAB; ++v) {
                                     if (v > az + bz) continue;
-                                    s += exy * Ez.e[az][bz][v] * Xh[t][u][v];
+                                    s += exy * Ez.e[az][bz][v] * Xh[hermite_index(t, u, v)];
                                 }
                             }
                         }

@@ -462,7 +462,7 @@ grad_one_electron_kernel(const ShellPairDev* __restrict__ pairs, int begin, int 
                                 for (int u = 0; u <= aa[1] + b[1]; ++u)
                                     for (int v = 0; v <= aa[2] + b[2]; ++v)
                                         acc += Ex.e[aa[0]][b[0]][t] * Ey.e[aa[1]][b[1]][u] * Ez.e[aa[2]][b[2]][v] *
-                                               R.r[t][u][v];
+                                               R(t, u, v);
                             dA += c * acc;
                         }
                         // operator centre: d/dC_k R_tuv(P - C) = -R_{tuv + 1_k}
@@ -471,7 +471,7 @@ grad_one_electron_kernel(const ShellPairDev* __restrict__ pairs, int begin, int 
                             for (int u = 0; u <= a[1] + b[1]; ++u)
                                 for (int v = 0; v <= a[2] + b[2]; ++v) {
                                     const double ev = Ex.e[a[0]][b[0]][t] * Ey.e[a[1]][b[1]][u] * Ez.e[a[2]][b[2]][v];
-                                    const double rv = (k == 0) ? R.r[t + 1][u][v] : (k == 1) ? R.r[t][u + 1][v] : R.r[t][u][v + 1];
+                                    const double rv = (k == 0) ? R(t + 1, u, v) : (k == 1) ? R(t, u + 1, v) : R(t, u, v + 1);
                                     dC -= ev * rv;
                                 }
                         gA[k] += dwv * dA;

@@ -211,8 +211,8 @@ __global__ void __launch_bounds__(kGradThreads) grad_class_kernel(const GradLaun
 #pragma unroll
                             for (int f = 0; f < PD; ++f)
                                 if (t + u + v + f <= LT) {
-                                    a0 += e0[2][f] * R.r[t][u][v + f];
-                                    aD += eD[2][f] * R.r[t][u][v + f];
+                                    a0 += e0[2][f] * R(t, u, v + f);
+                                    aD += eD[2][f] * R(t, u, v + f);
                                 }
                             z0[gidx(t, u, v)] = a0;
                             zD[gidx(t, u, v)] = aD;

@@ -221,15 +221,30 @@ struct HermiteE {
 };
 
 // ------------------------------------------------------- Hermite R (3D)
-// R[t][u][v] = R^{0}_{tuv} for t+u+v <= L, given Fs[n] = R^{n}_{000}.  In-place
-// evaluation: pass n overwrites levels k = L-n .. 1 in descending order, which
-// only reads R^{n+1} values of lower levels not yet overwritten in the pass.
+// Packed position of the Hermite index (t, u, v): levels k = t + u + v in
+// ascending order, within a level by descending t, then descending u.
+__host__ __device__ constexpr int hermite_index(int t, int u, int v)
+{
+    return (t + u + v) * (t + u + v + 1) * (t + u + v + 2) / 6 + (u + v) * (u + v + 1) / 2 + v;
+}
+
+// R(t, u, v) = R^{0}_{tuv} for t+u+v <= L, given Fs[n] = R^{n}_{000}, in packed
+// storage (nherm(L) values, so that fully unrolled kernels keep the table in
+// registers).  In-place evaluation: pass n overwrites levels k = L-n .. 1 in
+// descending order, which only reads R^{n+1} values of lower levels not yet
+// overwritten in the pass.
 template <class T, int L>
 struct HermiteR {
-    T r[L + 1][L + 1][L + 1];
+    T r[nherm(L)];
+    __host__ __device__ __forceinline__ T& operator()(int t, int u, int v) { return r[hermite_index(t, u, v)]; }
+    __host__ __device__ __forceinline__ const T& operator()(int t, int u, int v) const
+    {
+        return r[hermite_index(t, u, v)];
+    }
     __host__ __device__ __forceinline__ void build(const T (&Fs)[L + 1], T X, T Y, T Z)
     {
-        r[0][0][0] = Fs[L];
+        HermiteR& R = *this;
+        R(0, 0, 0) = Fs[L];
 #pragma unroll
         for (int n = L - 1; n >= 0; --n) {
 #pragma unroll
@@ -241,20 +256,20 @@ struct HermiteR {
                         const int v = k - t - u;
                         T val;
                         if (t > 0) {
-                            val = X * r[t - 1][u][v];
-                            if (t > 1) val += T(t - 1) * r[t - 2][u][v];
+                            val = X * R(t - 1, u, v);
+                            if (t > 1) val += T(t - 1) * R(t - 2, u, v);
                         } else if (u > 0) {
-                            val = Y * r[0][u - 1][v];
-                            if (u > 1) val += T(u - 1) * r[0][u - 2][v];
+                            val = Y * R(0, u - 1, v);
+                            if (u > 1) val += T(u - 1) * R(0, u - 2, v);
                         } else {
-                            val = Z * r[0][0][v - 1];
-                            if (v > 1) val += T(v - 1) * r[0][0][v - 2];
+                            val = Z * R(0, 0, v - 1);
+                            if (v > 1) val += T(v - 1) * R(0, 0, v - 2);
                         }
-                        r[t][u][v] = val;
+                        R(t, u, v) = val;
                     }
                 }
             }
-            r[0][0][0] = Fs[n];
+            R(0, 0, 0) = Fs[n];
         }
     }
 };

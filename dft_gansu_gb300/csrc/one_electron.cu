@@ -90,7 +90,7 @@ one_electron_kernel(const ShellPairDev* __restrict__ pairs, int begin, int count
 #pragma unroll
                             for (int v = 0; v <= L; ++v) {
                                 if (v > az + bz) continue;
-                                acc += Ex.e[ax][bx][t] * Ey.e[ay][by][u] * Ez.e[az][bz][v] * R.r[t][u][v];
+                                acc += Ex.e[ax][bx][t] * Ey.e[ay][by][u] * Ez.e[az][bz][v] * R(t, u, v);
                             }
                         }
                     }

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kRiThreads) three_center_kernel(const ThreeCen
                                         if (phi > pz) break;
                                         if (t + tau + u + nu + v + phi > L) continue;
                                         const double w = Ep.e[px][0][tau] * Ep.e[py][0][nu] * Ep.e[pz][0][phi] *
-                                                         R.r[t + tau][u + nu][v + phi];
+                                                         R(t + tau, u + nu, v + phi);
                                         s += ((tau + nu + phi) & 1) ? -w : w;
                                     }
                                 }

@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kRiGradThreads) ri_deriv_kernel(const RiDerivA
                                     for (int phi = 0; phi <= LP; ++phi) {
                                         if (phi > pz) break;
                                         const double c = Ep.e[px][0][tau] * Ep.e[py][0][nu] * Ep.e[pz][0][phi] *
-                                                         R.r[t + tau][u + nu][v + phi];
+                                                         R(t + tau, u + nu, v + phi);
                                         s += ((tau + nu + phi) & 1) ? -c : c;
                                     }
                                 }
