@@ -6,7 +6,9 @@
 //  2. shell pairs per class (la >= lb) with their primitive pairs: Gaussian
 //     product data, the prefactor K and the reference's primitive Schwarz
 //     bound Q = sqrt(max_comp (ab|ab)) (src/schwarz.txt:239-470), evaluated on
-//     the host with the same MD templates the kernels use;
+//     the host with the same MD templates the kernels use; the primitive
+//     pairs of a shell pair are stored by bound, largest first, so the
+//     kernels' primitive loops end at the first pair that fails the test;
 //  3. pairs of each class sorted by Qs = sum of primitive bounds (descending),
 //     so that for a bra the kets passing Qs_bra*Qs_ket >= thr form a prefix.
 //     Qs >= max primitive bound, so this contracted pre-test never drops a
@@ -336,6 +338,10 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
                             qm = std::max(qm, pp.Q);
                             t.pp.push_back(pp);
                         }
+                    // largest bound first: a kernel's primitive loop over this pair ends at
+                    // the first primitive pair that fails the Schwarz test
+                    std::stable_sort(t.pp.begin(), t.pp.end(),
+                                     [](const PrimPair64& x, const PrimPair64& y) { return x.Q > y.Q; });
                     t.sp.Qs = qs;
                     t.sp.Qmax = qm;
                     tmp.push_back(std::move(t));

@@ -124,14 +124,14 @@ __device__ int quartet_column(const ShellPairDev& bp, const ShellPairDev& kp, in
     const T qket_max = gk_.qmax;
     for (int ip = 0; ip < bp.pp_n; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
-        if (pb.Q * qket_max < thr) continue;
+        if (pb.Q * qket_max < thr) break;  // primitive pairs sorted by Q (descending)
         const T oo2p = T(0.5) * pb.invp;
         hermite_e_rt<T>(la, lb, pb.PAx, pb.PAx + gb_.x, oo2p, ex);
         hermite_e_rt<T>(la, lb, pb.PAy, pb.PAy + gb_.y, oo2p, ey);
         hermite_e_rt<T>(la, lb, pb.PAz, pb.PAz + gb_.z, oo2p, ez);
         for (int jq = 0; jq < kp.pp_n; ++jq) {
             const PP pk = pp[kp.pp_off + jq];
-            if (pb.Q * pk.Q < thr) continue;
+            if (pb.Q * pk.Q < thr) break;
             ++count;
             const T oo2q = T(0.5) * pk.invp;
             hermite_e_rt<T>(lc, ld, pk.PAx, pk.PAx + gk_.x, oo2q, fx);
@@ -188,6 +188,7 @@ __device__ int quartet_column(const ShellPairDev& bp, const ShellPairDev& kp, in
 template <class T>
 struct RuntimeColumn {
     static constexpr int kNAB = fock_column::kNAB;
+    static constexpr int kNA = 0, kNB = 0, kND = 0;  // runtime angular momenta
     __device__ static int eval(const ShellPairDev& bp, const ShellPairDev& kp, int cd,
                                const typename FockTypes<T>::PP* __restrict__ pp, const T* __restrict__ boys, T thr,
                                T* I)
@@ -224,7 +225,7 @@ __device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const S
     if constexpr (kPrefetch) pk_next = kpp[0];
     for (int ip = 0; ip < bp.pp_n; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
-        if (pb.Q * qket_max < thr) continue;
+        if (pb.Q * qket_max < thr) break;  // primitive pairs sorted by Q (descending)
         const T oo2p = T(0.5) * pb.invp;
         HermiteE<T, LA, LB> Ex, Ey, Ez;
         Ex.build(pb.PAx, pb.PAx + gb_.x, oo2p);
@@ -238,7 +239,10 @@ __device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const S
             } else {
                 pk = kpp[jq];
             }
-            if (pb.Q * pk.Q < thr) continue;
+            if (pb.Q * pk.Q < thr) {
+                if constexpr (kPrefetch) pk_next = kpp[0];
+                break;
+            }
             ++count;
             T e[3][PC];
             {
@@ -339,6 +343,7 @@ __device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const S
 template <class T, int LA, int LB, int LC, int LD>
 struct ClassColumn {
     static constexpr int kNAB = ncart(LA) * ncart(LB);
+    static constexpr int kNA = ncart(LA), kNB = ncart(LB), kND = ncart(LD);  // compile-time digestion bounds
     __device__ static int eval(const ShellPairDev& bp, const ShellPairDev& kp, int cd,
                                const typename FockTypes<T>::PP* __restrict__ pp, const T* __restrict__ boys, T thr,
                                T* I)
@@ -396,35 +401,45 @@ __global__ void __launch_bounds__(kFockThreads) column_kernel(const FockClassLau
         const T* __restrict__ Dp = static_cast<const T*>(L.density) + (active ? bp.mbase : 0);
         T* __restrict__ Jp = TierTypes<T>::J(L) + (active ? bp.mbase : 0);
         T* __restrict__ Kp = TierTypes<T>::K(L) + (active ? bp.mbase : 0);
-        const int na = ncart(bp.la), nb = ncart(bp.lb), nc = ncart(kp.la), nd = ncart(kp.lb);
+        // with a compile-time class every digestion bound is a constant, so the
+        // loops unroll and I stays in registers
+        constexpr bool kCT = Column::kNA > 0;
+        const int na = kCT ? Column::kNA : ncart(bp.la), nb = kCT ? Column::kNB : ncart(bp.lb);
+        const int nd = kCT ? Column::kND : ncart(kp.lb);
         const int ic = cd / (nd > 0 ? nd : 1), id = cd % (nd > 0 ? nd : 1);
         const int c = kp.bfA + ic, d = kp.bfB + id;
-        (void)nc;
         // J'_ab (partial over cd): warp-reduced when the bra is warp-uniform
         const int bra0 = __shfl_sync(0xffffffffu, bra, 0);
         const bool uniform_bra = __all_sync(0xffffffffu, (!active) || bra == bra0) && bra0 >= 0;
-        const int na0 = __shfl_sync(0xffffffffu, na, 0), nb0 = __shfl_sync(0xffffffffu, nb, 0);
+        const int na0 = kCT ? Column::kNA : __shfl_sync(0xffffffffu, na, 0);
+        const int nb0 = kCT ? Column::kNB : __shfl_sync(0xffffffffu, nb, 0);
         const int bfA0 = __shfl_sync(0xffffffffu, bp.bfA, 0), bfB0 = __shfl_sync(0xffffffffu, bp.bfB, 0);
         const int N0 = __shfl_sync(0xffffffffu, N, 0), mbase0 = __shfl_sync(0xffffffffu, active ? bp.mbase : 0, 0);
         T* __restrict__ Jp0 = TierTypes<T>::J(L) + mbase0;
         const T dcd = active ? Dp[c * N + d] : T(0);
         if (uniform_bra) {
+#pragma unroll
             for (int ab = 0; ab < na0 * nb0; ++ab) {
                 const T s = warp_sum(dcd * I[ab] * fsym);
                 if (lane == 0) atomicAdd(&Jp0[(bfA0 + ab / nb0) * N0 + bfB0 + ab % nb0], s);
             }
         } else if (active) {
+#pragma unroll
             for (int ab = 0; ab < na * nb; ++ab)
                 atomicAdd(&Jp[(bp.bfA + ab / nb) * N + bp.bfB + ab % nb], dcd * I[ab] * fsym);
         }
         if (!active) continue;
         T jcd = T(0);
+#pragma unroll
         for (int ia = 0; ia < na; ++ia)
+#pragma unroll
             for (int ib = 0; ib < nb; ++ib) jcd += Dp[(bp.bfA + ia) * N + bp.bfB + ib] * I[ia * nb + ib];
         atomicAdd(&Jp[c * N + d], jcd * fsym);
+#pragma unroll
         for (int ia = 0; ia < na; ++ia) {
             const int a = bp.bfA + ia;
             T kac = T(0), kad = T(0);
+#pragma unroll
             for (int ib = 0; ib < nb; ++ib) {
                 const int b = bp.bfB + ib;
                 kac += Dp[b * N + d] * I[ia * nb + ib];
@@ -433,9 +448,11 @@ __global__ void __launch_bounds__(kFockThreads) column_kernel(const FockClassLau
             atomicAdd(&Kp[a * N + c], kac * fsym);
             atomicAdd(&Kp[a * N + d], kad * fsym);
         }
+#pragma unroll
         for (int ib = 0; ib < nb; ++ib) {
             const int b = bp.bfB + ib;
             T kbd = T(0), kbc = T(0);
+#pragma unroll
             for (int ia = 0; ia < na; ++ia) {
                 const int a = bp.bfA + ia;
                 kbd += Dp[a * N + c] * I[ia * nb + ib];

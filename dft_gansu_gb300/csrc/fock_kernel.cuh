@@ -151,7 +151,9 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
     if constexpr (kPrefetch) pk_next = kpp[0];
     for (int ip = 0; ip < bp.pp_n; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
-        if (pb.Q * qket_max < thr) continue;
+        // the primitive pairs of a shell pair are sorted by Q (descending), so the
+        // first primitive quartet that fails the Schwarz test ends its loop
+        if (pb.Q * qket_max < thr) break;
         const T p = pb.p;
         HermiteE<T, LA, LB> Ex, Ey, Ez;
         const T oo2p = T(0.5) * pb.invp;
@@ -166,7 +168,10 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
             } else {
                 pk = kpp[jq];
             }
-            if (pb.Q * pk.Q < thr) continue;
+            if (pb.Q * pk.Q < thr) {
+                if constexpr (kPrefetch) pk_next = kpp[0];
+                break;
+            }
             ++count;
             const T q = pk.p;
             HermiteE<T, LC, LD> Fx, Fy, Fz;

@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
                 }
             for (int jq = 0; jq < kp.pp_n; ++jq) {
                 const PP pk = pp[kp.pp_off + jq];
-                if (pb.Q * pk.Q < thr) continue;
+                if (pb.Q * pk.Q < thr) break;  // primitive pairs sorted by Q (descending)
                 const T gamma2 = T(2) * (pk.p - pk.b);
                 const T oo2q = T(0.5) * pk.invp;
                 grad_e_table<T>(lc + 1, ld, pk.PAx, pk.PAx + kABx, oo2q, fx);

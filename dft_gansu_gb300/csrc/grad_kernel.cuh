@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kGradThreads) grad_class_kernel(const GradLaun
         T gA[3] = {0, 0, 0}, gP[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
         for (int jq = 0; jq < kp.pp_n; ++jq) {
             const PP pk = pp[kp.pp_off + jq];
-            if (pb.Q * pk.Q < thr) continue;
+            if (pb.Q * pk.Q < thr) break;
             const T gamma2 = T(2) * (pk.p - pk.b);
             const T oo2q = T(0.5) * pk.invp;
             // coefficient vectors of the item's (c, d), (-1)^tau folded in:
