@@ -31,7 +31,11 @@ METRIC = "SCF ms/iter & gradient ms, mixed vs FP64 on 1 GB300 at |ΔE|≤1e-6 Eh
 WORKLOAD = "RHF/6-31G* n-decane C10H22 (N=194 Cartesian, 238 primitive shells), zig-zag + N(0,0.02 A) jitter"
 MIXED_THRESHOLD = 0.1
 ANCHOR_THRESHOLD = 1e-2
-ANCHOR_MIXED_THRESHOLD = 1e-2
+# anchor FP32 cut and incremental drop: on decane 6-31G* (cut 0.1) |dE| vs FP64 = 8e-9 Eh and
+# max |d eps| = 1.1e-6 Eh at (3e-2, 3e-10), against 2.2e-8 / 1.7e-6 at (1e-2, 0) and 7.4e-8 /
+# 6.2e-6 at (1e-1, 3e-10)
+ANCHOR_MIXED_THRESHOLD = 3e-2
+INCREMENTAL_DROP = 3e-10
 CONV = 1e-8
 GUESSES = {"core": 0, "gwh": 1, "sad": 3}  # HF_GUESS_CORE / _GWH / _SAD
 # gradient FP32 cut: on decane cc-pVDZ max|g_mixed - g_FP64| = 1.6e-7 Eh/bohr at 1.0
@@ -327,7 +331,7 @@ def run_ours(args, rank, world):
     opts_mixed = {"convergence_threshold": CONV, "precision": gg.HF_PRECISION_MIXED,
                   "mixed_threshold": args.mixed_threshold, "incremental": 1, "rebuild_every": 0,
                   "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": args.anchor_threshold,
-                  "anchor_mixed_threshold": args.anchor_mixed_threshold}
+                  "anchor_mixed_threshold": args.anchor_mixed_threshold, "incremental_drop": args.incremental_drop}
     opts_fp64 = {"convergence_threshold": CONV}
     for o in (opts_mixed, opts_fp64):
         o["initial_guess"] = GUESSES[args.guess or "core"]
@@ -584,7 +588,8 @@ def run_ours(args, rank, world):
             "config": {"workload": WORKLOAD, "seed": args.seed, "precision": "mixed (full builds with every quartet "
                        f"FP32 while max|dD| >= {args.anchor_threshold}, one anchor build (FP64 where "
                        f"Q_ab*Q_cd*max|D| >= {args.anchor_mixed_threshold}, else FP32), then incremental dD builds "
-                       f"with FP32 quartets where Q_ab*Q_cd*max|dD| < {args.mixed_threshold})",
+                       f"with FP32 quartets where Q_ab*Q_cd*max|dD| < {args.mixed_threshold}, quartets with "
+                       f"Q_ab*Q_cd*(max |dD| over the 6 shell blocks read) < {args.incremental_drop} left out)",
                        "convergence": CONV, "l2": "flushed (512 MB write) before every step",
                        "initial_guess": args.guess or "core", "eigensolver": args.eigensolver,
                        "fock_schedule": args.schedule,
@@ -862,6 +867,8 @@ def main():
     ap.add_argument("--anchor-threshold", type=float, default=ANCHOR_THRESHOLD)
     ap.add_argument("--anchor-mixed-threshold", type=float, default=ANCHOR_MIXED_THRESHOLD,
                     help="FP32 cut of the anchor build on Q_ab*Q_cd*max|D| (0: an all-FP64 anchor)")
+    ap.add_argument("--incremental-drop", type=float, default=INCREMENTAL_DROP,
+                    help="dD builds leave out quartets with Q_ab*Q_cd*(block max |dD|) below this (0: Schwarz cut)")
     ap.add_argument("--sample-stride", type=int, default=4)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-gradient", action="store_true")

@@ -32,9 +32,11 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 GOLDEN = Path(__file__).parent / "golden"
 
-# the bench's mixed-tier options (bench.py: MIXED_THRESHOLD, ANCHOR_THRESHOLD, ANCHOR_MIXED_THRESHOLD)
+# the bench's mixed-tier options (bench.py: MIXED_THRESHOLD, ANCHOR_THRESHOLD, ANCHOR_MIXED_THRESHOLD,
+# INCREMENTAL_DROP)
 MIXED = {"precision": gg.HF_PRECISION_MIXED, "mixed_threshold": 0.1, "incremental": 1, "rebuild_every": 0,
-         "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": 1e-2, "anchor_mixed_threshold": 1e-2}
+         "full_build_precision": gg.HF_PRECISION_FP64, "anchor_threshold": 1e-2, "anchor_mixed_threshold": 3e-2,
+         "incremental_drop": 3e-10}
 
 
 def _np(t):
