@@ -191,7 +191,7 @@ double aux_prim_bound(int l, const PrimPair64& q, const double* boys)
 Engine::~Engine()
 {
     void* ptrs[] = {d_pairs,  d_pp64,   d_pp32,       d_boys64,     d_boys32,     d_scale,   d_atoms,
-                    d_entry_bra, d_entry_cnt, d_entry_lo0, d_pair_qs, d_off_static, d_cp_meta, plan.off64, plan.off32,
+                    d_entry_bra, d_entry_cnt, d_entry_lo0, d_entry_prim, d_pair_qs, d_off_static, d_cp_meta, plan.off64, plan.off32,
                     plan.lo32, d_Dp64, d_Dp32, d_Jp, d_Kp, d_Jp32, d_Kp32, d_scalar, d_counters, scf.S, scf.H, scf.X, scf.F,
                     scf.D, scf.Dprev, scf.G, scf.dD, scf.C, scf.W, scf.eps, scf.T1, scf.T2, scf.E, scf.Es,
                     scf.Fs, scf.work, scf.diis, scf.J, scf.K, scf.info, scf.work_j, d_grad, d_shell_atom, d_goff64, d_goff32,
@@ -401,11 +401,27 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
                     int cnt = lo;
                     if (X == Y) cnt = std::min(cnt, i - g.first + 1);  // each unordered pair once
                     if (cnt <= 0) continue;
-                    e->entry_bra.push_back(px.begin + i);
-                    e->entry_lo0.push_back(g.first);
-                    e->entry_cnt.push_back(cnt);
-                    acc += cnt;
-                    e->off_static.push_back(acc);
+                    e->unique_quartets += cnt;
+                    // a bra whose primitive loops are long is split over several entries, each
+                    // with a range of its primitive pairs (their partial integrals are digested
+                    // separately), so that no lane runs more than about kPrimPerItem primitive
+                    // quartets of a quartet while the others of its warp wait
+                    const ShellPairDev& bp = e->pairs[px.begin + i];
+                    const int nb = bp.pp_n, nk = e->pairs[py.begin + g.first].pp_n;
+                    const int nsplit = std::min(nb, std::max(1, (nb * nk + kPrimPerItem - 1) / kPrimPerItem));
+                    const int chunk = (nb + nsplit - 1) / nsplit;
+                    double qket = 0.0;  // largest primitive bound among the entry's kets
+                    for (int k = 0; k < cnt; ++k) qket = std::max(qket, e->pairs[py.begin + g.first + k].Qmax);
+                    for (int p0 = 0; p0 < nb; p0 += chunk) {
+                        // a later range whose largest bound cannot pass with any ket adds nothing
+                        if (p0 > 0 && e->pp64[bp.pp_off + p0].Q * qket < thr) break;
+                        e->entry_bra.push_back(px.begin + i);
+                        e->entry_lo0.push_back(g.first);
+                        e->entry_cnt.push_back(cnt);
+                        e->entry_prim.push_back(p0 | (std::min(nb, p0 + chunk) << 16));
+                        acc += cnt;
+                        e->off_static.push_back(acc);
+                    }
                 }
             }
             cp.nentry = static_cast<int>(e->entry_bra.size()) - cp.entry_begin;
@@ -452,6 +468,7 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
     e->d_entry_bra = dev_upload(e->entry_bra, st);
     e->d_entry_cnt = dev_upload(e->entry_cnt, st);
     e->d_entry_lo0 = dev_upload(lo0, st);
+    e->d_entry_prim = dev_upload(e->entry_prim, st);
     e->d_pair_qs = dev_upload(qs, st);
     e->d_off_static = dev_upload(e->off_static, st);
     {
@@ -493,7 +510,7 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
     e->bytes_h2d = static_cast<long long>(
         e->pairs.size() * sizeof(ShellPairDev) + e->pp64.size() * sizeof(PrimPair64) + pp32.size() * sizeof(PrimPair32) +
         boys.size() * (sizeof(double) + sizeof(float)) + e->scale.size() * sizeof(double) + atom4.size() * sizeof(double) +
-        (3 * e->entry_bra.size()) * sizeof(int) + qs.size() * sizeof(double) +
+        (4 * e->entry_bra.size()) * sizeof(int) + qs.size() * sizeof(double) +
         e->off_static.size() * sizeof(long long) + 4 * e->class_pairs.size() * sizeof(int));
     *out = reinterpret_cast<hf_engine*>(e.release());
     return HF_OK;
@@ -520,7 +537,7 @@ int hf_engine_stats(const hf_engine* eng, int* num_shells, long long* num_shell_
     const Engine* e = reinterpret_cast<const Engine*>(eng);
     if (num_shells) *num_shells = e->num_shells;
     if (num_shell_pairs) *num_shell_pairs = static_cast<long long>(e->pairs.size());
-    if (num_quartets) *num_quartets = e->total_survivors;
+    if (num_quartets) *num_quartets = e->unique_quartets;
     return HF_OK;
 }
 

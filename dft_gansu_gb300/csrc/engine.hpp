@@ -93,6 +93,9 @@ struct RiState;  // ri.hpp
 // chosen by hf_engine_autotune (0: kFockBlocksPerSm).
 constexpr int kMaxBranches = 8;
 constexpr int kFockBlocksPerSm = 16;
+// upper bound on the primitive quartets of one work item (bra primitive range x ket
+// primitive pairs) above which a bra's entry is split by primitive range
+constexpr int kPrimPerItem = 64;
 constexpr int kMaxFockGraphs = 16;
 struct FockSchedule {
     int nbranch = 1;
@@ -159,8 +162,10 @@ struct Engine {
     std::vector<ClassPair> class_pairs;
     std::vector<int> entry_bra, entry_cnt;  // per (bra, ket group) entry
     std::vector<int> entry_lo0;              // class-relative first ket of the entry's group
+    std::vector<int> entry_prim;             // bra primitive-pair range of the entry: first | (end << 16)
     std::vector<long long> off_static;      // per class pair, nentry+1 (packed: entry_begin + cp)
-    long long total_survivors = 0;
+    long long total_survivors = 0;          // work items (a split bra counts once per entry)
+    long long unique_quartets = 0;          // contracted quartets of the lists
     std::vector<double> prim_bound;         // per primitive of the input list pair (dense), filled lazily
 
     // device
@@ -174,6 +179,7 @@ struct Engine {
     int* d_entry_bra = nullptr;
     int* d_entry_cnt = nullptr;
     int* d_entry_lo0 = nullptr;
+    int* d_entry_prim = nullptr;
     double* d_pair_qs = nullptr;  // Qs per global pair (for the mixed plan)
     long long* d_off_static = nullptr;
     int* d_cp_meta = nullptr;     // per class pair: entry_begin | nentry | ket_base | off_base

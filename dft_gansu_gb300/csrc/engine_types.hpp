@@ -62,6 +62,8 @@ struct FockClassLaunch {
     const long long* off;          // nentry+1 prefix offsets
     const int* entry_bra;          // global bra pair index per entry
     const int* entry_lo;           // first ket (class-relative) per entry
+    const int* entry_prim = nullptr;  // bra primitive pairs [first, end) per entry as first | (end << 16);
+                                      // null: all of the bra's primitive pairs
     int nentry;
     int ket_base;                  // global index of the ket class's first pair
     int num_basis;

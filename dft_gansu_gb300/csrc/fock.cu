@@ -286,6 +286,7 @@ FockClassLaunch make_launch(Engine& e, int cpi, bool fp32, const long long* off,
     L.off = off + cp.entry_begin + cpi;
     L.entry_bra = e.d_entry_bra + cp.entry_begin;
     L.entry_lo = lo + cp.entry_begin;
+    L.entry_prim = e.d_entry_prim + cp.entry_begin;
     L.nentry = cp.nentry;
     L.ket_base = e.pair_classes[cp.Y].begin;
     L.num_basis = e.num_basis;

@@ -101,10 +101,10 @@ __device__ __forceinline__ void hermite_r_rt(int L, const T* Fs, T X, T Y, T Z, 
     }
 }
 
-// (ab|cd)' for all (a,b) and one ket component pair cd into I[ab]; returns
-// the primitive quartets evaluated
+// (ab|cd)' for all (a,b) and one ket component pair cd into I[ab], over the
+// bra's primitive pairs [ip0, ip1); returns the primitive quartets evaluated
 template <class T>
-__device__ int quartet_column(const ShellPairDev& bp, const ShellPairDev& kp, int cd,
+__device__ int quartet_column(const ShellPairDev& bp, const ShellPairDev& kp, int cd, int ip0, int ip1,
                               const typename FockTypes<T>::PP* __restrict__ pp, const T* __restrict__ boys_table, T thr,
                               T* I)
 {
@@ -122,7 +122,7 @@ __device__ int quartet_column(const ShellPairDev& bp, const ShellPairDev& kp, in
     int count = 0;
     const typename TierTypes<T>::Geom gb_(bp), gk_(kp);
     const T qket_max = gk_.qmax;
-    for (int ip = 0; ip < bp.pp_n; ++ip) {
+    for (int ip = ip0; ip < ip1; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
         if (pb.Q * qket_max < thr) break;  // primitive pairs sorted by Q (descending)
         const T oo2p = T(0.5) * pb.invp;
@@ -189,11 +189,11 @@ template <class T>
 struct RuntimeColumn {
     static constexpr int kNAB = fock_column::kNAB;
     static constexpr int kNA = 0, kNB = 0, kND = 0;  // runtime angular momenta
-    __device__ static int eval(const ShellPairDev& bp, const ShellPairDev& kp, int cd,
+    __device__ static int eval(const ShellPairDev& bp, const ShellPairDev& kp, int cd, int ip0, int ip1,
                                const typename FockTypes<T>::PP* __restrict__ pp, const T* __restrict__ boys, T thr,
                                T* I)
     {
-        return quartet_column<T>(bp, kp, cd, pp, boys, thr, I);
+        return quartet_column<T>(bp, kp, cd, ip0, ip1, pp, boys, thr, I);
     }
 };
 
@@ -202,7 +202,7 @@ struct RuntimeColumn {
 // zero-padded ket coefficient vectors ((-1)^tau folded in), and the ket contraction
 // is separable (z, y, then x stages of R).
 template <class T, int LA, int LB, int LC, int LD>
-__device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const ShellPairDev& kp, int cd,
+__device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const ShellPairDev& kp, int cd, int ip0, int ip1,
                                                  const typename FockTypes<T>::PP* __restrict__ pp,
                                                  const T* __restrict__ boys_table, T thr, T* I)
 {
@@ -223,7 +223,7 @@ __device__ __forceinline__ int quartet_column_ct(const ShellPairDev& bp, const S
     const PP* __restrict__ kpp = pp + kp.pp_off;
     PP pk_next;
     if constexpr (kPrefetch) pk_next = kpp[0];
-    for (int ip = 0; ip < bp.pp_n; ++ip) {
+    for (int ip = ip0; ip < ip1; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
         if (pb.Q * qket_max < thr) break;  // primitive pairs sorted by Q (descending)
         const T oo2p = T(0.5) * pb.invp;
@@ -344,11 +344,11 @@ template <class T, int LA, int LB, int LC, int LD>
 struct ClassColumn {
     static constexpr int kNAB = ncart(LA) * ncart(LB);
     static constexpr int kNA = ncart(LA), kNB = ncart(LB), kND = ncart(LD);  // compile-time digestion bounds
-    __device__ static int eval(const ShellPairDev& bp, const ShellPairDev& kp, int cd,
+    __device__ static int eval(const ShellPairDev& bp, const ShellPairDev& kp, int cd, int ip0, int ip1,
                                const typename FockTypes<T>::PP* __restrict__ pp, const T* __restrict__ boys, T thr,
                                T* I)
     {
-        return quartet_column_ct<T, LA, LB, LC, LD>(bp, kp, cd, pp, boys, thr, I);
+        return quartet_column_ct<T, LA, LB, LC, LD>(bp, kp, cd, ip0, ip1, pp, boys, thr, I);
     }
 };
 
@@ -368,12 +368,13 @@ __global__ void __launch_bounds__(kFockThreads) column_kernel(const FockClassLau
         const int cd = static_cast<int>(wid % ncd);
         const long long w = (wid / ncd) * 32 + lane;
         bool active = w < total;
-        int bra = -1, ket = -1;
+        int bra = -1, ket = -1, prim = -1;
         ShellPairDev bp{}, kp{};
         T fsym = T(0);
         const int e = find_entry_warp(L.off, L.nentry, (wid / ncd) * 32, w, total);
         if (active) {
             bra = __ldg(L.entry_bra + e);
+            prim = entry_prim_range(L, e);
             ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(w - __ldg(L.off + e));
             if (negligible_quartet(L, bra, ket)) {
                 active = false;
@@ -387,11 +388,12 @@ __global__ void __launch_bounds__(kFockThreads) column_kernel(const FockClassLau
             if (bp.A == bp.B) fsym *= T(0.5);
             if (kp.A == kp.B) fsym *= T(0.5);
             if (bra == ket) fsym *= T(0.5);
-            const int pq = Column::eval(bp, kp, cd, static_cast<const PP*>(L.prim_pairs),
+            const int ip0 = prim < 0 ? 0 : (prim & 0xffff), ip1 = prim < 0 ? bp.pp_n : (prim >> 16);
+            const int pq = Column::eval(bp, kp, cd, ip0, ip1, static_cast<const PP*>(L.prim_pairs),
                                         static_cast<const T*>(L.boys_table), static_cast<T>(L.schwarz_threshold), I);
             if (cd == 0) {
                 prim_quartets += pq;
-                ++contracted;
+                if (ip0 == 0) ++contracted;  // a quartet split over entries counts once
             }
         } else {
             for (int ab = 0; ab < Column::kNAB; ++ab) I[ab] = T(0);

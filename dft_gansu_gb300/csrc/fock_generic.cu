@@ -24,11 +24,14 @@ eri_generic_kernel(const FockClassLaunch L, int ncd, const double* __restrict__ 
         const long long qi = w / ncd;
         const int cd = static_cast<int>(w % ncd);
         const int e = find_entry(L.off, L.nentry, qi);
+        // a bra split over entries by primitive range: its first entry writes the whole quartet
+        const int prim = entry_prim_range(L, e);
+        if (prim > 0 && (prim & 0xffff) != 0) continue;
         const int bra = __ldg(L.entry_bra + e);
         const int ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(qi - __ldg(L.off + e));
         const ShellPairDev bp = L.pairs[bra];
         const ShellPairDev kp = L.pairs[ket];
-        quartet_column<double>(bp, kp, cd, static_cast<const PrimPair64*>(L.prim_pairs),
+        quartet_column<double>(bp, kp, cd, 0, bp.pp_n, static_cast<const PrimPair64*>(L.prim_pairs),
                                static_cast<const double*>(L.boys_table), L.schwarz_threshold, I);
         const int na = ncart(bp.la), nb = ncart(bp.lb), nd = ncart(kp.lb);
         const long long c = kp.bfA + cd / nd, d = kp.bfB + cd % nd;

@@ -127,10 +127,11 @@ struct TierTypes<float> {
 };
 
 // Accumulates the ket component pairs [CD0, CD1) of the contracted quartet
-// (AB|CD)' into I[ab][cd - CD0], over the primitive quartets that pass the
-// primitive Schwarz test.  Returns the number of primitive quartets.
+// (AB|CD)' into I[ab][cd - CD0], over the primitive quartets of the bra's
+// primitive pairs [ip0, ip1) that pass the primitive Schwarz test.  Returns the
+// number of primitive quartets.
 template <class T, int LA, int LB, int LC, int LD, int CD0, int CD1>
-__device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const ShellPairDev& kp,
+__device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const ShellPairDev& kp, int ip0, int ip1,
                                              const typename FockTypes<T>::PP* __restrict__ pp,
                                              const T* __restrict__ boys_table, T thr,
                                              T (&I)[ncart(LA) * ncart(LB)][CD1 - CD0])
@@ -149,7 +150,7 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
     const PP* __restrict__ kpp = pp + kp.pp_off;
     PP pk_next;
     if constexpr (kPrefetch) pk_next = kpp[0];
-    for (int ip = 0; ip < bp.pp_n; ++ip) {
+    for (int ip = ip0; ip < ip1; ++ip) {
         const PP pb = pp[bp.pp_off + ip];
         // the primitive pairs of a shell pair are sorted by Q (descending), so the
         // first primitive quartet that fails the Schwarz test ends its loop
@@ -257,7 +258,14 @@ __device__ __forceinline__ int quartet_block(const ShellPairDev& bp, const Shell
 struct QuartetRef {
     int bra, ket;
     bool active;
+    int prim;  // bra primitive-pair range first | (end << 16), or -1 for all
 };
+
+// bra primitive-pair range [ip0, ip1) of an entry (all of the bra's when the list has none)
+__device__ __forceinline__ int entry_prim_range(const FockClassLaunch& L, int e)
+{
+    return L.entry_prim ? __ldg(L.entry_prim + e) : -1;
+}
 
 // Density-weighted screening of one contracted quartet (incremental builds):
 // true when Qs_ab Qs_cd times the largest |dD| over the six shell blocks the
@@ -306,8 +314,9 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
         if (bp.A == bp.B) fsym *= T(0.5);
         if (kp.A == kp.B) fsym *= T(0.5);
         if (q.bra == q.ket) fsym *= T(0.5);
+        const int ip0 = q.prim < 0 ? 0 : (q.prim & 0xffff), ip1 = q.prim < 0 ? bp.pp_n : (q.prim >> 16);
         prim_quartets += quartet_block<T, LA, LB, LC, LD, CD0, CD1>(
-            bp, kp, static_cast<const PP*>(L.prim_pairs), static_cast<const T*>(L.boys_table),
+            bp, kp, ip0, ip1, static_cast<const PP*>(L.prim_pairs), static_cast<const T*>(L.boys_table),
             static_cast<T>(L.schwarz_threshold), I);
     }
 
@@ -440,16 +449,17 @@ fock_direct_kernel(const FockClassLaunch launch)
     for (long long wid = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; wid < nwarps;
          wid += warp_stride) {
         const long long w = wid * 32 + lane;
-        QuartetRef q{-1, -1, w < total};
+        QuartetRef q{-1, -1, w < total, -1};
         const int e = find_entry_warp(launch.off, launch.nentry, wid * 32, w, total);
         if (q.active) {
             q.bra = __ldg(launch.entry_bra + e);
+            q.prim = entry_prim_range(launch, e);
             q.ket = launch.ket_base + __ldg(launch.entry_lo + e) + static_cast<int>(w - __ldg(launch.off + e));
             if (negligible_quartet(launch, q.bra, q.ket)) {
                 q.active = false;  // screened lanes look like lanes past the end (bra = -1)
                 q.bra = q.ket = -1;
-            } else {
-                ++contracted;
+            } else if (q.prim < 0 || (q.prim & 0xffff) == 0) {
+                ++contracted;  // a quartet split over entries counts once
             }
         }
         process_quartet<T, LA, LB, LC, LD, 0, NCD>(launch, q, lane, prim_quartets);

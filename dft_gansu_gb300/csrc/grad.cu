@@ -95,10 +95,11 @@ __device__ __forceinline__ void grad_r_table(int L, const T* Fs, T X, T Y, T Z, 
 
 
 // Item offsets of a class pair's list: entry e owns cnt_e kets, each split into the
-// bra pair's pp_n primitive pairs, so one work item is one (ket, bra primitive pair).
+// entry's bra primitive pairs, so one work item is one (ket, bra primitive pair).
 // One block per class pair (the layout of the quartet plan's offsets).
 __global__ void __launch_bounds__(256) grad_items_kernel(const long long* __restrict__ off,
                                                          const int* __restrict__ entry_bra,
+                                                         const int* __restrict__ entry_prim,
                                                          const ShellPairDev* __restrict__ pairs,
                                                          const int* __restrict__ cp_meta, int ncp,
                                                          long long* __restrict__ goff)
@@ -111,7 +112,10 @@ __global__ void __launch_bounds__(256) grad_items_kernel(const long long* __rest
     for (int start = 0; start < ne; start += blockDim.x) {
         const int i = start + threadIdx.x;
         long long v = 0;
-        if (i < ne) v = (off[ob + i + 1] - off[ob + i]) * static_cast<long long>(pairs[entry_bra[eb + i]].pp_n);
+        if (i < ne) {
+            const int pr = entry_prim[eb + i];
+            v = (off[ob + i + 1] - off[ob + i]) * static_cast<long long>((pr >> 16) - (pr & 0xffff));
+        }
         part[threadIdx.x] = v;
         __syncthreads();
         for (int o = 1; o < blockDim.x; o <<= 1) {  // inclusive Hillis-Steele scan
@@ -164,8 +168,9 @@ __global__ void __launch_bounds__(kGradThreads) grad_eri_kernel(const GradLaunch
         const int bra = __ldg(L.entry_bra + e);
         const ShellPairDev bp = L.pairs[bra];
         const long long item = w - __ldg(G.goff + e);
-        const int ip = static_cast<int>(item % bp.pp_n);
-        const int ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(item / bp.pp_n);
+        const int pr = __ldg(L.entry_prim + e), nip = (pr >> 16) - (pr & 0xffff);
+        const int ip = (pr & 0xffff) + static_cast<int>(item % nip);
+        const int ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(item / nip);
         const ShellPairDev kp = L.pairs[ket];
         const int la = bp.la, lb = bp.lb, lc = kp.la, ld = kp.lb;
         const int na = ncart(la), nb = ncart(lb), nd = ncart(ld);
@@ -549,11 +554,12 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
     if (!e.d_goff64 && (cudaMalloc(&e.d_goff64, sizeof(long long) * noff) != cudaSuccess ||
                         cudaMalloc(&e.d_goff32, sizeof(long long) * noff) != cudaSuccess))
         return set_error("cudaMalloc of gradient item offsets failed"), HF_ERR_OUT_OF_MEMORY;
-    grad_items_kernel<<<ncp, 256, 0, s>>>(mixed ? e.plan.off64 : e.d_off_static, e.d_entry_bra, e.d_pairs, e.d_cp_meta,
-                                          ncp, e.d_goff64);
+    grad_items_kernel<<<ncp, 256, 0, s>>>(mixed ? e.plan.off64 : e.d_off_static, e.d_entry_bra, e.d_entry_prim,
+                                          e.d_pairs, e.d_cp_meta, ncp, e.d_goff64);
     GB_LAUNCH_CHECK();
     if (mixed) {
-        grad_items_kernel<<<ncp, 256, 0, s>>>(e.plan.off32, e.d_entry_bra, e.d_pairs, e.d_cp_meta, ncp, e.d_goff32);
+        grad_items_kernel<<<ncp, 256, 0, s>>>(e.plan.off32, e.d_entry_bra, e.d_entry_prim, e.d_pairs, e.d_cp_meta, ncp,
+                                              e.d_goff32);
         GB_LAUNCH_CHECK();
     }
     const size_t sgrad_bytes = sizeof(double) * 3 * natom;
@@ -582,6 +588,7 @@ int rhf_gradient(Engine& e, const double* d_D, const double* d_W, double* h_grad
             G.L.off = off + cp.entry_begin + c;
             G.L.entry_bra = e.d_entry_bra + cp.entry_begin;
             G.L.entry_lo = lo + cp.entry_begin;
+            G.L.entry_prim = e.d_entry_prim + cp.entry_begin;
             G.L.nentry = cp.nentry;
             G.L.ket_base = Y.begin;
             G.L.num_basis = e.num_basis;

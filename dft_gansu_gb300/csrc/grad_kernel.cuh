@@ -71,8 +71,9 @@ __global__ void __launch_bounds__(kGradThreads) grad_class_kernel(const GradLaun
         const int bra = __ldg(L.entry_bra + e);
         const ShellPairDev bp = L.pairs[bra];
         const long long item = w - __ldg(G.goff + e);
-        const int ip = static_cast<int>(item % bp.pp_n);
-        const int ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(item / bp.pp_n);
+        const int pr = __ldg(L.entry_prim + e), nip = (pr >> 16) - (pr & 0xffff);
+        const int ip = (pr & 0xffff) + static_cast<int>(item % nip);
+        const int ket = L.ket_base + __ldg(L.entry_lo + e) + static_cast<int>(item / nip);
         const ShellPairDev kp = L.pairs[ket];
         const int ic = cdi / ND, id = cdi % ND;
         int c[3], d[3];

@@ -11,6 +11,7 @@
 // The DIIS B matrix, its bordered FP64 solve (partial-pivot Gaussian
 // elimination, the algorithm of the reference's getrf/getrs) and the
 // extrapolation all run on the device: no host round trip per DIIS step.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -1168,9 +1169,12 @@ static int rhf_scf_run(hf_engine* eng, int num_electrons, const hf_scf_options* 
         if (incremental) {
             sub_kernel<<<grid_nn(nn), 256, 0, s>>>(w.D, w.Dprev, nn, w.dD);
             GB_LAUNCH_CHECK();
-            if ((r = build_jk(e, w.dD, nullptr, nullptr, opt.precision, opt.mixed_threshold, s,
-                              opt.incremental_drop > 0.0 ? opt.incremental_drop : -1.0)))
-                return r;
+            // the contributions left out change from one build to the next, so the drop is
+            // capped by the convergence threshold (each left-out term stays 30x below it)
+            const double drop = opt.incremental_drop > 0.0
+                                    ? std::min(opt.incremental_drop, 0.03 * opt.convergence_threshold)
+                                    : -1.0;
+            if ((r = build_jk(e, w.dD, nullptr, nullptr, opt.precision, opt.mixed_threshold, s, drop))) return r;
         } else {
             const int prec = (opt.precision == HF_PRECISION_MIXED) ? opt.full_build_precision : opt.precision;
             if ((r = build_jk(e, w.D, nullptr, nullptr, prec, opt.mixed_threshold, s))) return r;

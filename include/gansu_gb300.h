@@ -322,7 +322,7 @@ typedef struct {
                                        anchor takes quartets with Q_ab*Q_cd*max|D| below this in FP32 */
     double incremental_drop;        /* incremental dD builds (direct): quartets whose Qs_ab*Qs_cd times the
                                        largest |dD| of the shell blocks they read is below this are left out
-                                       (0: the Schwarz threshold) */
+                                       (0: the Schwarz threshold); capped at 0.03 * convergence_threshold */
 } hf_scf_options;
 
 /* Fock-matrix update between iterations (Convergence_RHF_DIIS / _Damping,

@@ -3,7 +3,9 @@
 The reference diagonalises F' every iteration (computeCoefficientMatrix,
 src/gpu_manager.cu:529-599); purification must give the same aufbau density
 whenever the HOMO-LUMO gap is open.  Tolerances: SCF energies within 1e-9 Eh of
-the syevd SCF (convergence threshold 1e-10), orbital energies within 1e-6 Eh.
+the syevd SCF (convergence threshold 1e-10 on |dE|), orbital energies within
+1e-5 Eh (the energy is stationary, so |dE| < 1e-10 leaves the density, and the
+orbital energies of two SCFs that stop at different iterations, ~1e-5 apart).
 Sizes: N <= 512 runs the fused single-launch purification (csrc/purify.cu),
 larger N the SP2/McWeeny library calls; both check the purified projector
 (trace = nocc to 1e-6, idempotency to 1e-8) and a failed check reruns the SCF
@@ -40,7 +42,7 @@ def test_fused_purification_matches_diagonalisation(built_library, cuda, name, a
     assert rd["converged"] == 1 and rp["converged"] == 1
     assert rp["eigensolver_used"] == gg.HF_EIGEN_PURIFICATION
     assert abs(rp["total_energy"] - rd["total_energy"]) < 1e-9
-    np.testing.assert_allclose(rp["orbital_energies"].cpu().numpy(), rd["orbital_energies"].cpu().numpy(), atol=1e-6)
+    np.testing.assert_allclose(rp["orbital_energies"].cpu().numpy(), rd["orbital_energies"].cpu().numpy(), atol=1e-5)
     eng.close()
 
 
