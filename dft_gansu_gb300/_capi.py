@@ -82,6 +82,7 @@ class ScfOptions(C.Structure):
         ("purification_max_steps", C.c_int),
         ("anchor_mixed_threshold", C.c_double),
         ("incremental_drop", C.c_double),
+        ("pre_anchor_drop", C.c_double),
     ]
 
 

@@ -958,6 +958,7 @@ void hf_scf_options_default(hf_scf_options* o)
     o->purification_max_steps = 0;
     o->anchor_mixed_threshold = 0.0;
     o->incremental_drop = 0.0;
+    o->pre_anchor_drop = 0.0;
     o->eigensolver = 0;
     o->verbose = 0;
 }
@@ -1145,14 +1146,15 @@ static int rhf_scf_run(hf_engine* eng, int num_electrons, const hf_scf_options* 
             if (!first && (r = ri_absmax_diff(e, w.D, w.Dprev, &dmax, s))) return r;
             const bool low = first || dmax >= opt.anchor_threshold;
             // the pre-anchor builds only steer the density towards the anchor: quartets whose
-            // bound is below kPreAnchorDrop are left out of them (the anchor builds every
-            // quartet the Schwarz screen keeps: in FP64, or with anchor_mixed_threshold > 0
-            // the quartets with Q_ab Q_cd max|D| below it in FP32)
+            // bound is below pre_anchor_drop (kPreAnchorDrop by default) are left out of them
+            // (the anchor builds every quartet the Schwarz screen keeps: in FP64, or with
+            // anchor_mixed_threshold > 0 the quartets with Q_ab Q_cd max|D| below it in FP32)
             const bool mixed_anchor = opt.anchor_mixed_threshold > 0.0;
+            const double pre_drop = opt.pre_anchor_drop > 0.0 ? opt.pre_anchor_drop : kPreAnchorDrop;
             if ((r = build_jk(e, w.D, nullptr, nullptr,
                               (low || mixed_anchor) ? HF_PRECISION_MIXED : HF_PRECISION_FP64,
                               low ? std::numeric_limits<double>::infinity() : opt.anchor_mixed_threshold, s,
-                              low ? kPreAnchorDrop : -1.0)))
+                              low ? pre_drop : -1.0)))
                 return r;
             if (!low) anchored = true;
             fock_from_jk_kernel<<<grid_nn(nn), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.last_mixed ? e.d_Jp32 : nullptr,

@@ -323,6 +323,9 @@ typedef struct {
     double incremental_drop;        /* incremental dD builds (direct): quartets whose Qs_ab*Qs_cd times the
                                        largest |dD| of the shell blocks they read is below this are left out
                                        (0: the Schwarz threshold); capped at 0.03 * convergence_threshold */
+    double pre_anchor_drop;         /* mixed tier, direct builds before the anchor: quartets whose
+                                       Qs_ab*Qs_cd*max|D| is below this are left out of those builds
+                                       (0: 1e-6); the anchor and later builds are not affected */
 } hf_scf_options;
 
 /* Fock-matrix update between iterations (Convergence_RHF_DIIS / _Damping,
