@@ -20,6 +20,7 @@
 #include <map>
 #include <memory>
 #include <numeric>
+#include <thread>
 
 #include "engine.hpp"
 #include "md_math.cuh"
@@ -29,7 +30,9 @@ namespace gb {
 // sqrt(2 pi^{5/2}) folded into every primitive-pair prefactor K
 static const double kKFold = std::sqrt(2.0 * std::pow(kPi, 2.5));
 
-void host_boys_table(std::vector<double>& table)
+namespace {
+
+void compute_boys_table(std::vector<double>& table)
 {
     table.assign(static_cast<size_t>(kBoysRows) * kBoysPoints, 0.0);
     for (int k = 0; k < kBoysPoints; ++k)
@@ -55,6 +58,19 @@ void host_boys_table(std::vector<double>& table)
             table[boys_at(n - 1, k)] = static_cast<double>(f);
         }
     }
+}
+
+}  // namespace
+
+// the table depends on nothing but the grid: computed once per process
+void host_boys_table(std::vector<double>& table)
+{
+    static const std::vector<double> cached = [] {
+        std::vector<double> t;
+        compute_boys_table(t);
+        return t;
+    }();
+    table = cached;
 }
 
 namespace {
@@ -100,6 +116,23 @@ double prim_pair_bound_t(const PrimPair64& pp, double abx, double aby, double ab
             mx = std::max(mx, std::fabs(s) * cf * cf);
         }
     return std::sqrt(mx);
+}
+
+// f(0) .. f(n - 1) over up to 16 host threads (static chunks); f must not share writes
+template <class F>
+void parallel_for(int n, const F& f)
+{
+    const int nt = std::max(1, std::min({n / 64, 16, static_cast<int>(std::thread::hardware_concurrency())}));
+    if (nt <= 1) {
+        for (int k = 0; k < n; ++k) f(k);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&, t] {
+            for (int k = t; k < n; k += nt) f(k);
+        });
+    for (auto& th : pool) th.join();
 }
 
 template <class T>
@@ -299,83 +332,114 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
     std::vector<double> boys;
     host_boys_table(boys);
 
-    // ---- shell pairs per class
+    // ---- shell pairs per class: every class's (A, B) list first, then the primitive
+    // pairs and their Schwarz bounds of all of them over host threads in one pass
+    // (each shell pair writes its own slice of one primitive-pair array)
+    struct Todo {
+        int A, B, m, la, lb;
+    };
+    std::vector<Todo> todo;
+    std::vector<int> class_todo0;  // first todo entry of each (la, lb) class, in class order
     for (int la = 0; la <= kMaxL; ++la)
         for (int lb = 0; lb <= la; ++lb) {
-            PairClass pc{la, lb, static_cast<int>(e->pairs.size()), 0};
-            struct Tmp {
-                ShellPairDev sp;
-                std::vector<PrimPair64> pp;
-                int mol;
-            };
-            std::vector<Tmp> tmp;
+            class_todo0.push_back(static_cast<int>(todo.size()));
             for (int m = 0; m < nmol; ++m)
-            for (int A : mol_shells[m]) {
-                if (e->shells[A].l != la) continue;
-                for (int B : mol_shells[m]) {
-                    if (e->shells[B].l != lb) continue;
-                    if (la == lb && B > A) continue;
-                    const Shell& sa = e->shells[A];
-                    const Shell& sb = e->shells[B];
-                    const double Ac[3] = {sa.x, sa.y, sa.z}, Bc[3] = {sb.x, sb.y, sb.z};
-                    Tmp t;
-                    t.sp = ShellPairDev{};
-                    t.sp.A = A; t.sp.B = B;
-                    t.sp.bfA = sa.bf - e->mol_bf0[m];  // molecule-local function indices
-                    t.sp.bfB = sb.bf - e->mol_bf0[m];
-                    t.sp.la = la; t.sp.lb = lb;
-                    t.sp.mbase = static_cast<int>(e->mol_base[m]);
-                    t.sp.mn = e->mol_n[m];
-                    t.mol = m;
-                    t.sp.ABx = Ac[0] - Bc[0]; t.sp.ABy = Ac[1] - Bc[1]; t.sp.ABz = Ac[2] - Bc[2];
-                    double qs = 0.0, qm = 0.0;
-                    for (int i = 0; i < sa.nprim; ++i)
-                        for (int j = 0; j < sb.nprim; ++j) {
-                            PrimPair64 pp = make_prim_pair(sh_alpha[sa.prim_off + i], sh_coef[sa.prim_off + i], Ac,
-                                                           sh_alpha[sb.prim_off + j], sh_coef[sb.prim_off + j], Bc);
-                            pp.Q = prim_pair_bound(la, lb, pp, t.sp.ABx, t.sp.ABy, t.sp.ABz, boys.data());
-                            qs += pp.Q;
-                            qm = std::max(qm, pp.Q);
-                            t.pp.push_back(pp);
-                        }
-                    // largest bound first: a kernel's primitive loop over this pair ends at
-                    // the first primitive pair that fails the Schwarz test
-                    std::stable_sort(t.pp.begin(), t.pp.end(),
-                                     [](const PrimPair64& x, const PrimPair64& y) { return x.Q > y.Q; });
-                    t.sp.Qs = qs;
-                    t.sp.Qmax = qm;
-                    tmp.push_back(std::move(t));
+                for (int A : mol_shells[m]) {
+                    if (e->shells[A].l != la) continue;
+                    for (int B : mol_shells[m]) {
+                        if (e->shells[B].l != lb) continue;
+                        if (la == lb && B > A) continue;
+                        todo.push_back(Todo{A, B, m, la, lb});
+                    }
                 }
-            }
-            // groups of equal primitive-pair count (so the lanes of a warp run
-            // the same primitive loops), each group sorted by Qs descending
-            std::stable_sort(tmp.begin(), tmp.end(), [](const Tmp& a, const Tmp& b) {
-                if (a.mol != b.mol) return a.mol < b.mol;
-                if (a.pp.size() != b.pp.size()) return a.pp.size() > b.pp.size();
-                return a.sp.Qs > b.sp.Qs;
-            });
-            for (size_t k = 0; k < tmp.size(); ++k) {
-                Tmp& t = tmp[k];
-                if (k == 0 || tmp[k - 1].pp.size() != t.pp.size() || tmp[k - 1].mol != t.mol) {
-                    pc.groups.push_back({static_cast<int>(k), 0});
-                    pc.group_mol.push_back(t.mol);
-                }
-                pc.groups.back().second++;
-                t.sp.pp_off = static_cast<int>(e->pp64.size());
-                t.sp.pp_n = static_cast<int>(t.pp.size());
-                t.sp.fABx = static_cast<float>(t.sp.ABx);
-                t.sp.fABy = static_cast<float>(t.sp.ABy);
-                t.sp.fABz = static_cast<float>(t.sp.ABz);
-                t.sp.fQmax = static_cast<float>(t.sp.Qmax);
-                e->pp64.insert(e->pp64.end(), t.pp.begin(), t.pp.end());
-                e->pairs.push_back(t.sp);
-            }
-            pc.count = static_cast<int>(tmp.size());
-            e->pair_classes.push_back(pc);
         }
+    class_todo0.push_back(static_cast<int>(todo.size()));
+    std::vector<size_t> pp0(todo.size() + 1, 0);  // slice of each shell pair in pp_all
+    for (size_t k = 0; k < todo.size(); ++k)
+        pp0[k + 1] = pp0[k] + static_cast<size_t>(e->shells[todo[k].A].nprim) * e->shells[todo[k].B].nprim;
+    std::vector<PrimPair64> pp_all(pp0.back());
+    std::vector<ShellPairDev> sp_all(todo.size());
+    parallel_for(static_cast<int>(todo.size()), [&](int k) {
+        const int A = todo[k].A, B = todo[k].B, m = todo[k].m, la = todo[k].la, lb = todo[k].lb;
+        const Shell& sa = e->shells[A];
+        const Shell& sb = e->shells[B];
+        const double Ac[3] = {sa.x, sa.y, sa.z}, Bc[3] = {sb.x, sb.y, sb.z};
+        ShellPairDev& sp = sp_all[k];
+        sp = ShellPairDev{};
+        sp.A = A; sp.B = B;
+        sp.bfA = sa.bf - e->mol_bf0[m];  // molecule-local function indices
+        sp.bfB = sb.bf - e->mol_bf0[m];
+        sp.la = la; sp.lb = lb;
+        sp.mbase = static_cast<int>(e->mol_base[m]);
+        sp.mn = e->mol_n[m];
+        sp.ABx = Ac[0] - Bc[0]; sp.ABy = Ac[1] - Bc[1]; sp.ABz = Ac[2] - Bc[2];
+        PrimPair64* pp = pp_all.data() + pp0[k];
+        double qs = 0.0, qm = 0.0;
+        for (int i = 0; i < sa.nprim; ++i)
+            for (int j = 0; j < sb.nprim; ++j) {
+                PrimPair64 q = make_prim_pair(sh_alpha[sa.prim_off + i], sh_coef[sa.prim_off + i], Ac,
+                                              sh_alpha[sb.prim_off + j], sh_coef[sb.prim_off + j], Bc);
+                q.Q = prim_pair_bound(la, lb, q, sp.ABx, sp.ABy, sp.ABz, boys.data());
+                qs += q.Q;
+                qm = std::max(qm, q.Q);
+                pp[i * sb.nprim + j] = q;
+            }
+        // largest bound first: a kernel's primitive loop over this pair ends at
+        // the first primitive pair that fails the Schwarz test
+        std::stable_sort(pp, pp + (pp0[k + 1] - pp0[k]),
+                         [](const PrimPair64& x, const PrimPair64& y) { return x.Q > y.Q; });
+        sp.Qs = qs;
+        sp.Qmax = qm;
+        sp.pp_n = static_cast<int>(pp0[k + 1] - pp0[k]);
+    });
+    e->pp64.reserve(pp_all.size());
+    {
+        int ci = 0;
+        for (int la = 0; la <= kMaxL; ++la)
+            for (int lb = 0; lb <= la; ++lb, ++ci) {
+                PairClass pc{la, lb, static_cast<int>(e->pairs.size()), 0};
+                // groups of equal primitive-pair count (so the lanes of a warp run
+                // the same primitive loops), each group sorted by Qs descending
+                std::vector<int> order;
+                for (int k = class_todo0[ci]; k < class_todo0[ci + 1]; ++k) order.push_back(k);
+                std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                    if (todo[a].m != todo[b].m) return todo[a].m < todo[b].m;
+                    if (sp_all[a].pp_n != sp_all[b].pp_n) return sp_all[a].pp_n > sp_all[b].pp_n;
+                    return sp_all[a].Qs > sp_all[b].Qs;
+                });
+                for (size_t r = 0; r < order.size(); ++r) {
+                    const int k = order[r];
+                    ShellPairDev sp = sp_all[k];
+                    const int mol = todo[k].m;
+                    if (r == 0 || sp_all[order[r - 1]].pp_n != sp.pp_n || todo[order[r - 1]].m != mol) {
+                        pc.groups.push_back({static_cast<int>(r), 0});
+                        pc.group_mol.push_back(mol);
+                    }
+                    pc.groups.back().second++;
+                    sp.pp_off = static_cast<int>(e->pp64.size());
+                    sp.fABx = static_cast<float>(sp.ABx);
+                    sp.fABy = static_cast<float>(sp.ABy);
+                    sp.fABz = static_cast<float>(sp.ABz);
+                    sp.fQmax = static_cast<float>(sp.Qmax);
+                    e->pp64.insert(e->pp64.end(), pp_all.begin() + pp0[k], pp_all.begin() + pp0[k + 1]);
+                    e->pairs.push_back(sp);
+                }
+                pc.count = static_cast<int>(order.size());
+                e->pair_classes.push_back(pc);
+            }
+    }
 
     // ---- class pairs and bra entries (contracted pre-screen on Qs)
     const double thr = schwarz_threshold;
+    // running maximum of the primitive bound Qmax over the kets of each group (kets are
+    // sorted by Qs): the largest primitive bound among a group's first k kets
+    std::vector<double> qmax_run(e->pairs.size());
+    for (const PairClass& pc : e->pair_classes)
+        for (const auto& g : pc.groups)
+            for (int k = 0; k < g.second; ++k) {
+                const int idx = pc.begin + g.first + k;
+                qmax_run[idx] = (k == 0) ? e->pairs[idx].Qmax : std::max(qmax_run[idx - 1], e->pairs[idx].Qmax);
+            }
     for (int X = 0; X < static_cast<int>(e->pair_classes.size()); ++X)
         for (int Y = 0; Y <= X; ++Y) {
             const PairClass& px = e->pair_classes[X];
@@ -410,8 +474,7 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
                     const int nb = bp.pp_n, nk = e->pairs[py.begin + g.first].pp_n;
                     const int nsplit = std::min(nb, std::max(1, (nb * nk + kPrimPerItem - 1) / kPrimPerItem));
                     const int chunk = (nb + nsplit - 1) / nsplit;
-                    double qket = 0.0;  // largest primitive bound among the entry's kets
-                    for (int k = 0; k < cnt; ++k) qket = std::max(qket, e->pairs[py.begin + g.first + k].Qmax);
+                    const double qket = qmax_run[py.begin + g.first + cnt - 1];  // largest among the entry's kets
                     for (int p0 = 0; p0 < nb; p0 += chunk) {
                         // a later range whose largest bound cannot pass with any ket adds nothing
                         if (p0 > 0 && e->pp64[bp.pp_off + p0].Q * qket < thr) break;
