@@ -61,6 +61,9 @@ int gemm_rm(cublasHandle_t h, bool ta, bool tb, int n, const double* A, const do
     return HF_OK;
 }
 
+// eigenvalues of S below this are dropped from X = U s^{-1/2} (src/hf.cu:171-243)
+constexpr double kOrthoCut = 1e-6;
+
 __global__ void transform_kernel(const double* __restrict__ W, const double* __restrict__ s, int n,
                                  double* __restrict__ X)
 {
@@ -69,7 +72,7 @@ __global__ void transform_kernel(const double* __restrict__ W, const double* __r
          k += static_cast<long long>(gridDim.x) * blockDim.x) {
         const int i = static_cast<int>(k / n), c = static_cast<int>(k % n);
         const double v = s[c];
-        const double d = (v < 1e-6) ? 0.0 : 1.0 / sqrt(v);
+        const double d = (v < kOrthoCut) ? 0.0 : 1.0 / sqrt(v);
         X[k] = W[static_cast<long long>(c) * n + i] * d;  // U[i][c] * s_c^{-1/2}
     }
 }
@@ -556,6 +559,65 @@ int syevd(Engine& e, const double* A, cudaStream_t s, int solver = 0)
     if (cusolverDnDsyevd(e.cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, w.n, w.W, w.n, w.eps, w.work,
                          w.lwork, w.info) != CUSOLVER_STATUS_SUCCESS)
         return set_error("cusolverDnDsyevd failed"), HF_ERR_SOLVER;
+    return HF_OK;
+}
+
+__global__ void identity_kernel(int n, double* __restrict__ X)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        X[k] = (k / n == k % n) ? 1.0 : 0.0;
+}
+
+// B = A - c I (n x n)
+__global__ void shift_diagonal_kernel(const double* __restrict__ A, int n, double c, double* __restrict__ B)
+{
+    const long long nn = static_cast<long long>(n) * n;
+    for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < nn;
+         k += static_cast<long long>(gridDim.x) * blockDim.x)
+        B[k] = A[k] - ((k / n == k % n) ? c : 0.0);
+}
+
+// The reference's X = U s^{-1/2} drops the eigenvectors of S with s < 1e-6.  When S - 1e-6 I
+// is positive definite no eigenvalue is dropped, and then any X with X^T S X = I spanning the
+// whole space gives the same densities, orbitals (up to sign) and orbital energies; the
+// purified loop never needs the eigenvectors of S, so X = L^{-T} from S = L L^T (two potrf and
+// one trsm instead of an eigendecomposition).  *used = false: S fails the test (or the
+// workspace is too small) and the caller builds the canonical X.
+int cholesky_orthogonalizer(Engine& e, const double* S, cudaStream_t s, bool* used)
+{
+    auto& w = e.scf;
+    *used = false;
+    const int n = w.n;
+    const long long nn = static_cast<long long>(n) * n;
+    int lwork = 0;
+    if (cusolverDnDpotrf_bufferSize(e.cusolver, CUBLAS_FILL_MODE_LOWER, n, w.T1, n, &lwork) !=
+            CUSOLVER_STATUS_SUCCESS ||
+        lwork > w.lwork)
+        return HF_OK;
+    shift_diagonal_kernel<<<grid_nn(nn), 256, 0, s>>>(S, n, kOrthoCut, w.T1);
+    GB_LAUNCH_CHECK();
+    if (cusolverDnDpotrf(e.cusolver, CUBLAS_FILL_MODE_LOWER, n, w.T1, n, w.work, w.lwork, w.info) !=
+        CUSOLVER_STATUS_SUCCESS)
+        return set_error("cusolverDnDpotrf failed"), HF_ERR_SOLVER;
+    int info = -1;
+    GB_CUDA_TRY(cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (info != 0) return HF_OK;  // an eigenvalue at or below the cut: canonical orthogonalization
+    // S is symmetric, so its row-major array is also its column-major one; the column-major
+    // factor L gives the column-major L^{-1}, i.e. the row-major L^{-T} = X
+    GB_CUDA_TRY(cudaMemcpyAsync(w.T1, S, nn * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (cusolverDnDpotrf(e.cusolver, CUBLAS_FILL_MODE_LOWER, n, w.T1, n, w.work, w.lwork, w.info) !=
+        CUSOLVER_STATUS_SUCCESS)
+        return set_error("cusolverDnDpotrf failed"), HF_ERR_SOLVER;
+    identity_kernel<<<grid_nn(nn), 256, 0, s>>>(n, w.X);
+    GB_LAUNCH_CHECK();
+    const double one = 1.0;
+    if (cublasDtrsm(e.cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                    w.T1, n, w.X, n) != CUBLAS_STATUS_SUCCESS)
+        return set_error("cublasDtrsm failed"), HF_ERR_SOLVER;
+    *used = true;
     return HF_OK;
 }
 
@@ -1213,12 +1275,18 @@ static int rhf_scf_run(hf_engine* eng, int num_electrons, const hf_scf_options* 
         if ((st = compute_eri_tensor(e, e.d_eri, s))) return st;
     }
     if ((st = core_hamiltonian(e, w.S, w.H, s))) return st;
-    if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
-    if ((st = orthogonalizer(e, opt, s))) return st;
-    GB_LAUNCH_CHECK();
     // purification needs no orbitals; the RI K build takes an orthonormal basis of the
     // occupied space from the projector (occupied_from_projector)
     const bool purify = opt.eigensolver == HF_EIGEN_PURIFICATION;
+    bool chol = false;  // the DIIS error must not depend on X, nor X be the caller's
+    if (purify && !use_ri && !opt.orthogonalizer && diis_x(opt) == 0 &&
+        (st = cholesky_orthogonalizer(e, w.S, s, &chol)))
+        return st;
+    if (!chol) {
+        if ((st = syevd(e, w.S, s, opt.eigensolver))) return st;
+        if ((st = orthogonalizer(e, opt, s))) return st;
+    }
+    GB_LAUNCH_CHECK();
     bool occ_seeded = false;
     auto density_from = [&](const double* Fm) -> int {
         int r;
