@@ -434,8 +434,18 @@ __device__ __forceinline__ void process_quartet(const FockClassLaunch& L, const 
     }
 }
 
+// Resident blocks per SM the FP32 class kernels are compiled for (their loads are the
+// latency they wait on, so occupancy buys more than registers): 8 (64 registers) for the
+// classes of at most 9 integrals, 5 (96) up to 27, 3 (168) up to 54; the larger FP32
+// classes and the FP64 kernels (bound by the FP64 pipe) keep the compiler's choice.
 template <class T, int LA, int LB, int LC, int LD>
-__global__ void __launch_bounds__(kFockThreads)
+struct FockMinBlocks {
+    static constexpr int NI = ncart(LA) * ncart(LB) * ncart(LC) * ncart(LD);
+    static constexpr int value = sizeof(T) == 8 ? 1 : (NI <= 9 ? 8 : (NI <= 27 ? 5 : (NI <= 54 ? 3 : 1)));
+};
+
+template <class T, int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(kFockThreads, (FockMinBlocks<T, LA, LB, LC, LD>::value))
 fock_direct_kernel(const FockClassLaunch launch)
 {
     static_assert(FockSplit<T, LA, LB, LC, LD>::value == 1, "large classes use the generic kernel");
