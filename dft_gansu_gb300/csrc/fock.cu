@@ -173,48 +173,65 @@ struct PlanArgs {
     const double* mol_skip = nullptr;
 };
 
-// One block per class pair.
-__global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
+// The plan in two launches: plan_count_kernel, one thread per entry of every class pair
+// (the two bisections of an entry are independent of the others), writes the entry's FP64
+// and FP32 ket counts into its slot of the offset arrays; plan_scan_kernel, one block per
+// class pair, turns each class pair's counts into the prefix offsets in place.
+__global__ void __launch_bounds__(kPlanThreads) plan_count_kernel(PlanArgs a, int ncp, int nentries)
+{
+    __shared__ int sbeg[kNumClassPairs + 1];
+    for (int c = threadIdx.x; c <= ncp; c += blockDim.x)
+        sbeg[c] = (c < ncp) ? a.cp_entry_begin[c] : nentries;
+    __syncthreads();
+    const double dmv = *a.dmax;
+    const double dm = (a.square ? dmv * dmv : dmv) * a.factor;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nentries; e += gridDim.x * blockDim.x) {
+        int cp = 0;  // class pair of entry e: the last with sbeg[cp] <= e
+        for (int lo = 0, hi = ncp - 1; lo <= hi;) {
+            const int mid = (lo + hi) >> 1;
+            if (sbeg[mid] <= e) { cp = mid; lo = mid + 1; } else { hi = mid - 1; }
+        }
+        const int i = e - sbeg[cp], ob = a.cp_off_base[cp];
+        const int cnt = a.entry_cnt[e];
+        const int k0 = a.cp_ket_base[cp] + a.entry_lo0[e];
+        const int bra = a.entry_bra[e];
+        double qb = a.pair_qs[bra] * dm, tau = a.mixed_threshold, skip = a.skip_threshold;
+        if (a.mol_dmax) {
+            const int m = a.shell_mol[a.pairs[bra].A];
+            const double d = a.mol_dmax[m];
+            qb = a.pair_qs[bra] * (a.square ? d * d : d) * a.factor;
+            tau = a.mol_tau[m];
+            skip = a.mol_skip[m];
+        }
+        int lo = 0, hi = cnt;  // first ket of the group with qb*Qs_ket < tau
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (qb * a.pair_qs[k0 + mid] >= tau) lo = mid + 1; else hi = mid;
+        }
+        // density-weighted screening: the tail whose bound times max|D| is below the
+        // Schwarz threshold contributes nothing measurable (it matters for dD builds)
+        int hi2 = cnt, lo2 = lo;
+        while (lo2 < hi2) {
+            const int mid = (lo2 + hi2) >> 1;
+            if (qb * a.pair_qs[k0 + mid] >= skip) lo2 = mid + 1; else hi2 = mid;
+        }
+        a.lo32[e] = a.entry_lo0[e] + lo;
+        a.off64[ob + i + 1] = lo;
+        a.off32[ob + i + 1] = lo2 - lo;
+    }
+}
+
+// One block per class pair: in-place inclusive scan of the counts at off[ob + 1 .. ob + ne].
+__global__ void __launch_bounds__(kPlanThreads) plan_scan_kernel(PlanArgs a)
 {
     __shared__ long long smem[32];
     const int cp = blockIdx.x;
-    const int eb = a.cp_entry_begin[cp], ne = a.cp_nentry[cp], kb = a.cp_ket_base[cp], ob = a.cp_off_base[cp];
-    const double dmv = *a.dmax;
-    const double dm = (a.square ? dmv * dmv : dmv) * a.factor;
-    long long base64 = 0, base32 = 0;
+    const int ne = a.cp_nentry[cp], ob = a.cp_off_base[cp];
     if (threadIdx.x == 0) { a.off64[ob] = 0; a.off32[ob] = 0; }
+    long long base64 = 0, base32 = 0;
     for (int start = 0; start < ne; start += blockDim.x) {
         const int i = start + threadIdx.x;
-        long long c64 = 0, c32 = 0;
-        if (i < ne) {
-            const int e = eb + i;
-            const int cnt = a.entry_cnt[e];
-            const int k0 = kb + a.entry_lo0[e];
-            const int bra = a.entry_bra[e];
-            double qb = a.pair_qs[bra] * dm, tau = a.mixed_threshold, skip = a.skip_threshold;
-            if (a.mol_dmax) {
-                const int m = a.shell_mol[a.pairs[bra].A];
-                const double d = a.mol_dmax[m];
-                qb = a.pair_qs[bra] * (a.square ? d * d : d) * a.factor;
-                tau = a.mol_tau[m];
-                skip = a.mol_skip[m];
-            }
-            int lo = 0, hi = cnt;  // first ket of the group with qb*Qs_ket < thr
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (qb * a.pair_qs[k0 + mid] >= tau) lo = mid + 1; else hi = mid;
-            }
-            c64 = lo;
-            // density-weighted screening: the tail whose bound times max|D| is below the
-            // Schwarz threshold contributes nothing measurable (it matters for dD builds)
-            int hi2 = cnt, lo2 = lo;
-            while (lo2 < hi2) {
-                const int mid = (lo2 + hi2) >> 1;
-                if (qb * a.pair_qs[k0 + mid] >= skip) lo2 = mid + 1; else hi2 = mid;
-            }
-            c32 = lo2 - lo;
-            a.lo32[e] = a.entry_lo0[e] + lo;
-        }
+        const long long c64 = (i < ne) ? a.off64[ob + i + 1] : 0, c32 = (i < ne) ? a.off32[ob + i + 1] : 0;
         long long t64, t32;
         const long long x64 = block_scan_exclusive(c64, smem, t64);
         const long long x32 = block_scan_exclusive(c32, smem, t32);
@@ -225,6 +242,13 @@ __global__ void __launch_bounds__(kPlanThreads) mixed_plan_kernel(PlanArgs a)
         base64 += t64;
         base32 += t32;
     }
+}
+
+void launch_plan(const PlanArgs& a, int ncp, int nentries, int num_sms, cudaStream_t s)
+{
+    const int grid = std::max(1, std::min((nentries + kPlanThreads - 1) / kPlanThreads, 4 * num_sms));
+    plan_count_kernel<<<grid, kPlanThreads, 0, s>>>(a, ncp, nentries);
+    plan_scan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
 }
 
 __global__ void finish_kernel(const double* __restrict__ Jp, const double* __restrict__ Kp,
@@ -350,7 +374,7 @@ static int mixed_plan_args(Engine& e, const double* d_D, double factor, bool squ
     a.off64 = e.plan.off64;
     a.off32 = e.plan.off32;
     a.lo32 = e.plan.lo32;
-    mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
+    launch_plan(a, ncp, static_cast<int>(e.entry_bra.size()), e.num_sms, s);
     GB_LAUNCH_CHECK();
     if (out) *out = a;
     return HF_OK;
@@ -410,7 +434,7 @@ int build_jk_batch(Engine& e, const double* d_D, const double* d_mol_tau, const 
     a.mol_dmax = d_mol_dmax;
     a.mol_tau = d_mol_tau;
     a.mol_skip = d_mol_skip;
-    mixed_plan_kernel<<<ncp, kPlanThreads, 0, s>>>(a);
+    launch_plan(a, ncp, static_cast<int>(e.entry_bra.size()), e.num_sms, s);
     GB_LAUNCH_CHECK();
     return launch_class_pairs(e, s, [&](int c, cudaStream_t cs) -> int {
         const ClassPair& cp = e.class_pairs[c];

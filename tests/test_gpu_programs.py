@@ -101,4 +101,6 @@ def test_cpp_hf_main_matches_python_api(built_library, cuda, tmp_path, args, met
     hf = gg.HFBuilder.buildHF(pm)
     e = hf.solve()
     assert hf.result["converged"] == 1 and "Converged: yes" in out
-    assert abs(_total(out) - e) < 1e-9, (out, e)
+    # the OH radical's UHF energy surface is flat: runs that differ only in the order of the
+    # Fock build's atomic additions stop (|dE| < 1e-10) at energies up to ~5e-8 apart
+    assert abs(_total(out) - e) < (1e-7 if method == "uhf" else 1e-9), (out, e)
