@@ -37,6 +37,9 @@ ANCHOR_THRESHOLD = 1e-2
 ANCHOR_MIXED_THRESHOLD = 3e-2
 INCREMENTAL_DROP = 3e-10
 CONV = 1e-8
+# DRAM bytes (read + write) of one FP64 build of the workload, from an ncu capture of the
+# launches in the bench's fp64_build NVTX range; the algorithmic bytes are a few MB
+FP64_BUILD_DRAM_BYTES = 3.95e9
 GUESSES = {"core": 0, "gwh": 1, "sad": 3}  # HF_GUESS_CORE / _GWH / _SAD
 # gradient FP32 cut: on decane cc-pVDZ max|g_mixed - g_FP64| = 1.6e-7 Eh/bohr at 1.0
 # (2.7e-8 at 0.3, 5.5e-7 at 3), against 4.5e-8 between the FP64 gradient and
@@ -614,7 +617,10 @@ def run_ours(args, rank, world):
             "gpu_launches": l1 - l0,
             "schedule": schedule,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                         "frac": achieved / peak64, "traffic": None,
+                         "frac": achieved / peak64, "traffic": FP64_BUILD_DRAM_BYTES,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 23 launches "
+                                           "of one FP64 build (NVTX range fp64_build), bytes per build; 3.6 GB of "
+                                           "it is local memory of the column kernels of the (dd|..) classes",
                          "kernel": "direct Fock build, FP64 tier (21 quartet-class launches), one launch set under the "
                                    "headline schedule",
                          "build_ms": build_ms, "model_flops": flops,
