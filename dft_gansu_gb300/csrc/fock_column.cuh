@@ -352,8 +352,11 @@ struct ClassColumn {
     }
 };
 
+// FP32: compiled for 4 resident blocks per SM (128 registers; the latency-bound FP32 tier
+// gains more from warps than it loses to the extra spills: mixed SCF 3.04-3.29 -> 2.93
+// ms/iter in an A/B on one box); FP64 (pipe-bound) keeps the compiler's choice
 template <class T, class Column>
-__global__ void __launch_bounds__(kFockThreads) column_kernel(const FockClassLaunch L, int ncd)
+__global__ void __launch_bounds__(kFockThreads, (sizeof(T) == 4 ? 4 : 1)) column_kernel(const FockClassLaunch L, int ncd)
 {
     using PP = typename FockTypes<T>::PP;
     const long long total = L.off[L.nentry];
