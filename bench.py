@@ -740,7 +740,7 @@ def run_water_batch(args, rank, world):
 
     def use(name):
         if name == "tuned":
-            batch.set_fock_schedule(tune["num_branches"], grid_caps=tune)
+            batch.set_fock_schedule(tune["num_branches"], use_graph=True, grid_caps=tune)
         else:
             batch.set_fock_schedule(1, grid_caps="default")
 

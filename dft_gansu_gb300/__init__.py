@@ -164,7 +164,8 @@ class _FockScheduleMixin:
 
     def set_fock_schedule(self, num_branches: int = 1, use_graph: bool = False, grid_caps=None):
         """Class launches on num_branches concurrent streams; use_graph replays each
-        distinct build from a CUDA graph (single-molecule engines).  grid_caps: a
+        distinct build from a CUDA graph (single-molecule engines; for a batch, the
+        SCF iteration's purified density step and Fock build).  grid_caps: a
         schedule from autotune() or fock_schedule() of an engine over the same
         molecules (cap_fp64, cap_fp32, branch lists), applied without timing, or
         "default" for 16 blocks per SM everywhere; None keeps the caps in force."""

@@ -412,8 +412,17 @@ struct Batch {
     double* bounds = nullptr;
     unsigned char* square = nullptr;
     int* d_nocc = nullptr;
+    // graphs of the iteration's density and Fock steps (replayed when the schedule asks)
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        int uses = 0;
+        bool failed = false;
+        long long launches = 0;
+    } density_graph, fock_graph;
     ~Batch()
     {
+        for (StepGraph* g : {&density_graph, &fock_graph})
+            if (g->exec) cudaGraphExecDestroy(g->exec);
         if (d_ebase) cudaFree(d_ebase);
         if (params) cusolverDnDestroyParams(params);
         for (void* p : {static_cast<void*>(P32a), static_cast<void*>(P32b), static_cast<void*>(P32c),
@@ -506,11 +515,20 @@ int batch_syev(Batch& b, double* A, double* evals, cudaStream_t s)
 // C and D from F for every molecule: F' = X^T F X, eigenvectors V, C = X V, D = 2 C_occ C_occ^T
 int batch_purify(Batch& b, cudaStream_t s);
 
+// cuBLAS on stream s; while a graph is captured on the schedule's capture stream it
+// runs on the engine-owned workspace (its own pool may allocate, which a capture forbids)
+void bind_cublas(Engine& e, cudaStream_t s)
+{
+    cublasSetStream(e.cublas, s);
+    if (s == e.sched.capture && e.sched.cublas_ws)
+        cublasSetWorkspace(e.cublas, e.sched.cublas_ws, kCublasCaptureWorkspace);
+}
+
 int batch_density(Batch& b, const double* F, cudaStream_t s)
 {
     Engine& e = *b.e;
     BatchState& w = b.w;
-    cublasSetStream(e.cublas, s);
+    bind_cublas(e, s);
     for (const Group& g : b.groups) {
         const long long o = g.base;
         if (gemm_batched(e.cublas, false, false, g.n, g.n, 1.0, F + o, g.n, w.X + o, g.n, 0.0, w.T1 + o, g.count) ||
@@ -612,6 +630,51 @@ int batch_fock(Batch& b, cudaStream_t s)
     batch_fock_kernel<<<grid_of(e.nelem), 256, 0, s>>>(e.d_Jp, e.d_Kp, e.d_scale, b.w.H, e.block_map(),
                                                        e.d_mol_active, b.w.F);
     GB_LAUNCH_CHECK();
+    return HF_OK;
+}
+
+// One step of the batch iteration (body(stream) issues its launches) under the engine's
+// graph schedule: ordinary launches on the first call, captured on the schedule's
+// capture stream on the second, replayed from then on.  The step reads the batch's
+// buffers (F, D, the active flags, the per-molecule phase) at replay, so it may be
+// captured once the iteration's launch sequence no longer changes.  A failed capture
+// leaves the step on ordinary launches.
+template <class Body>
+int run_step(Batch& b, Batch::StepGraph& g, cudaStream_t s, Body body)
+{
+    Engine& e = *b.e;
+    FockSchedule& S = e.sched;
+    if (!S.use_graph || g.failed || (!g.exec && g.uses++ == 0)) return body(s);
+    if (!g.exec) {
+        int st = schedule_streams(e);
+        if (st) return st;
+        if (!S.cublas_ws) GB_CUDA_TRY(cudaMalloc(&S.cublas_ws, kCublasCaptureWorkspace));
+        const long long l0 = launch_count();
+        cudaGraph_t graph = nullptr;
+        cudaError_t ce = cudaStreamBeginCapture(S.capture, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+            st = body(S.capture);
+            ce = cudaStreamEndCapture(S.capture, &graph);
+        }
+        bind_cublas(e, s);
+        const long long recorded = launch_count() - l0;
+        count_launches(-recorded);  // recorded, not launched
+        cudaGraphExec_t exec = nullptr;
+        if (!st && ce == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+            g.exec = exec;
+            g.launches = recorded;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        if (!g.exec) {
+            cudaGetLastError();  // capture errors are not sticky; clear the last-error slot
+            g.failed = true;
+            clear_error();
+            return body(s);
+        }
+    }
+    GB_CUDA_TRY(cudaGraphLaunch(g.exec, s));
+    count_launches(g.launches);
+    ++S.graph_replays;
     return HF_OK;
 }
 
@@ -778,9 +841,21 @@ int hf_batch_rhf_scf(hf_engine* eng, const int* num_electrons, const hf_scf_opti
     double diag_ms = 0.0, fock_ms = 0.0;
     while (iter < opt.max_iter) {
         cudaEventRecord(p0, s);
-        if ((st = batch_density(b, w.F, s))) return st;
+        // the purified density step and the Fock build have the same launches every
+        // iteration (after the first build, whose phase rule differs): graph-replayed
+        // under the schedule's use_graph; batched syev stays on ordinary launches
+        if (b.purify) {
+            if ((st = run_step(b, b.density_graph, s, [&](cudaStream_t cs) { return batch_density(b, w.F, cs); })))
+                return st;
+        } else if ((st = batch_density(b, w.F, s))) {
+            return st;
+        }
         cudaEventRecord(p1, s);
-        if ((st = batch_fock(b, s))) return st;
+        if (b.mixed && b.first_build) {
+            if ((st = batch_fock(b, s))) return st;
+        } else if ((st = run_step(b, b.fock_graph, s, [&](cudaStream_t cs) { return batch_fock(b, cs); }))) {
+            return st;
+        }
         cudaEventRecord(p2, s);
         batch_energy_kernel<<<nmol, 256, 0, s>>>(w.D, w.H, w.F, e.block_map(), w.energy);
         GB_LAUNCH_CHECK();

@@ -83,3 +83,26 @@ def test_batch_mixed_tier_matches_single_molecule_rule(built_library, cuda):
         single = eng.rhf_scf(m.num_electrons, mixed)
         assert single["converged"] == 1 and abs(a["total_energy"] - single["total_energy"]) < 1e-7
         eng.close()
+
+
+@pytest.mark.parametrize("precision", [gg.HF_PRECISION_FP64, gg.HF_PRECISION_MIXED])
+def test_batch_steps_replayed_from_graphs(built_library, cuda, precision):
+    """Under use_graph the batch iteration's purified density step and its Fock build
+    are captured once and replayed every later iteration; the energies equal those
+    of ordinary launches (only atomic summation orders differ)."""
+    clusters = geometry.water_cluster_set(8, nmax=4, seed=11)
+    mols = [gg.Molecular(c, gg.basis_path("6-31g")) for c in clusters]
+    batch = gg.Batch(mols)
+    opts = dict(CONV, eigensolver=gg.HF_EIGEN_PURIFICATION, initial_guess=gg.HF_GUESS_SAD, precision=precision)
+    if precision == gg.HF_PRECISION_MIXED:
+        opts.update(mixed_threshold=0.1, incremental=1, anchor_threshold=1e-2)
+    ref, _, _ = batch.rhf_scf(opts)
+    batch.set_fock_schedule(2, use_graph=True)
+    before = batch.graph_stats()["replays"]
+    res, _, iters = batch.rhf_scf(opts)
+    replays = batch.graph_stats()["replays"] - before
+    # iterations + 1 passes: the first runs ordinary launches, the second captures and replays
+    assert iters >= 3 and replays >= 2 * (iters - 1)
+    for a, b in zip(ref, res):
+        assert a["converged"] == 1 and b["converged"] == 1
+        assert abs(a["total_energy"] - b["total_energy"]) < 1e-8
