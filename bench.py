@@ -657,6 +657,16 @@ def run_c60_ri(args, rank, world):
         atoms = geometry.c60(jitter=0.01, seed=args.seed)
         label = ("RI-JK RHF/cc-pVDZ + cc-pVDZ-RIFIT C60 (N=900, naux=3960 Cartesian), "
                  "truncated icosahedron 1.40/1.45 A + N(0,0.01 A) jitter")
+    # the kernels and solver libraries of the B build load on their first use in a process:
+    # one untimed B build of a water molecule with the same bases first
+    try:
+        w_mol = gg.Molecular(geometry.water(), gg.basis_path("cc-pvdz"))
+        w_eng = gg.Engine(w_mol, 1e-12)
+        w_eng.set_auxiliary_basis(gg.Molecular(geometry.water(), gg.basis_path("cc-pvdz-rifit")))
+        w_eng.ri_intermediate_b(want=False)
+        w_eng.close()
+    except Exception as ex:  # the timed build below then includes the first-use cost
+        print(f"B-build warm-up failed: {ex}", file=sys.stderr)
     mol = gg.Molecular(atoms, gg.basis_path("cc-pvdz"))
     aux = gg.Molecular(atoms, gg.basis_path("cc-pvdz-rifit"))
     eng = gg.Engine(mol, 1e-12)
