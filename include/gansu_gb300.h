@@ -155,7 +155,8 @@ int hf_compute_jk_direct(hf_engine* eng, const double* d_density, double* d_J, d
  * captured into a CUDA graph on its second call and replayed from then on (so is
  * the RHF loop's purification density, HF_EIGEN_PURIFICATION); the
  * graph reads the buffers at replay, so their contents may change between calls,
- * not their addresses.  Batch engines use the branches, not the graphs. */
+ * not their addresses.  On batch engines (hf_batch_rhf_scf) use_graph replays the
+ * SCF iteration's purified density step and its Fock build instead. */
 int hf_engine_set_fock_schedule(hf_engine* eng, int num_branches, int use_graph);
 
 typedef struct {

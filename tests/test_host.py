@@ -236,3 +236,34 @@ def test_reference_side_plugin_compiles_against_reference_headers(tmp_path):
                     f"-I{root / 'dft_gansu_gb300' / 'plugin'}", "-c",
                     str(root / "dft_gansu_gb300" / "plugin" / "plugin_check.cu"), "-o", str(tmp_path / "p.o")],
                    check=True)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the header's structs (dft_gansu_gb300/_capi.py) have the
+    C layout: sizeof and every field's offset from a C program built with gcc."""
+    import ctypes
+    import shutil
+    import subprocess
+    from dft_gansu_gb300 import _capi
+    root = Path(__file__).resolve().parents[1]
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    structs = {"hf_primitive_shell": _capi.PrimitiveShell, "hf_atom": _capi.Atom,
+               "hf_scf_options": _capi.ScfOptions, "hf_scf_result": _capi.ScfResult,
+               "hf_autotune_report": _capi.AutotuneReport}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "gansu_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'    printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{root / 'include'}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
