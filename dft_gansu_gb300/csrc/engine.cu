@@ -335,32 +335,32 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
     // ---- shell pairs per class: every class's (A, B) list first, then the primitive
     // pairs and their Schwarz bounds of all of them over host threads in one pass
     // (each shell pair writes its own slice of one primitive-pair array)
-    struct Todo {
+    struct PairJob {
         int A, B, m, la, lb;
     };
-    std::vector<Todo> todo;
-    std::vector<int> class_todo0;  // first todo entry of each (la, lb) class, in class order
+    std::vector<PairJob> jobs;
+    std::vector<int> class_job0;  // first job of each (la, lb) class, in class order
     for (int la = 0; la <= kMaxL; ++la)
         for (int lb = 0; lb <= la; ++lb) {
-            class_todo0.push_back(static_cast<int>(todo.size()));
+            class_job0.push_back(static_cast<int>(jobs.size()));
             for (int m = 0; m < nmol; ++m)
                 for (int A : mol_shells[m]) {
                     if (e->shells[A].l != la) continue;
                     for (int B : mol_shells[m]) {
                         if (e->shells[B].l != lb) continue;
                         if (la == lb && B > A) continue;
-                        todo.push_back(Todo{A, B, m, la, lb});
+                        jobs.push_back(PairJob{A, B, m, la, lb});
                     }
                 }
         }
-    class_todo0.push_back(static_cast<int>(todo.size()));
-    std::vector<size_t> pp0(todo.size() + 1, 0);  // slice of each shell pair in pp_all
-    for (size_t k = 0; k < todo.size(); ++k)
-        pp0[k + 1] = pp0[k] + static_cast<size_t>(e->shells[todo[k].A].nprim) * e->shells[todo[k].B].nprim;
+    class_job0.push_back(static_cast<int>(jobs.size()));
+    std::vector<size_t> pp0(jobs.size() + 1, 0);  // slice of each shell pair in pp_all
+    for (size_t k = 0; k < jobs.size(); ++k)
+        pp0[k + 1] = pp0[k] + static_cast<size_t>(e->shells[jobs[k].A].nprim) * e->shells[jobs[k].B].nprim;
     std::vector<PrimPair64> pp_all(pp0.back());
-    std::vector<ShellPairDev> sp_all(todo.size());
-    parallel_for(static_cast<int>(todo.size()), [&](int k) {
-        const int A = todo[k].A, B = todo[k].B, m = todo[k].m, la = todo[k].la, lb = todo[k].lb;
+    std::vector<ShellPairDev> sp_all(jobs.size());
+    parallel_for(static_cast<int>(jobs.size()), [&](int k) {
+        const int A = jobs[k].A, B = jobs[k].B, m = jobs[k].m, la = jobs[k].la, lb = jobs[k].lb;
         const Shell& sa = e->shells[A];
         const Shell& sb = e->shells[B];
         const double Ac[3] = {sa.x, sa.y, sa.z}, Bc[3] = {sb.x, sb.y, sb.z};
@@ -401,17 +401,17 @@ int build_engine(const MolInput* mols, int nmol, double schwarz_threshold, hf_en
                 // groups of equal primitive-pair count (so the lanes of a warp run
                 // the same primitive loops), each group sorted by Qs descending
                 std::vector<int> order;
-                for (int k = class_todo0[ci]; k < class_todo0[ci + 1]; ++k) order.push_back(k);
+                for (int k = class_job0[ci]; k < class_job0[ci + 1]; ++k) order.push_back(k);
                 std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-                    if (todo[a].m != todo[b].m) return todo[a].m < todo[b].m;
+                    if (jobs[a].m != jobs[b].m) return jobs[a].m < jobs[b].m;
                     if (sp_all[a].pp_n != sp_all[b].pp_n) return sp_all[a].pp_n > sp_all[b].pp_n;
                     return sp_all[a].Qs > sp_all[b].Qs;
                 });
                 for (size_t r = 0; r < order.size(); ++r) {
                     const int k = order[r];
                     ShellPairDev sp = sp_all[k];
-                    const int mol = todo[k].m;
-                    if (r == 0 || sp_all[order[r - 1]].pp_n != sp.pp_n || todo[order[r - 1]].m != mol) {
+                    const int mol = jobs[k].m;
+                    if (r == 0 || sp_all[order[r - 1]].pp_n != sp.pp_n || jobs[order[r - 1]].m != mol) {
                         pc.groups.push_back({static_cast<int>(r), 0});
                         pc.group_mol.push_back(mol);
                     }
